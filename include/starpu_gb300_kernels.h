@@ -1,0 +1,98 @@
+/*
+ * starpu_gb300_kernels.h -- C-ABI of the GB300 (sm_103a) kernel layer.
+ *
+ * This is the thin layer that the StarPU codelets' cuda_funcs call in place of
+ * the vendor libraries.  Plain pointers and sizes only; every matrix is
+ * column-major (StarPU matrix interface: nx rows contiguous, ld >= nx).
+ * `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ * Every entry point only enqueues work on that stream and returns; none
+ * synchronises, none allocates device memory.
+ *
+ * Return codes: 0 = enqueued, GB300_EINVAL = bad argument (nothing enqueued),
+ * GB300_ENOTSUP = unsupported option, GB300_ECUDA = a launch failed (the CUDA
+ * error string is available from starpu_gb300_last_error()).
+ * Numeric failure (a non-positive pivot) is not a return code: it is written
+ * to the device status word *d_info (LAPACK convention: 0 = success, k > 0 =
+ * the leading minor of order k is not positive definite) without trapping.
+ */
+#ifndef STARPU_GB300_KERNELS_H
+#define STARPU_GB300_KERNELS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB300_OK 0
+#define GB300_EINVAL (-22)
+#define GB300_ENOTSUP (-95)
+#define GB300_ENOMEM (-12)
+#define GB300_ECUDA (-1000)
+#define GB300_ETIMEDOUT (-110)
+#define GB300_EDOM (-33)
+
+/* Message of the last CUDA error seen by this library in the calling thread. */
+const char *starpu_gb300_last_error(void);
+
+/* ---------------- tile codelet bodies (one tile, FP32 / FP64) ------------- */
+
+/* In-place lower Cholesky of the n x n tile A.
+ * Replaces cusolverDnSpotrf(handle, LOWER, n, A, lda, work, lwork, devInfo)
+ * of examples/cholesky/cholesky_kernels.c:354 (and the MAGMA / host-loop
+ * fallbacks at :369 and :391-416).  No workspace is needed. d_info may be NULL. */
+int starpu_gb300_spotrf_tile(void *stream, int n, float *A, int lda, int *d_info);
+int starpu_gb300_dpotrf_tile(void *stream, int n, double *A, int lda, int *d_info);
+
+/* B[m x n] <- alpha * B * L^{-T}, L n x n lower non-unit (alpha must be 1).
+ * Replaces cublasStrsm(RIGHT, LOWER, TRANS, NON_UNIT, m, n, &1, L, ldl, B, ldb)
+ * of examples/cholesky/cholesky_kernels.c:258. */
+int starpu_gb300_strsm_rltn_tile(void *stream, int m, int n, float alpha, const float *L, int ldl, float *B, int ldb);
+int starpu_gb300_dtrsm_rltn_tile(void *stream, int m, int n, double alpha, const double *L, int ldl, double *B, int ldb);
+
+/* C[n x n] (lower) <- alpha * A * A^T + beta * C, A n x k.
+ * Replaces cublasSsyrk(LOWER, N, n, k, &-1, A, lda, &1, C, ldc) of
+ * examples/cholesky/cholesky_kernels.c:177. */
+int starpu_gb300_ssyrk_ln_tile(void *stream, int n, int k, float alpha, const float *A, int lda, float beta, float *C, int ldc);
+int starpu_gb300_dsyrk_ln_tile(void *stream, int n, int k, double alpha, const double *A, int lda, double beta, double *C, int ldc);
+
+/* C[m x n] <- alpha * A * B^T + beta * C, A m x k, B n x k.
+ * Replaces cublasSgemm(N, T, m, n, k, &-1, A, lda, B, ldb, &1, C, ldc) of
+ * examples/cholesky/cholesky_kernels.c:98. */
+int starpu_gb300_sgemm_nt_tile(void *stream, int m, int n, int k, float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc);
+int starpu_gb300_dgemm_nt_tile(void *stream, int m, int n, int k, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc);
+
+/* ---------------- whole matrix, plain precision --------------------------- */
+
+/* Tiled right-looking Cholesky of the whole n x n matrix with tile nb (0 =
+ * 512): the DAG of examples/cholesky/cholesky_implicit.c:244-318 (POTRF k,
+ * TRSM m>k, SYRK/GEMM) with the tasks of one step fused into whole-panel
+ * launches.  Only the lower triangle is read and written. */
+int starpu_gb300_spotrf(void *stream, int n, float *A, int lda, int nb, int *d_info);
+int starpu_gb300_dpotrf(void *stream, int n, double *A, int lda, int nb, int *d_info);
+
+/* Solve A X = B with the lower factor L from *potrf (LAPACK xPOTRS, uplo=L,
+ * min-dgels/base/SRC/dpotrs.c), B n x nrhs overwritten by X. */
+int starpu_gb300_spotrs(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb);
+int starpu_gb300_dpotrs(void *stream, int n, int nrhs, const double *L, int ldl, double *B, int ldb);
+
+/* ---------------- device memory helpers for hosts without a CUDA binding -- */
+
+void *starpu_gb300_device_malloc(size_t bytes);
+int starpu_gb300_device_free(void *p);
+void *starpu_gb300_host_malloc_pinned(size_t bytes);
+int starpu_gb300_host_free_pinned(void *p);
+int starpu_gb300_memcpy_h2d(void *stream, void *dst, const void *src, size_t bytes);
+int starpu_gb300_memcpy_d2h(void *stream, void *dst, const void *src, size_t bytes);
+int starpu_gb300_memset(void *stream, void *dst, int value, size_t bytes);
+int starpu_gb300_stream_sync(void *stream);
+void *starpu_gb300_stream_create(void);
+int starpu_gb300_stream_destroy(void *stream);
+int starpu_gb300_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STARPU_GB300_KERNELS_H */

@@ -1,0 +1,224 @@
+"""ORACLE -- test infrastructure only (tests/, smoke(), bench.py cpu_baseline).
+
+ctypes binding of ``oracle/lib/liboracle.so`` (the C restatement of the
+reference's tiled Cholesky plus the StarPU-CPU-path port) and, where it was
+built from the reference tree, of ``oracle/_ref/libref_lapack.so`` (CLAPACK
+dpotrf/dpotrs from min-dgels).  The product never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "lib", "liboracle.so")
+REFLIB = os.path.join(HERE, "_ref", "libref_lapack.so")
+REF_TREE = os.environ.get("STARPU_REFERENCE_TREE", "/root/reference")
+
+_o = None
+_r = None
+_blas_ready = False
+
+vp, ci, cd, cu64 = C.c_void_p, C.c_int, C.c_double, C.c_uint64
+
+
+def build(with_ref: bool = True) -> None:
+    """Compile the restatement; also the reference CLAPACK when the tree is present."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if with_ref and os.path.isdir(os.path.join(REF_TREE, "min-dgels")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+
+
+def lib() -> C.CDLL:
+    global _o
+    if _o is None:
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+                os.path.getmtime(os.path.join(HERE, f)) for f in ("chol_oracle.c", "cpu_chol.c")):
+            build(with_ref=False)
+        o = C.CDLL(LIB)
+        o.oracle_hilbert_f32.argtypes = [ci, vp, ci]
+        o.oracle_normal_matrix.argtypes = [ci, ci, cu64, vp, ci]
+        o.oracle_uniform_rhs.argtypes = [ci, ci, cu64, vp, ci]
+        o.oracle_spd_gram.argtypes = [ci, cu64, cd, vp, ci]
+        o.oracle_chunk.argtypes = [ci, ci, ci, vp, vp]
+        o.oracle_potrf_tiled_f32.argtypes = [ci, vp, ci, ci]
+        o.oracle_potrf_tiled_f64.argtypes = [ci, vp, ci, ci]
+        o.oracle_potrs_f32.argtypes = [ci, ci, vp, ci, vp, ci]
+        o.oracle_potrs_f64.argtypes = [ci, ci, vp, ci, vp, ci]
+        o.oracle_check_hilbert_f32.argtypes = [ci, vp, ci, C.c_float, vp]
+        o.oracle_llt_residual.argtypes = [ci, vp, ci, vp, ci, ci]
+        o.oracle_llt_residual.restype = cd
+        o.oracle_backward_error.argtypes = [ci, ci, vp, ci, vp, ci, vp, ci, vp]
+        o.oracle_backward_error.restype = cd
+        o.oracle_flops_potrf.argtypes = [cd]
+        o.oracle_flops_potrf.restype = cd
+        o.oracle_dsposv_ir.argtypes = [ci, ci, vp, ci, vp, ci, vp, ci, ci, cd, ci, vp]
+        o.cpu_chol_init.argtypes = [C.c_char_p]
+        o.cpu_chol_potrf_tiled_f32.argtypes = [ci, vp, ci, ci, ci]
+        o.cpu_chol_potrf_tiled_f64.argtypes = [ci, vp, ci, ci, ci]
+        o.cpu_chol_potrs_f64.argtypes = [ci, ci, vp, ci, vp, ci, ci]
+        o.cpu_chol_set_blas_threads.argtypes = [ci]
+        _o = o
+    return _o
+
+
+def ref_lib() -> C.CDLL | None:
+    """CLAPACK from the reference tree (only where it was built)."""
+    global _r
+    if _r is None and os.path.exists(REFLIB):
+        _r = C.CDLL(REFLIB)
+    return _r
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ---------------------------------------------------------------- inputs
+def hilbert_f32(n: int) -> np.ndarray:
+    A = np.empty((n, n), dtype=np.float32, order="F")
+    lib().oracle_hilbert_f32(n, _p(A), n)
+    return A
+
+
+def normal_matrix(rows: int, cols: int, seed: int) -> np.ndarray:
+    B = np.empty((rows, cols), dtype=np.float64, order="F")
+    lib().oracle_normal_matrix(rows, cols, seed, _p(B), rows)
+    return B
+
+
+def uniform_rhs(n: int, nrhs: int, seed: int) -> np.ndarray:
+    B = np.empty((n, nrhs), dtype=np.float64, order="F")
+    lib().oracle_uniform_rhs(n, nrhs, seed, _p(B), n)
+    return B
+
+
+def spd_gram(n: int, seed: int, alpha: float) -> np.ndarray:
+    A = np.empty((n, n), dtype=np.float64, order="F")
+    lib().oracle_spd_gram(n, seed, alpha, _p(A), n)
+    return A
+
+
+def alpha_for_kappa(kappa: float) -> float:
+    """Shift alpha so that (4 + alpha) / alpha = kappa for B B^T / n with B
+    square iid N(0,1): its spectrum fills the Marchenko-Pastur range [0, 4]."""
+    return 4.0 / (kappa - 1.0)
+
+
+def chunk(n: int, parts: int, i: int) -> tuple[int, int]:
+    s, o = C.c_int(), C.c_int()
+    lib().oracle_chunk(n, parts, i, C.byref(s), C.byref(o))
+    return s.value, o.value
+
+
+# ------------------------------------------------------------ algorithms
+def potrf_tiled(A: np.ndarray, nblocks: int) -> tuple[np.ndarray, int]:
+    L = np.array(A, order="F", copy=True)
+    n = L.shape[0]
+    f = lib().oracle_potrf_tiled_f32 if L.dtype == np.float32 else lib().oracle_potrf_tiled_f64
+    info = f(n, _p(L), n, nblocks)
+    return L, info
+
+
+def potrs(L: np.ndarray, B: np.ndarray) -> np.ndarray:
+    L = np.asfortranarray(L)
+    X = np.array(B, order="F", copy=True, dtype=L.dtype)
+    n, nrhs = X.shape
+    f = lib().oracle_potrs_f32 if L.dtype == np.float32 else lib().oracle_potrs_f64
+    f(n, nrhs, _p(L), L.shape[0], _p(X), n)
+    return X
+
+
+def check_hilbert(L: np.ndarray, tol: float = 1e-4) -> tuple[int, float]:
+    e = C.c_double()
+    bad = lib().oracle_check_hilbert_f32(L.shape[0], _p(np.asfortranarray(L)), L.shape[0], tol, C.byref(e))
+    return bad, e.value
+
+
+def llt_residual(A: np.ndarray, L: np.ndarray) -> float:
+    A = np.asfortranarray(A, dtype=np.float64)
+    L = np.asfortranarray(L)
+    return lib().oracle_llt_residual(A.shape[0], _p(A), A.shape[0], _p(L), L.shape[0], int(L.dtype == np.float32))
+
+
+def backward_error(A: np.ndarray, X: np.ndarray, B: np.ndarray) -> tuple[float, np.ndarray]:
+    A = np.asfortranarray(A, dtype=np.float64)
+    X = np.asfortranarray(X, dtype=np.float64)
+    B = np.asfortranarray(B, dtype=np.float64)
+    be = np.empty(X.shape[1])
+    w = lib().oracle_backward_error(A.shape[0], X.shape[1], _p(A), A.shape[0], _p(X), X.shape[0], _p(B),
+                                    B.shape[0], _p(be))
+    return w, be
+
+
+def flops_potrf(n: float) -> float:
+    return lib().oracle_flops_potrf(float(n))
+
+
+def dsposv_ir(A, B, nblocks, tol=1e-12, max_iter=30):
+    A = np.asfortranarray(A, dtype=np.float64)
+    B = np.asfortranarray(B, dtype=np.float64)
+    X = np.zeros_like(B, order="F")
+    be = C.c_double()
+    it = lib().oracle_dsposv_ir(A.shape[0], B.shape[1], _p(A), A.shape[0], _p(B), B.shape[0], _p(X), X.shape[0],
+                                nblocks, tol, max_iter, C.byref(be))
+    return X, it, be.value
+
+
+# ------------------------------------------------------ reference CLAPACK
+def ref_dpotrf(A: np.ndarray) -> tuple[np.ndarray, int]:
+    r = ref_lib()
+    if r is None:
+        raise FileNotFoundError("oracle/_ref/libref_lapack.so not built")
+    L = np.array(A, dtype=np.float64, order="F", copy=True)
+    n = C.c_long(L.shape[0])
+    info = C.c_long(0)
+    r._starpu_dpotrf_(b"L", C.byref(n), _p(L), C.byref(n), C.byref(info))
+    return L, info.value
+
+
+def ref_dpotrs(L: np.ndarray, B: np.ndarray) -> np.ndarray:
+    r = ref_lib()
+    X = np.array(B, dtype=np.float64, order="F", copy=True)
+    n, nrhs = C.c_long(L.shape[0]), C.c_long(X.shape[1])
+    info = C.c_long(0)
+    r._starpu_dpotrs_(b"L", C.byref(n), C.byref(nrhs), _p(np.asfortranarray(L)), C.byref(n), _p(X), C.byref(n),
+                      C.byref(info))
+    assert info.value == 0
+    return X
+
+
+# -------------------------------------------------- StarPU CPU path port
+def openblas_path() -> str | None:
+    try:
+        import scipy
+    except ImportError:
+        return None
+    d = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+    c = sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so*")))
+    return c[0] if c else None
+
+
+def cpu_init() -> bool:
+    global _blas_ready
+    if not _blas_ready:
+        p = openblas_path()
+        if p is None:
+            return False
+        _blas_ready = lib().cpu_chol_init(p.encode()) == 0
+    return _blas_ready
+
+
+def cpu_potrf_tiled(A: np.ndarray, nblocks: int, nthreads: int) -> int:
+    assert cpu_init(), "scipy OpenBLAS not available"
+    f = lib().cpu_chol_potrf_tiled_f32 if A.dtype == np.float32 else lib().cpu_chol_potrf_tiled_f64
+    return f(A.shape[0], _p(A), A.shape[0], nblocks, nthreads)
+
+
+def cpu_potrs(L: np.ndarray, B: np.ndarray, nthreads: int) -> int:
+    assert cpu_init()
+    return lib().cpu_chol_potrs_f64(L.shape[0], B.shape[1], _p(L), L.shape[0], _p(B), B.shape[0], nthreads)

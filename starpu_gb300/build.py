@@ -1,0 +1,107 @@
+"""Build of the native library ``starpu_gb300/lib/libstarpu_gb300.so``.
+
+One shared object holds the C runtime (StarPU API subset), the C-ABI kernel
+layer and every sm_103a CUDA kernel.  Sources are compiled in parallel with
+nvcc (``-gencode arch=compute_103a,code=sm_103a``) and gcc, in-tree, with an
+mtime check so repeated builds are cheap.  No cmake.
+"""
+from __future__ import annotations
+
+import glob
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+LIBDIR = os.path.join(HERE, "lib")
+OBJDIR = os.path.join(LIBDIR, "obj")
+LIBNAME = "libstarpu_gb300.so"
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def lib_path() -> str:
+    return os.path.join(LIBDIR, LIBNAME)
+
+
+def _headers() -> list[str]:
+    hs = glob.glob(os.path.join(INCLUDE, "*.h"))
+    for ext in ("*.h", "*.cuh"):
+        hs += glob.glob(os.path.join(CSRC, "**", ext), recursive=True)
+    return hs
+
+
+def _stale(obj: str, src: str, deps_mtime: float) -> bool:
+    if not os.path.exists(obj):
+        return True
+    m = os.path.getmtime(obj)
+    return m < os.path.getmtime(src) or m < deps_mtime
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+    if r.stdout.strip() and os.environ.get("GB300_BUILD_VERBOSE"):
+        sys.stderr.write(r.stdout)
+
+
+def sources() -> tuple[list[str], list[str]]:
+    cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "kernels", "*.cu")))
+    c = sorted(glob.glob(os.path.join(CSRC, "runtime", "*.c")) + glob.glob(os.path.join(CSRC, "codelets", "*.c")))
+    return cu, c
+
+
+def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
+    """Compile every source that changed and relink the library; return its path."""
+    if not os.path.exists(NVCC):
+        raise RuntimeError(f"nvcc not found at {NVCC}")
+    os.makedirs(OBJDIR, exist_ok=True)
+    deps = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(__file__)])
+    cu, c = sources()
+    inc = ["-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
+    jobs = []
+    objs = []
+    for src in cu:
+        rel = os.path.relpath(src, CSRC).replace(os.sep, "_")
+        obj = os.path.join(OBJDIR, rel + ".o")
+        objs.append(obj)
+        if _stale(obj, src, deps):
+            cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+                   "-c", src, "-o", obj, *inc, *(extra_nvcc or [])]
+            if verbose or os.environ.get("GB300_PTXAS_VERBOSE"):
+                cmd.insert(1, "-Xptxas=-v")
+            jobs.append(cmd)
+    for src in c:
+        rel = os.path.relpath(src, CSRC).replace(os.sep, "_")
+        obj = os.path.join(OBJDIR, rel + ".o")
+        objs.append(obj)
+        if _stale(obj, src, deps):
+            jobs.append(["gcc", "-O2", "-g", "-fPIC", "-std=gnu11", "-Wall", "-Wno-unused-function", "-pthread",
+                         "-DSTARPU_GB300_BUILDING_LIB", "-c", src, "-o", obj, *inc])
+    if jobs:
+        with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+            list(ex.map(_run, jobs))
+    out = lib_path()
+    if jobs or not os.path.exists(out):
+        tmp = out + ".tmp"
+        _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "shared",
+              "-Xlinker", "-rpath=" + os.path.join(CUDA_HOME, "lib64"), "-lpthread", "-ldl", "-lm"])
+        os.replace(tmp, out)
+    return out
+
+
+def clean() -> None:
+    if os.path.isdir(LIBDIR):
+        shutil.rmtree(LIBDIR)
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

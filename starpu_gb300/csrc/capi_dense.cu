@@ -1,0 +1,266 @@
+// C-ABI over the SIMT dense kernels: tile codelet bodies (POTRF/TRSM/SYRK/GEMM
+// on one tile, FP32 and FP64) and the whole-matrix tiled factorisation and
+// triangular solves composed from them.  Every entry point only enqueues work
+// on the caller's stream and returns; nothing here synchronises or allocates.
+#include "kernels/simt_blas.cuh"
+#include "gb300_internal.h"
+#include "starpu_gb300_kernels.h"
+
+#include <algorithm>
+
+namespace gb300 {
+
+static inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
+
+template <typename T, bool TA, bool TB, int BM, int BN, int BK, int TM, int TN>
+static void gemm_launch(cudaStream_t s, bool lower, int m, int n, int k, T alpha, const T *A, long lda, const T *B,
+                        long ldb, T beta, T *C, long ldc)
+{
+    constexpr int NT = (BM / TM) * (BN / TN);
+    // the lower-triangular form is only ever used as C -= A A^T (N,T)
+    if constexpr (!TA && TB && BM == BN) {
+        if (lower) {
+            long tb = cdiv(m, BM);
+            gemm_simt_kernel<T, TA, TB, BM, BN, BK, TM, TN, true>
+                <<<dim3((unsigned)(tb * (tb + 1) / 2)), NT, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+            return;
+        }
+    }
+    {
+        gemm_simt_kernel<T, TA, TB, BM, BN, BK, TM, TN, false>
+            <<<dim3(cdiv(m, BM), cdiv(n, BN)), NT, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    }
+}
+
+template <typename T> struct simt_cfg;
+// FP32: 128x128 block tiles, 8x8 per thread; narrow variant for few columns (RHS blocks).
+template <> struct simt_cfg<float> {
+    template <bool TA, bool TB>
+    static void run(cudaStream_t s, bool lower, int m, int n, int k, float al, const float *A, long lda,
+                    const float *B, long ldb, float be, float *C, long ldc)
+    {
+        if (!lower && n <= 32)
+            gemm_launch<float, TA, TB, 128, 32, 8, 8, 2>(s, lower, m, n, k, al, A, lda, B, ldb, be, C, ldc);
+        else
+            gemm_launch<float, TA, TB, 128, 128, 8, 8, 8>(s, lower, m, n, k, al, A, lda, B, ldb, be, C, ldc);
+    }
+};
+// FP64: 64x64 block tiles, 4x4 per thread.
+template <> struct simt_cfg<double> {
+    template <bool TA, bool TB>
+    static void run(cudaStream_t s, bool lower, int m, int n, int k, double al, const double *A, long lda,
+                    const double *B, long ldb, double be, double *C, long ldc)
+    {
+        if (!lower && n <= 16)
+            gemm_launch<double, TA, TB, 64, 16, 8, 4, 2>(s, lower, m, n, k, al, A, lda, B, ldb, be, C, ldc);
+        else
+            gemm_launch<double, TA, TB, 64, 64, 8, 4, 4>(s, lower, m, n, k, al, A, lda, B, ldb, be, C, ldc);
+    }
+};
+
+template <typename T>
+void gemm(cudaStream_t s, bool ta, bool tb, bool lower, int m, int n, int k, T alpha, const T *A, long lda,
+          const T *B, long ldb, T beta, T *C, long ldc)
+{
+    if (m <= 0 || n <= 0) return;
+    if (!ta && !tb) simt_cfg<T>::template run<false, false>(s, lower, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    else if (!ta && tb) simt_cfg<T>::template run<false, true>(s, lower, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    else if (ta && !tb) simt_cfg<T>::template run<true, false>(s, lower, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    else simt_cfg<T>::template run<true, true>(s, lower, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+// B[m x nc] <- B * L^{-T}, blocked by SMALL_W columns: small triangular solve
+// of one column block, then a GEMM update of the remaining columns.
+template <typename T>
+void trsm_rltn(cudaStream_t s, int m, int nc, const T *L, long ldl, T *B, long ldb)
+{
+    if (m <= 0 || nc <= 0) return;
+    constexpr int SMALL_W = small_w<T>::value;
+    for (int j0 = 0; j0 < nc; j0 += SMALL_W) {
+        const int w = std::min(SMALL_W, nc - j0);
+        const T *Ljj = L + j0 + (long)j0 * ldl;
+        T *Bj = B + (long)j0 * ldb;
+        if (w == SMALL_W)
+            trsm_rltn_small_kernel<T, SMALL_W, true><<<cdiv(m, 128), 128, 0, s>>>(m, w, Ljj, ldl, Bj, ldb);
+        else
+            trsm_rltn_small_kernel<T, SMALL_W, false><<<cdiv(m, 128), 128, 0, s>>>(m, w, Ljj, ldl, Bj, ldb);
+        const int rest = nc - j0 - w;
+        if (rest > 0)
+            gemm<T>(s, false, true, false, m, rest, w, T(-1), Bj, ldb, L + (j0 + w) + (long)j0 * ldl, ldl, T(1),
+                    B + (long)(j0 + w) * ldb, ldb);
+    }
+}
+
+// Right-looking tiled Cholesky with tile nb: POTRF(k), TRSM of the whole
+// column panel below it, then the lower-triangular trailing update.  This is
+// the loop of examples/cholesky/cholesky_implicit.c:244-318 with the tasks of
+// one step k fused into whole-panel launches.  Diagonal blocks larger than
+// SMALL_W are themselves factored by the same algorithm with tile SMALL_W.
+template <typename T>
+void potrf_tiled(cudaStream_t s, int n, T *A, long lda, int nb, int *info, int info_base)
+{
+    constexpr int SMALL_W = small_w<T>::value;
+    if (nb <= 0) nb = n;
+    for (int k0 = 0; k0 < n; k0 += nb) {
+        const int kb = std::min(nb, n - k0);
+        T *Akk = A + k0 + (long)k0 * lda;
+        if (kb <= SMALL_W)
+            potf2_small_kernel<T, SMALL_W><<<1, 256, 0, s>>>(kb, Akk, lda, info, info_base + k0);
+        else
+            potrf_tiled<T>(s, kb, Akk, lda, SMALL_W, info, info_base + k0);
+        const int m = n - k0 - kb;
+        if (m > 0) {
+            T *P = A + (k0 + kb) + (long)k0 * lda;
+            trsm_rltn<T>(s, m, kb, Akk, lda, P, lda);
+            gemm<T>(s, false, true, true, m, m, kb, T(-1), P, lda, P, lda, T(1), A + (k0 + kb) + (long)(k0 + kb) * lda,
+                    lda);
+        }
+    }
+}
+
+// POTRS with a lower factor: L y = b (forward), then L^T x = y (backward),
+// blocked by SMALL_W rows; min-dgels/base/SRC/dpotrs.c does the same two
+// sweeps through dtrsm.
+template <typename T>
+void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, long ldb)
+{
+    if (n <= 0 || nrhs <= 0) return;
+    constexpr int SMALL_W = small_w<T>::value;
+    const unsigned g = cdiv(nrhs, 64);
+    for (int j0 = 0; j0 < n; j0 += SMALL_W) {
+        const int w = std::min(SMALL_W, n - j0);
+        trsm_left_small_kernel<T, SMALL_W, false><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
+        const int rest = n - j0 - w;
+        if (rest > 0)
+            gemm<T>(s, false, false, false, rest, nrhs, w, T(-1), L + (j0 + w) + (long)j0 * ldl, ldl, B + j0, ldb,
+                    T(1), B + j0 + w, ldb);
+    }
+    const int last = ((n - 1) / SMALL_W) * SMALL_W;
+    for (int j0 = last; j0 >= 0; j0 -= SMALL_W) {
+        const int w = std::min(SMALL_W, n - j0);
+        trsm_left_small_kernel<T, SMALL_W, true><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
+        if (j0 > 0)
+            gemm<T>(s, true, false, false, j0, nrhs, w, T(-1), L + j0, ldl, B + j0, ldb, T(1), B, ldb);
+    }
+}
+
+template void gemm<float>(cudaStream_t, bool, bool, bool, int, int, int, float, const float *, long, const float *,
+                          long, float, float *, long);
+template void gemm<double>(cudaStream_t, bool, bool, bool, int, int, int, double, const double *, long,
+                           const double *, long, double, double *, long);
+template void trsm_rltn<float>(cudaStream_t, int, int, const float *, long, float *, long);
+template void trsm_rltn<double>(cudaStream_t, int, int, const double *, long, double *, long);
+template void potrf_tiled<float>(cudaStream_t, int, float *, long, int, int *, int);
+template void potrf_tiled<double>(cudaStream_t, int, double *, long, int, int *, int);
+template void potrs_blocked<float>(cudaStream_t, int, int, const float *, long, float *, long);
+template void potrs_blocked<double>(cudaStream_t, int, int, const double *, long, double *, long);
+
+} // namespace gb300
+
+using namespace gb300;
+
+#define GB300_STREAM(s) ((cudaStream_t)(s))
+
+extern "C" {
+
+// ---- tile codelet bodies -------------------------------------------------
+
+int starpu_gb300_spotrf_tile(void *stream, int n, float *A, int lda, int *d_info)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1)) return GB300_EINVAL;
+    if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), GB300_STREAM(stream));
+    if (n) potrf_tiled<float>(GB300_STREAM(stream), n, A, lda, small_w<float>::value, d_info, 0);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_dpotrf_tile(void *stream, int n, double *A, int lda, int *d_info)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1)) return GB300_EINVAL;
+    if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), GB300_STREAM(stream));
+    if (n) potrf_tiled<double>(GB300_STREAM(stream), n, A, lda, small_w<double>::value, d_info, 0);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_strsm_rltn_tile(void *stream, int m, int n, float alpha, const float *L, int ldl, float *B, int ldb)
+{
+    if (m < 0 || n < 0 || ldl < (n > 1 ? n : 1) || ldb < (m > 1 ? m : 1)) return GB300_EINVAL;
+    if (alpha != 1.0f) return GB300_ENOTSUP;
+    trsm_rltn<float>(GB300_STREAM(stream), m, n, L, ldl, B, ldb);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_dtrsm_rltn_tile(void *stream, int m, int n, double alpha, const double *L, int ldl, double *B, int ldb)
+{
+    if (m < 0 || n < 0 || ldl < (n > 1 ? n : 1) || ldb < (m > 1 ? m : 1)) return GB300_EINVAL;
+    if (alpha != 1.0) return GB300_ENOTSUP;
+    trsm_rltn<double>(GB300_STREAM(stream), m, n, L, ldl, B, ldb);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_ssyrk_ln_tile(void *stream, int n, int k, float alpha, const float *A, int lda, float beta, float *C,
+                               int ldc)
+{
+    if (n < 0 || k < 0 || lda < (n > 1 ? n : 1) || ldc < (n > 1 ? n : 1)) return GB300_EINVAL;
+    gemm<float>(GB300_STREAM(stream), false, true, true, n, n, k, alpha, A, lda, A, lda, beta, C, ldc);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_dsyrk_ln_tile(void *stream, int n, int k, double alpha, const double *A, int lda, double beta,
+                               double *C, int ldc)
+{
+    if (n < 0 || k < 0 || lda < (n > 1 ? n : 1) || ldc < (n > 1 ? n : 1)) return GB300_EINVAL;
+    gemm<double>(GB300_STREAM(stream), false, true, true, n, n, k, alpha, A, lda, A, lda, beta, C, ldc);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_sgemm_nt_tile(void *stream, int m, int n, int k, float alpha, const float *A, int lda, const float *B,
+                               int ldb, float beta, float *C, int ldc)
+{
+    if (m < 0 || n < 0 || k < 0 || lda < (m > 1 ? m : 1) || ldb < (n > 1 ? n : 1) || ldc < (m > 1 ? m : 1))
+        return GB300_EINVAL;
+    gemm<float>(GB300_STREAM(stream), false, true, false, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_dgemm_nt_tile(void *stream, int m, int n, int k, double alpha, const double *A, int lda,
+                               const double *B, int ldb, double beta, double *C, int ldc)
+{
+    if (m < 0 || n < 0 || k < 0 || lda < (m > 1 ? m : 1) || ldb < (n > 1 ? n : 1) || ldc < (m > 1 ? m : 1))
+        return GB300_EINVAL;
+    gemm<double>(GB300_STREAM(stream), false, true, false, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    return gb300_last_launch_status();
+}
+
+// ---- whole-matrix plain-precision factorisation and solve -----------------
+
+int starpu_gb300_spotrf(void *stream, int n, float *A, int lda, int nb, int *d_info)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1) || nb < 0) return GB300_EINVAL;
+    if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), GB300_STREAM(stream));
+    if (n) potrf_tiled<float>(GB300_STREAM(stream), n, A, lda, nb ? nb : 512, d_info, 0);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_dpotrf(void *stream, int n, double *A, int lda, int nb, int *d_info)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1) || nb < 0) return GB300_EINVAL;
+    if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), GB300_STREAM(stream));
+    if (n) potrf_tiled<double>(GB300_STREAM(stream), n, A, lda, nb ? nb : 512, d_info, 0);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_spotrs(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb)
+{
+    if (n < 0 || nrhs < 0 || ldl < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1)) return GB300_EINVAL;
+    potrs_blocked<float>(GB300_STREAM(stream), n, nrhs, L, ldl, B, ldb);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_dpotrs(void *stream, int n, int nrhs, const double *L, int ldl, double *B, int ldb)
+{
+    if (n < 0 || nrhs < 0 || ldl < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1)) return GB300_EINVAL;
+    potrs_blocked<double>(GB300_STREAM(stream), n, nrhs, L, ldl, B, ldb);
+    return gb300_last_launch_status();
+}
+
+} // extern "C"

@@ -1,0 +1,27 @@
+// Internal declarations shared by the CUDA translation units of the kernel
+// layer (not part of the public C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include "starpu_gb300_kernels.h"
+
+namespace gb300 {
+
+// Width of the register-blocked small triangular kernels and of the
+// unblocked diagonal POTRF leaf: 64 columns in FP32, 32 in FP64 (a 64-wide
+// FP64 row does not fit the register file without spilling).
+template <typename T> struct small_w { static constexpr int value = 64; };
+template <> struct small_w<double> { static constexpr int value = 32; };
+
+template <typename T>
+void gemm(cudaStream_t s, bool ta, bool tb, bool lower, int m, int n, int k, T alpha, const T *A, long lda,
+          const T *B, long ldb, T beta, T *C, long ldc);
+template <typename T> void trsm_rltn(cudaStream_t s, int m, int nc, const T *L, long ldl, T *B, long ldb);
+template <typename T> void potrf_tiled(cudaStream_t s, int n, T *A, long lda, int nb, int *info, int info_base);
+template <typename T> void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, long ldb);
+
+} // namespace gb300
+
+// Records the CUDA error (if any) of the most recent launch in this thread and
+// maps it to a GB300_* return code.
+extern "C" int gb300_last_launch_status(void);
+extern "C" int gb300_record_cuda_error(cudaError_t e);
