@@ -77,6 +77,34 @@ int starpu_gb300_dpotrf(void *stream, int n, double *A, int lda, int nb, int *d_
 int starpu_gb300_spotrs(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb);
 int starpu_gb300_dpotrs(void *stream, int n, int nrhs, const double *L, int ldl, double *B, int ldb);
 
+/* ---------------- tensor-core trailing update (tcgen05, sm_103a) ---------- */
+
+/* P (m x k FP32, column-major, ldp) -> hi = bf16(P), lo = bf16(P - hi), both
+ * stored K-major (row i = P[i, 0..k), row stride ldk elements, ldk % 8 == 0,
+ * 16-byte aligned).  lo may be NULL.  Columns k..ldk-1 are written as 0. */
+int starpu_gb300_split_bf16(void *stream, int m, int k, const float *P, int ldp, void *hi, void *lo, int ldk);
+
+/* C[m x n] (FP32, column-major) -= A B^T on the tensor cores, A = m x k and
+ * B = n x k BF16 K-major (the layout starpu_gb300_split_bf16 writes).
+ * nterms = 1: A_hi B_hi^T.  nterms = 3: A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T
+ * (split-BF16, ~2^-16 relative).  lower = 1 (requires m == n): only elements
+ * with row >= col are written (the SYRK form).  This is the fused GEMM/SYRK
+ * trailing update that replaces cublasSgemm(N,T) / cublasSsyrk(L,N) of
+ * examples/cholesky/cholesky_kernels.c:98,177 for every tile of one step.
+ * d_err: device status word, set non-zero if an internal wait timed out. */
+int starpu_gb300_tc_update(void *stream, int m, int n, int k, const void *a_hi, const void *a_lo, int lda,
+                           const void *b_hi, const void *b_lo, int ldb, int nterms, int lower, float *C, int ldc,
+                           int *d_err);
+
+/* Bytes of BF16 panel workspace starpu_gb300_spotrf_tc needs. */
+size_t starpu_gb300_spotrf_tc_workspace(int n, int nb);
+
+/* Tiled Cholesky of an FP32 matrix (tile nb): FP32 POTRF of the diagonal
+ * tile and FP32 panel TRSM, trailing update on the tensor cores with the
+ * panel split to BF16 (nterms 1 or 3, as in starpu_gb300_tc_update). */
+int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int nterms, void *work, size_t lwork,
+                           int *d_info, int *d_err);
+
 /* ---------------- device memory helpers for hosts without a CUDA binding -- */
 
 void *starpu_gb300_device_malloc(size_t bytes);

@@ -1,0 +1,206 @@
+// Host side of the tensor-core trailing update: TMA descriptor encoding, the
+// FP32 -> split-BF16 (K-major) panel converter, and the C-ABI entry points
+// that use them (the bare update, and the tiled factorisation whose trailing
+// updates run on the tensor cores).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <mutex>
+#include <stdio.h>
+
+#include "gb300_internal.h"
+#include "kernels/tc_update.cuh"
+#include "starpu_gb300_kernels.h"
+#include "starpu_gb300_solver.h"
+
+namespace gb300 {
+
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static std::once_flag g_encode_once;
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    std::call_once(g_encode_once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        else
+            cudaGetLastError();
+    });
+    return g_encode;
+}
+
+// K-major BF16 matrix [rows x K] with row stride ld (elements, ld*2 % 16 == 0),
+// box = 64 (K) x box_rows, 128-byte swizzle, zero fill out of bounds.
+static int make_kmajor_map(CUtensorMap *map, const void *base, int rows, int K, long ld, int box_rows)
+{
+    auto enc = encode_fn();
+    if (!enc) return GB300_ENOTSUP;
+    if (((uintptr_t)base & 15) || ((ld * 2) & 15)) return GB300_EINVAL;
+    cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)ld * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TCU_BK, (cuuint32_t)box_rows};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), gdim, gstride, box, estride,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? GB300_OK : GB300_EINVAL;
+}
+
+static int num_sms()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// P (m x k FP32, column-major, ldp) -> hi = bf16(P), lo = bf16(P - hi), both
+// K-major (row i holds P[i, 0..k)), row stride ldk; columns k..ldk-1 zeroed.
+// 32x32 tiles transposed through shared memory: coalesced on both sides.
+__global__ void split_bf16_kmajor_kernel(int m, int k, const float *__restrict__ P, long ldp,
+                                         __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo, long ldk)
+{
+    __shared__ float t[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+        const int r = r0 + threadIdx.x, col = c0 + c;
+        t[c][threadIdx.x] = (r < m && col < k) ? P[r + (long)col * ldp] : 0.0f;
+    }
+    __syncthreads();
+    for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+        const int r = r0 + rr, col = c0 + threadIdx.x;
+        if (r < m && col < ldk) {
+            const float v = t[threadIdx.x][rr];
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            hi[(long)r * ldk + col] = h;
+            if (lo) lo[(long)r * ldk + col] = __float2bfloat16_rn(v - __bfloat162float(h));
+        }
+    }
+}
+
+int split_bf16(cudaStream_t s, int m, int k, const float *P, long ldp, void *hi, void *lo, long ldk)
+{
+    if (m <= 0 || k <= 0) return GB300_OK;
+    dim3 g((m + 31) / 32, (unsigned)((ldk + 31) / 32));
+    split_bf16_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo, ldk);
+    return gb300_last_launch_status();
+}
+
+int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void *a_lo, long lda, const void *b_hi,
+              const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err)
+{
+    if (m <= 0 || n <= 0 || K <= 0) return GB300_OK;
+    if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!a_lo || !b_lo)) || (lower && m != n) || !d_err)
+        return GB300_EINVAL;
+    CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
+    int rc;
+    if ((rc = make_kmajor_map(&ta_hi, a_hi, m, K, lda, TCU_BM))) return rc;
+    if ((rc = make_kmajor_map(&tb_hi, b_hi, n, K, ldb, TCU_BN))) return rc;
+    if (nterms == 3) {
+        if ((rc = make_kmajor_map(&ta_lo, a_lo, m, K, lda, TCU_BM))) return rc;
+        if ((rc = make_kmajor_map(&tb_lo, b_lo, n, K, ldb, TCU_BN))) return rc;
+    } else {
+        ta_lo = ta_hi;
+        tb_lo = tb_hi;
+    }
+    TcUpdateArgs a;
+    a.C = C;
+    a.ldc = ldc;
+    a.m = m;
+    a.n = n;
+    a.K = K;
+    a.nterms = nterms;
+    a.lower = lower;
+    a.tiles_m = (m + TCU_BM - 1) / TCU_BM;
+    a.tiles_n = (n + TCU_BN - 1) / TCU_BN;
+    if (lower) {
+        long cnt = 0;
+        for (int tn = 0; 2 * tn < a.tiles_m; ++tn) cnt += a.tiles_m - 2 * tn;
+        a.num_tiles = (int)cnt;
+    } else {
+        a.num_tiles = a.tiles_m * a.tiles_n;
+    }
+    a.err = d_err;
+    a.wait_budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TCU_SMEM);
+        attr_set = true;
+    }
+    const int grid = std::min(a.num_tiles, num_sms());
+    tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, a);
+    return gb300_last_launch_status();
+}
+
+// Tiled right-looking Cholesky of an FP32 matrix whose trailing updates run on
+// the tensor cores (split-BF16 when nterms == 3).  POTRF of the diagonal tile
+// and the panel TRSM stay in FP32 SIMT.  `panel` holds 2 * n * ldk BF16
+// (hi and lo halves), ldk = nb rounded up to 64.
+int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err)
+{
+    const long ldk = ((long)nb + 63) / 64 * 64;
+    __nv_bfloat16 *hi = (__nv_bfloat16 *)panel;
+    __nv_bfloat16 *lo = hi + (long)n * ldk;
+    for (int k0 = 0; k0 < n; k0 += nb) {
+        const int kb = std::min(nb, n - k0);
+        float *Akk = A + k0 + (long)k0 * lda;
+        potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
+        const int m = n - k0 - kb;
+        if (m <= 0) break;
+        float *P = A + (k0 + kb) + (long)k0 * lda;
+        trsm_rltn<float>(s, m, kb, Akk, lda, P, lda);
+        int rc = split_bf16(s, m, kb, P, lda, hi, nterms == 3 ? lo : nullptr, ldk);
+        if (rc) return rc;
+        rc = tc_update(s, m, m, kb, hi, lo, ldk, hi, lo, ldk, nterms, 1, A + (k0 + kb) + (long)(k0 + kb) * lda, lda,
+                       d_err);
+        if (rc) return rc;
+    }
+    return gb300_last_launch_status();
+}
+
+} // namespace gb300
+
+using namespace gb300;
+
+extern "C" {
+
+int starpu_gb300_split_bf16(void *stream, int m, int k, const float *P, int ldp, void *hi, void *lo, int ldk)
+{
+    if (m < 0 || k < 0 || ldp < (m > 1 ? m : 1) || ldk < k) return GB300_EINVAL;
+    return split_bf16((cudaStream_t)stream, m, k, P, ldp, hi, lo, ldk);
+}
+
+int starpu_gb300_tc_update(void *stream, int m, int n, int k, const void *a_hi, const void *a_lo, int lda,
+                           const void *b_hi, const void *b_lo, int ldb, int nterms, int lower, float *C, int ldc,
+                           int *d_err)
+{
+    if (m < 0 || n < 0 || k < 0 || ldc < (m > 1 ? m : 1) || lda < k || ldb < k) return GB300_EINVAL;
+    return tc_update((cudaStream_t)stream, m, n, k, a_hi, a_lo, lda, b_hi, b_lo, ldb, nterms, lower, C, ldc, d_err);
+}
+
+size_t starpu_gb300_spotrf_tc_workspace(int n, int nb)
+{
+    const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64;
+    return 2 * (size_t)n * ldk * 2;
+}
+
+int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int nterms, void *work, size_t lwork,
+                           int *d_info, int *d_err)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1) || nb <= 0 || (nterms != 1 && nterms != 3) || !d_err) return GB300_EINVAL;
+    if (lwork < starpu_gb300_spotrf_tc_workspace(n, nb) || !work) return GB300_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), s);
+    if (!n) return GB300_OK;
+    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err);
+}
+
+} // extern "C"
