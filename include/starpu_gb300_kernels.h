@@ -119,6 +119,26 @@ void *starpu_gb300_stream_create(void);
 int starpu_gb300_stream_destroy(void *stream);
 int starpu_gb300_device_count(void);
 
+/* CUDA events (timing on a stream from hosts without a CUDA binding). */
+void *starpu_gb300_event_create(void);
+int starpu_gb300_event_record(void *event, void *stream);
+double starpu_gb300_event_elapsed_ms(void *start, void *end); /* waits for `end` */
+int starpu_gb300_event_destroy(void *event);
+
+/* ---------------- measurement --------------------------------------------
+ * Number of kernels this library has launched since it was loaded. */
+unsigned long long starpu_gb300_launch_count(void);
+
+/* Per-kernel-class profiling, the counterpart of StarPU's per-task profiling
+ * information (STARPU_PROFILING, src/profiling/profiling.c): when enabled,
+ * each launch of a profiled class is bracketed by CUDA events on its own
+ * stream and its algorithmic flops / bytes are recorded.  Classes:
+ * 0 = tensor-core trailing update, 1 = panel (POTRF + TRSM + split),
+ * 2 = FP64 residual, 3 = triangular solves.  _get resolves pending events. */
+void starpu_gb300_profiling_enable(int on);
+void starpu_gb300_profiling_reset(void);
+int starpu_gb300_profiling_get(int kind, unsigned long long *launches, double *total_ms, double *flops, double *bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,62 @@ extern "C" {
 int starpu_gb300_gen_normal(void *stream, int rows, int cols, uint64_t seed, double *B, int ldb);
 int starpu_gb300_gen_uniform_rhs(void *stream, int n, int nrhs, uint64_t seed, double *B, int ldb);
 int starpu_gb300_gen_spd_gram(void *stream, int n, uint64_t seed, double alpha, double *A, int lda, double *work);
+/* A_ii += delta (re-targets the conditioning of B B^T / n + alpha I). */
+int starpu_gb300_shift_diagonal(void *stream, int n, double *A, int lda, double delta);
+/* cudaSetDevice for hosts without a CUDA binding (one process per GPU). */
+int starpu_gb300_set_device(int device);
+int starpu_gb300_memcpy_d2d(void *stream, void *dst, const void *src, size_t bytes);
+
+/* ---------------- mixed precision + FP64 iterative refinement ------------ */
+
+/* Outcome of one starpu_gb300_dsposv call. */
+typedef struct starpu_gb300_ir_info {
+    int status;            /* 0 converged; GB300_EDOM factor failed; GB300_ETIMEDOUT not converged */
+    int iterations;        /* refinement corrections applied */
+    int factor_terms;      /* BF16 products per trailing-update term (1 or 3) */
+    int potrf_info;        /* LAPACK-style info of the low-precision factorisation */
+    double backward_error; /* max over RHS of ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) */
+    double anorm;          /* ||A||_inf */
+} starpu_gb300_ir_info;
+
+/* Bytes of device workspace starpu_gb300_dsposv needs (tile nb, 0 = 1024). */
+size_t starpu_gb300_dsposv_workspace(int n, int nrhs, int nb);
+
+/* Solve A X = B (A SPD, FP64, full symmetric storage) with an FP32-storage
+ * tiled Cholesky whose trailing updates run on the tensor cores (split-BF16,
+ * nterms = 3, or plain BF16, nterms = 1), then FP64 iterative refinement:
+ * r = b - A x in FP64, correction solved with the low-precision factor,
+ * x += d in FP64, until every column's normwise backward error <= tol or
+ * max_iter corrections were applied (LAPACK dsposv semantics).  X is output
+ * only.  Synchronises the stream once per refinement step to read the error.
+ * Returns 0, GB300_EDOM (low-precision factor not positive definite) or
+ * GB300_ETIMEDOUT (no convergence); *info (may be NULL) gets the details. */
+int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                        int ldx, int nb, int nterms, double tol, int max_iter, void *work, size_t lwork,
+                        starpu_gb300_ir_info *info);
+
+/* Persistent solver context: owns a stream and device buffers for systems up
+ * to n_max x n_max with up to nrhs_max right-hand sides, so that repeated
+ * solves allocate nothing.  _dsposv_host takes HOST buffers (pinned for full
+ * copy bandwidth), copies A and B in, solves as starpu_gb300_dsposv, copies X
+ * out and synchronises. */
+typedef struct starpu_gb300_solver starpu_gb300_solver;
+starpu_gb300_solver *starpu_gb300_solver_create(int n_max, int nrhs_max, int nb, int nterms);
+int starpu_gb300_solver_destroy(starpu_gb300_solver *solver);
+void *starpu_gb300_solver_stream(starpu_gb300_solver *solver);
+int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *solver, int n, int nrhs, const double *A, int lda,
+                                    const double *B, int ldb, double *X, int ldx, double tol, int max_iter,
+                                    starpu_gb300_ir_info *info);
+
+/* Normwise backward error of X for A X = B, per column, computed on the
+ * device in FP64 (||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf));
+ * synchronises and writes nrhs values to berr_host. */
+size_t starpu_gb300_backward_error_workspace(int n, int nrhs);
+int starpu_gb300_backward_error(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
+                                const double *B, int ldb, void *work, size_t lwork, double *berr_host);
+
+/* Plain FP64 solve: dpotrf (tile nb) + dpotrs, A and B overwritten (LAPACK dposv). */
+int starpu_gb300_dposv(void *stream, int n, int nrhs, double *A, int lda, double *B, int ldb, int nb, int *d_info);
 
 #ifdef __cplusplus
 }

@@ -21,13 +21,13 @@ static void gemm_launch(cudaStream_t s, bool lower, int m, int n, int k, T alpha
     if constexpr (!TA && TB && BM == BN) {
         if (lower) {
             long tb = cdiv(m, BM);
-            gemm_simt_kernel<T, TA, TB, BM, BN, BK, TM, TN, true>
+            gb300_count_launch(), gemm_simt_kernel<T, TA, TB, BM, BN, BK, TM, TN, true>
                 <<<dim3((unsigned)(tb * (tb + 1) / 2)), NT, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
             return;
         }
     }
     {
-        gemm_simt_kernel<T, TA, TB, BM, BN, BK, TM, TN, false>
+        gb300_count_launch(), gemm_simt_kernel<T, TA, TB, BM, BN, BK, TM, TN, false>
             <<<dim3(cdiv(m, BM), cdiv(n, BN)), NT, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     }
 }
@@ -81,9 +81,9 @@ void trsm_rltn(cudaStream_t s, int m, int nc, const T *L, long ldl, T *B, long l
         const T *Ljj = L + j0 + (long)j0 * ldl;
         T *Bj = B + (long)j0 * ldb;
         if (w == SMALL_W)
-            trsm_rltn_small_kernel<T, SMALL_W, true><<<cdiv(m, 128), 128, 0, s>>>(m, w, Ljj, ldl, Bj, ldb);
+            gb300_count_launch(), trsm_rltn_small_kernel<T, SMALL_W, true><<<cdiv(m, 128), 128, 0, s>>>(m, w, Ljj, ldl, Bj, ldb);
         else
-            trsm_rltn_small_kernel<T, SMALL_W, false><<<cdiv(m, 128), 128, 0, s>>>(m, w, Ljj, ldl, Bj, ldb);
+            gb300_count_launch(), trsm_rltn_small_kernel<T, SMALL_W, false><<<cdiv(m, 128), 128, 0, s>>>(m, w, Ljj, ldl, Bj, ldb);
         const int rest = nc - j0 - w;
         if (rest > 0)
             gemm<T>(s, false, true, false, m, rest, w, T(-1), Bj, ldb, L + (j0 + w) + (long)j0 * ldl, ldl, T(1),
@@ -105,7 +105,7 @@ void potrf_tiled(cudaStream_t s, int n, T *A, long lda, int nb, int *info, int i
         const int kb = std::min(nb, n - k0);
         T *Akk = A + k0 + (long)k0 * lda;
         if (kb <= SMALL_W)
-            potf2_small_kernel<T, SMALL_W><<<1, 256, 0, s>>>(kb, Akk, lda, info, info_base + k0);
+            gb300_count_launch(), potf2_small_kernel<T, SMALL_W><<<1, 256, 0, s>>>(kb, Akk, lda, info, info_base + k0);
         else
             potrf_tiled<T>(s, kb, Akk, lda, SMALL_W, info, info_base + k0);
         const int m = n - k0 - kb;
@@ -129,7 +129,7 @@ void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, 
     const unsigned g = cdiv(nrhs, 64);
     for (int j0 = 0; j0 < n; j0 += SMALL_W) {
         const int w = std::min(SMALL_W, n - j0);
-        trsm_left_small_kernel<T, SMALL_W, false><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
+        gb300_count_launch(), trsm_left_small_kernel<T, SMALL_W, false><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
         const int rest = n - j0 - w;
         if (rest > 0)
             gemm<T>(s, false, false, false, rest, nrhs, w, T(-1), L + (j0 + w) + (long)j0 * ldl, ldl, B + j0, ldb,
@@ -138,7 +138,7 @@ void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, 
     const int last = ((n - 1) / SMALL_W) * SMALL_W;
     for (int j0 = last; j0 >= 0; j0 -= SMALL_W) {
         const int w = std::min(SMALL_W, n - j0);
-        trsm_left_small_kernel<T, SMALL_W, true><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
+        gb300_count_launch(), trsm_left_small_kernel<T, SMALL_W, true><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
         if (j0 > 0)
             gemm<T>(s, true, false, false, j0, nrhs, w, T(-1), L + j0, ldl, B + j0, ldb, T(1), B, ldb);
     }

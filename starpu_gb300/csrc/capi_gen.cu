@@ -85,6 +85,12 @@ __global__ void symmetrize_shift_kernel(int n, double alpha, double *__restrict_
     }
 }
 
+__global__ void shift_diagonal_kernel(int n, double delta, double *__restrict__ A, long lda)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        A[i + i * lda] += delta;
+}
+
 } // namespace gb300
 
 using namespace gb300;
@@ -95,7 +101,7 @@ int starpu_gb300_gen_normal(void *stream, int rows, int cols, uint64_t seed, dou
 {
     if (rows < 0 || cols < 0 || ldb < (rows > 1 ? rows : 1)) return GB300_EINVAL;
     if (!rows || !cols) return GB300_OK;
-    gen_normal_kernel<<<(rows + 127) / 128, 128, 0, (cudaStream_t)stream>>>(rows, cols, seed, B, ldb);
+    gb300_count_launch(), gen_normal_kernel<<<(rows + 127) / 128, 128, 0, (cudaStream_t)stream>>>(rows, cols, seed, B, ldb);
     return gb300_last_launch_status();
 }
 
@@ -103,7 +109,7 @@ int starpu_gb300_gen_uniform_rhs(void *stream, int n, int nrhs, uint64_t seed, d
 {
     if (n < 0 || nrhs < 0 || ldb < (n > 1 ? n : 1)) return GB300_EINVAL;
     if (!n || !nrhs) return GB300_OK;
-    gen_uniform_rhs_kernel<<<(nrhs + 63) / 64, 64, 0, (cudaStream_t)stream>>>(n, nrhs, seed, B, ldb);
+    gb300_count_launch(), gen_uniform_rhs_kernel<<<(nrhs + 63) / 64, 64, 0, (cudaStream_t)stream>>>(n, nrhs, seed, B, ldb);
     return gb300_last_launch_status();
 }
 
@@ -116,8 +122,23 @@ int starpu_gb300_gen_spd_gram(void *stream, int n, uint64_t seed, double alpha, 
     if (rc) return rc;
     gemm<double>(s, false, true, true, n, n, n, 1.0 / (double)n, work, n, work, n, 0.0, A, lda);
     dim3 g((n + 31) / 32, (n + 31) / 32);
-    symmetrize_shift_kernel<<<g, dim3(32, 8), 0, s>>>(n, alpha, A, lda);
+    gb300_count_launch(), symmetrize_shift_kernel<<<g, dim3(32, 8), 0, s>>>(n, alpha, A, lda);
     return gb300_last_launch_status();
+}
+
+int starpu_gb300_shift_diagonal(void *stream, int n, double *A, int lda, double delta)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1)) return GB300_EINVAL;
+    if (!n) return GB300_OK;
+    gb300_count_launch(), shift_diagonal_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(n, delta, A, lda);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_set_device(int device) { return gb300_record_cuda_error(cudaSetDevice(device)); }
+
+int starpu_gb300_memcpy_d2d(void *stream, void *dst, const void *src, size_t bytes)
+{
+    return gb300_record_cuda_error(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
 }
 
 } // extern "C"

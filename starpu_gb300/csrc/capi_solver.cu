@@ -1,0 +1,368 @@
+// Mixed-precision SPD solve with FP64 iterative refinement (LAPACK dsposv
+// semantics, no reference counterpart: the reference Cholesky is FP32
+// factorisation only, examples/cholesky/cholesky_kernels.c:53-55).
+//
+//   W = fp32(A)                       (lower triangle, fused with ||A||_inf)
+//   W = L L^T                         tensor-core tiled Cholesky (split-BF16)
+//   x = fp64(L^-T L^-1 fp32(b))
+//   repeat: r = b - A x   (FP64)      backward error ||r||/(||A|| ||x|| + ||b||)
+//           x += fp64(L^-T L^-1 fp32(r))
+// until every right-hand side meets `tol` or `max_iter` corrections ran.
+// FP64 is used only for A, the residual and the solution accumulation.
+#include <algorithm>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "gb300_internal.h"
+#include "starpu_gb300_kernels.h"
+#include "starpu_gb300_solver.h"
+
+namespace gb300 {
+
+int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err);
+
+// One CTA per column j of A: writes the lower part of column j to W in FP32
+// and folds sum_i |A_ij| (= row sum of the symmetric A) into *anorm.
+__global__ void convert_lower_norm_kernel(int n, const double *__restrict__ A, long lda, float *__restrict__ W,
+                                          long ldw, unsigned long long *anorm_bits)
+{
+    const long j = blockIdx.x;
+    const double *a = A + j * lda;
+    float *w = W ? W + j * ldw : nullptr;
+    double s = 0.0;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = a[i];
+        s += fabs(v);
+        if (w && i >= j) w[i] = (float)v;
+    }
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) atomicMax(anorm_bits, (unsigned long long)__double_as_longlong(s));
+    }
+}
+
+// y (FP32, n x nrhs) = fp32(x) ; used for b and r
+__global__ void to_f32_kernel(int n, int nrhs, const double *__restrict__ x, long ldx, float *__restrict__ y, long ldy)
+{
+    const long j = blockIdx.y;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        y[i + j * ldy] = (float)x[i + j * ldx];
+}
+
+// x (FP64) = (accumulate ? x : 0) + fp64(y), skipping converged columns
+__global__ void accumulate_kernel(int n, int nrhs, const float *__restrict__ y, long ldy, double *__restrict__ x,
+                                  long ldx, int accumulate, const int *__restrict__ done)
+{
+    const long j = blockIdx.y;
+    if (done && done[j]) return;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        x[i + j * ldx] = (accumulate ? x[i + j * ldx] : 0.0) + (double)y[i + j * ldy];
+}
+
+// R = B (copy) before the GEMM R -= A X
+__global__ void copy_f64_kernel(int n, const double *__restrict__ B, long ldb, double *__restrict__ R, long ldr)
+{
+    const long j = blockIdx.y;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        R[i + j * ldr] = B[i + j * ldb];
+}
+
+// Per right-hand side j (one CTA): berr_j = ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf);
+// done_j = berr_j <= tol.
+__global__ void backward_error_kernel(int n, const double *__restrict__ R, long ldr, const double *__restrict__ X,
+                                      long ldx, const double *__restrict__ B, long ldb,
+                                      const unsigned long long *anorm_bits, double tol, double *berr, int *done)
+{
+    const long j = blockIdx.x;
+    double rm = 0, xm = 0, bm = 0;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) {
+        rm = fmax(rm, fabs(R[i + j * ldr]));
+        xm = fmax(xm, fabs(X[i + j * ldx]));
+        bm = fmax(bm, fabs(B[i + j * ldb]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        rm = fmax(rm, __shfl_down_sync(0xffffffffu, rm, o));
+        xm = fmax(xm, __shfl_down_sync(0xffffffffu, xm, o));
+        bm = fmax(bm, __shfl_down_sync(0xffffffffu, bm, o));
+    }
+    __shared__ double s[3][32];
+    if ((threadIdx.x & 31) == 0) {
+        s[0][threadIdx.x >> 5] = rm;
+        s[1][threadIdx.x >> 5] = xm;
+        s[2][threadIdx.x >> 5] = bm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            rm = fmax(rm, s[0][w]);
+            xm = fmax(xm, s[1][w]);
+            bm = fmax(bm, s[2][w]);
+        }
+        const double an = __longlong_as_double((long long)*anorm_bits);
+        const double den = an * xm + bm;
+        const double e = den > 0 ? rm / den : (rm > 0 ? INFINITY : 0.0);
+        berr[j] = e;
+        done[j] = (e <= tol) ? 1 : 0;
+    }
+}
+
+struct SolverWs {
+    float *W;              // n x n FP32 working factor (ld = n)
+    void *panel;           // split-BF16 panels
+    double *R;             // n x nrhs FP64 residual
+    float *Y;              // n x nrhs FP32 right-hand side / correction
+    double *berr;          // nrhs
+    int *done;             // nrhs
+    unsigned long long *anorm_bits;
+    int *info, *err;
+    size_t panel_bytes;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
+{
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    const size_t oW = take((size_t)n * n * sizeof(float));
+    const size_t panel_bytes = starpu_gb300_spotrf_tc_workspace(n, nb);
+    const size_t oP = take(panel_bytes);
+    const size_t oR = take((size_t)n * nrhs * sizeof(double));
+    const size_t oY = take((size_t)n * nrhs * sizeof(float));
+    const size_t oE = take((size_t)nrhs * sizeof(double));
+    const size_t oD = take((size_t)nrhs * sizeof(int));
+    const size_t oS = take(4 * sizeof(unsigned long long));
+    if (ws && base) {
+        char *b = (char *)base;
+        ws->W = (float *)(b + oW);
+        ws->panel = b + oP;
+        ws->panel_bytes = panel_bytes;
+        ws->R = (double *)(b + oR);
+        ws->Y = (float *)(b + oY);
+        ws->berr = (double *)(b + oE);
+        ws->done = (int *)(b + oD);
+        ws->anorm_bits = (unsigned long long *)(b + oS);
+        ws->info = (int *)(b + oS + 8);
+        ws->err = (int *)(b + oS + 12);  // read back together with info
+    }
+    return off;
+}
+
+} // namespace gb300
+
+using namespace gb300;
+
+extern "C" {
+
+size_t starpu_gb300_dsposv_workspace(int n, int nrhs, int nb)
+{
+    if (n < 0 || nrhs < 0) return 0;
+    if (nb <= 0) nb = 1024;
+    return layout(n, nrhs, nb, nullptr, nullptr);
+}
+
+int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                        int ldx, int nb, int nterms, double tol, int max_iter, void *work, size_t lwork,
+                        starpu_gb300_ir_info *out)
+{
+    if (out) memset(out, 0, sizeof *out);
+    if (n < 0 || nrhs < 0 || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ldx < (n > 1 ? n : 1) ||
+        (nterms != 1 && nterms != 3) || max_iter < 0 || !(tol >= 0))
+        return GB300_EINVAL;
+    if (nb <= 0) nb = 1024;
+    if (!work || lwork < starpu_gb300_dsposv_workspace(n, nrhs, nb)) return GB300_EINVAL;
+    if (!n || !nrhs) return GB300_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    SolverWs ws;
+    layout(n, nrhs, nb, work, &ws);
+
+    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
+    cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(ws.done, 0, nrhs * sizeof(int), s);
+    gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits);
+    int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err);
+    if (rc) return rc;
+    // initial solve in FP32
+    gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n);
+    potrs_blocked<float>(s, n, nrhs, ws.W, n, ws.Y, n);
+    gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 0, nullptr);
+    int hinfo[2] = {0, 0};
+    if ((rc = gb300_record_cuda_error(cudaMemcpyAsync(hinfo, ws.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))))
+        return rc;
+    if ((rc = gb300_record_cuda_error(cudaStreamSynchronize(s)))) return rc;
+    if (out) {
+        out->potrf_info = hinfo[0];
+        out->factor_terms = nterms;
+    }
+    if (hinfo[1]) {
+        if (out) out->status = GB300_ETIMEDOUT;
+        return GB300_ETIMEDOUT;
+    }
+    if (hinfo[0]) {
+        if (out) out->status = GB300_EDOM;
+        return GB300_EDOM;
+    }
+    double *hberr = (double *)malloc(sizeof(double) * (size_t)nrhs);
+    int status = GB300_ETIMEDOUT;
+    int it = 0;
+    double worst = INFINITY;
+    for (;; ++it) {
+        int slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
+        gb300_count_launch(), copy_f64_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, B, ldb, ws.R, n);
+        gemm<double>(s, false, false, false, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, ws.R, n);
+        gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
+        gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb, ws.anorm_bits, tol, ws.berr, ws.done);
+        if ((rc = gb300_record_cuda_error(
+                 cudaMemcpyAsync(hberr, ws.berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s))))
+            break;
+        if ((rc = gb300_record_cuda_error(cudaStreamSynchronize(s)))) break;
+        worst = 0;
+        for (int j = 0; j < nrhs; ++j) worst = fmax(worst, hberr[j]);
+        if (worst <= tol) {
+            status = GB300_OK;
+            break;
+        }
+        if (it >= max_iter) break;
+        gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.R, n, ws.Y, n);
+        slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
+        potrs_blocked<float>(s, n, nrhs, ws.W, n, ws.Y, n);
+        gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
+        gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 1, ws.done);
+    }
+    free(hberr);
+    if (rc) return rc;
+    if (out) {
+        out->iterations = it;
+        out->backward_error = worst;
+        out->status = status;
+        unsigned long long ab = 0;
+        cudaMemcpy(&ab, ws.anorm_bits, sizeof ab, cudaMemcpyDeviceToHost);
+        double an;
+        memcpy(&an, &ab, sizeof an);
+        out->anorm = an;
+    }
+    return status;
+}
+
+// ---- persistent solver context: device buffers sized once, host-buffer calls
+
+struct starpu_gb300_solver {
+    int n_max, nrhs_max, nb, nterms;
+    cudaStream_t stream;
+    double *A, *B, *X;
+    void *work;
+    size_t lwork;
+};
+
+starpu_gb300_solver *starpu_gb300_solver_create(int n_max, int nrhs_max, int nb, int nterms)
+{
+    if (n_max <= 0 || nrhs_max <= 0 || (nterms != 1 && nterms != 3)) return nullptr;
+    starpu_gb300_solver *h = (starpu_gb300_solver *)calloc(1, sizeof *h);
+    h->n_max = n_max;
+    h->nrhs_max = nrhs_max;
+    h->nb = nb > 0 ? nb : 1024;
+    h->nterms = nterms;
+    h->lwork = starpu_gb300_dsposv_workspace(n_max, nrhs_max, h->nb);
+    bool ok = gb300_record_cuda_error(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) == GB300_OK &&
+              gb300_record_cuda_error(cudaMalloc(&h->A, sizeof(double) * (size_t)n_max * n_max)) == GB300_OK &&
+              gb300_record_cuda_error(cudaMalloc(&h->B, sizeof(double) * (size_t)n_max * nrhs_max)) == GB300_OK &&
+              gb300_record_cuda_error(cudaMalloc(&h->X, sizeof(double) * (size_t)n_max * nrhs_max)) == GB300_OK &&
+              gb300_record_cuda_error(cudaMalloc(&h->work, h->lwork)) == GB300_OK;
+    if (!ok) {
+        starpu_gb300_solver_destroy(h);
+        return nullptr;
+    }
+    return h;
+}
+
+int starpu_gb300_solver_destroy(starpu_gb300_solver *h)
+{
+    if (!h) return GB300_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->A);
+    cudaFree(h->B);
+    cudaFree(h->X);
+    cudaFree(h->work);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    free(h);
+    return GB300_OK;
+}
+
+void *starpu_gb300_solver_stream(starpu_gb300_solver *h) { return h ? (void *)h->stream : nullptr; }
+
+int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, const double *A, int lda,
+                                    const double *B, int ldb, double *X, int ldx, double tol, int max_iter,
+                                    starpu_gb300_ir_info *info)
+{
+    if (!h || n < 0 || nrhs < 0 || n > h->n_max || nrhs > h->nrhs_max || lda < n || ldb < n || ldx < n)
+        return GB300_EINVAL;
+    if (!n || !nrhs) return GB300_OK;
+    cudaStream_t s = h->stream;
+    int rc;
+    if ((rc = gb300_record_cuda_error(cudaMemcpy2DAsync(h->A, sizeof(double) * n, A, sizeof(double) * lda,
+                                                         sizeof(double) * n, n, cudaMemcpyHostToDevice, s))))
+        return rc;
+    if ((rc = gb300_record_cuda_error(cudaMemcpy2DAsync(h->B, sizeof(double) * n, B, sizeof(double) * ldb,
+                                                         sizeof(double) * n, nrhs, cudaMemcpyHostToDevice, s))))
+        return rc;
+    int status = starpu_gb300_dsposv(s, n, nrhs, h->A, n, h->B, n, h->X, n, h->nb, h->nterms, tol, max_iter, h->work,
+                                     h->lwork, info);
+    if (status != GB300_OK && status != GB300_ETIMEDOUT) return status;
+    if ((rc = gb300_record_cuda_error(cudaMemcpy2DAsync(X, sizeof(double) * ldx, h->X, sizeof(double) * n,
+                                                         sizeof(double) * n, nrhs, cudaMemcpyDeviceToHost, s))))
+        return rc;
+    if ((rc = gb300_record_cuda_error(cudaStreamSynchronize(s)))) return rc;
+    return status;
+}
+
+size_t starpu_gb300_backward_error_workspace(int n, int nrhs)
+{
+    return align256((size_t)n * nrhs * sizeof(double)) + align256((size_t)nrhs * (sizeof(double) + sizeof(int))) +
+           256;
+}
+
+int starpu_gb300_backward_error(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
+                                const double *B, int ldb, void *work, size_t lwork, double *berr_host)
+{
+    if (n <= 0 || nrhs <= 0 || lda < n || ldx < n || ldb < n || !work || !berr_host ||
+        lwork < starpu_gb300_backward_error_workspace(n, nrhs))
+        return GB300_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    char *w = (char *)work;
+    double *R = (double *)w;
+    w += align256((size_t)n * nrhs * sizeof(double));
+    double *berr = (double *)w;
+    int *done = (int *)(berr + nrhs);
+    w += align256((size_t)nrhs * (sizeof(double) + sizeof(int)));
+    unsigned long long *an = (unsigned long long *)w;
+    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
+    cudaMemsetAsync(an, 0, sizeof *an, s);
+    gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, nullptr, 0, an);
+    gb300_count_launch(), copy_f64_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, B, ldb, R, n);
+    gemm<double>(s, false, false, false, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, n);
+    gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, R, n, X, ldx, B, ldb, an, 0.0, berr, done);
+    int rc = gb300_record_cuda_error(cudaMemcpyAsync(berr_host, berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+    if (rc) return rc;
+    return gb300_record_cuda_error(cudaStreamSynchronize(s));
+}
+
+// Plain FP64 solve (LAPACK dposv): the baseline the mixed path is measured against.
+int starpu_gb300_dposv(void *stream, int n, int nrhs, double *A, int lda, double *B, int ldb, int nb, int *d_info)
+{
+    int rc = starpu_gb300_dpotrf(stream, n, A, lda, nb, d_info);
+    if (rc) return rc;
+    return starpu_gb300_dpotrs(stream, n, nrhs, A, lda, B, ldb);
+}
+
+} // extern "C"

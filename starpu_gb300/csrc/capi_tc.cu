@@ -90,7 +90,7 @@ int split_bf16(cudaStream_t s, int m, int k, const float *P, long ldp, void *hi,
 {
     if (m <= 0 || k <= 0) return GB300_OK;
     dim3 g((m + 31) / 32, (unsigned)((ldk + 31) / 32));
-    split_bf16_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo, ldk);
+    gb300_count_launch(), split_bf16_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo, ldk);
     return gb300_last_launch_status();
 }
 
@@ -136,7 +136,7 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
         attr_set = true;
     }
     const int grid = std::min(a.num_tiles, num_sms());
-    tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, a);
+    gb300_count_launch(), tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, a);
     return gb300_last_launch_status();
 }
 
@@ -152,15 +152,26 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
     for (int k0 = 0; k0 < n; k0 += nb) {
         const int kb = std::min(nb, n - k0);
         float *Akk = A + k0 + (long)k0 * lda;
-        potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
         const int m = n - k0 - kb;
-        if (m <= 0) break;
+        int slot = gb300_prof_begin(s, GB300_PROF_PANEL);
+        potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
+        if (m <= 0) {
+            gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0, 4.0 * kb * kb);
+            break;
+        }
         float *P = A + (k0 + kb) + (long)k0 * lda;
         trsm_rltn<float>(s, m, kb, Akk, lda, P, lda);
         int rc = split_bf16(s, m, kb, P, lda, hi, nterms == 3 ? lo : nullptr, ldk);
+        gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0 + (double)m * kb * kb,
+                       4.0 * kb * kb + 8.0 * m * kb + 2.0 * m * ldk * (nterms == 3 ? 2 : 1));
         if (rc) return rc;
+        slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
         rc = tc_update(s, m, m, kb, hi, lo, ldk, hi, lo, ldk, nterms, 1, A + (k0 + kb) + (long)(k0 + kb) * lda, lda,
                        d_err);
+        // algorithmic work: the lower triangle (incl. diagonal) of an m x m rank-kb update per term;
+        // bytes: C lower read + write in FP32 plus one read of each BF16 panel
+        gb300_prof_end(s, slot, (double)nterms * kb * (double)m * (m + 1.0),
+                       8.0 * m * (m + 1.0) / 2.0 + 2.0 * m * ldk * (nterms == 3 ? 2 : 1));
         if (rc) return rc;
     }
     return gb300_last_launch_status();

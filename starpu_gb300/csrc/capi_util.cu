@@ -1,9 +1,85 @@
 // Error reporting and device-memory helpers of the C-ABI.
 #include "gb300_internal.h"
+#include <atomic>
+#include <mutex>
 #include <stdio.h>
 #include <string.h>
+#include <vector>
 
 static thread_local char g_last_error[256] = "";
+static std::atomic<unsigned long long> g_launches{0};
+
+extern "C" void gb300_count_launch(void) { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// ---- profiling: CUDA-event pairs per launch, resolved lazily -------------
+namespace {
+struct ProfRec {
+    cudaEvent_t e0, e1;
+    int kind;
+    double flops, bytes;
+};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::vector<ProfRec> g_prof_pending;
+std::vector<cudaEvent_t> g_event_pool;
+struct ProfAgg {
+    unsigned long long launches = 0;
+    double ms = 0, flops = 0, bytes = 0;
+} g_prof_agg[GB300_PROF_KINDS];
+
+cudaEvent_t pool_get()
+{
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void resolve_locked()
+{
+    for (auto &r : g_prof_pending) {
+        cudaEventSynchronize(r.e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, r.e0, r.e1);
+        auto &a = g_prof_agg[r.kind];
+        a.launches++;
+        a.ms += ms;
+        a.flops += r.flops;
+        a.bytes += r.bytes;
+        g_event_pool.push_back(r.e0);
+        g_event_pool.push_back(r.e1);
+    }
+    g_prof_pending.clear();
+}
+} // namespace
+
+extern "C" int gb300_prof_begin(cudaStream_t s, int kind)
+{
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    if (!g_prof_on) return -1;
+    ProfRec r;
+    r.e0 = pool_get();
+    r.e1 = pool_get();
+    r.kind = kind;
+    r.flops = r.bytes = 0;
+    cudaEventRecord(r.e0, s);
+    g_prof_pending.push_back(r);
+    return (int)g_prof_pending.size() - 1;
+}
+
+extern "C" void gb300_prof_end(cudaStream_t s, int slot, double flops, double bytes)
+{
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    if (slot < 0 || slot >= (int)g_prof_pending.size()) return;
+    ProfRec &r = g_prof_pending[slot];
+    r.flops = flops;
+    r.bytes = bytes;
+    cudaEventRecord(r.e1, s);
+}
 
 extern "C" int gb300_record_cuda_error(cudaError_t e)
 {
@@ -64,6 +140,59 @@ void *starpu_gb300_stream_create(void)
 }
 
 int starpu_gb300_stream_destroy(void *stream) { return gb300_record_cuda_error(cudaStreamDestroy((cudaStream_t)stream)); }
+
+unsigned long long starpu_gb300_launch_count(void) { return g_launches.load(); }
+
+void starpu_gb300_profiling_enable(int on)
+{
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    if (!on) resolve_locked();
+    g_prof_on = on != 0;
+}
+
+void starpu_gb300_profiling_reset(void)
+{
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    resolve_locked();
+    for (auto &a : g_prof_agg) a = ProfAgg();
+}
+
+int starpu_gb300_profiling_get(int kind, unsigned long long *launches, double *total_ms, double *flops, double *bytes)
+{
+    if (kind < 0 || kind >= GB300_PROF_KINDS) return GB300_EINVAL;
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    resolve_locked();
+    if (launches) *launches = g_prof_agg[kind].launches;
+    if (total_ms) *total_ms = g_prof_agg[kind].ms;
+    if (flops) *flops = g_prof_agg[kind].flops;
+    if (bytes) *bytes = g_prof_agg[kind].bytes;
+    return GB300_OK;
+}
+
+void *starpu_gb300_event_create(void)
+{
+    cudaEvent_t e = nullptr;
+    if (gb300_record_cuda_error(cudaEventCreate(&e)) != GB300_OK) return nullptr;
+    return (void *)e;
+}
+
+int starpu_gb300_event_record(void *event, void *stream)
+{
+    return gb300_record_cuda_error(cudaEventRecord((cudaEvent_t)event, (cudaStream_t)stream));
+}
+
+double starpu_gb300_event_elapsed_ms(void *start, void *end)
+{
+    float ms = -1.0f;
+    if (cudaEventSynchronize((cudaEvent_t)end) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, (cudaEvent_t)start, (cudaEvent_t)end) != cudaSuccess) {
+        gb300_record_cuda_error(cudaGetLastError());
+        return -1.0;
+    }
+    return ms;
+}
+
+int starpu_gb300_event_destroy(void *event) { return gb300_record_cuda_error(cudaEventDestroy((cudaEvent_t)event)); }
 
 int starpu_gb300_device_count(void)
 {

@@ -25,3 +25,15 @@ template <typename T> void potrs_blocked(cudaStream_t s, int n, int nrhs, const 
 // maps it to a GB300_* return code.
 extern "C" int gb300_last_launch_status(void);
 extern "C" int gb300_record_cuda_error(cudaError_t e);
+
+// Every kernel launch site of the library calls this (it feeds
+// starpu_gb300_launch_count()).
+extern "C" void gb300_count_launch(void);
+
+// Per-kernel-class timing (the profiling mode of starpu_gb300_profiling_*):
+// prof_begin/prof_end bracket one launch with CUDA events on its stream when
+// profiling is enabled; both are no-ops otherwise.
+enum gb300_prof_kind { GB300_PROF_TC_UPDATE = 0, GB300_PROF_PANEL = 1, GB300_PROF_RESIDUAL = 2, GB300_PROF_SOLVE = 3,
+                       GB300_PROF_KINDS = 4 };
+extern "C" int gb300_prof_begin(cudaStream_t s, int kind);
+extern "C" void gb300_prof_end(cudaStream_t s, int slot, double algorithmic_flops, double algorithmic_bytes);

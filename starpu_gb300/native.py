@@ -109,6 +109,12 @@ def check(rc: int, what: str = "") -> None:
         raise RuntimeError(f"{what} failed with {rc}: {msg.decode() if msg else ''}")
 
 
+class IrInfo(C.Structure):
+    """ctypes mirror of starpu_gb300_ir_info (include/starpu_gb300_solver.h)."""
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("factor_terms", C.c_int), ("potrf_info", C.c_int),
+                ("backward_error", C.c_double), ("anorm", C.c_double)]
+
+
 class Stream:
     """A non-blocking CUDA stream owned by the native library."""
 

@@ -1,0 +1,120 @@
+"""GPU parity of the mixed-precision solve (tensor-core factor + FP64
+iterative refinement) against the FP64 oracle: the normwise backward error
+must reach 1e-12 and the solution must match the FP64 LAPACK-style solution
+to within the conditioning."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from starpu_gb300 import DeviceBuffer
+from starpu_gb300.native import IrInfo, check
+
+pytestmark = pytest.mark.gpu
+
+GB300_EDOM = -33
+GB300_ETIMEDOUT = -110
+
+
+def solve(gpu, A, B, nb, nterms, tol=1e-12, max_iter=30):
+    n, nrhs = B.shape
+    dA, dB = DeviceBuffer.from_array(A), DeviceBuffer.from_array(B)
+    dX = DeviceBuffer(n * nrhs * 8)
+    lw = gpu.starpu_gb300_dsposv_workspace(n, nrhs, nb)
+    W = DeviceBuffer(lw)
+    info = IrInfo()
+    rc = gpu.starpu_gb300_dsposv(None, n, nrhs, dA.ptr, n, dB.ptr, n, dX.ptr, n, nb, nterms, tol, max_iter, W.ptr, lw,
+                                 C.byref(info))
+    X = dX.download((n, nrhs), np.float64)
+    # inputs are read-only
+    np.testing.assert_array_equal(dA.download(A.shape, np.float64), A)
+    return rc, info, X
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e4])
+@pytest.mark.parametrize("nterms", [3, 1])
+def test_dsposv_reaches_fp64_backward_error(gpu, oracle, kappa, nterms):
+    n, nb, nrhs = 1024, 256, 4
+    A = oracle.spd_gram(n, 31, oracle.alpha_for_kappa(kappa))
+    B = oracle.uniform_rhs(n, nrhs, 32)
+    rc, info, X = solve(gpu, A, B, nb, nterms)
+    assert rc == 0 and info.status == 0, (rc, info.status, info.iterations, info.backward_error)
+    be, _ = oracle.backward_error(A, X, B)
+    assert be <= 1e-12
+    assert abs(be - info.backward_error) <= 1e-13 + 0.01 * be  # device-side norm agrees with the oracle's
+    L = np.tril(oracle.potrf_tiled(A, 4)[0])
+    Xo = oracle.potrs(L, B)
+    fwd = np.max(np.abs(X - Xo)) / np.max(np.abs(Xo))
+    assert fwd <= 50 * kappa * 1e-15
+    if nterms == 3:
+        assert info.iterations <= 6
+
+
+def test_dsposv_ill_conditioned_reports_status(gpu, oracle):
+    n, nb, nrhs = 768, 256, 2
+    A = oracle.spd_gram(n, 33, oracle.alpha_for_kappa(1e6))
+    B = oracle.uniform_rhs(n, nrhs, 34)
+    rc, info, X = solve(gpu, A, B, nb, 3, max_iter=40)
+    assert rc in (0, GB300_ETIMEDOUT, GB300_EDOM)
+    if rc == 0:
+        be, _ = oracle.backward_error(A, X, B)
+        assert be <= 1e-12
+
+
+def test_dsposv_not_spd(gpu):
+    n = 300
+    A = np.eye(n)
+    A[100, 100] = -2.0
+    B = np.ones((n, 1))
+    rc, info, X = solve(gpu, A, B, 128, 3)
+    assert rc == GB300_EDOM and info.potrf_info == 101
+
+
+def test_solver_context_host_buffers_match_device_call(gpu, oracle):
+    n, nrhs, nb = 700, 3, 256
+    A = oracle.spd_gram(n, 41, 0.5)
+    B = oracle.uniform_rhs(n, nrhs, 42)
+    h = gpu.starpu_gb300_solver_create(n, nrhs, nb, 3)
+    assert h
+    try:
+        X = np.zeros((n, nrhs), order="F")
+        info = IrInfo()
+        rc = gpu.starpu_gb300_solver_dsposv_host(h, n, nrhs, A.ctypes.data, n, B.ctypes.data, n, X.ctypes.data, n,
+                                                  1e-12, 30, C.byref(info))
+        assert rc == 0
+        rc2, info2, X2 = solve(gpu, A, B, nb, 3)
+        assert rc2 == 0
+        np.testing.assert_array_equal(X, X2)  # same kernels, same order: bit-identical
+        assert info.iterations == info2.iterations
+    finally:
+        gpu.starpu_gb300_solver_destroy(h)
+
+
+def test_dposv_plain_fp64(gpu, oracle):
+    n, nrhs = 900, 5
+    A = oracle.spd_gram(n, 51, 1.0)
+    B = oracle.uniform_rhs(n, nrhs, 52)
+    dA, dB = DeviceBuffer.from_array(A), DeviceBuffer.from_array(B)
+    info = DeviceBuffer.from_array(np.zeros(1, np.int32))
+    check(gpu.starpu_gb300_dposv(None, n, nrhs, dA.ptr, n, dB.ptr, n, 256, info.ptr))
+    X = dB.download((n, nrhs), np.float64)
+    be, _ = oracle.backward_error(A, X, B)
+    assert be <= 1e-14
+
+
+def test_profiling_counts_kernel_classes(gpu, oracle):
+    n, nb, nrhs = 1024, 256, 2
+    A = oracle.spd_gram(n, 61, 1.0)
+    B = oracle.uniform_rhs(n, nrhs, 62)
+    c0 = gpu.starpu_gb300_launch_count()
+    gpu.starpu_gb300_profiling_reset()
+    gpu.starpu_gb300_profiling_enable(1)
+    rc, info, X = solve(gpu, A, B, nb, 3)
+    gpu.starpu_gb300_profiling_enable(0)
+    assert rc == 0
+    assert gpu.starpu_gb300_launch_count() > c0
+    launches, ms, fl = C.c_ulonglong(), C.c_double(), C.c_double()
+    gpu.starpu_gb300_profiling_get(0, C.byref(launches), C.byref(ms), C.byref(fl), None)
+    assert launches.value == n // nb - 1 and ms.value > 0
+    expected = sum(3 * nb * (n - (k + 1) * nb) * (n - (k + 1) * nb + 1.0) for k in range(n // nb - 1))
+    assert abs(fl.value - expected) <= 1e-9 * expected
