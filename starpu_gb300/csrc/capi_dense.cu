@@ -121,24 +121,42 @@ void potrf_tiled(cudaStream_t s, int n, T *A, long lda, int nb, int *info, int i
 // POTRS with a lower factor: L y = b (forward), then L^T x = y (backward),
 // blocked by SMALL_W rows; min-dgels/base/SRC/dpotrs.c does the same two
 // sweeps through dtrsm.
+// Block width of the POTRS sweeps: 128 rows (FP32) / 64 rows (FP64) per
+// diagonal solve, so a sweep over n rows costs n / W diagonal solves and
+// n / W GEMM updates.
+template <typename T> struct potrs_w { static constexpr int value = 128; };
+template <> struct potrs_w<double> { static constexpr int value = 64; };
+
+template <typename T, bool TRANS>
+static void trsv_block(cudaStream_t s, int w, int nrhs, const T *L, long ldl, T *B, long ldb)
+{
+    constexpr int W = potrs_w<T>::value;
+    constexpr size_t smem = (size_t)(W * (W + 1) + W * 16) * sizeof(T);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(trsv_block_kernel<T, W, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    gb300_count_launch(), trsv_block_kernel<T, W, TRANS><<<cdiv(nrhs, 16), 128, smem, s>>>(w, nrhs, L, ldl, B, ldb);
+}
+
 template <typename T>
 void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, long ldb)
 {
     if (n <= 0 || nrhs <= 0) return;
-    constexpr int SMALL_W = small_w<T>::value;
-    const unsigned g = cdiv(nrhs, 64);
-    for (int j0 = 0; j0 < n; j0 += SMALL_W) {
-        const int w = std::min(SMALL_W, n - j0);
-        gb300_count_launch(), trsm_left_small_kernel<T, SMALL_W, false><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
+    constexpr int W = potrs_w<T>::value;
+    for (int j0 = 0; j0 < n; j0 += W) {
+        const int w = std::min(W, n - j0);
+        trsv_block<T, false>(s, w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
         const int rest = n - j0 - w;
         if (rest > 0)
             gemm<T>(s, false, false, false, rest, nrhs, w, T(-1), L + (j0 + w) + (long)j0 * ldl, ldl, B + j0, ldb,
                     T(1), B + j0 + w, ldb);
     }
-    const int last = ((n - 1) / SMALL_W) * SMALL_W;
-    for (int j0 = last; j0 >= 0; j0 -= SMALL_W) {
-        const int w = std::min(SMALL_W, n - j0);
-        gb300_count_launch(), trsm_left_small_kernel<T, SMALL_W, true><<<g, 64, 0, s>>>(w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
+    const int last = ((n - 1) / W) * W;
+    for (int j0 = last; j0 >= 0; j0 -= W) {
+        const int w = std::min(W, n - j0);
+        trsv_block<T, true>(s, w, nrhs, L + j0 + (long)j0 * ldl, ldl, B + j0, ldb);
         if (j0 > 0)
             gemm<T>(s, true, false, false, j0, nrhs, w, T(-1), L + j0, ldl, B + j0, ldb, T(1), B, ldb);
     }

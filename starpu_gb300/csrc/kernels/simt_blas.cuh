@@ -290,6 +290,60 @@ __global__ void __launch_bounds__(64) trsm_left_small_kernel(int w, int nrhs, co
 }
 
 // ---------------------------------------------------------------------------
+// Diagonal-block solve of the blocked POTRS with wide blocks (w <= W, W up
+// to 128): L_ii (w x w) and 16 right-hand-side columns of the block are
+// staged in shared memory; each column is owned by 8 consecutive lanes that
+// compute one row at a time as a dot product split 8 ways and reduced with
+// shuffles, so rows advance with warp-level synchronisation only.
+//   TRANS = false: y_r = (b_r - sum_{c<r} L_rc y_c) / L_rr,  r = 0..w-1
+//   TRANS = true : x_r = (y_r - sum_{c>r} L_cr x_c) / L_rr,  r = w-1..0
+// Launch: ceil(nrhs / 16) CTAs of 128 threads, dynamic shared memory
+// (W * (W + 1) + W * 16) * sizeof(T).
+// ---------------------------------------------------------------------------
+template <typename T, int W, bool TRANS>
+__global__ void __launch_bounds__(128) trsv_block_kernel(int w, int nrhs, const T *__restrict__ L, long ldl,
+                                                         T *__restrict__ B, long ldb)
+{
+    extern __shared__ __align__(16) unsigned char trsv_smem[];
+    T *Ls = (T *)trsv_smem;            // [W][W+1], Ls[r * (W+1) + c] = L(r, c)
+    T *Ys = Ls + W * (W + 1);          // [16][W]
+    const int tid = threadIdx.x;
+    const int col0 = blockIdx.x * 16;
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+        const int r = idx % w, c = idx / w;
+        Ls[r * (W + 1) + c] = (r >= c) ? L[(long)r + (long)c * ldl] : T(0);
+    }
+    for (int idx = tid; idx < 16 * w; idx += blockDim.x) {
+        const int r = idx % w, j = idx / w;
+        Ys[j * W + r] = (col0 + j < nrhs) ? B[(long)r + (long)(col0 + j) * ldb] : T(0);
+    }
+    __syncthreads();
+    const int j = tid >> 3;      // right-hand side owned by this group of 8 lanes
+    const int l8 = tid & 7;
+    T *y = Ys + j * W;
+    const unsigned gmask = 0xFFu << ((tid & 31) & ~7);
+    for (int s = 0; s < w; ++s) {
+        const int r = TRANS ? (w - 1 - s) : s;
+        T acc = T(0);
+        if (!TRANS) {
+            for (int c = l8; c < r; c += 8) acc = fma(Ls[r * (W + 1) + c], y[c], acc);
+        } else {
+            for (int c = r + 1 + l8; c < w; c += 8) acc = fma(Ls[c * (W + 1) + r], y[c], acc);
+        }
+        acc += __shfl_xor_sync(gmask, acc, 1);
+        acc += __shfl_xor_sync(gmask, acc, 2);
+        acc += __shfl_xor_sync(gmask, acc, 4);
+        if (l8 == 0) y[r] = (y[r] - acc) / Ls[r * (W + 1) + r];
+        __syncwarp(gmask);
+    }
+    __syncthreads();
+    for (int idx = tid; idx < 16 * w; idx += blockDim.x) {
+        const int r = idx % w, jj = idx / w;
+        if (col0 + jj < nrhs) B[(long)r + (long)(col0 + jj) * ldb] = Ys[jj * W + r];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Elementwise helpers.
 // ---------------------------------------------------------------------------
 template <typename TO, typename TI>

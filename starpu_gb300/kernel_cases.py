@@ -1,0 +1,122 @@
+"""Single-kernel cases for profiling (ncu) and quick timing, through the C-ABI.
+
+    python -m starpu_gb300.kernel_cases tc_update --m 8192 --k 1024 --nterms 3 --reps 3
+    python -m starpu_gb300.kernel_cases residual  --n 16384 --nrhs 16 --reps 3
+    python -m starpu_gb300.kernel_cases potrs     --n 16384 --nrhs 16 --reps 3
+    python -m starpu_gb300.kernel_cases spotrf_tc --n 8192  --nb 1024 --nterms 3 --reps 2
+    python -m starpu_gb300.kernel_cases dpotrf    --n 8192  --nb 512 --reps 2
+
+Each case allocates its operands once, runs `--reps` launches of the same
+shape and prints the mean time per launch measured with CUDA events.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+
+import numpy as np
+
+from . import load
+from .native import DeviceBuffer, check
+
+
+def _timed(L, fn, reps):
+    fn()
+    check(L.starpu_gb300_stream_sync(None))
+    e0, e1 = L.starpu_gb300_event_create(), L.starpu_gb300_event_create()
+    check(L.starpu_gb300_event_record(e0, None))
+    for _ in range(reps):
+        fn()
+    check(L.starpu_gb300_event_record(e1, None))
+    ms = L.starpu_gb300_event_elapsed_ms(e0, e1) / reps
+    L.starpu_gb300_event_destroy(e0)
+    L.starpu_gb300_event_destroy(e1)
+    return ms
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["tc_update", "residual", "potrs", "spotrf_tc", "dpotrf"])
+    ap.add_argument("--m", type=int, default=8192)
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--k", type=int, default=1024)
+    ap.add_argument("--nb", type=int, default=1024)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--nterms", type=int, default=3)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    L = load()
+    out = {"case": a.case}
+    if a.case == "tc_update":
+        m, k = a.m, a.k
+        ldk = (k + 63) // 64 * 64
+        P = DeviceBuffer(4 * m * k)
+        hi, lo = DeviceBuffer(2 * m * ldk), DeviceBuffer(2 * m * ldk)
+        Cb = DeviceBuffer(4 * m * m)
+        err = DeviceBuffer.from_array(np.zeros(1, np.int32))
+        check(L.starpu_gb300_memset(None, P.ptr, 0, 4 * m * k))
+        check(L.starpu_gb300_memset(None, Cb.ptr, 0, 4 * m * m))
+        check(L.starpu_gb300_split_bf16(None, m, k, P.ptr, m, hi.ptr, lo.ptr, ldk))
+        ms = _timed(L, lambda: check(L.starpu_gb300_tc_update(None, m, m, k, hi.ptr, lo.ptr, ldk, hi.ptr, lo.ptr, ldk,
+                                                               a.nterms, 1, Cb.ptr, m, err.ptr)), a.reps)
+        fl = a.nterms * k * m * (m + 1.0)
+        out.update(ms=ms, tflops=fl / ms / 1e9, algorithmic_bytes=8.0 * m * (m + 1) / 2 + 2.0 * m * ldk * 2)
+    elif a.case in ("residual", "potrs"):
+        n, nrhs = a.n, a.nrhs
+        A = DeviceBuffer(8 * n * n)
+        W = DeviceBuffer(8 * n * n)
+        Bd, Xd = DeviceBuffer(8 * n * nrhs), DeviceBuffer(8 * n * nrhs)
+        check(L.starpu_gb300_gen_spd_gram(None, n, 3, 1.0, A.ptr, n, W.ptr))
+        check(L.starpu_gb300_gen_uniform_rhs(None, n, nrhs, 4, Bd.ptr, n))
+        check(L.starpu_gb300_gen_uniform_rhs(None, n, nrhs, 5, Xd.ptr, n))
+        if a.case == "residual":
+            lw = L.starpu_gb300_backward_error_workspace(n, nrhs)
+            BW = DeviceBuffer(lw)
+            be = np.zeros(nrhs)
+            ms = _timed(L, lambda: check(L.starpu_gb300_backward_error(None, n, nrhs, A.ptr, n, Xd.ptr, n, Bd.ptr, n,
+                                                                        BW.ptr, lw, be.ctypes.data)), a.reps)
+            out.update(ms=ms, tflops=2.0 * n * n * nrhs / ms / 1e9, algorithmic_bytes=8.0 * n * n)
+        else:
+            # FP32 sweeps (the refinement's correction solve) with the lower part of a
+            # diagonally dominant matrix as the factor
+            i = np.arange(n, dtype=np.float32)
+            Lh = np.asfortranarray(1.0 / (1.0 + i[:, None] + i[None, :]), dtype=np.float32)
+            Lh[np.diag_indices(n)] += n
+            F = DeviceBuffer.from_array(Lh)
+            Y = DeviceBuffer.from_array(np.ones((n, nrhs), np.float32))
+            ms = _timed(L, lambda: check(L.starpu_gb300_spotrs(None, n, nrhs, F.ptr, n, Y.ptr, n)), a.reps)
+            out.update(ms=ms, gbs=4.0 * n * n / ms / 1e6)
+    elif a.case == "spotrf_tc":
+        n, nb = a.n, a.nb
+        from_host = np.empty((n, n), np.float32, order="F")
+        i = np.arange(n, dtype=np.float32)
+        from_host[:] = 1.0 / (1.0 + i[:, None] + i[None, :])
+        from_host[np.diag_indices(n)] += n
+        F = DeviceBuffer.from_array(from_host)
+        ws = L.starpu_gb300_spotrf_tc_workspace(n, nb)
+        Wk = DeviceBuffer(ws)
+        info, err = DeviceBuffer(4), DeviceBuffer.from_array(np.zeros(1, np.int32))
+
+        def run():
+            F.upload(from_host)
+            check(L.starpu_gb300_spotrf_tc(None, n, F.ptr, n, nb, a.nterms, Wk.ptr, ws, info.ptr, err.ptr))
+        ms = _timed(L, run, a.reps)
+        out.update(ms_including_upload=ms)
+    elif a.case == "dpotrf":
+        n, nb = a.n, a.nb
+        A = DeviceBuffer(8 * n * n)
+        W = DeviceBuffer(8 * n * n)
+        check(L.starpu_gb300_gen_spd_gram(None, n, 3, 1.0, A.ptr, n, W.ptr))
+        info = DeviceBuffer(4)
+
+        def run():
+            check(L.starpu_gb300_memcpy_d2d(None, W.ptr, A.ptr, 8 * n * n))
+            check(L.starpu_gb300_dpotrf(None, n, W.ptr, n, nb, info.ptr))
+        ms = _timed(L, run, a.reps)
+        out.update(ms=ms, gflops=n ** 3 / 3 / ms / 1e6)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -45,7 +45,8 @@ def test_dsposv_reaches_fp64_backward_error(gpu, oracle, kappa, nterms):
     L = np.tril(oracle.potrf_tiled(A, 4)[0])
     Xo = oracle.potrs(L, B)
     fwd = np.max(np.abs(X - Xo)) / np.max(np.abs(Xo))
-    assert fwd <= 50 * kappa * 1e-15
+    # normwise bound: forward error <= cond * backward error (norm-equivalence factor sqrt(n))
+    assert fwd <= 10 * kappa * np.sqrt(n) * max(be, 1e-16)
     if nterms == 3:
         assert info.iterations <= 6
 
