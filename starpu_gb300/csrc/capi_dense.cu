@@ -3,6 +3,7 @@
 // triangular solves composed from them.  Every entry point only enqueues work
 // on the caller's stream and returns; nothing here synchronises or allocates.
 #include "kernels/simt_blas.cuh"
+#include "kernels/trsv_sweep.cuh"
 #include "gb300_internal.h"
 #include "starpu_gb300_kernels.h"
 
@@ -161,6 +162,52 @@ void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, 
             gemm<T>(s, true, false, false, j0, nrhs, w, T(-1), L + j0, ldl, B + j0, ldb, T(1), B, ldb);
     }
 }
+
+// ---- single-launch POTRS sweeps with inverted 64 x 64 diagonal blocks ------
+
+template <typename T>
+size_t potrs_sweep_workspace(int n)
+{
+    const size_t nblk = ((size_t)n + 63) / 64;
+    return ((nblk * 64 * 64 * sizeof(T) + 255) & ~(size_t)255) + (((nblk + 2) * sizeof(int) + 255) & ~(size_t)255);
+}
+
+// Invert every diagonal 64 x 64 block of L (once per factorisation).
+template <typename T>
+void potrs_sweep_prepare(cudaStream_t s, int n, const T *L, long ldl, void *ws)
+{
+    if (n <= 0) return;
+    const unsigned nblk = cdiv(n, 64);
+    gb300_count_launch(), invert_diag_blocks_kernel<T, 64><<<nblk, 64, 0, s>>>(n, L, ldl, (T *)ws);
+}
+
+// L y = b then L^T x = y, one launch per sweep and group of 16 columns.
+template <typename T>
+void potrs_sweep(cudaStream_t s, int n, int nrhs, const T *L, long ldl, void *ws, T *B, long ldb, int *err)
+{
+    if (n <= 0 || nrhs <= 0) return;
+    const int nblk = (int)cdiv(n, 64);
+    const T *Linv = (const T *)ws;
+    int *flags = (int *)((char *)ws + (((size_t)nblk * 64 * 64 * sizeof(T) + 255) & ~(size_t)255));
+    unsigned *ticket = (unsigned *)(flags + nblk);
+    const unsigned long long budget = 2000000000ull;  // 2 s per wait: far above any legitimate stall
+    for (int c0 = 0; c0 < nrhs; c0 += 16) {
+        const int nr = std::min(16, nrhs - c0);
+        cudaMemsetAsync(flags, 0, (nblk + 1) * sizeof(int), s);
+        gb300_count_launch(), trsv_sweep_kernel<T, 64, false>
+            <<<nblk, 256, 0, s>>>(n, nr, L, ldl, Linv, B + (long)c0 * ldb, ldb, ticket, flags, err, budget);
+        cudaMemsetAsync(flags, 0, (nblk + 1) * sizeof(int), s);
+        gb300_count_launch(), trsv_sweep_kernel<T, 64, true>
+            <<<nblk, 256, 0, s>>>(n, nr, L, ldl, Linv, B + (long)c0 * ldb, ldb, ticket, flags, err, budget);
+    }
+}
+
+template size_t potrs_sweep_workspace<float>(int);
+template size_t potrs_sweep_workspace<double>(int);
+template void potrs_sweep_prepare<float>(cudaStream_t, int, const float *, long, void *);
+template void potrs_sweep_prepare<double>(cudaStream_t, int, const double *, long, void *);
+template void potrs_sweep<float>(cudaStream_t, int, int, const float *, long, void *, float *, long, int *);
+template void potrs_sweep<double>(cudaStream_t, int, int, const double *, long, void *, double *, long, int *);
 
 template void gemm<float>(cudaStream_t, bool, bool, bool, int, int, int, float, const float *, long, const float *,
                           long, float, float *, long);

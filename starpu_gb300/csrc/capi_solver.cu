@@ -118,6 +118,7 @@ struct SolverWs {
     void *panel;           // split-BF16 panels
     double *R;             // n x nrhs FP64 residual
     float *Y;              // n x nrhs FP32 right-hand side / correction
+    void *sweep;           // inverted diagonal blocks + flags of the POTRS sweeps
     double *berr;          // nrhs
     int *done;             // nrhs
     unsigned long long *anorm_bits;
@@ -140,6 +141,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t oP = take(panel_bytes);
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
+    const size_t oT = take(potrs_sweep_workspace<float>(n));
     const size_t oE = take((size_t)nrhs * sizeof(double));
     const size_t oD = take((size_t)nrhs * sizeof(int));
     const size_t oS = take(4 * sizeof(unsigned long long));
@@ -150,6 +152,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->panel_bytes = panel_bytes;
         ws->R = (double *)(b + oR);
         ws->Y = (float *)(b + oY);
+        ws->sweep = b + oT;
         ws->berr = (double *)(b + oE);
         ws->done = (int *)(b + oD);
         ws->anorm_bits = (unsigned long long *)(b + oS);
@@ -193,9 +196,12 @@ int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda,
     gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits);
     int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err);
     if (rc) return rc;
+    potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
     // initial solve in FP32
     gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n);
-    potrs_blocked<float>(s, n, nrhs, ws.W, n, ws.Y, n);
+    int slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
+    potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
+    gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
     gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 0, nullptr);
     int hinfo[2] = {0, 0};
     if ((rc = gb300_record_cuda_error(cudaMemcpyAsync(hinfo, ws.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))))
@@ -218,7 +224,7 @@ int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda,
     int it = 0;
     double worst = INFINITY;
     for (;; ++it) {
-        int slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
+        slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
         gb300_count_launch(), copy_f64_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, B, ldb, ws.R, n);
         gemm<double>(s, false, false, false, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, ws.R, n);
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
@@ -236,7 +242,7 @@ int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda,
         if (it >= max_iter) break;
         gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.R, n, ws.Y, n);
         slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
-        potrs_blocked<float>(s, n, nrhs, ws.W, n, ws.Y, n);
+        potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
         gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 1, ws.done);
     }

@@ -18,6 +18,11 @@ void gemm(cudaStream_t s, bool ta, bool tb, bool lower, int m, int n, int k, T a
 template <typename T> void trsm_rltn(cudaStream_t s, int m, int nc, const T *L, long ldl, T *B, long ldb);
 template <typename T> void potrf_tiled(cudaStream_t s, int n, T *A, long lda, int nb, int *info, int info_base);
 template <typename T> void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, long ldb);
+// single-launch sweeps: workspace = inverted 64x64 diagonal blocks + flags
+template <typename T> size_t potrs_sweep_workspace(int n);
+template <typename T> void potrs_sweep_prepare(cudaStream_t s, int n, const T *L, long ldl, void *ws);
+template <typename T>
+void potrs_sweep(cudaStream_t s, int n, int nrhs, const T *L, long ldl, void *ws, T *B, long ldb, int *err);
 
 } // namespace gb300
 

@@ -183,6 +183,9 @@ __global__ void __launch_bounds__(256) potf2_small_kernel(int n, T *__restrict__
     }
     if (tid == 0) bad = 0;
     __syncthreads();
+    // 256 threads as 64 rows x 4 column lanes: no integer division in the loop
+    const int ti = tid % NMAX, tc = tid / NMAX;
+    constexpr int CL = 256 / NMAX;
     for (int z = 0; z < n; ++z) {
         if (tid == 0) {
             T d = a[z][z];
@@ -194,12 +197,11 @@ __global__ void __launch_bounds__(256) potf2_small_kernel(int n, T *__restrict__
         }
         __syncthreads();
         const T inv = T(1) / a[z][z];
-        for (int i = z + 1 + tid; i < n; i += blockDim.x) a[i][z] *= inv;
+        if (tc == 0 && ti > z && ti < n) a[ti][z] *= inv;
         __syncthreads();
-        const int rem = n - z - 1;
-        for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
-            int i = z + 1 + idx % rem, c = z + 1 + idx / rem;
-            if (i >= c) a[i][c] = fma(-a[i][z], a[c][z], a[i][c]);
+        if (ti > z && ti < n) {
+            const T liz = a[ti][z];
+            for (int c = z + 1 + tc; c <= ti; c += CL) a[ti][c] = fma(-liz, a[c][z], a[ti][c]);
         }
         __syncthreads();
     }

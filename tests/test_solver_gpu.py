@@ -31,8 +31,8 @@ def solve(gpu, A, B, nb, nterms, tol=1e-12, max_iter=30):
     return rc, info, X
 
 
-@pytest.mark.parametrize("kappa", [1e2, 1e4])
-@pytest.mark.parametrize("nterms", [3, 1])
+# plain BF16 (nterms=1, u ~ 4e-3) only refines when kappa * u < 1: kappa = 1e2
+@pytest.mark.parametrize("kappa,nterms", [(1e2, 3), (1e4, 3), (1e2, 1)])
 def test_dsposv_reaches_fp64_backward_error(gpu, oracle, kappa, nterms):
     n, nb, nrhs = 1024, 256, 4
     A = oracle.spd_gram(n, 31, oracle.alpha_for_kappa(kappa))
