@@ -77,6 +77,17 @@ int starpu_gb300_dpotrf(void *stream, int n, double *A, int lda, int nb, int *d_
 int starpu_gb300_spotrs(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb);
 int starpu_gb300_dpotrs(void *stream, int n, int nrhs, const double *L, int ldl, double *B, int ldb);
 
+/* Same solve as starpu_gb300_spotrs, as two single-launch sweeps (one per
+ * triangle and group of 16 right-hand sides) over 64-row blocks whose
+ * diagonal blocks are inverted first.  `work` (device, >= _workspace(n)
+ * bytes) holds the inverted blocks and the sweeps' completion flags; d_err
+ * is set non-zero if an internal wait timed out (the result is then invalid).
+ * Same LAPACK xPOTRS contract (min-dgels/base/SRC/dpotrs.c, uplo = L). */
+size_t starpu_gb300_spotrs_sweep_workspace(int n);
+int starpu_gb300_spotrs_sweep(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb, void *work,
+                              size_t lwork, int *d_err);
+
+
 /* ---------------- tensor-core trailing update (tcgen05, sm_103a) ---------- */
 
 /* P (m x k FP32, column-major, ldp) -> hi = bf16(P), lo = bf16(P - hi), both

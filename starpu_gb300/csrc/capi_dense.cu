@@ -328,4 +328,22 @@ int starpu_gb300_dpotrs(void *stream, int n, int nrhs, const double *L, int ldl,
     return gb300_last_launch_status();
 }
 
+size_t starpu_gb300_spotrs_sweep_workspace(int n)
+{
+    if (n <= 0) return 0;
+    return potrs_sweep_workspace<float>(n) + 256;
+}
+
+int starpu_gb300_spotrs_sweep(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb, void *work,
+                              size_t lwork, int *d_err)
+{
+    if (n < 0 || nrhs < 0 || ldl < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1)) return GB300_EINVAL;
+    if (!n || !nrhs) return GB300_OK;
+    if (!work || lwork < starpu_gb300_spotrs_sweep_workspace(n) || !d_err) return GB300_EINVAL;
+    cudaStream_t s = GB300_STREAM(stream);
+    potrs_sweep_prepare<float>(s, n, L, ldl, work);
+    potrs_sweep<float>(s, n, nrhs, L, ldl, work, B, ldb, d_err);
+    return gb300_last_launch_status();
+}
+
 } // extern "C"

@@ -88,6 +88,8 @@ extern "C" int gb300_record_cuda_error(cudaError_t e)
     return GB300_ECUDA;
 }
 
+extern "C" void gb300_set_error(const char *msg) { snprintf(g_last_error, sizeof g_last_error, "%s", msg); }
+
 extern "C" int gb300_last_launch_status(void)
 {
     return gb300_record_cuda_error(cudaGetLastError());

@@ -30,6 +30,8 @@ void potrs_sweep(cudaStream_t s, int n, int nrhs, const T *L, long ldl, void *ws
 // maps it to a GB300_* return code.
 extern "C" int gb300_last_launch_status(void);
 extern "C" int gb300_record_cuda_error(cudaError_t e);
+// Sets the message returned by starpu_gb300_last_error() for a non-CUDA error.
+extern "C" void gb300_set_error(const char *msg);
 
 // Every kernel launch site of the library calls this (it feeds
 // starpu_gb300_launch_count()).

@@ -142,6 +142,33 @@ def test_spotrs_fp32(gpu, oracle):
     assert be <= 1e-6
 
 
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (63, 3), (64, 16), (65, 17), (1000, 40), (4097, 16)])
+def test_spotrs_sweep_matches_blocked_and_oracle(gpu, oracle, n, nrhs):
+    A = oracle.spd_gram(min(n, 1200), 8, 2.0) if n <= 1200 else None
+    if A is None:  # diagonally dominant FP32 input for the large case (oracle Gram is O(n^3))
+        i = np.arange(n, dtype=np.float64)
+        A = 1.0 / (1.0 + i[:, None] + i[None, :]) + n * np.eye(n)
+    L = np.tril(oracle.potrf_tiled(A.astype(np.float32), max(1, n // 512))[0])
+    Bm = oracle.uniform_rhs(n, nrhs, 9).astype(np.float32)
+    dL = up(L)
+    d1, d2 = up(Bm), up(Bm)
+    lw = gpu.starpu_gb300_spotrs_sweep_workspace(n)
+    W = DeviceBuffer(lw)
+    err = info_buf()
+    check(gpu.starpu_gb300_spotrs_sweep(None, n, nrhs, dL.ptr, n, d1.ptr, n, W.ptr, lw, err.ptr))
+    check(gpu.starpu_gb300_spotrs(None, n, nrhs, dL.ptr, n, d2.ptr, n))
+    X1, X2 = down(d1, Bm), down(d2, Bm)
+    assert err.download((1,), np.int32)[0] == 0
+    Xo = oracle.potrs(L, Bm)
+    scale = np.max(np.abs(Xo))
+    assert np.max(np.abs(X1 - Xo)) <= 1e-4 * scale
+    assert np.max(np.abs(X1 - X2)) <= 1e-4 * scale
+    # deterministic: the fixed accumulation order gives bit-identical repeats
+    d3 = up(Bm)
+    check(gpu.starpu_gb300_spotrs_sweep(None, n, nrhs, dL.ptr, n, d3.ptr, n, W.ptr, lw, err.ptr))
+    np.testing.assert_array_equal(down(d3, Bm), X1)
+
+
 def test_not_spd_sets_info_without_fault(gpu):
     n = 200
     A = np.eye(n) * 4.0
