@@ -87,6 +87,19 @@ size_t starpu_gb300_spotrs_sweep_workspace(int n);
 int starpu_gb300_spotrs_sweep(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb, void *work,
                               size_t lwork, int *d_err);
 
+/* Allocation-free variant of starpu_gb300_spotrs_sweep.  It has no
+ * counterpart in the reference.  For callers that must not allocate device
+ * memory -- a codelet body running inside a runtime that owns all device
+ * buffers, a serving or real-time loop -- it takes no workspace: its scratch
+ * is one static device array sized for n <= STARPU_GB300_NOALLOC_MAX_N (about
+ * 4 MiB, held by every GPU that loads the library until the process exits).
+ * Larger n is rejected with GB300_EINVAL.  It calls no allocator.  The first
+ * call on a device (with it current) looks the array's address up once; make
+ * it before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller.  d_err may be NULL. */
+#define STARPU_GB300_NOALLOC_MAX_N 16384
+int starpu_gb300_spotrs_noalloc(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb,
+                                int *d_err);
 
 /* ---------------- tensor-core trailing update (tcgen05, sm_103a) ---------- */
 
