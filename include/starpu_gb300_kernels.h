@@ -44,6 +44,10 @@ const char *starpu_gb300_last_error(void);
  * fallbacks at :369 and :391-416).  No workspace is needed. d_info may be NULL. */
 int starpu_gb300_spotrf_tile(void *stream, int n, float *A, int lda, int *d_info);
 int starpu_gb300_dpotrf_tile(void *stream, int n, double *A, int lda, int *d_info);
+/* Same, accumulating into a status word that is not reset: the first failing
+ * tile's info (relative to the tile) is kept across many tiles of one run. */
+int starpu_gb300_spotrf_tile_status(void *stream, int n, float *A, int lda, int *d_status);
+int starpu_gb300_dpotrf_tile_status(void *stream, int n, double *A, int lda, int *d_status);
 
 /* B[m x n] <- alpha * B * L^{-T}, L n x n lower non-unit (alpha must be 1).
  * Replaces cublasStrsm(RIGHT, LOWER, TRANS, NON_UNIT, m, n, &1, L, ldl, B, ldb)

@@ -1,0 +1,9 @@
+/*
+ * starpu_hipblas.h -- kept so that sources written for StarPU include it unchanged; the
+ * declarations it would add live in starpu_cuda.h (included by starpu.h).
+ * The GB300 runtime does not link the vendor libraries.
+ */
+#ifndef STARPU_HIPBLAS_H
+#define STARPU_HIPBLAS_H
+#include "starpu.h"
+#endif

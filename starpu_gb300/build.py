@@ -53,10 +53,43 @@ def _run(cmd: list[str]) -> None:
         sys.stderr.write(r.stdout)
 
 
+CHOL_LIBNAME = "libstarpu_gb300_chol.so"
+EXAMPLES = ["chol_implicit_gb300"]
+
+
+def chol_lib_path() -> str:
+    return os.path.join(LIBDIR, CHOL_LIBNAME)
+
+
+def example_path(name: str) -> str:
+    return os.path.join(LIBDIR, name)
+
+
 def sources() -> tuple[list[str], list[str]]:
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "kernels", "*.cu")))
-    c = sorted(glob.glob(os.path.join(CSRC, "runtime", "*.c")) + glob.glob(os.path.join(CSRC, "codelets", "*.c")))
+    c = sorted(glob.glob(os.path.join(CSRC, "runtime", "*.c")))
     return cu, c
+
+
+def _build_codelets_and_examples(main_changed: bool) -> None:
+    """libstarpu_gb300_chol.so (the Cholesky codelets) and the example drivers,
+    linked against libstarpu_gb300.so."""
+    inc = ["-I" + INCLUDE, "-I" + os.path.join(CUDA_HOME, "include")]
+    rpath = "-Wl,-rpath," + LIBDIR + ":" + os.path.join(CUDA_HOME, "lib64")
+    deps = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(lib_path())])
+    csrcs = sorted(glob.glob(os.path.join(CSRC, "codelets", "*.c")))
+    out = chol_lib_path()
+    if main_changed or not os.path.exists(out) or any(_stale(out, s, deps) for s in csrcs):
+        _run(["gcc", "-O2", "-g", "-fPIC", "-std=gnu11", "-Wall", "-shared", "-o", out + ".tmp", *csrcs, *inc,
+              "-L" + LIBDIR, "-lstarpu_gb300", rpath])
+        os.replace(out + ".tmp", out)
+    for ex in EXAMPLES:
+        src = os.path.join(CSRC, "examples", ex + ".c")
+        exe = example_path(ex)
+        if main_changed or _stale(exe, src, max(deps, os.path.getmtime(out))):
+            _run(["gcc", "-O2", "-g", "-std=gnu11", "-Wall", "-o", exe + ".tmp", src, *inc, "-L" + LIBDIR,
+                  "-lstarpu_gb300_chol", "-lstarpu_gb300", rpath, "-lm", "-lpthread"])
+            os.replace(exe + ".tmp", exe)
 
 
 def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
@@ -90,11 +123,13 @@ def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
         with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
             list(ex.map(_run, jobs))
     out = lib_path()
-    if jobs or not os.path.exists(out):
+    main_changed = bool(jobs) or not os.path.exists(out)
+    if main_changed:
         tmp = out + ".tmp"
         _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "shared",
               "-Xlinker", "-rpath=" + os.path.join(CUDA_HOME, "lib64"), "-lpthread", "-ldl", "-lm"])
         os.replace(tmp, out)
+    _build_codelets_and_examples(main_changed)
     return out
 
 

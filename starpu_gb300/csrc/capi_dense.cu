@@ -246,6 +246,20 @@ int starpu_gb300_dpotrf_tile(void *stream, int n, double *A, int lda, int *d_inf
     return gb300_last_launch_status();
 }
 
+int starpu_gb300_spotrf_tile_status(void *stream, int n, float *A, int lda, int *d_status)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1)) return GB300_EINVAL;
+    if (n) potrf_tiled<float>(GB300_STREAM(stream), n, A, lda, small_w<float>::value, d_status, 0);
+    return gb300_last_launch_status();
+}
+
+int starpu_gb300_dpotrf_tile_status(void *stream, int n, double *A, int lda, int *d_status)
+{
+    if (n < 0 || lda < (n > 1 ? n : 1)) return GB300_EINVAL;
+    if (n) potrf_tiled<double>(GB300_STREAM(stream), n, A, lda, small_w<double>::value, d_status, 0);
+    return gb300_last_launch_status();
+}
+
 int starpu_gb300_strsm_rltn_tile(void *stream, int m, int n, float alpha, const float *L, int ldl, float *B, int ldb)
 {
     if (m < 0 || n < 0 || ldl < (n > 1 ? n : 1) || ldb < (m > 1 ? m : 1)) return GB300_EINVAL;

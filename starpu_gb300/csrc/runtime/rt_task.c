@@ -1,0 +1,524 @@
+/*
+ * Tasks: creation, starpu_task_insert argument parsing
+ * (include/starpu_task_util.h semantics), implicit data dependencies
+ * (sequential consistency: a writer depends on the last writer and every
+ * reader since; a reader depends on the last writer -- the edges of
+ * src/core/dependencies/implicit_data_deps.c), tags, termination and waits.
+ */
+#include <stdarg.h>
+
+#include "rt_internal.h"
+
+void starpu_codelet_init(struct starpu_codelet *cl) { memset(cl, 0, sizeof *cl); }
+
+void starpu_task_init(struct starpu_task *t)
+{
+    memset(t, 0, sizeof *t);
+    t->sequential_consistency = 1;
+    t->detach = 1;
+    t->priority = STARPU_DEFAULT_PRIO;
+    t->status = STARPU_TASK_INIT;
+    t->magic = 42;
+}
+
+struct starpu_task *starpu_task_create(void)
+{
+    struct starpu_task *t = malloc(sizeof *t);
+    starpu_task_init(t);
+    t->destroy = 1;
+    return t;
+}
+
+void starpu_task_clean(struct starpu_task *t)
+{
+    if (t->cl_arg_free && t->cl_arg) free(t->cl_arg);
+    if (t->callback_arg_free && t->callback_arg) free(t->callback_arg);
+    t->cl_arg = NULL;
+    t->callback_arg = NULL;
+}
+
+void starpu_task_destroy(struct starpu_task *t)
+{
+    if (!t) return;
+    starpu_task_clean(t);
+    free(t);
+}
+
+struct starpu_task *starpu_task_get_current(void) { return rt_current_task_get(); }
+
+int starpu_task_nsubmitted(void) { return (int)rt.nsubmitted; }
+
+int starpu_task_nready(void)
+{
+    int n = 0;
+    rt_lock();
+    for (int i = 0; i < rt.nworkers; ++i) n += rt.workers[i].hn;
+    rt_unlock();
+    return n;
+}
+
+/* ----------------------------------------------------------------- tags */
+
+struct tag_entry {
+    starpu_tag_t id;
+    struct rt_job *job;     /* last submitted task with this tag (NULL once done) */
+    int done;               /* completed (or notified from the application) */
+    starpu_tag_t *deps;
+    int ndeps;
+    struct rt_job **waiters; /* tasks waiting for this tag before any task carrying it was submitted */
+    int nwaiters, capwaiters;
+    struct tag_entry *next;
+};
+
+static void tag_add_waiter(struct tag_entry *e, struct rt_job *j)
+{
+    if (e->nwaiters == e->capwaiters) {
+        e->capwaiters = e->capwaiters ? 2 * e->capwaiters : 4;
+        e->waiters = realloc(e->waiters, sizeof *e->waiters * e->capwaiters);
+    }
+    e->waiters[e->nwaiters++] = j;
+    j->ndeps++;
+}
+
+/* called with the runtime lock held when tag e becomes done */
+static void tag_release_waiters(struct tag_entry *e)
+{
+    for (int i = 0; i < e->nwaiters; ++i) {
+        struct rt_job *u = e->waiters[i];
+        if (--u->ndeps == 0 && !rt.graph_mode) {
+            u->task->status = STARPU_TASK_READY;
+            rt_sched_push(u);
+        }
+    }
+    e->nwaiters = 0;
+}
+
+#define TAG_BUCKETS 4096
+static struct tag_entry *tags[TAG_BUCKETS];
+static pthread_cond_t tag_cond = PTHREAD_COND_INITIALIZER;
+
+static struct tag_entry *tag_get(starpu_tag_t id, int create)
+{
+    unsigned b = (unsigned)((id ^ (id >> 29) ^ (id >> 47)) % TAG_BUCKETS);
+    for (struct tag_entry *e = tags[b]; e; e = e->next)
+        if (e->id == id) return e;
+    if (!create) return NULL;
+    struct tag_entry *e = calloc(1, sizeof *e);
+    e->id = id;
+    e->next = tags[b];
+    tags[b] = e;
+    return e;
+}
+
+void starpu_tag_declare_deps_array(starpu_tag_t id, unsigned ndeps, starpu_tag_t *array)
+{
+    rt_lock();
+    struct tag_entry *e = tag_get(id, 1);
+    e->deps = realloc(e->deps, sizeof(starpu_tag_t) * (e->ndeps + ndeps));
+    for (unsigned i = 0; i < ndeps; ++i) e->deps[e->ndeps++] = array[i];
+    rt_unlock();
+}
+
+void starpu_tag_declare_deps(starpu_tag_t id, unsigned ndeps, ...)
+{
+    starpu_tag_t *a = malloc(sizeof(starpu_tag_t) * (ndeps ? ndeps : 1));
+    va_list ap;
+    va_start(ap, ndeps);
+    for (unsigned i = 0; i < ndeps; ++i) a[i] = va_arg(ap, starpu_tag_t);
+    va_end(ap);
+    starpu_tag_declare_deps_array(id, ndeps, a);
+    free(a);
+}
+
+int starpu_tag_wait_array(unsigned ntags, starpu_tag_t *id)
+{
+    rt_flush_and_wait();
+    rt_lock();
+    for (unsigned i = 0; i < ntags; ++i) {
+        struct tag_entry *e = tag_get(id[i], 1);
+        while (!e->done) pthread_cond_wait(&tag_cond, &rt.lock);
+    }
+    rt_unlock();
+    return 0;
+}
+
+int starpu_tag_wait(starpu_tag_t id) { return starpu_tag_wait_array(1, &id); }
+
+void starpu_tag_remove(starpu_tag_t id)
+{
+    rt_lock();
+    struct tag_entry *e = tag_get(id, 0);
+    if (e) {
+        e->done = 0;
+        e->job = NULL;
+        free(e->deps);
+        e->deps = NULL;
+        e->ndeps = 0;
+    }
+    rt_unlock();
+}
+
+void starpu_tag_notify_from_apps(starpu_tag_t id)
+{
+    rt_lock();
+    struct tag_entry *e = tag_get(id, 1);
+    e->done = 1;
+    tag_release_waiters(e);
+    pthread_cond_broadcast(&tag_cond);
+    rt_unlock();
+}
+
+/* ---------------------------------------------------------- dependencies */
+
+static void add_edge(struct rt_job *from, struct rt_job *to)
+{
+    if (!from || from == to || from->terminated) return;
+    if (from->nsucc && from->succ[from->nsucc - 1] == to) return; /* same pair twice in a row */
+    if (from->nsucc == from->capsucc) {
+        from->capsucc = from->capsucc ? 2 * from->capsucc : 4;
+        from->succ = realloc(from->succ, sizeof *from->succ * from->capsucc);
+    }
+    from->succ[from->nsucc++] = to;
+    to->ndeps++;
+    if (to->nprev == to->capprev) {
+        to->capprev = to->capprev ? 2 * to->capprev : 4;
+        to->prev = realloc(to->prev, sizeof *to->prev * to->capprev);
+    }
+    to->prev[to->nprev++] = from;
+}
+
+static void add_reader(starpu_data_handle_t h, struct rt_job *j)
+{
+    if (h->nreaders == h->capreaders) {
+        h->capreaders = h->capreaders ? 2 * h->capreaders : 8;
+        h->readers = realloc(h->readers, sizeof *h->readers * h->capreaders);
+    }
+    h->readers[h->nreaders++] = j;
+}
+
+int rt_can_execute(struct rt_worker *w, struct starpu_task *t)
+{
+    struct starpu_codelet *cl = t->cl;
+    if (!cl) return 1;
+    uint32_t where = t->where ? t->where : cl->where;
+    if (w->type == STARPU_CUDA_WORKER) {
+        if (where && !(where & STARPU_CUDA)) return 0;
+        if (!cl->cuda_funcs[0]) return 0;
+    } else {
+        if (where && !(where & STARPU_CPU)) return 0;
+        if (!cl->cpu_funcs[0]) return 0;
+    }
+    if (t->execute_on_a_specific_worker && (int)t->workerid != w->id) return 0;
+    if (cl->can_execute && !cl->can_execute((unsigned)w->id, t, 0)) return 0;
+    return 1;
+}
+
+int starpu_task_submit(struct starpu_task *t)
+{
+    STARPU_ASSERT(rt.initialized);
+    if (t->cl) {
+        int nb = t->cl->nbuffers >= 0 ? t->cl->nbuffers : t->nbuffers;
+        t->nbuffers = nb;
+        STARPU_ASSERT_MSG(nb <= STARPU_NMAXBUFS, "too many buffers (%d)", nb);
+        for (int i = 0; i < nb; ++i)
+            if (!t->modes[i]) t->modes[i] = t->cl->modes[i];
+        int ok = 0;
+        for (int w = 0; w < rt.nworkers && !ok; ++w) ok = rt_can_execute(&rt.workers[w], t);
+        if (!ok) return -ENODEV;
+    }
+    struct rt_job *j = calloc(1, sizeof *j);
+    j->task = t;
+    j->worker = -1;
+    j->heap_index = -1;
+    t->starpu_private = j;
+    t->status = STARPU_TASK_BLOCKED;
+    int sync = t->synchronous;
+
+    rt_lock();
+    j->seq = rt.seq++;
+    rt.nsubmitted++;
+    j->ndeps = 1; /* held until submission completes */
+    if (t->sequential_consistency) {
+        for (int i = 0; i < t->nbuffers; ++i) {
+            starpu_data_handle_t h = t->handles[i];
+            enum starpu_data_access_mode m = t->modes[i];
+            if (!h || (m & STARPU_SCRATCH) || (m & STARPU_REDUX)) continue;
+            if (m & STARPU_W) {
+                add_edge(h->last_writer, j);
+                for (int r = 0; r < h->nreaders; ++r) add_edge(h->readers[r], j);
+                h->nreaders = 0;
+                h->last_writer = j;
+            } else if (m & STARPU_R) {
+                add_edge(h->last_writer, j);
+                add_reader(h, j);
+            }
+        }
+    }
+    if (t->use_tag) {
+        struct tag_entry *e = tag_get(t->tag_id, 1);
+        for (int d = 0; d < e->ndeps; ++d) {
+            struct tag_entry *p = tag_get(e->deps[d], 1);
+            if (p->done) continue;
+            if (p->job) add_edge(p->job, j);
+            else tag_add_waiter(p, j); /* its task is not submitted yet */
+        }
+        e->job = j;
+        e->done = 0;
+        j->tag = t->tag_id;
+        j->has_tag = 1;
+    }
+    if (rt.graph_mode) {
+        if (rt.npending == rt.cappending) {
+            rt.cappending = rt.cappending ? 2 * rt.cappending : 1024;
+            rt.pending = realloc(rt.pending, sizeof *rt.pending * rt.cappending);
+        }
+        j->graph_slot = rt.npending;
+        rt.pending[rt.npending++] = j;
+        j->ndeps--;
+    } else if (--j->ndeps == 0) {
+        t->status = STARPU_TASK_READY;
+        rt_sched_push(j);
+    }
+    rt_unlock();
+    if (sync) starpu_task_wait(t);
+    return 0;
+}
+
+/* Called with the runtime lock NOT held, after the job's work completed. */
+void rt_job_terminate(struct rt_job *j, double measured_us)
+{
+    struct starpu_task *t = j->task;
+    if (t->cl && t->cl->model && measured_us > 0) {
+        int w = j->worker;
+        rt_perfmodel_feedback(t, w >= 0 ? rt.workers[w].type : STARPU_CUDA_WORKER, measured_us);
+    }
+    if (t->callback_func) t->callback_func(t->callback_arg);
+    rt_lock();
+    j->terminated = 1;
+    t->status = STARPU_TASK_FINISHED;
+    for (int i = 0; i < t->nbuffers; ++i)
+        if (t->handles[i]) rt_data_forget_job(t->handles[i], j);
+    for (int s = 0; s < j->nsucc; ++s) {
+        struct rt_job *u = j->succ[s];
+        if (--u->ndeps == 0 && !rt.graph_mode) {
+            u->task->status = STARPU_TASK_READY;
+            rt_sched_push(u);
+        }
+    }
+    if (j->has_tag) {
+        struct tag_entry *e = tag_get(j->tag, 1);
+        if (e->job == j) {
+            e->done = 1;
+            e->job = NULL;
+            tag_release_waiters(e);
+        }
+        pthread_cond_broadcast(&tag_cond);
+    }
+    int destroy = t->destroy && t->detach;
+    t->starpu_private = NULL;
+    free(j->succ);
+    free(j->prev);
+    free(j);
+    rt.nsubmitted--;
+    pthread_cond_broadcast(&rt.all_done);
+    rt_unlock();
+    if (destroy) starpu_task_destroy(t);
+}
+
+/* Graph mode: hand every pending job to the CUDA driver as one graph. */
+void rt_flush_and_wait(void)
+{
+    if (rt.graph_mode) {
+        rt_lock();
+        struct rt_job **jobs = rt.pending;
+        int n = rt.npending;
+        rt.pending = NULL;
+        rt.npending = rt.cappending = 0;
+        rt_unlock();
+        if (n) rt_cuda_graph_flush(jobs, n);
+        free(jobs);
+    }
+}
+
+int starpu_task_wait_for_all(void)
+{
+    if (!rt.initialized) return 0;
+    rt_flush_and_wait();
+    rt_lock();
+    while (rt.nsubmitted > 0) pthread_cond_wait(&rt.all_done, &rt.lock);
+    rt_unlock();
+    return 0;
+}
+
+int starpu_task_wait_for_n_submitted(unsigned n)
+{
+    rt_flush_and_wait();
+    rt_lock();
+    while (rt.nsubmitted > (long)n) pthread_cond_wait(&rt.all_done, &rt.lock);
+    rt_unlock();
+    return 0;
+}
+
+int starpu_task_wait(struct starpu_task *t)
+{
+    rt_flush_and_wait();
+    rt_lock();
+    while (t->status != STARPU_TASK_FINISHED) pthread_cond_wait(&rt.all_done, &rt.lock);
+    rt_unlock();
+    return 0;
+}
+
+/* ----------------------------------------------------------- task_insert */
+
+static int build_task(struct starpu_task *t, struct starpu_codelet *cl, va_list ap)
+{
+    t->cl = cl;
+    int nb = 0;
+    int type;
+    while ((type = va_arg(ap, int)) != 0) {
+        if ((type & ~((1 << STARPU_MODE_SHIFT) - 1)) == 0) {
+            /* an access mode (possibly with flags) followed by a handle */
+            starpu_data_handle_t h = va_arg(ap, starpu_data_handle_t);
+            STARPU_ASSERT_MSG(nb < STARPU_NMAXBUFS, "too many data in task_insert");
+            t->handles[nb] = h;
+            t->modes[nb] = (enum starpu_data_access_mode)type;
+            nb++;
+        } else if (type == STARPU_DATA_ARRAY) {
+            starpu_data_handle_t *hs = va_arg(ap, starpu_data_handle_t *);
+            int n = va_arg(ap, int);
+            for (int i = 0; i < n; ++i, ++nb) {
+                t->handles[nb] = hs[i];
+                t->modes[nb] = cl->modes[nb];
+            }
+        } else if (type == STARPU_DATA_MODE_ARRAY) {
+            struct starpu_data_descr *ds = va_arg(ap, struct starpu_data_descr *);
+            int n = va_arg(ap, int);
+            for (int i = 0; i < n; ++i, ++nb) {
+                t->handles[nb] = ds[i].handle;
+                t->modes[nb] = ds[i].mode;
+            }
+        } else if (type == STARPU_VALUE) {
+            void *p = va_arg(ap, void *);
+            size_t sz = va_arg(ap, size_t);
+            /* packed as in starpu_codelet_pack_args: [size][bytes]... appended */
+            size_t old = t->cl_arg_size;
+            t->cl_arg = realloc(t->cl_arg, old + sizeof(size_t) + sz);
+            memcpy((char *)t->cl_arg + old, &sz, sizeof(size_t));
+            memcpy((char *)t->cl_arg + old + sizeof(size_t), p, sz);
+            t->cl_arg_size = old + sizeof(size_t) + sz;
+            t->cl_arg_free = 1;
+        } else if (type == STARPU_CL_ARGS || type == STARPU_CL_ARGS_NFREE) {
+            t->cl_arg = va_arg(ap, void *);
+            t->cl_arg_size = va_arg(ap, size_t);
+            t->cl_arg_free = type == STARPU_CL_ARGS;
+        } else if (type == STARPU_CALLBACK) {
+            t->callback_func = va_arg(ap, void (*)(void *));
+        } else if (type == STARPU_CALLBACK_WITH_ARG) {
+            t->callback_func = va_arg(ap, void (*)(void *));
+            t->callback_arg = va_arg(ap, void *);
+        } else if (type == STARPU_CALLBACK_ARG) {
+            t->callback_arg = va_arg(ap, void *);
+        } else if (type == STARPU_PRIORITY) {
+            t->priority = va_arg(ap, int);
+        } else if (type == STARPU_FLOPS) {
+            t->flops = va_arg(ap, double);
+        } else if (type == STARPU_NAME) {
+            t->name = va_arg(ap, const char *);
+        } else if (type == STARPU_TAG || type == STARPU_TAG_ONLY) {
+            t->tag_id = va_arg(ap, starpu_tag_t);
+            t->use_tag = type == STARPU_TAG;
+        } else if (type == STARPU_EXECUTE_ON_WORKER) {
+            int w = va_arg(ap, int);
+            if (w >= 0) {
+                t->execute_on_a_specific_worker = 1;
+                t->workerid = (unsigned)w;
+            }
+        } else if (type == STARPU_EXECUTE_WHERE) {
+            t->where = (uint32_t)va_arg(ap, unsigned long long);
+        } else if (type == STARPU_SCHED_CTX) {
+            t->sched_ctx = va_arg(ap, unsigned);
+        } else if (type == STARPU_TASK_SYNCHRONOUS) {
+            t->synchronous = va_arg(ap, int);
+        } else if (type == STARPU_SEQUENTIAL_CONSISTENCY) {
+            t->sequential_consistency = va_arg(ap, unsigned);
+        } else if (type == STARPU_TASK_COLOR) {
+            (void)va_arg(ap, int);
+        } else if (type == STARPU_POSSIBLY_PARALLEL) {
+            (void)va_arg(ap, unsigned);
+        } else if (type == STARPU_TASK_NO_SUBMITORDER) {
+            t->no_submitorder = va_arg(ap, unsigned);
+        } else if (type == STARPU_EXECUTE_ON_NODE || type == STARPU_EXECUTE_ON_DATA) {
+            (void)va_arg(ap, void *);
+        } else {
+            fprintf(stderr, "[starpu_gb300] unsupported task_insert argument %d\n", type);
+            return -EINVAL;
+        }
+    }
+    t->nbuffers = nb;
+    if (cl && cl->nbuffers >= 0)
+        STARPU_ASSERT_MSG(cl->nbuffers == nb, "codelet %s expects %d buffers, %d given", cl->name ? cl->name : "?",
+                          cl->nbuffers, nb);
+    return 0;
+}
+
+struct starpu_task *starpu_task_build(struct starpu_codelet *cl, ...)
+{
+    struct starpu_task *t = starpu_task_create();
+    va_list ap;
+    va_start(ap, cl);
+    int rc = build_task(t, cl, ap);
+    va_end(ap);
+    if (rc) {
+        starpu_task_destroy(t);
+        return NULL;
+    }
+    return t;
+}
+
+static int vinsert(struct starpu_codelet *cl, va_list ap)
+{
+    struct starpu_task *t = starpu_task_create();
+    int rc = build_task(t, cl, ap);
+    if (rc) {
+        starpu_task_destroy(t);
+        return rc;
+    }
+    rc = starpu_task_submit(t);
+    if (rc) starpu_task_destroy(t);
+    return rc;
+}
+
+int starpu_task_insert(struct starpu_codelet *cl, ...)
+{
+    va_list ap;
+    va_start(ap, cl);
+    int rc = vinsert(cl, ap);
+    va_end(ap);
+    return rc;
+}
+
+int starpu_insert_task(struct starpu_codelet *cl, ...)
+{
+    va_list ap;
+    va_start(ap, cl);
+    int rc = vinsert(cl, ap);
+    va_end(ap);
+    return rc;
+}
+
+/* Unpack STARPU_VALUE arguments in order: each destination pointer receives
+ * the bytes of the corresponding packed value. */
+void starpu_codelet_unpack_args(void *cl_arg, ...)
+{
+    va_list ap;
+    va_start(ap, cl_arg);
+    char *p = (char *)cl_arg;
+    void *dst;
+    while ((dst = va_arg(ap, void *)) != NULL) {
+        size_t sz;
+        memcpy(&sz, p, sizeof sz);
+        memcpy(dst, p + sizeof sz, sz);
+        p += sizeof sz + sz;
+    }
+    va_end(ap);
+}

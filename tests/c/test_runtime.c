@@ -1,0 +1,197 @@
+/*
+ * Runtime tests of libstarpu_gb300.so on CPU workers (no GPU needed), in the
+ * style of the reference's tests/main/insert_task*.c,
+ * tests/datawizard/data_implicit_deps.c, partition_*.c and tests/perfmodels/*.c.
+ * Prints "ok <name>" per test; exit status 0 when every test passed.
+ */
+#include <math.h>
+#include <starpu.h>
+#include <unistd.h>
+
+static int failures = 0;
+#define CHECK(cond, name)                                                         \
+    do {                                                                          \
+        if (cond) printf("ok %s\n", name);                                        \
+        else {                                                                    \
+            printf("FAIL %s (%s:%d)\n", name, __FILE__, __LINE__);                \
+            failures++;                                                           \
+        }                                                                         \
+    } while (0)
+
+/* ---------------- codelets ---------------- */
+
+/* v[0] = v[0] * 10 + digit (digit passed by value): order-sensitive */
+static void append_digit(void *descr[], void *arg)
+{
+    int digit;
+    starpu_codelet_unpack_args(arg, &digit, NULL);
+    long *v = (long *)STARPU_VARIABLE_GET_PTR(descr[0]);
+    usleep(1000 * (digit % 3));
+    *v = *v * 10 + digit;
+}
+static struct starpu_codelet cl_append = {.cpu_funcs = {append_digit}, .nbuffers = 1, .modes = {STARPU_RW}};
+
+/* dst = src (copy), slow so that a missing dependency would show */
+static void copy_var(void *descr[], void *arg)
+{
+    (void)arg;
+    usleep(2000);
+    *(long *)STARPU_VARIABLE_GET_PTR(descr[1]) = *(long *)STARPU_VARIABLE_GET_PTR(descr[0]);
+}
+static struct starpu_codelet cl_copy = {.cpu_funcs = {copy_var}, .nbuffers = 2, .modes = {STARPU_R, STARPU_W}};
+
+/* matrix tile += 1 */
+static void tile_inc(void *descr[], void *arg)
+{
+    (void)arg;
+    float *p = (float *)STARPU_MATRIX_GET_PTR(descr[0]);
+    size_t nx = STARPU_MATRIX_GET_NX(descr[0]), ny = STARPU_MATRIX_GET_NY(descr[0]),
+           ld = STARPU_MATRIX_GET_LD(descr[0]);
+    for (size_t j = 0; j < ny; ++j)
+        for (size_t i = 0; i < nx; ++i) p[i + j * ld] += 1.0f;
+}
+static struct starpu_perfmodel inc_model = {.type = STARPU_HISTORY_BASED, .symbol = "gb300_test_tile_inc"};
+static struct starpu_codelet cl_inc = {
+    .cpu_funcs = {tile_inc}, .nbuffers = 1, .modes = {STARPU_RW}, .model = &inc_model, .name = "inc"};
+
+static void noop(void *descr[], void *arg) { (void)descr; (void)arg; }
+static void noop_cuda(void *descr[], void *arg) { (void)descr; (void)arg; }
+static struct starpu_codelet cl_cuda_only = {.cuda_funcs = {noop_cuda}, .nbuffers = 0};
+static struct starpu_codelet cl_noop = {.cpu_funcs = {noop}, .nbuffers = 0};
+
+static int cb_count = 0;
+static void cb(void *arg) { __sync_fetch_and_add(&cb_count, *(int *)arg); }
+
+int main(void)
+{
+    setenv("STARPU_NCUDA", "0", 0);
+    int ret = starpu_init(NULL);
+    CHECK(ret == 0, "init");
+    CHECK(starpu_cpu_worker_get_count() >= 1, "cpu_workers");
+
+    /* 1. sequential consistency on one variable: RW tasks run in submission order */
+    {
+        long v = 0;
+        starpu_data_handle_t h;
+        starpu_variable_data_register(&h, STARPU_MAIN_RAM, (uintptr_t)&v, sizeof v);
+        for (int d = 1; d <= 9; ++d)
+            starpu_task_insert(&cl_append, STARPU_VALUE, &d, sizeof d, STARPU_RW, h, 0);
+        starpu_task_wait_for_all();
+        starpu_data_unregister(h);
+        CHECK(v == 123456789, "rw_chain_order");
+    }
+    /* 2. RAW / WAR: b = a; a = 5 (the write must wait for the read); c = b */
+    {
+        long a = 7, b = 0, c = 0;
+        starpu_data_handle_t ha, hb, hc;
+        starpu_variable_data_register(&ha, STARPU_MAIN_RAM, (uintptr_t)&a, sizeof a);
+        starpu_variable_data_register(&hb, STARPU_MAIN_RAM, (uintptr_t)&b, sizeof b);
+        starpu_variable_data_register(&hc, STARPU_MAIN_RAM, (uintptr_t)&c, sizeof c);
+        starpu_task_insert(&cl_copy, STARPU_R, ha, STARPU_W, hb, 0);
+        int five = 5;
+        long zero = 0;
+        (void)zero;
+        starpu_task_insert(&cl_append, STARPU_VALUE, &five, sizeof five, STARPU_RW, ha, 0); /* a = 75 */
+        starpu_task_insert(&cl_copy, STARPU_R, hb, STARPU_W, hc, 0);
+        starpu_task_wait_for_all();
+        starpu_data_unregister(ha);
+        starpu_data_unregister(hb);
+        starpu_data_unregister(hc);
+        CHECK(b == 7 && c == 7 && a == 75, "raw_war_edges");
+    }
+    /* 3. 2-level block filters with a ragged remainder, tasks on tiles, unpartition */
+    {
+        const unsigned n = 10, nb = 3;
+        float *m = calloc(n * n, sizeof *m);
+        starpu_data_handle_t h;
+        starpu_matrix_data_register(&h, STARPU_MAIN_RAM, (uintptr_t)m, n, n, n, sizeof(float));
+        struct starpu_data_filter f = {.filter_func = starpu_matrix_filter_block, .nchildren = nb};
+        struct starpu_data_filter f2 = {.filter_func = starpu_matrix_filter_vertical_block, .nchildren = nb};
+        starpu_data_map_filters(h, 2, &f, &f2);
+        int shapes_ok = 1;
+        for (unsigned i = 0; i < nb; ++i)
+            for (unsigned j = 0; j < nb; ++j) {
+                starpu_data_handle_t t = starpu_data_get_sub_data(h, 2, i, j);
+                size_t ex_nx = n / nb + (i < n % nb), ex_ny = n / nb + (j < n % nb);
+                shapes_ok &= starpu_matrix_get_nx(t) == ex_nx && starpu_matrix_get_ny(t) == ex_ny;
+                for (unsigned r = 0; r <= i + j; ++r) starpu_task_insert(&cl_inc, STARPU_RW, t, 0);
+            }
+        starpu_task_wait_for_all();
+        starpu_data_unpartition(h, STARPU_MAIN_RAM);
+        starpu_data_unregister(h);
+        int vals_ok = 1;
+        for (unsigned jj = 0; jj < n; ++jj)
+            for (unsigned ii = 0; ii < n; ++ii) {
+                unsigned bi = ii < 4 ? 0 : ii < 7 ? 1 : 2, bj = jj < 4 ? 0 : jj < 7 ? 1 : 2;
+                vals_ok &= m[ii + jj * n] == (float)(bi + bj + 1);
+            }
+        free(m);
+        CHECK(shapes_ok, "filter_ragged_shapes");
+        CHECK(vals_ok, "tile_tasks_and_unpartition");
+    }
+    /* 4. callbacks, priorities, task_build/destroy, -ENODEV */
+    {
+        int one = 1;
+        for (int i = 0; i < 20; ++i)
+            starpu_task_insert(&cl_noop, STARPU_CALLBACK_WITH_ARG, cb, &one, STARPU_PRIORITY, i, 0);
+        starpu_task_wait_for_all();
+        CHECK(cb_count == 20, "callbacks");
+        struct starpu_task *t = starpu_task_build(&cl_noop, 0);
+        CHECK(t && t->cl == &cl_noop, "task_build");
+        t->destroy = 0;
+        starpu_task_destroy(t);
+        CHECK(starpu_task_insert(&cl_cuda_only, 0) == -ENODEV, "enodev_without_cuda_worker");
+        CHECK(STARPU_MAX_PRIO == INT_MAX && STARPU_MIN_PRIO == INT_MIN, "unbounded_priorities");
+    }
+    /* 5. tags: C depends on A and B through declared tag dependencies */
+    {
+        long v = 0;
+        starpu_data_handle_t h;
+        starpu_variable_data_register(&h, STARPU_MAIN_RAM, (uintptr_t)&v, sizeof v);
+        starpu_tag_declare_deps((starpu_tag_t)3, 2, (starpu_tag_t)1, (starpu_tag_t)2);
+        int d1 = 1, d2 = 2, d3 = 3;
+        starpu_task_insert(&cl_append, STARPU_VALUE, &d3, sizeof d3, STARPU_TAG, (starpu_tag_t)3, STARPU_RW, h,
+                           STARPU_SEQUENTIAL_CONSISTENCY, 0, 0);
+        starpu_task_insert(&cl_append, STARPU_VALUE, &d1, sizeof d1, STARPU_TAG, (starpu_tag_t)1, STARPU_RW, h,
+                           STARPU_SEQUENTIAL_CONSISTENCY, 0, 0);
+        starpu_task_insert(&cl_append, STARPU_VALUE, &d2, sizeof d2, STARPU_TAG, (starpu_tag_t)2, STARPU_RW, h,
+                           STARPU_SEQUENTIAL_CONSISTENCY, 0, 0);
+        starpu_tag_wait((starpu_tag_t)3);
+        starpu_task_wait_for_all();
+        starpu_data_unregister(h);
+        /* 3 runs last; 1 and 2 may run in either order (no data ordering requested) */
+        CHECK(v == 123 || v == 213, "tag_dependencies");
+    }
+    /* 6. history perfmodel: calibrated after enough runs, saved and reloaded */
+    {
+        float tile[64 * 64] = {0};
+        starpu_data_handle_t h;
+        starpu_matrix_data_register(&h, STARPU_MAIN_RAM, (uintptr_t)tile, 64, 64, 64, sizeof(float));
+        for (int i = 0; i < 12; ++i) starpu_task_insert(&cl_inc, STARPU_RW, h, 0);
+        starpu_task_wait_for_all();
+        struct starpu_task *t = starpu_task_build(&cl_inc, STARPU_RW, h, 0);
+        double len = starpu_task_expected_length(t, starpu_worker_get_perf_archtype(0, 0), 0);
+        t->destroy = 0;
+        starpu_task_destroy(t);
+        starpu_data_unregister(h);
+        CHECK(!isnan(len) && len >= 0, "perfmodel_calibrated");
+        CHECK(starpu_save_history_based_model(&inc_model) == 0, "perfmodel_saved");
+        char path[1024];
+        starpu_perfmodel_get_model_path("gb300_test_tile_inc", path, sizeof path);
+        FILE *f = fopen(path, "r");
+        char line[256] = "";
+        if (f) {
+            fgets(line, sizeof line, f);
+            fgets(line, sizeof line, f);
+            fgets(line, sizeof line, f);
+            fclose(f);
+        }
+        CHECK(f && atoi(line) == 45, "perfmodel_file_version_45");
+        struct starpu_perfmodel loaded;
+        CHECK(starpu_perfmodel_load_symbol("gb300_test_tile_inc", &loaded) == 0, "perfmodel_reload");
+        starpu_perfmodel_unload_model(&loaded);
+    }
+    starpu_shutdown();
+    printf("%s\n", failures ? "FAILED" : "ALL OK");
+    return failures ? 1 : 0;
+}
