@@ -69,11 +69,14 @@ def _ctype(decl: str):
     raise TypeError(f"unmapped C type in prototype: {decl!r}")
 
 
+# Public headers whose starpu_gb300_* functions live in libstarpu_gb300.so
+# (starpu_gb300_chol.h belongs to the codelet library libstarpu_gb300_chol.so).
+MAIN_HEADERS = ("starpu_gb300_kernels.h", "starpu_gb300_solver.h")
+
+
 def _bind(dll: C.CDLL) -> None:
     inc = os.path.join(_build.ROOT, "include")
-    for h in sorted(os.listdir(inc)):
-        if not h.startswith("starpu_gb300") or not h.endswith(".h"):
-            continue
+    for h in MAIN_HEADERS:
         for name, (ret, args) in header_prototypes(os.path.join(inc, h)).items():
             fn = getattr(dll, name)  # raises AttributeError if the symbol is missing
             fn.restype = _ctype(ret) if ret != "void" else None

@@ -1,0 +1,69 @@
+"""The C-ABI libraries load (no GPU needed) and export every function that
+the public headers in include/ declare; argument checking happens before any
+device work."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(ROOT, "include")
+
+
+def declared_functions(header):
+    txt = open(os.path.join(INC, header)).read()
+    txt = re.sub(r"/\*.*?\*/", " ", txt, flags=re.S)
+    txt = re.sub(r"#define[^\n]*(\\\n[^\n]*)*", " ", txt)
+    txt = re.sub(r"#[^\n]*", " ", txt)
+    names = set()
+    for m in re.finditer(r"\b(starpu_\w+)\s*\(([^;{}]*?)\)\s*(__attribute__\s*\(\(.*?\)\))?\s*;", txt, flags=re.S):
+        # skip function-pointer members "(*name)(...)"
+        pre = txt[max(0, m.start() - 2):m.start()]
+        if "(*" in pre or "*" == pre.strip()[-1:]:
+            continue
+        names.add(m.group(1))
+    return names
+
+
+@pytest.fixture(scope="module")
+def libs():
+    import starpu_gb300
+    from starpu_gb300 import build as _b  # noqa: F401
+    starpu_gb300.build()
+    main = starpu_gb300.load()
+    chol = C.CDLL(os.path.join(ROOT, "starpu_gb300", "lib", "libstarpu_gb300_chol.so"))
+    return main, chol
+
+
+def test_every_declared_function_is_exported(libs):
+    main, chol = libs
+    headers = sorted(h for h in os.listdir(INC) if h.endswith(".h"))
+    missing = []
+    total = 0
+    for h in headers:
+        lib = chol if h == "starpu_gb300_chol.h" else main
+        for name in sorted(declared_functions(h)):
+            total += 1
+            if not hasattr(lib, name):
+                missing.append(f"{h}: {name}")
+    assert total > 100
+    assert not missing, missing
+
+
+def test_codelet_library_defines_the_reference_symbols(libs):
+    _, chol = libs
+    for sym in ("cl_potrf", "cl_trsm", "cl_syrk", "cl_gemm", "chol_model_potrf", "chol_model_gemm", "scratch",
+                "devInfo", "cholesky_kernel_init", "cholesky_kernel_fini"):
+        assert hasattr(chol, sym), sym
+
+
+def test_invalid_arguments_are_rejected_without_a_gpu(libs):
+    main, _ = libs
+    EINVAL = -22
+    assert main.starpu_gb300_sgemm_nt_tile(None, -1, 1, 1, 1.0, None, 1, None, 1, 0.0, None, 1) == EINVAL
+    assert main.starpu_gb300_dpotrf(None, 10, None, 5, 0, None) == EINVAL
+    assert main.starpu_gb300_spotrs_noalloc(None, 16385, 1, None, 16385, None, 16385, None) == EINVAL
+    assert main.starpu_gb300_dsposv(None, 10, 1, None, 10, None, 10, None, 10, 0, 2, 1e-12, 10, None, 0, None) == EINVAL
+    assert main.starpu_gb300_dsposv_workspace(32768, 16, 1024) > 4 * 32768 * 32768
+    assert main.starpu_gb300_launch_count() == 0
