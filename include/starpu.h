@@ -206,6 +206,11 @@ void starpu_vector_data_register(starpu_data_handle_t *handle, int home_node, ui
 void starpu_data_unregister(starpu_data_handle_t handle);
 void starpu_data_unregister_no_coherency(starpu_data_handle_t handle);
 void starpu_data_set_name(starpu_data_handle_t handle, const char *name);
+void starpu_data_set_coordinates(starpu_data_handle_t handle, unsigned dimensions, ...);
+void starpu_data_set_default_sequential_consistency_flag(unsigned flag);
+unsigned starpu_data_get_default_sequential_consistency_flag(void);
+void starpu_data_set_sequential_consistency_flag(starpu_data_handle_t handle, unsigned flag);
+unsigned starpu_data_get_sequential_consistency_flag(starpu_data_handle_t handle);
 void starpu_data_wont_use(starpu_data_handle_t handle);
 void starpu_data_invalidate(starpu_data_handle_t handle);
 int starpu_data_acquire(starpu_data_handle_t handle, enum starpu_data_access_mode mode);

@@ -1,0 +1,8 @@
+/*
+ * starpu_data_filters.h -- kept so that sources written for StarPU include it unchanged; its
+ * declarations are part of starpu.h in this implementation.
+ */
+#ifndef STARPU_DATA_FILTERS_H
+#define STARPU_DATA_FILTERS_H
+#include "starpu.h"
+#endif

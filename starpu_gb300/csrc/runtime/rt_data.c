@@ -14,10 +14,28 @@
 
 #include "rt_internal.h"
 
+static int default_seq = 1;
+
 static void init_handle(struct _starpu_data_state *h)
 {
     memset(h, 0, sizeof *h);
     h->root = h;
+    h->seq_consistency = default_seq;
+}
+
+void starpu_data_set_default_sequential_consistency_flag(unsigned flag) { default_seq = flag != 0; }
+unsigned starpu_data_get_default_sequential_consistency_flag(void) { return (unsigned)default_seq; }
+void starpu_data_set_sequential_consistency_flag(starpu_data_handle_t h, unsigned flag)
+{
+    h->seq_consistency = flag != 0;
+}
+unsigned starpu_data_get_sequential_consistency_flag(starpu_data_handle_t h) { return (unsigned)h->seq_consistency; }
+
+/* coordinates only label data for traces / MPI placement: accepted and ignored */
+void starpu_data_set_coordinates(starpu_data_handle_t h, unsigned dimensions, ...)
+{
+    (void)h;
+    (void)dimensions;
 }
 
 void starpu_matrix_data_register(starpu_data_handle_t *handle, int home_node, uintptr_t ptr, size_t ld, size_t nx,
@@ -188,6 +206,7 @@ void starpu_data_partition(starpu_data_handle_t h, struct starpu_data_filter *f)
         c->elemsize = h->elemsize;
         c->parent = h;
         c->root = h->root;
+        c->seq_consistency = h->seq_consistency;
         /* the child's RAM view, computed by the filter from the parent's */
         struct starpu_matrix_interface pr = h->mat[RT_NODE_RAM];
         pr.offset = 0;

@@ -50,6 +50,7 @@ struct _starpu_data_state {
     struct _starpu_data_state **children;
     int partitioned;
     /* sequential consistency */
+    int seq_consistency;        /* implicit dependencies on this handle (inherited by children) */
     struct rt_job *last_writer;
     struct rt_job **readers;
     int nreaders, capreaders;
@@ -74,6 +75,7 @@ struct rt_job {
     int heap_index;
     starpu_tag_t tag;
     int has_tag;
+    int tag_waits;              /* tags awaited whose task is not submitted yet */
 };
 
 struct rt_worker {
@@ -98,6 +100,7 @@ struct rt_state {
     struct rt_worker workers[STARPU_NMAXWORKERS];
     int nworkers, ncpu, ncuda;
     int graph_mode;             /* CUDA-only runs: whole-DAG CUDA graphs */
+    int default_seq_consistency;
     int paused;
     uint64_t seq;
     long nsubmitted;            /* submitted and not terminated */

@@ -242,7 +242,7 @@ int starpu_task_submit(struct starpu_task *t)
         for (int i = 0; i < t->nbuffers; ++i) {
             starpu_data_handle_t h = t->handles[i];
             enum starpu_data_access_mode m = t->modes[i];
-            if (!h || (m & STARPU_SCRATCH) || (m & STARPU_REDUX)) continue;
+            if (!h || !h->seq_consistency || (m & STARPU_SCRATCH) || (m & STARPU_REDUX)) continue;
             if (m & STARPU_W) {
                 add_edge(h->last_writer, j);
                 for (int r = 0; r < h->nreaders; ++r) add_edge(h->readers[r], j);
@@ -260,10 +260,21 @@ int starpu_task_submit(struct starpu_task *t)
             struct tag_entry *p = tag_get(e->deps[d], 1);
             if (p->done) continue;
             if (p->job) add_edge(p->job, j);
-            else tag_add_waiter(p, j); /* its task is not submitted yet */
+            else {
+                tag_add_waiter(p, j); /* its task is not submitted yet */
+                j->tag_waits++;
+            }
         }
         e->job = j;
         e->done = 0;
+        /* tasks that waited for this tag before it had a task now depend on it */
+        for (int w = 0; w < e->nwaiters; ++w) {
+            struct rt_job *u = e->waiters[w];
+            add_edge(j, u);
+            u->ndeps--;
+            u->tag_waits--;
+        }
+        e->nwaiters = 0;
         j->tag = t->tag_id;
         j->has_tag = 1;
     }
@@ -300,6 +311,11 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
         if (t->handles[i]) rt_data_forget_job(t->handles[i], j);
     for (int s = 0; s < j->nsucc; ++s) {
         struct rt_job *u = j->succ[s];
+        for (int p = 0; p < u->nprev; ++p) /* keep predecessor lists free of finished jobs */
+            if (u->prev[p] == j) {
+                u->prev[p] = u->prev[--u->nprev];
+                --p;
+            }
         if (--u->ndeps == 0 && !rt.graph_mode) {
             u->task->status = STARPU_TASK_READY;
             rt_sched_push(u);
@@ -325,19 +341,82 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
     if (destroy) starpu_task_destroy(t);
 }
 
-/* Graph mode: hand every pending job to the CUDA driver as one graph. */
+/* Graph mode: hand the pending jobs to the CUDA driver as one graph, in a
+ * topological order of their edges (submission order where it is one).
+ * Jobs still waiting for a tag that has no task yet -- and every job that
+ * depends on them -- stay pending for a later flush. */
 void rt_flush_and_wait(void)
 {
-    if (rt.graph_mode) {
-        rt_lock();
-        struct rt_job **jobs = rt.pending;
-        int n = rt.npending;
-        rt.pending = NULL;
-        rt.npending = rt.cappending = 0;
+    if (!rt.graph_mode) return;
+    rt_lock();
+    int n = rt.npending;
+    if (!n) {
         rt_unlock();
-        if (n) rt_cuda_graph_flush(jobs, n);
-        free(jobs);
+        return;
     }
+    struct rt_job **pend = rt.pending;
+    /* mark: 1 = in this batch, 2 = deferred */
+    char *state = calloc(n, 1);
+    for (int k = 0; k < n; ++k) pend[k]->graph_slot = k;
+    for (int k = 0; k < n; ++k) {
+        struct rt_job *j = pend[k];
+        int defer = j->tag_waits > 0;
+        for (int p = 0; p < j->nprev && !defer; ++p) {
+            struct rt_job *q = j->prev[p];
+            if (!q->terminated && q->graph_slot >= 0 && q->graph_slot < n && pend[q->graph_slot] == q &&
+                state[q->graph_slot] == 2)
+                defer = 1;
+        }
+        state[k] = defer ? 2 : 1;
+    }
+    /* Kahn's algorithm over in-batch edges, smallest submission index first */
+    int *indeg = calloc(n, sizeof(int));
+    struct rt_job **batch = malloc(sizeof *batch * n);
+    struct rt_job **keep = malloc(sizeof *keep * n);
+    int nb = 0, nk = 0;
+    for (int k = 0; k < n; ++k) {
+        if (state[k] != 1) continue;
+        struct rt_job *j = pend[k];
+        for (int p = 0; p < j->nprev; ++p) {
+            struct rt_job *q = j->prev[p];
+            if (!q->terminated && q->graph_slot >= 0 && q->graph_slot < n && pend[q->graph_slot] == q &&
+                state[q->graph_slot] == 1)
+                indeg[k]++;
+        }
+    }
+    int *ready = malloc(sizeof(int) * n);
+    int nr = 0;
+    for (int k = 0; k < n; ++k)
+        if (state[k] == 1 && indeg[k] == 0) ready[nr++] = k;
+    while (nr > 0) {
+        /* pop the smallest index (ready is kept sorted by insertion below) */
+        int best = 0;
+        for (int i = 1; i < nr; ++i)
+            if (ready[i] < ready[best]) best = i;
+        int k = ready[best];
+        ready[best] = ready[--nr];
+        batch[nb++] = pend[k];
+        struct rt_job *j = pend[k];
+        for (int s = 0; s < j->nsucc; ++s) {
+            struct rt_job *u = j->succ[s];
+            int us = u->graph_slot;
+            if (us >= 0 && us < n && pend[us] == u && state[us] == 1 && --indeg[us] == 0) ready[nr++] = us;
+        }
+    }
+    for (int k = 0; k < n; ++k)
+        if (state[k] == 2) keep[nk++] = pend[k];
+    STARPU_ASSERT_MSG(nb + nk == n, "task graph has a cycle");
+    rt.pending = keep;
+    rt.npending = nk;
+    rt.cappending = n;
+    for (int k = 0; k < nk; ++k) keep[k]->graph_slot = k;
+    free(pend);
+    free(state);
+    free(indeg);
+    free(ready);
+    rt_unlock();
+    if (nb) rt_cuda_graph_flush(batch, nb);
+    free(batch);
 }
 
 int starpu_task_wait_for_all(void)

@@ -75,6 +75,34 @@ def test_unchanged_reference_driver_on_cpu_workers(args):
     assert m and int(m.group(1)) == int(args[1]) and float(m.group(3)) > 0, r.stdout
 
 
+def test_unchanged_tile_tag_driver_explicit_tag_dependencies():
+    """cholesky_tile_tag.c: tasks built with starpu_task_create, dependencies
+    only through starpu_tag_declare_deps (default sequential consistency off)."""
+    exe = _ref_driver("_ref/cholesky_tile_tag_cpu")
+    for ncpu in (1, 4):
+        r = subprocess.run([exe, "-size", "2048", "-nblocks", "8", "-check"], env=_env(STARPU_NCUDA=0, STARPU_NCPU=ncpu),
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert re.search(r"^2048\t\d+\t[\d.]+", r.stdout, re.M)
+
+
+def test_unchanged_tag_driver_entry_task_submitted_last():
+    """cholesky_tag.c submits POTRF(0) last: every other task waits for its tag
+    before that task exists.  Its own -check is not used: its GEMM task passes
+    the operands as (A_nk, A_mk) (examples/cholesky/cholesky_tag.h:145-146),
+    i.e. computes C_mn -= A_nk A_mk^T, and the reference's 1e-4 check fails on
+    a few elements by a hair for every worker count; the run itself must
+    complete and be identical for 1 and 4 workers."""
+    exe = _ref_driver("_ref/cholesky_tag_cpu")
+    outs = []
+    for ncpu in (1, 4):
+        r = subprocess.run([exe, "-size", "1024", "-nblocks", "8", "-check"], env=_env(STARPU_NCUDA=0, STARPU_NCPU=ncpu),
+                           capture_output=True, text=True, timeout=300)
+        m = re.search(r"Error\[(\d+), (\d+)\] --> ([\d.]+)", r.stderr)
+        outs.append(m.groups() if m else None)
+    assert outs[0] is not None and outs[0] == outs[1], outs
+
+
 def test_unchanged_reference_driver_links_gb300_codelets():
     exe = _ref_driver("_ref/cholesky_implicit_gb300")
     r = subprocess.run([exe, "-size", "256", "-nblocks", "2"], env=_env(STARPU_NCUDA=0, STARPU_NCPU=2),
