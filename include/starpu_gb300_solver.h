@@ -79,6 +79,29 @@ size_t starpu_gb300_backward_error_workspace(int n, int nrhs);
 int starpu_gb300_backward_error(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
                                 const double *B, int ldb, void *work, size_t lwork, double *berr_host);
 
+/* ---------------- batched: many independent systems, one persistent launch
+ * System i: order n[i] (1..1024), A_i FP64 column-major (ld n[i]) at
+ * A + a_off[i], B_i and X_i (n[i] x nrhs, ld n[i]) at B / X + b_off[i]
+ * (offsets in elements; n, a_off, b_off are HOST arrays).  Each system is
+ * factored in FP32 (blocked, block size from the tuning table) and refined in
+ * FP64 until its backward error <= tol or max_iter corrections.  nrhs <= 8.
+ * Synchronous: on return status[i] (host, may be NULL) holds the number of
+ * corrections (>= 0), -k if the FP32 factor met a non-positive pivot k, or
+ * -1000 if it did not converge; berr[i] (host, may be NULL) the final error. */
+size_t starpu_gb300_dposv_batched_workspace(int nsys, const int *n, int nrhs);
+int starpu_gb300_dposv_batched(void *stream, int nsys, const int *n, const double *A, const long long *a_off,
+                               const double *B, const long long *b_off, double *X, int nrhs, double tol,
+                               int max_iter, void *work, size_t lwork, int *status, double *berr);
+
+/* Autotuner of the batched solve: times every candidate block size (16, 32,
+ * 64) on a batch of each size bucket (n <= 32, 64, ..., 1024), keeps the
+ * fastest and stores the table next to the history perfmodels
+ * (<perfmodel dir>/codelets/45/gb300_chol_tuning.<hostname>); later calls in
+ * any process load it.  systems_per_bucket / reps <= 0 pick defaults. */
+int starpu_gb300_batched_autotune(int systems_per_bucket, int reps);
+/* Current block size per bucket (6 buckets); returns the bucket count. */
+int starpu_gb300_batched_get_tuning(signed char *nb_per_bucket, int nbuckets);
+
 /* Plain FP64 solve: dpotrf (tile nb) + dpotrs, A and B overwritten (LAPACK dposv). */
 int starpu_gb300_dposv(void *stream, int n, int nrhs, double *A, int lda, double *B, int ldb, int nb, int *d_info);
 
