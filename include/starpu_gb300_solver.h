@@ -102,6 +102,54 @@ int starpu_gb300_batched_autotune(int systems_per_bucket, int reps);
 /* Current block size per bucket (6 buckets); returns the bucket count. */
 int starpu_gb300_batched_get_tuning(signed char *nb_per_bucket, int nbuckets);
 
+/* ---------------- serving: a request loop with continuous batching --------
+ * A server owns `executors` worker threads, each with its own CUDA stream and
+ * buffers for systems up to max_n x max_n with max_nrhs right-hand sides.
+ * Submitted requests wait in an admission queue; whenever an executor is free
+ * it takes either every queued request with n <= 1024 (up to 512) as one
+ * batched persistent launch, or the oldest larger request, so requests that
+ * arrive while others run are admitted as executors and memory free up and
+ * their work overlaps on the device.  Factors of requests with a non-zero
+ * matrix_id stay on the device (FP64 A + FP32 factor, LRU) for later
+ * requests with the same id (repeat right-hand sides: no refactorisation).
+ * Device memory (executor buffers + cached factors) stays within
+ * hbm_budget_bytes; a request that cannot be cached is still served.
+ * mode 0: mixed precision + refinement (the path above); mode 1: the plain
+ * baseline -- every request alone, FP64 dposv, one at a time.
+ * A, B may be host or device pointers; X is written where it points. */
+typedef struct starpu_gb300_request {
+    int n, nrhs;
+    const double *A;        /* n x n, ld n (read only when the factor is not cached) */
+    const double *B;        /* n x nrhs, ld n */
+    double *X;              /* n x nrhs, ld n (output) */
+    uint64_t matrix_id;     /* 0: do not cache the factor */
+    double tol;             /* backward error target (<= 0: 1e-12) */
+    int max_iter;           /* refinement steps allowed (<= 0: 30) */
+    /* filled by the server */
+    int status;             /* 0 ok, GB300_EDOM, GB300_ETIMEDOUT, GB300_EINVAL, ... */
+    int iterations;
+    int cache_hit;          /* 1 when a cached factor was reused */
+    int batched;            /* 1 when served inside a batched launch */
+    double backward_error;
+    double submit_us, start_us, end_us;  /* starpu_timing_now() clock */
+    int done;
+    int reserved;
+} starpu_gb300_request;
+
+typedef struct starpu_gb300_server starpu_gb300_server;
+starpu_gb300_server *starpu_gb300_server_create(size_t hbm_budget_bytes, int executors, int max_n, int max_nrhs,
+                                                int mode);
+/* Queue a request (the struct must stay valid until it is done).  0 or GB300_EINVAL. */
+int starpu_gb300_server_submit(starpu_gb300_server *server, starpu_gb300_request *req);
+/* Block until req is done; returns req->status. */
+int starpu_gb300_server_wait(starpu_gb300_server *server, starpu_gb300_request *req);
+/* Block until every submitted request is done. */
+int starpu_gb300_server_drain(starpu_gb300_server *server);
+/* Counters: served, batched launches, cache hits, evictions, bytes in use (may be NULL). */
+int starpu_gb300_server_stats(starpu_gb300_server *server, unsigned long long *served, unsigned long long *batches,
+                              unsigned long long *cache_hits, unsigned long long *evictions, size_t *bytes_in_use);
+int starpu_gb300_server_destroy(starpu_gb300_server *server);
+
 /* Plain FP64 solve: dpotrf (tile nb) + dpotrs, A and B overwritten (LAPACK dposv). */
 int starpu_gb300_dposv(void *stream, int n, int nrhs, double *A, int lda, double *B, int ldb, int nb, int *d_info);
 

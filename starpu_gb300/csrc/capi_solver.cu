@@ -136,15 +136,18 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         off = align256(off + bytes);
         return o;
     };
+    // what the factor phase leaves behind comes first and does not depend on
+    // nrhs, so a kept factor can be refined later with any nrhs up to the
+    // workspace's capacity
     const size_t oW = take((size_t)n * n * sizeof(float));
     const size_t panel_bytes = starpu_gb300_spotrf_tc_workspace(n, nb);
     const size_t oP = take(panel_bytes);
+    const size_t oT = take(potrs_sweep_workspace<float>(n));
+    const size_t oS = take(4 * sizeof(unsigned long long));
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
-    const size_t oT = take(potrs_sweep_workspace<float>(n));
     const size_t oE = take((size_t)nrhs * sizeof(double));
     const size_t oD = take((size_t)nrhs * sizeof(int));
-    const size_t oS = take(4 * sizeof(unsigned long long));
     if (ws && base) {
         char *b = (char *)base;
         ws->W = (float *)(b + oW);
@@ -162,47 +165,22 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     return off;
 }
 
-} // namespace gb300
 
-using namespace gb300;
-
-extern "C" {
-
-size_t starpu_gb300_dsposv_workspace(int n, int nrhs, int nb)
+// Factor phase of the mixed solve: W = fp32(A) (lower) with ||A||_inf, the
+// tensor-core tiled Cholesky of W and the inverted diagonal blocks the POTRS
+// sweeps use.  Synchronises once to read the factorisation status.  The
+// workspace then holds everything a later refine phase needs, so a factor can
+// be kept on the device and reused for new right-hand sides.
+int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
+                  starpu_gb300_ir_info *out)
 {
-    if (n < 0 || nrhs < 0) return 0;
-    if (nb <= 0) nb = 1024;
-    return layout(n, nrhs, nb, nullptr, nullptr);
-}
-
-int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
-                        int ldx, int nb, int nterms, double tol, int max_iter, void *work, size_t lwork,
-                        starpu_gb300_ir_info *out)
-{
-    if (out) memset(out, 0, sizeof *out);
-    if (n < 0 || nrhs < 0 || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ldx < (n > 1 ? n : 1) ||
-        (nterms != 1 && nterms != 3) || max_iter < 0 || !(tol >= 0))
-        return GB300_EINVAL;
-    if (nb <= 0) nb = 1024;
-    if (!work || lwork < starpu_gb300_dsposv_workspace(n, nrhs, nb)) return GB300_EINVAL;
-    if (!n || !nrhs) return GB300_OK;
-    cudaStream_t s = (cudaStream_t)stream;
     SolverWs ws;
     layout(n, nrhs, nb, work, &ws);
-
-    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
-    cudaMemsetAsync(ws.done, 0, nrhs * sizeof(int), s);
     gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits);
     int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err);
     if (rc) return rc;
     potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
-    // initial solve in FP32
-    gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n);
-    int slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
-    potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
-    gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
-    gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 0, nullptr);
     int hinfo[2] = {0, 0};
     if ((rc = gb300_record_cuda_error(cudaMemcpyAsync(hinfo, ws.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))))
         return rc;
@@ -219,9 +197,27 @@ int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda,
         if (out) out->status = GB300_EDOM;
         return GB300_EDOM;
     }
+    return GB300_OK;
+}
+
+// Refine phase: x = L^-T L^-1 b in FP32, then FP64 refinement with the factor
+// left in the workspace by dsposv_factor (for the same A).
+int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                  int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out)
+{
+    SolverWs ws;
+    layout(n, nrhs, nb, work, &ws);
+    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
+    cudaMemsetAsync(ws.done, 0, nrhs * sizeof(int), s);
+    cudaMemsetAsync(ws.err, 0, sizeof(int), s);
+    gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n);
+    int slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
+    potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
+    gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
+    gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 0, nullptr);
     double *hberr = (double *)malloc(sizeof(double) * (size_t)nrhs);
     int status = GB300_ETIMEDOUT;
-    int it = 0;
+    int it = 0, rc = 0;
     double worst = INFINITY;
     for (;; ++it) {
         slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
@@ -253,12 +249,43 @@ int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda,
         out->backward_error = worst;
         out->status = status;
         unsigned long long ab = 0;
-        cudaMemcpy(&ab, ws.anorm_bits, sizeof ab, cudaMemcpyDeviceToHost);
+        cudaMemcpyAsync(&ab, ws.anorm_bits, sizeof ab, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
         double an;
         memcpy(&an, &ab, sizeof an);
         out->anorm = an;
     }
     return status;
+}
+
+} // namespace gb300
+
+using namespace gb300;
+
+extern "C" {
+
+size_t starpu_gb300_dsposv_workspace(int n, int nrhs, int nb)
+{
+    if (n < 0 || nrhs < 0) return 0;
+    if (nb <= 0) nb = 1024;
+    return layout(n, nrhs, nb, nullptr, nullptr);
+}
+
+int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                        int ldx, int nb, int nterms, double tol, int max_iter, void *work, size_t lwork,
+                        starpu_gb300_ir_info *out)
+{
+    if (out) memset(out, 0, sizeof *out);
+    if (n < 0 || nrhs < 0 || lda < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ldx < (n > 1 ? n : 1) ||
+        (nterms != 1 && nterms != 3) || max_iter < 0 || !(tol >= 0))
+        return GB300_EINVAL;
+    if (nb <= 0) nb = 1024;
+    if (!work || lwork < starpu_gb300_dsposv_workspace(n, nrhs, nb)) return GB300_EINVAL;
+    if (!n || !nrhs) return GB300_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = gb300::dsposv_factor(s, n, nrhs, A, lda, nb, nterms, work, out);
+    if (rc) return rc;
+    return gb300::dsposv_refine(s, n, nrhs, A, lda, B, ldb, X, ldx, nb, tol, max_iter, work, out);
 }
 
 // ---- persistent solver context: device buffers sized once, host-buffer calls

@@ -3,8 +3,15 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "starpu_gb300_kernels.h"
+#include "starpu_gb300_solver.h"
 
 namespace gb300 {
+
+// the two phases of starpu_gb300_dsposv (capi_solver.cu)
+int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
+                  starpu_gb300_ir_info *out);
+int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                  int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out);
 
 // Width of the register-blocked small triangular kernels and of the
 // unblocked diagonal POTRF leaf: 64 columns in FP32, 32 in FP64 (a 64-wide

@@ -118,6 +118,15 @@ class IrInfo(C.Structure):
                 ("backward_error", C.c_double), ("anorm", C.c_double)]
 
 
+class Request(C.Structure):
+    """ctypes mirror of starpu_gb300_request (include/starpu_gb300_solver.h)."""
+    _fields_ = [("n", C.c_int), ("nrhs", C.c_int), ("A", C.c_void_p), ("B", C.c_void_p), ("X", C.c_void_p),
+                ("matrix_id", C.c_uint64), ("tol", C.c_double), ("max_iter", C.c_int), ("status", C.c_int),
+                ("iterations", C.c_int), ("cache_hit", C.c_int), ("batched", C.c_int),
+                ("backward_error", C.c_double), ("submit_us", C.c_double), ("start_us", C.c_double),
+                ("end_us", C.c_double), ("done", C.c_int), ("reserved", C.c_int)]
+
+
 class Stream:
     """A non-blocking CUDA stream owned by the native library."""
 
