@@ -207,6 +207,136 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------- config 4: batched uneven systems
+def bench_batched(L, nsys=4096, nrhs=4, seed=2024):
+    """4096 independent SPD systems, n log-uniform in [32, 1024],
+    A = B B^T / n + I, 4 RHS: one persistent launch (FP32 factor + FP64
+    refinement per system)."""
+    import numpy as np
+    from starpu_gb300 import DeviceBuffer
+    from starpu_gb300.native import check
+    rng = np.random.default_rng(seed)
+    ns = np.clip(np.exp(rng.uniform(np.log(32), np.log(1024), nsys)).astype(np.int32), 32, 1024).astype(np.int32)
+    a_off = np.zeros(nsys, np.int64)
+    b_off = np.zeros(nsys, np.int64)
+    a_off[1:] = np.cumsum(ns.astype(np.int64) ** 2)[:-1]
+    b_off[1:] = np.cumsum(ns.astype(np.int64) * nrhs)[:-1]
+    atot, btot = int((ns.astype(np.int64) ** 2).sum()), int((ns.astype(np.int64) * nrhs).sum())
+    dA, dB, dX = DeviceBuffer(8 * atot), DeviceBuffer(8 * btot), DeviceBuffer(8 * btot)
+    wk = DeviceBuffer(8 * 1024 * 1024)
+    for i in range(nsys):
+        n = int(ns[i])
+        check(L.starpu_gb300_gen_spd_gram(None, n, 7000 + i, 1.0, dA.ptr + 8 * int(a_off[i]), n, wk.ptr))
+        check(L.starpu_gb300_gen_uniform_rhs(None, n, nrhs, 9000 + i, dB.ptr + 8 * int(b_off[i]), n))
+    check(L.starpu_gb300_stream_sync(None))
+    lw = L.starpu_gb300_dposv_batched_workspace(nsys, ns.ctypes.data, nrhs)
+    W = DeviceBuffer(lw)
+    st, be = np.zeros(nsys, np.int32), np.zeros(nsys)
+    flops = float((ns.astype(np.float64) ** 3 / 3 + 2 * ns.astype(np.float64) ** 2 * nrhs).sum())
+
+    def call():
+        check(L.starpu_gb300_dposv_batched(None, nsys, ns.ctypes.data, dA.ptr, a_off.ctypes.data, dB.ptr,
+                                           b_off.ctypes.data, dX.ptr, nrhs, 1e-12, 20, W.ptr, lw, st.ctypes.data,
+                                           be.ctypes.data))
+    call()
+    ts = []
+    for _ in range(3):
+        e0, e1 = L.starpu_gb300_event_create(), L.starpu_gb300_event_create()
+        check(L.starpu_gb300_event_record(e0, None))
+        call()
+        check(L.starpu_gb300_event_record(e1, None))
+        ts.append(L.starpu_gb300_event_elapsed_ms(e0, e1))
+    ms = min(ts)
+    tune = (C.c_byte * 6)()
+    L.starpu_gb300_batched_get_tuning(tune, 6)
+    return {"workload": f"{nsys} SPD systems, n log-uniform [32,1024], A=B*B^T/n+I, {nrhs} RHS, one persistent launch",
+            "ms": ms, "gflops": flops / (ms * 1e-3) / 1e9, "systems_per_s": nsys / (ms * 1e-3),
+            "max_backward_error": float(be.max()), "all_converged": bool((st >= 0).all()),
+            "corrections_max": int(st.max()), "tuning_nb_per_bucket": list(tune)}
+
+
+# --------------------------------------------------------- config 5: serving
+def bench_serving(L, nreq=160, seed=5, repeat_frac=0.3, executors=4):
+    """Poisson stream of solve requests: n log-uniform [64, 8192], 1-16 RHS,
+    kappa log-uniform [1e2, 1e6], 30 % repeat right-hand sides on a cached
+    device factor, 120 GB HBM budget.  Ours (continuous batching, executors
+    overlapping, factor cache, mixed precision) against per-request plain
+    launches (one at a time, FP64 dposv): throughput at saturation, then
+    p50 / p99 latency under the same Poisson arrival rate."""
+    import numpy as np
+    from starpu_gb300 import DeviceBuffer
+    from starpu_gb300.native import Request, check
+    rng = np.random.default_rng(seed)
+    ndistinct = int(nreq * (1 - repeat_frac)) + 1
+    sizes = np.clip(np.exp(rng.uniform(np.log(64), np.log(8192), ndistinct)).astype(int), 64, 8192)
+    kappas = np.exp(rng.uniform(np.log(1e2), np.log(1e6), ndistinct))
+    mats = []
+    wk = DeviceBuffer(8 * 8192 * 8192)
+    for i, (n, k) in enumerate(zip(sizes, kappas)):
+        d = DeviceBuffer(8 * int(n) * int(n))
+        check(L.starpu_gb300_gen_spd_gram(None, int(n), 100 + i, 4.0 / (k - 1.0), d.ptr, int(n), wk.ptr))
+        mats.append((int(n), d))
+    del wk
+    check(L.starpu_gb300_stream_sync(None))
+    # request trace: first use of every matrix, then repeats of earlier ones (30 %)
+    trace = []
+    seen = []
+    for q in range(nreq):
+        if seen and rng.random() < repeat_frac:
+            mi = int(rng.choice(seen))
+        else:
+            mi = len(seen) if len(seen) < ndistinct else int(rng.choice(seen))
+            if mi not in seen:
+                seen.append(mi)
+        nrhs = int(rng.integers(1, 17))
+        n = mats[mi][0]
+        B = np.asfortranarray(rng.uniform(-1, 1, (n, nrhs)))
+        trace.append((mi, nrhs, B))
+    flops_new = lambda n, r: n ** 3 / 3 + 2 * n * n * r  # noqa: E731
+
+    def run(mode, nexec, arrivals=None):
+        sv = L.starpu_gb300_server_create(120 * (1 << 30), nexec, 8192, 16, mode)
+        assert sv, L.starpu_gb300_last_error()
+        reqs, keep = [], []
+        t0 = time.perf_counter()
+        for q, (mi, nrhs, B) in enumerate(trace):
+            n, d = mats[mi]
+            X = np.zeros_like(B)
+            r = Request()
+            r.n, r.nrhs, r.A, r.B, r.X = n, nrhs, d.ptr, B.ctypes.data, X.ctypes.data
+            r.matrix_id = (mi + 1) if mode == 0 else 0
+            r.tol, r.max_iter = 1e-12, 40
+            if arrivals is not None:
+                delay = t0 + arrivals[q] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            check(L.starpu_gb300_server_submit(sv, C.byref(r)))
+            reqs.append(r)
+            keep.append(X)
+        L.starpu_gb300_server_drain(sv)
+        wall = time.perf_counter() - t0
+        st = [C.c_ulonglong() for _ in range(4)]
+        L.starpu_gb300_server_stats(sv, *[C.byref(x) for x in st], None)
+        L.starpu_gb300_server_destroy(sv)
+        lat = np.array([(r.end_us - r.submit_us) / 1e3 for r in reqs])
+        ok = all(r.status == 0 for r in reqs)
+        berr = max(r.backward_error for r in reqs) if mode == 0 else None
+        return {"solves_per_s": len(reqs) / wall, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "all_ok": ok, "max_backward_error": berr,
+                "batched_launches": st[1].value, "cache_hits": st[2].value}
+    ours_sat = run(0, executors)
+    plain_sat = run(1, 1)
+    rate = 0.7 * plain_sat["solves_per_s"]  # a load the plain baseline can sustain
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    ours_lat = run(0, executors, arrivals)
+    plain_lat = run(1, 1, arrivals)
+    return {"workload": f"{nreq} requests, n log-uniform [64,8192], 1-16 RHS, kappa log-uniform [1e2,1e6], "
+                        f"{int(repeat_frac * 100)}% repeat RHS, 120 GB budget, {executors} executors",
+            "saturation": {"ours": ours_sat, "plain_per_request": plain_sat,
+                           "speedup_solves_per_s": ours_sat["solves_per_s"] / plain_sat["solves_per_s"]},
+            "poisson_rate_per_s": rate, "at_rate": {"ours": ours_lat, "plain_per_request": plain_lat}}
+
+
 # ------------------------------------------------------------------ GPU path
 def run_ours(args):
     import numpy as np
@@ -393,6 +523,10 @@ def run_ours(args):
         L.starpu_gb300_host_free_pinned(hB)
         L.starpu_gb300_host_free_pinned(hX)
 
+    # ---- configs 4 and 5
+    batched = bench_batched(L) if not args.no_batched else None
+    serving = bench_serving(L) if not args.no_serving else None
+
     # ---- CPU baseline (rank 0, N=1 only): StarPU CPU path port on a bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -412,7 +546,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}", "generation_s": gen_s},
             "backward_error": max(berrs), "iterations": iters,
             "vs_fp64_plain_same_n": (value / world / fp64_same["gflops"]) if fp64_same else None,
-            "fp64_plain": fp64, "kappa_sweep": sweep,
+            "fp64_plain": fp64, "kappa_sweep": sweep, "batched": batched, "serving": serving,
             "roofline": roofline, "kernels": prof,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         }
@@ -443,6 +577,8 @@ def main():
     ap.add_argument("--no-fp64-same-n", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # timing rule: at least 3 untimed warm-up steps
     if args.impl == "reference":
