@@ -128,8 +128,10 @@ int starpu_gb300_tc_update(void *stream, int m, int n, int k, const void *a_hi, 
 size_t starpu_gb300_spotrf_tc_workspace(int n, int nb);
 
 /* Tiled Cholesky of an FP32 matrix (tile nb): FP32 POTRF of the diagonal
- * tile and FP32 panel TRSM, trailing update on the tensor cores with the
- * panel split to BF16 (nterms 1 or 3, as in starpu_gb300_tc_update). */
+ * tile (CUDA cores), its explicit inverse, the panel TRSM as one split-BF16
+ * tensor-core product P * L_kk^-T, and the trailing update on the tensor
+ * cores with the panel split to BF16 (nterms 1 or 3, as in
+ * starpu_gb300_tc_update). */
 int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int nterms, void *work, size_t lwork,
                            int *d_info, int *d_err);
 

@@ -8,6 +8,7 @@
 #include "starpu_gb300_kernels.h"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace gb300 {
 
@@ -68,6 +69,54 @@ void gemm(cudaStream_t s, bool ta, bool tb, bool lower, int m, int n, int k, T a
     else if (!ta && tb) simt_cfg<T>::template run<false, true>(s, lower, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     else if (ta && !tb) simt_cfg<T>::template run<true, false>(s, lower, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     else simt_cfg<T>::template run<true, true>(s, lower, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+// `batch` independent products C_z = alpha * A_z B_z + beta * C_z (no
+// transposes), A_z = A + z * astride and likewise for B and C: one launch.
+template <typename T>
+void gemm_batched_nn(cudaStream_t s, int m, int n, int k, T alpha, const T *A, long lda, long astride, const T *B,
+                     long ldb, long bstride, T beta, T *C, long ldc, long cstride, int batch)
+{
+    if (m <= 0 || n <= 0 || batch <= 0) return;
+    if constexpr (std::is_same<T, float>::value)
+        gb300_count_launch(), gemm_simt_kernel<T, false, false, 128, 128, 8, 8, 8, false>
+            <<<dim3(cdiv(m, 128), cdiv(n, 128), batch), 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, -1,
+                                                                    cstride, astride, bstride);
+    else
+        gb300_count_launch(), gemm_simt_kernel<T, false, false, 64, 64, 8, 4, 4, false>
+            <<<dim3(cdiv(m, 64), cdiv(n, 64), batch), 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, -1,
+                                                                  cstride, astride, bstride);
+}
+
+// Linv (n x n, ld ldi, strictly upper part zeroed) = inverse of the lower
+// triangle of L: the 64 x 64 diagonal blocks by forward substitution, then
+// doubling -- neighbouring inverted blocks of order h combine as
+//   [L11 0; L21 L22]^-1 = [I11 0; -I22 (L21 I11)  I22],
+// every pair of one level in one batched launch per product.  scratch holds
+// >= n * n / 4 elements.
+template <typename T>
+void trtri_lower(cudaStream_t s, int n, const T *L, long ldl, T *Linv, long ldi, T *scratch)
+{
+    if (n <= 0) return;
+    cudaMemset2DAsync(Linv, ldi * sizeof(T), 0, n * sizeof(T), n, s);
+    gb300_count_launch(), invert_diag_blocks_kernel<T, 64>
+        <<<cdiv(n, 64), 64, 0, s>>>(n, L, ldl, Linv, ldi, 64 * (ldi + 1), true);
+    for (int h = 64; h < n; h *= 2) {
+        const int full = n / (2 * h);  // pairs whose halves both have order h
+        const long sl = 2L * h * (ldl + 1), si = 2L * h * (ldi + 1);
+        if (full > 0) {
+            gemm_batched_nn<T>(s, h, h, h, T(1), L + h, ldl, sl, Linv, ldi, si, T(0), scratch, h, (long)h * h, full);
+            gemm_batched_nn<T>(s, h, h, h, T(-1), Linv + h + (long)h * ldi, ldi, si, scratch, h, (long)h * h, T(0),
+                               Linv + h, ldi, si, full);
+        }
+        const int o = full * 2 * h, r = n - o - h;  // a last pair whose second half has order r < h
+        if (r > 0) {
+            gemm<T>(s, false, false, false, r, h, h, T(1), L + (o + h) + (long)o * ldl, ldl, Linv + o + (long)o * ldi,
+                    ldi, T(0), scratch, r);
+            gemm<T>(s, false, false, false, r, h, r, T(-1), Linv + (o + h) + (long)(o + h) * ldi, ldi, scratch, r, T(0),
+                    Linv + (o + h) + (long)o * ldi, ldi);
+        }
+    }
 }
 
 // B[m x nc] <- B * L^{-T}, blocked by SMALL_W columns: small triangular solve
@@ -178,10 +227,10 @@ void potrs_sweep_prepare(cudaStream_t s, int n, const T *L, long ldl, void *ws)
 {
     if (n <= 0) return;
     const unsigned nblk = cdiv(n, 64);
-    gb300_count_launch(), invert_diag_blocks_kernel<T, 64><<<nblk, 64, 0, s>>>(n, L, ldl, (T *)ws);
+    gb300_count_launch(), invert_diag_blocks_kernel<T, 64><<<nblk, 64, 0, s>>>(n, L, ldl, (T *)ws, 64, 64 * 64, false);
 }
 
-// L y = b then L^T x = y, one launch per sweep and group of 16 columns.
+// L y = b then L^T x = y, one launch per sweep and group of 16 columns (FP32).
 template <typename T>
 void potrs_sweep(cudaStream_t s, int n, int nrhs, const T *L, long ldl, void *ws, T *B, long ldb, int *err)
 {
@@ -191,14 +240,21 @@ void potrs_sweep(cudaStream_t s, int n, int nrhs, const T *L, long ldl, void *ws
     int *flags = (int *)((char *)ws + (((size_t)nblk * 64 * 64 * sizeof(T) + 255) & ~(size_t)255));
     unsigned *ticket = (unsigned *)(flags + nblk);
     const unsigned long long budget = 2000000000ull;  // 2 s per wait: far above any legitimate stall
+    static_assert(std::is_same<T, float>::value, "the single-launch sweeps are FP32");
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(trsv_sweep_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SWEEP_SMEM);
+        cudaFuncSetAttribute(trsv_sweep_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SWEEP_SMEM);
+        attr_set = true;
+    }
     for (int c0 = 0; c0 < nrhs; c0 += 16) {
         const int nr = std::min(16, nrhs - c0);
         cudaMemsetAsync(flags, 0, (nblk + 1) * sizeof(int), s);
-        gb300_count_launch(), trsv_sweep_kernel<T, 64, false>
-            <<<nblk, 256, 0, s>>>(n, nr, L, ldl, Linv, B + (long)c0 * ldb, ldb, ticket, flags, err, budget);
+        gb300_count_launch(), trsv_sweep_kernel<false>
+            <<<nblk, 256, SWEEP_SMEM, s>>>(n, nr, L, ldl, Linv, B + (long)c0 * ldb, ldb, ticket, flags, err, budget);
         cudaMemsetAsync(flags, 0, (nblk + 1) * sizeof(int), s);
-        gb300_count_launch(), trsv_sweep_kernel<T, 64, true>
-            <<<nblk, 256, 0, s>>>(n, nr, L, ldl, Linv, B + (long)c0 * ldb, ldb, ticket, flags, err, budget);
+        gb300_count_launch(), trsv_sweep_kernel<true>
+            <<<nblk, 256, SWEEP_SMEM, s>>>(n, nr, L, ldl, Linv, B + (long)c0 * ldb, ldb, ticket, flags, err, budget);
     }
 }
 
@@ -207,7 +263,6 @@ template size_t potrs_sweep_workspace<double>(int);
 template void potrs_sweep_prepare<float>(cudaStream_t, int, const float *, long, void *);
 template void potrs_sweep_prepare<double>(cudaStream_t, int, const double *, long, void *);
 template void potrs_sweep<float>(cudaStream_t, int, int, const float *, long, void *, float *, long, int *);
-template void potrs_sweep<double>(cudaStream_t, int, int, const double *, long, void *, double *, long, int *);
 
 template void gemm<float>(cudaStream_t, bool, bool, bool, int, int, int, float, const float *, long, const float *,
                           long, float, float *, long);
@@ -216,6 +271,7 @@ template void gemm<double>(cudaStream_t, bool, bool, bool, int, int, int, double
 template void trsm_rltn<float>(cudaStream_t, int, int, const float *, long, float *, long);
 template void trsm_rltn<double>(cudaStream_t, int, int, const double *, long, double *, long);
 template void potrf_tiled<float>(cudaStream_t, int, float *, long, int, int *, int);
+template void trtri_lower<float>(cudaStream_t, int, const float *, long, float *, long, float *);
 template void potrf_tiled<double>(cudaStream_t, int, double *, long, int, int *, int);
 template void potrs_blocked<float>(cudaStream_t, int, int, const float *, long, float *, long);
 template void potrs_blocked<double>(cudaStream_t, int, int, const double *, long, double *, long);

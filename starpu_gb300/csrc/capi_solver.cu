@@ -16,6 +16,8 @@
 #include <string.h>
 
 #include "gb300_internal.h"
+#include "kernels/residual_df.cuh"
+#include "kernels/simt_blas.cuh"
 #include "starpu_gb300_kernels.h"
 #include "starpu_gb300_solver.h"
 
@@ -48,22 +50,46 @@ __global__ void convert_lower_norm_kernel(int n, const double *__restrict__ A, l
     }
 }
 
-// y (FP32, n x nrhs) = fp32(x) ; used for b and r
-__global__ void to_f32_kernel(int n, int nrhs, const double *__restrict__ x, long ldx, float *__restrict__ y, long ldy)
+// y (FP32, n x nrhs) = fp32(x_j * 2^-e_j); used for b and r.  The power-of-two
+// column scale (e_j = exponent of max |x_j|) keeps the FP32 solve away from
+// overflow and from underflow once the residual has become small.
+__global__ void to_f32_kernel(int n, int nrhs, const double *__restrict__ x, long ldx, float *__restrict__ y, long ldy,
+                              const int *__restrict__ exps)
 {
     const long j = blockIdx.y;
+    const int e = exps[j];
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        y[i + j * ldy] = (float)x[i + j * ldx];
+        y[i + j * ldy] = (float)scalbn(x[i + j * ldx], -e);
 }
 
-// x (FP64) = (accumulate ? x : 0) + fp64(y), skipping converged columns
+// x (FP64) = (accumulate ? x : 0) + fp64(y_j) * 2^e_j, skipping converged columns
 __global__ void accumulate_kernel(int n, int nrhs, const float *__restrict__ y, long ldy, double *__restrict__ x,
-                                  long ldx, int accumulate, const int *__restrict__ done)
+                                  long ldx, int accumulate, const int *__restrict__ done, const int *__restrict__ exps)
 {
     const long j = blockIdx.y;
     if (done && done[j]) return;
+    const int e = exps[j];
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        x[i + j * ldx] = (accumulate ? x[i + j * ldx] : 0.0) + (double)y[i + j * ldy];
+        x[i + j * ldx] = (accumulate ? x[i + j * ldx] : 0.0) + scalbn((double)y[i + j * ldy], e);
+}
+
+// exponent of the largest magnitude of v (0 for zero or non-finite), as FP32 column scales use
+__device__ __forceinline__ int column_exp(double v) { return (v > 0.0 && isfinite(v)) ? ilogb(v) : 0; }
+
+// e_j = exponent of max_i |M_ij| (one CTA per column)
+__global__ void colmax_exp_kernel(int n, const double *__restrict__ M, long ldm, int *__restrict__ exps)
+{
+    const long j = blockIdx.x;
+    double m = 0.0;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(M[i + j * ldm]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+        exps[j] = column_exp(m);
+    }
 }
 
 // R = B (copy) before the GEMM R -= A X
@@ -74,11 +100,88 @@ __global__ void copy_f64_kernel(int n, const double *__restrict__ B, long ldb, d
         R[i + j * ldr] = B[i + j * ldb];
 }
 
+// R = B + sum_z P_z, the K-split partials of -A X, added in a fixed order
+__global__ void residual_reduce_kernel(int n, int nrhs, int nk, const double *__restrict__ B, long ldb,
+                                       const double *__restrict__ P, double *__restrict__ R, long ldr)
+{
+    const long j = blockIdx.y;
+    const long stride = (long)n * nrhs;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double v = B[i + j * ldb];
+        for (int z = 0; z < nk; ++z) v += P[z * stride + i + j * (long)n];
+        R[i + j * ldr] = v;
+    }
+}
+
+// K chunks of the residual so that the grid holds enough equal CTAs for the
+// hardware scheduler to balance 152 SMs (a few hundred CTAs of equal size
+// leave some SMs one CTA behind the others).
+static int residual_nk(int n, int nrhs)
+{
+    const long tiles = (long)((n + 63) / 64) * ((nrhs + 15) / 16);
+    long nk = (8192 + tiles - 1) / tiles;
+    if (nk > 32) nk = 32;
+    if (nk < 1) nk = 1;
+    while (nk > 1 && (long)n / nk < 64) --nk;
+    return (int)nk;
+}
+
+// R = B - A X in FP64 (A n x n, X / B / R n x nrhs), deterministic split-K
+static void residual_f64(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx,
+                         const double *B, long ldb, double *R, long ldr, double *partials)
+{
+    const int nk = residual_nk(n, nrhs);
+    const int kchunk = ((n + nk - 1) / nk + 7) / 8 * 8;
+    dim3 grid((n + 63) / 64, (nrhs + 15) / 16, nk);
+    gb300_count_launch(), gemm_simt_kernel<double, false, false, 64, 16, 8, 4, 2, false>
+        <<<grid, 128, 0, s>>>(n, nrhs, n, -1.0, A, lda, X, ldx, 0.0, partials, n, kchunk, (long)n * nrhs);
+    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
+    gb300_count_launch(), residual_reduce_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, nk, B, ldb, partials, R, ldr);
+}
+
+// K chunk of the double-float residual: a multiple of the flush length, with
+// enough chunks for ~16 CTAs per SM over the row blocks
+static int residual_df_kchunk(int n, int nrhs)
+{
+    const long tiles = (long)((n + RDF_BM - 1) / RDF_BM) * ((nrhs + 15) / 16);
+    long nk = (16 * 152 + tiles - 1) / tiles;
+    nk = std::max(1L, std::min(32L, nk));
+    const long step = (long)RDF_BK * RDF_FLUSH;
+    long kc = ((n + nk - 1) / nk + step - 1) / step * step;
+    return (int)std::max(kc, step);
+}
+
+// FP64 partials the residual needs, either form
+static size_t residual_partials(int n, int nrhs)
+{
+    const int kc = residual_df_kchunk(n, nrhs);
+    const long nz = std::max(1, (n + kc - 1) / kc);
+    return (size_t)std::max<long>(residual_nk(n, nrhs), nz) * n * nrhs;
+}
+
+// R = B - A X with the double-float product on the FP32 pipe (~2^-47 relative
+// per 128-term block, partials reduced in FP64 in a fixed order).  anorm_bits:
+// an upper bound of max |A_ij| (||A||_inf) as FP64 bits.  xs: n x 16 * groups
+// float2, sx: nrhs ints.
+static void residual_df(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx,
+                        const double *B, long ldb, double *R, long ldr, double *partials, float2 *xs, int *sx,
+                        const unsigned long long *anorm_bits)
+{
+    const int kc = residual_df_kchunk(n, nrhs);
+    const int nz = (n + kc - 1) / kc;
+    gb300_count_launch(), df_split_x_kernel<<<nrhs, 256, 0, s>>>(n, X, ldx, xs, sx);
+    dim3 grid((n + RDF_BM - 1) / RDF_BM, (nrhs + 15) / 16, nz);
+    gb300_count_launch(), residual_df_kernel<<<grid, 256, 0, s>>>(n, nrhs, A, lda, xs, sx, anorm_bits, kc, partials);
+    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
+    gb300_count_launch(), residual_reduce_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, nz, B, ldb, partials, R, ldr);
+}
+
 // Per right-hand side j (one CTA): berr_j = ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf);
 // done_j = berr_j <= tol.
 __global__ void backward_error_kernel(int n, const double *__restrict__ R, long ldr, const double *__restrict__ X,
                                       long ldx, const double *__restrict__ B, long ldb,
-                                      const unsigned long long *anorm_bits, double tol, double *berr, int *done)
+                                      const unsigned long long *anorm_bits, double tol, double *berr, int *done,
+                                      int *rexp)
 {
     const long j = blockIdx.x;
     double rm = 0, xm = 0, bm = 0;
@@ -110,6 +213,7 @@ __global__ void backward_error_kernel(int n, const double *__restrict__ R, long 
         const double e = den > 0 ? rm / den : (rm > 0 ? INFINITY : 0.0);
         berr[j] = e;
         done[j] = (e <= tol) ? 1 : 0;
+        if (rexp) rexp[j] = column_exp(rm);  // scale of the next FP32 correction solve
     }
 }
 
@@ -119,8 +223,12 @@ struct SolverWs {
     double *R;             // n x nrhs FP64 residual
     float *Y;              // n x nrhs FP32 right-hand side / correction
     void *sweep;           // inverted diagonal blocks + flags of the POTRS sweeps
+    double *partials;      // K-split partials of the residual
+    float2 *xs;            // double-float split of X (n x 16 per group of 16 columns)
+    int *sx;               // per-column scale exponents of X
     double *berr;          // nrhs
     int *done;             // nrhs
+    int *rexp;             // nrhs: power-of-two scales of the FP32 right-hand sides
     unsigned long long *anorm_bits;
     int *info, *err;
     size_t panel_bytes;
@@ -148,6 +256,10 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
     const size_t oE = take((size_t)nrhs * sizeof(double));
     const size_t oD = take((size_t)nrhs * sizeof(int));
+    const size_t oQ = take(residual_partials(n, nrhs) * sizeof(double));
+    const size_t oX = take((size_t)n * 16 * ((nrhs + 15) / 16) * sizeof(float2));
+    const size_t oI = take((size_t)nrhs * sizeof(int));
+    const size_t oJ = take((size_t)nrhs * sizeof(int));
     if (ws && base) {
         char *b = (char *)base;
         ws->W = (float *)(b + oW);
@@ -156,6 +268,10 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->R = (double *)(b + oR);
         ws->Y = (float *)(b + oY);
         ws->sweep = b + oT;
+        ws->partials = (double *)(b + oQ);
+        ws->xs = (float2 *)(b + oX);
+        ws->sx = (int *)(b + oI);
+        ws->rexp = (int *)(b + oJ);
         ws->berr = (double *)(b + oE);
         ws->done = (int *)(b + oD);
         ws->anorm_bits = (unsigned long long *)(b + oS);
@@ -165,6 +281,16 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     return off;
 }
 
+
+static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws)
+{
+    cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
+    gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits);
+    int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err);
+    if (rc) return rc;
+    potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
+    return gb300_last_launch_status();
+}
 
 // Factor phase of the mixed solve: W = fp32(A) (lower) with ||A||_inf, the
 // tensor-core tiled Cholesky of W and the inverted diagonal blocks the POTRS
@@ -176,15 +302,11 @@ int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int
 {
     SolverWs ws;
     layout(n, nrhs, nb, work, &ws);
-    cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
-    gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits);
-    int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err);
-    if (rc) return rc;
-    potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
+    int rc = factor_phase(s, n, nb, nterms, A, lda, ws);
     int hinfo[2] = {0, 0};
-    if ((rc = gb300_record_cuda_error(cudaMemcpyAsync(hinfo, ws.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s))))
-        return rc;
-    if ((rc = gb300_record_cuda_error(cudaStreamSynchronize(s)))) return rc;
+    if (!rc) rc = gb300_record_cuda_error(cudaMemcpyAsync(hinfo, ws.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (!rc) rc = gb300_record_cuda_error(cudaStreamSynchronize(s));
+    if (rc) return rc;
     if (out) {
         out->potrf_info = hinfo[0];
         out->factor_terms = nterms;
@@ -210,21 +332,23 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
     const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
     cudaMemsetAsync(ws.done, 0, nrhs * sizeof(int), s);
     cudaMemsetAsync(ws.err, 0, sizeof(int), s);
-    gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n);
+    gb300_count_launch(), colmax_exp_kernel<<<nrhs, 256, 0, s>>>(n, B, ldb, ws.rexp);
+    gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n, ws.rexp);
     int slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
     potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
     gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
-    gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 0, nullptr);
+    gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 0, nullptr,
+                                                                           ws.rexp);
     double *hberr = (double *)malloc(sizeof(double) * (size_t)nrhs);
     int status = GB300_ETIMEDOUT;
     int it = 0, rc = 0;
     double worst = INFINITY;
     for (;; ++it) {
         slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
-        gb300_count_launch(), copy_f64_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, B, ldb, ws.R, n);
-        gemm<double>(s, false, false, false, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, ws.R, n);
+        residual_df(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx, ws.anorm_bits);
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
-        gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb, ws.anorm_bits, tol, ws.berr, ws.done);
+        gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb, ws.anorm_bits, tol, ws.berr, ws.done,
+                                                                     ws.rexp);
         if ((rc = gb300_record_cuda_error(
                  cudaMemcpyAsync(hberr, ws.berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s))))
             break;
@@ -236,11 +360,12 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
             break;
         }
         if (it >= max_iter) break;
-        gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.R, n, ws.Y, n);
+        gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.R, n, ws.Y, n, ws.rexp);
         slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
         potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
-        gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 1, ws.done);
+        gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 1, ws.done,
+                                                                               ws.rexp);
     }
     free(hberr);
     if (rc) return rc;
@@ -370,7 +495,7 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
 size_t starpu_gb300_backward_error_workspace(int n, int nrhs)
 {
     return align256((size_t)n * nrhs * sizeof(double)) + align256((size_t)nrhs * (sizeof(double) + sizeof(int))) +
-           256;
+           256 + align256(residual_partials(n, nrhs) * sizeof(double));
 }
 
 int starpu_gb300_backward_error(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
@@ -387,12 +512,11 @@ int starpu_gb300_backward_error(void *stream, int n, int nrhs, const double *A, 
     int *done = (int *)(berr + nrhs);
     w += align256((size_t)nrhs * (sizeof(double) + sizeof(int)));
     unsigned long long *an = (unsigned long long *)w;
-    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
+    double *partials = (double *)(w + 256);
     cudaMemsetAsync(an, 0, sizeof *an, s);
     gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, nullptr, 0, an);
-    gb300_count_launch(), copy_f64_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, B, ldb, R, n);
-    gemm<double>(s, false, false, false, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, n);
-    gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, R, n, X, ldx, B, ldb, an, 0.0, berr, done);
+    residual_f64(s, n, nrhs, A, lda, X, ldx, B, ldb, R, n, partials);
+    gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, R, n, X, ldx, B, ldb, an, 0.0, berr, done, nullptr);
     int rc = gb300_record_cuda_error(cudaMemcpyAsync(berr_host, berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
     if (rc) return rc;
     return gb300_record_cuda_error(cudaStreamSynchronize(s));

@@ -95,7 +95,7 @@ int split_bf16(cudaStream_t s, int m, int k, const float *P, long ldp, void *hi,
 }
 
 int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void *a_lo, long lda, const void *b_hi,
-              const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err)
+              const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0)
 {
     if (m <= 0 || n <= 0 || K <= 0) return GB300_OK;
     if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!a_lo || !b_lo)) || (lower && m != n) || !d_err)
@@ -119,6 +119,7 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
     a.K = K;
     a.nterms = nterms;
     a.lower = lower;
+    a.store = store;
     a.tiles_m = (m + TCU_BM - 1) / TCU_BM;
     a.tiles_n = (n + TCU_BN - 1) / TCU_BN;
     if (lower) {
@@ -140,15 +141,41 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
     return gb300_last_launch_status();
 }
 
-// Tiled right-looking Cholesky of an FP32 matrix whose trailing updates run on
-// the tensor cores (split-BF16 when nterms == 3).  POTRF of the diagonal tile
-// and the panel TRSM stay in FP32 SIMT.  `panel` holds 2 * n * ldk BF16
-// (hi and lo halves), ldk = nb rounded up to 64.
-int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err)
+// Workspace of potrf_tc for order n and tile nb (ldk = nb rounded up to 64):
+// the split panel (hi, lo: n x ldk BF16 each), the inverse of the diagonal
+// tile (ldk x ldk FP32) and its split (hi, lo), and the doubling scratch of
+// the triangular inverse (ldk * ldk / 4 FP32).
+struct TcWs {
+    __nv_bfloat16 *hi, *lo, *ihi, *ilo;
+    float *linv, *scratch;
+};
+static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
+{
+    const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64;
+    const size_t panel = (size_t)n * ldk * 2, inv = ldk * ldk;
+    if (w && base) {
+        char *b = (char *)base;
+        w->hi = (__nv_bfloat16 *)b;
+        w->lo = w->hi + (size_t)n * ldk;
+        w->linv = (float *)(b + 2 * panel);
+        w->ihi = (__nv_bfloat16 *)(w->linv + inv);
+        w->ilo = w->ihi + inv;
+        w->scratch = (float *)(w->ilo + inv);
+    }
+    return 2 * panel + inv * 4 + 2 * inv * 2 + inv;  // scratch: inv / 4 floats
+}
+
+// Tiled right-looking Cholesky of an FP32 matrix on the tensor cores
+// (split-BF16 products when nterms == 3).  Step k: FP32 POTRF of the
+// diagonal tile (SIMT), its inverse (64 x 64 blocks + batched doubling), the
+// panel TRSM  P <- P L_kk^-T  as one split-BF16 product P * Linv^T (store
+// form, always 3 products), then the trailing update  A22 -= P P^T  (lower).
+int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err)
 {
     const long ldk = ((long)nb + 63) / 64 * 64;
-    __nv_bfloat16 *hi = (__nv_bfloat16 *)panel;
-    __nv_bfloat16 *lo = hi + (long)n * ldk;
+    TcWs w;
+    tc_ws_layout(n, nb, work, &w);
+    const int np = nterms == 3 ? 2 : 1;
     for (int k0 = 0; k0 < n; k0 += nb) {
         const int kb = std::min(nb, n - k0);
         float *Akk = A + k0 + (long)k0 * lda;
@@ -160,18 +187,23 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
             break;
         }
         float *P = A + (k0 + kb) + (long)k0 * lda;
-        trsm_rltn<float>(s, m, kb, Akk, lda, P, lda);
-        int rc = split_bf16(s, m, kb, P, lda, hi, nterms == 3 ? lo : nullptr, ldk);
+        trtri_lower<float>(s, kb, Akk, lda, w.linv, ldk, w.scratch);
+        int rc = split_bf16(s, kb, kb, w.linv, ldk, w.ihi, w.ilo, ldk);
+        if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, w.lo, ldk);
+        if (!rc) rc = tc_update(s, m, kb, kb, w.hi, w.lo, ldk, w.ihi, w.ilo, ldk, 3, 0, P, lda, d_err, 1);
+        if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, np > 1 ? w.lo : nullptr, ldk);
+        // algorithmic work of the panel: POTRF kb^3/3 + TRSM m kb^2; bytes: the
+        // tile and the panel read and written once, the BF16 panel written
         gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0 + (double)m * kb * kb,
-                       4.0 * kb * kb + 8.0 * m * kb + 2.0 * m * ldk * (nterms == 3 ? 2 : 1));
+                       8.0 * kb * kb + 8.0 * m * kb + 2.0 * m * ldk * np);
         if (rc) return rc;
         slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
-        rc = tc_update(s, m, m, kb, hi, lo, ldk, hi, lo, ldk, nterms, 1, A + (k0 + kb) + (long)(k0 + kb) * lda, lda,
-                       d_err);
+        rc = tc_update(s, m, m, kb, w.hi, w.lo, ldk, w.hi, w.lo, ldk, nterms, 1, A + (k0 + kb) + (long)(k0 + kb) * lda,
+                       lda, d_err);
         // algorithmic work: the lower triangle (incl. diagonal) of an m x m rank-kb update per term;
         // bytes: C lower read + write in FP32 plus one read of each BF16 panel
         gb300_prof_end(s, slot, (double)nterms * kb * (double)m * (m + 1.0),
-                       8.0 * m * (m + 1.0) / 2.0 + 2.0 * m * ldk * (nterms == 3 ? 2 : 1));
+                       8.0 * m * (m + 1.0) / 2.0 + 2.0 * m * ldk * np);
         if (rc) return rc;
     }
     return gb300_last_launch_status();
@@ -197,11 +229,7 @@ int starpu_gb300_tc_update(void *stream, int m, int n, int k, const void *a_hi, 
     return tc_update((cudaStream_t)stream, m, n, k, a_hi, a_lo, lda, b_hi, b_lo, ldb, nterms, lower, C, ldc, d_err);
 }
 
-size_t starpu_gb300_spotrf_tc_workspace(int n, int nb)
-{
-    const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64;
-    return 2 * (size_t)n * ldk * 2;
-}
+size_t starpu_gb300_spotrf_tc_workspace(int n, int nb) { return tc_ws_layout(n < 0 ? 0 : n, nb, nullptr, nullptr); }
 
 int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int nterms, void *work, size_t lwork,
                            int *d_info, int *d_err)

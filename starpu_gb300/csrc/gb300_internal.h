@@ -24,6 +24,8 @@ void gemm(cudaStream_t s, bool ta, bool tb, bool lower, int m, int n, int k, T a
           const T *B, long ldb, T beta, T *C, long ldc);
 template <typename T> void trsm_rltn(cudaStream_t s, int m, int nc, const T *L, long ldl, T *B, long ldb);
 template <typename T> void potrf_tiled(cudaStream_t s, int n, T *A, long lda, int nb, int *info, int info_base);
+// Linv = inverse of the lower triangle of L (n x n, ld ldi, upper part zeroed); scratch >= n*n/4 elements
+template <typename T> void trtri_lower(cudaStream_t s, int n, const T *L, long ldl, T *Linv, long ldi, T *scratch);
 template <typename T> void potrs_blocked(cudaStream_t s, int n, int nrhs, const T *L, long ldl, T *B, long ldb);
 // single-launch sweeps: workspace = inverted 64x64 diagonal blocks + flags
 template <typename T> size_t potrs_sweep_workspace(int n);

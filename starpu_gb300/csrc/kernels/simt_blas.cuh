@@ -31,11 +31,29 @@ template <typename T> struct vec2_of;
 template <> struct vec2_of<float> { typedef float2 type; };
 template <> struct vec2_of<double> { typedef double2 type; };
 
+// K split (kchunk > 0): blockIdx.z takes the K range [z*kchunk, (z+1)*kchunk)
+// and writes its partial product to C + z*cstride (beta applies to each
+// partial); a separate pass reduces the partials in a fixed order, so the
+// result does not depend on scheduling.
+// Batch (kchunk < 0): blockIdx.z is the problem index; its A, B and C start
+// at A + z*astride, B + z*bstride, C + z*cstride.
 template <typename T, bool TA, bool TB, int BM, int BN, int BK, int TM, int TN, bool LOWER>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 gemm_simt_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, long lda,
-                 const T *__restrict__ B, long ldb, T beta, T *__restrict__ C, long ldc)
+                 const T *__restrict__ B, long ldb, T beta, T *__restrict__ C, long ldc, int kchunk = 0,
+                 long cstride = 0, long astride = 0, long bstride = 0)
 {
+    if (kchunk > 0) {
+        const int kz = blockIdx.z * kchunk;
+        k = min(kchunk, k - kz);
+        A += TA ? (long)kz : (long)kz * lda;
+        B += TB ? (long)kz * ldb : (long)kz;
+        C += (long)blockIdx.z * cstride;
+    } else if (kchunk < 0) {
+        A += (long)blockIdx.z * astride;
+        B += (long)blockIdx.z * bstride;
+        C += (long)blockIdx.z * cstride;
+    }
     constexpr int RG = BM / TM;            // row groups
     constexpr int CG = BN / TN;            // column groups
     constexpr int NT = RG * CG;
@@ -164,8 +182,8 @@ gemm_simt_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, long lda
 }
 
 // ---------------------------------------------------------------------------
-// Unblocked Cholesky of one n x n (n <= 64) diagonal block, lower, in shared
-// memory.  Same arithmetic as the reference CPU codelet loop
+// Unblocked Cholesky of one n x n (n <= NMAX) diagonal block, lower, held in
+// registers.  Same arithmetic as the reference CPU codelet loop
 // (examples/cholesky/cholesky_kernels.c:329-342): lambda = sqrt(a_zz),
 // scale the column by 1/lambda, rank-1 update of the trailing lower part.
 // A non-positive (or NaN) pivot records info = info_base + z + 1 (LAPACK
@@ -174,40 +192,49 @@ gemm_simt_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, long lda
 template <typename T, int NMAX>
 __global__ void __launch_bounds__(256) potf2_small_kernel(int n, T *__restrict__ A, long lda, int *info, int info_base)
 {
-    __shared__ T a[NMAX][NMAX + 1];
-    __shared__ int bad;
+    // 256 threads as NMAX rows x CL column lanes; thread (ti, tc) keeps row ti,
+    // columns tc, tc + CL, ... in registers.  The step loop is unrolled so
+    // that column z lives in a fixed register of its owners; the owners
+    // publish column z through a double-buffered shared vector (one barrier
+    // per step), every thread scales its two factors by 1/sqrt(a_zz) itself.
+    constexpr int CL = 256 / NMAX, NC = NMAX / CL;
+    __shared__ T col[2][NMAX];
     const int tid = threadIdx.x;
-    for (int idx = tid; idx < n * n; idx += blockDim.x) {
-        int i = idx % n, j = idx / n;
-        a[i][j] = (i >= j) ? A[(long)i + (long)j * lda] : T(0);
-    }
-    if (tid == 0) bad = 0;
-    __syncthreads();
-    // 256 threads as 64 rows x 4 column lanes: no integer division in the loop
     const int ti = tid % NMAX, tc = tid / NMAX;
-    constexpr int CL = 256 / NMAX;
-    for (int z = 0; z < n; ++z) {
-        if (tid == 0) {
-            T d = a[z][z];
-            if (!(d > T(0))) {
-                if (!bad && info) atomicCAS(info, 0, info_base + z + 1);
-                bad = 1;
-            }
-            a[z][z] = sqrt(d);
-        }
-        __syncthreads();
-        const T inv = T(1) / a[z][z];
-        if (tc == 0 && ti > z && ti < n) a[ti][z] *= inv;
-        __syncthreads();
-        if (ti > z && ti < n) {
-            const T liz = a[ti][z];
-            for (int c = z + 1 + tc; c <= ti; c += CL) a[ti][c] = fma(-liz, a[c][z], a[ti][c]);
-        }
-        __syncthreads();
+    T a[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+        const int c = tc + q * CL;
+        a[q] = (ti < n && c <= ti) ? A[(long)ti + (long)c * lda] : T(0);
     }
-    for (int idx = tid; idx < n * n; idx += blockDim.x) {
-        int i = idx % n, j = idx / n;
-        if (i >= j) A[(long)i + (long)j * lda] = a[i][j];
+    bool bad = false;
+#pragma unroll
+    for (int z = 0; z < NMAX; ++z) {
+        if (z >= n) break;
+        T *cz = col[z & 1];
+        if (tc == z % CL) cz[ti] = a[z / CL];  // owners of column z publish it (rows < z hold 0)
+        __syncthreads();
+        const T d = cz[z];
+        if (!(d > T(0)) && !bad) {
+            bad = true;
+            if (tid == 0 && info) atomicCAS(info, 0, info_base + z + 1);
+        }
+        const T lzz = sqrt(d);
+        const T inv = T(1) / lzz;
+        const T li = cz[ti] * inv;
+        if (tc == z % CL) a[z / CL] = (ti == z) ? lzz : (ti > z ? li : a[z / CL]);
+        if (ti > z) {
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                const int c = tc + q * CL;
+                if (c > z && c <= ti) a[q] = fma(-li, cz[c] * inv, a[q]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+        const int c = tc + q * CL;
+        if (ti < n && c <= ti) A[(long)ti + (long)c * lda] = a[q];
     }
 }
 

@@ -52,6 +52,7 @@ struct TcUpdateArgs {
     int K;             // elements per term (panel width)
     int nterms;        // 1 or 3
     int lower;         // 1: only elements with row >= col (square trailing matrix)
+    int store;         // 1: C = sum (C is not read), 0: C -= sum
     int tiles_m, tiles_n, num_tiles;
     int *err;
     unsigned long long wait_budget_ns;
@@ -272,13 +273,15 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                     for (int j = 0; j < 32; ++j) {
                         const int col = c0 + j;
                         const bool w = col < args.n && (!args.lower || row >= col);
-                        cv[j] = w ? crow[(long)col * args.ldc] : 0.0f;
+                        cv[j] = (w && !args.store) ? crow[(long)col * args.ldc] : 0.0f;
                     }
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const int col = c0 + j;
                         const bool w = col < args.n && (!args.lower || row >= col);
-                        if (w) crow[(long)col * args.ldc] = cv[j] - __uint_as_float(r[j]);
+                        if (w)
+                            crow[(long)col * args.ldc] =
+                                args.store ? __uint_as_float(r[j]) : cv[j] - __uint_as_float(r[j]);
                     }
                 }
             }

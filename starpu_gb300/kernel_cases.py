@@ -3,6 +3,8 @@
     python -m starpu_gb300.kernel_cases tc_update --m 8192 --k 1024 --nterms 3 --reps 3
     python -m starpu_gb300.kernel_cases residual  --n 16384 --nrhs 16 --reps 3
     python -m starpu_gb300.kernel_cases potrs     --n 16384 --nrhs 16 --reps 3
+    python -m starpu_gb300.kernel_cases sweep     --n 16384 --nrhs 16 --reps 3
+    python -m starpu_gb300.kernel_cases dsposv    --n 8192  --nb 1024 --nrhs 16 --reps 2
     python -m starpu_gb300.kernel_cases spotrf_tc --n 8192  --nb 1024 --nterms 3 --reps 2
     python -m starpu_gb300.kernel_cases dpotrf    --n 8192  --nb 512 --reps 2
 
@@ -37,7 +39,8 @@ def _timed(L, fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["tc_update", "residual", "potrs", "spotrf_tc", "dpotrf"])
+    ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv"])
+    ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--k", type=int, default=1024)
@@ -62,7 +65,7 @@ def main(argv=None):
                                                                a.nterms, 1, Cb.ptr, m, err.ptr)), a.reps)
         fl = a.nterms * k * m * (m + 1.0)
         out.update(ms=ms, tflops=fl / ms / 1e9, algorithmic_bytes=8.0 * m * (m + 1) / 2 + 2.0 * m * ldk * 2)
-    elif a.case in ("residual", "potrs"):
+    elif a.case in ("residual", "potrs", "sweep"):
         n, nrhs = a.n, a.nrhs
         A = DeviceBuffer(8 * n * n)
         W = DeviceBuffer(8 * n * n)
@@ -85,7 +88,15 @@ def main(argv=None):
             Lh[np.diag_indices(n)] += n
             F = DeviceBuffer.from_array(Lh)
             Y = DeviceBuffer.from_array(np.ones((n, nrhs), np.float32))
-            ms = _timed(L, lambda: check(L.starpu_gb300_spotrs(None, n, nrhs, F.ptr, n, Y.ptr, n)), a.reps)
+            if a.case == "potrs":
+                ms = _timed(L, lambda: check(L.starpu_gb300_spotrs(None, n, nrhs, F.ptr, n, Y.ptr, n)), a.reps)
+            else:
+                lw = L.starpu_gb300_spotrs_sweep_workspace(n)
+                SW = DeviceBuffer(lw)
+                err = DeviceBuffer.from_array(np.zeros(1, np.int32))
+                ms = _timed(L, lambda: check(L.starpu_gb300_spotrs_sweep(None, n, nrhs, F.ptr, n, Y.ptr, n, SW.ptr, lw,
+                                                                          err.ptr)), a.reps)
+            # both sweeps read the lower triangle of L once: 2 * 4 * n^2 / 2 bytes
             out.update(ms=ms, gbs=4.0 * n * n / ms / 1e6)
     elif a.case == "spotrf_tc":
         n, nb = a.n, a.nb
@@ -115,6 +126,21 @@ def main(argv=None):
             check(L.starpu_gb300_dpotrf(None, n, W.ptr, n, nb, info.ptr))
         ms = _timed(L, run, a.reps)
         out.update(ms=ms, gflops=n ** 3 / 3 / ms / 1e6)
+    elif a.case == "dsposv":
+        from .native import IrInfo
+        n, nb, nrhs = a.n, a.nb, a.nrhs
+        A = DeviceBuffer(8 * n * n)
+        W = DeviceBuffer(8 * n * n)
+        Bd, Xd = DeviceBuffer(8 * n * nrhs), DeviceBuffer(8 * n * nrhs)
+        check(L.starpu_gb300_gen_spd_gram(None, n, 3, 4.0 / (a.kappa - 1.0), A.ptr, n, W.ptr))
+        check(L.starpu_gb300_gen_uniform_rhs(None, n, nrhs, 4, Bd.ptr, n))
+        lw = L.starpu_gb300_dsposv_workspace(n, nrhs, nb)
+        Wk = DeviceBuffer(lw)
+        info = IrInfo()
+        ms = _timed(L, lambda: check(L.starpu_gb300_dsposv(None, n, nrhs, A.ptr, n, Bd.ptr, n, Xd.ptr, n, nb, a.nterms,
+                                                            1e-12, 30, Wk.ptr, lw, C.byref(info))), a.reps)
+        out.update(ms=ms, gflops=(n ** 3 / 3 + 2.0 * n * n * nrhs) / ms / 1e6, iterations=info.iterations,
+                   backward_error=info.backward_error)
     print(json.dumps(out))
 
 

@@ -51,6 +51,23 @@ def test_dsposv_reaches_fp64_backward_error(gpu, oracle, kappa, nterms):
         assert info.iterations <= 6
 
 
+@pytest.mark.parametrize("scale", [1e-34, 1e36])
+def test_dsposv_scaled_matrix_residual(gpu, oracle, scale):
+    """The refinement residual is formed from FP32 hi/lo pairs after scaling A
+    and each column of X by powers of two, and each FP32 correction solve runs
+    on a power-of-two-scaled residual: with A ~ 1e-34 or 1e36, whose low
+    parts and late corrections lie far below FP32's normal range, the system
+    must refine like an unscaled one."""
+    n, nb, nrhs = 640, 128, 3
+    A = oracle.spd_gram(n, 43, oracle.alpha_for_kappa(1e3)) * scale
+    B = oracle.uniform_rhs(n, nrhs, 44)
+    rc, info, X = solve(gpu, A, B, nb, 3)
+    assert rc == 0 and info.status == 0, (rc, info.iterations, info.backward_error)
+    be, _ = oracle.backward_error(A, X, B)
+    assert be <= 1e-12
+    assert abs(be - info.backward_error) <= 1e-13 + 0.01 * be
+
+
 def test_dsposv_ill_conditioned_reports_status(gpu, oracle):
     n, nb, nrhs = 768, 256, 2
     A = oracle.spd_gram(n, 33, oracle.alpha_for_kappa(1e6))
