@@ -522,6 +522,8 @@ def run_ours(args):
         for _ in range(max(1, min(args.warmup, 2))):
             e2e_step()
         dist.barrier()
+        L.starpu_gb300_profiling_reset()
+        L.starpu_gb300_profiling_enable(1)
         t0 = time.perf_counter()
         lat = []
         for _ in range(args.steps):
@@ -529,11 +531,18 @@ def run_ours(args):
             e2e_step()
             lat.append(time.perf_counter() - s0)
         te = dist.max((time.perf_counter() - t0) / args.steps)
-        e2e = {"value": world * flops / te / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
+        L.starpu_gb300_profiling_enable(0)
+        la, tms, by = C.c_ulonglong(), C.c_double(), C.c_double()
+        L.starpu_gb300_profiling_get(5, C.byref(la), C.byref(tms), None, C.byref(by))
+        xfer = {"ms_per_step": tms.value / args.steps, "bytes_per_step": by.value / args.steps,
+                "gbs": (by.value / (tms.value * 1e-3) / 1e9) if tms.value else None}
+        # the host path moves A's lower triangle as 512-column trapezoidal panels
+        h2d = sum(8 * (n - j0) * min(512, n - j0) for j0 in range(0, n, 512)) + 8 * n * nrhs
+        e2e = {"value": world * flops / te / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 8 * n * nrhs, "ms_per_step": te * 1e3,
                "solves_per_s": world / te, "p50_ms": 1e3 * statistics.median(lat),
                "p99_ms": 1e3 * sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))],
-               "backward_error": einfo.backward_error, "iterations": einfo.iterations}
+               "backward_error": einfo.backward_error, "iterations": einfo.iterations, "transfers": xfer}
         L.starpu_gb300_solver_destroy(ctx)
         L.starpu_gb300_host_free_pinned(hA)
         L.starpu_gb300_host_free_pinned(hB)

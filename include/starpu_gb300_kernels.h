@@ -164,7 +164,9 @@ unsigned long long starpu_gb300_launch_count(void);
  * each launch of a profiled class is bracketed by CUDA events on its own
  * stream and its algorithmic flops / bytes are recorded.  Classes:
  * 0 = tensor-core trailing update, 1 = panel (POTRF + TRSM + split),
- * 2 = FP64 residual, 3 = triangular solves.  _get resolves pending events. */
+ * 2 = refinement residual, 3 = triangular solves, 4 = batched solves,
+ * 5 = host<->device transfers of the solver context (bytes = bytes moved).
+ * _get resolves pending events. */
 void starpu_gb300_profiling_enable(int on);
 void starpu_gb300_profiling_reset(void);
 int starpu_gb300_profiling_get(int kind, unsigned long long *launches, double *total_ms, double *flops, double *bytes);

@@ -46,12 +46,14 @@ typedef struct starpu_gb300_ir_info {
 /* Bytes of device workspace starpu_gb300_dsposv needs (tile nb, 0 = 1024). */
 size_t starpu_gb300_dsposv_workspace(int n, int nrhs, int nb);
 
-/* Solve A X = B (A SPD, FP64, full symmetric storage) with an FP32-storage
- * tiled Cholesky whose trailing updates run on the tensor cores (split-BF16,
- * nterms = 3, or plain BF16, nterms = 1), then FP64 iterative refinement:
- * r = b - A x in FP64, correction solved with the low-precision factor,
- * x += d in FP64, until every column's normwise backward error <= tol or
- * max_iter corrections were applied (LAPACK dsposv semantics).  X is output
+/* Solve A X = B (A SPD, FP64; only the lower triangle of A is read, LAPACK
+ * dsposv with uplo = 'L') with an FP32-storage tiled Cholesky whose panel
+ * TRSM and trailing updates run on the tensor cores (split-BF16, nterms = 3,
+ * or plain BF16, nterms = 1), then iterative refinement: r = b - A x with
+ * ~2^-47 relative accuracy (double-float on the FP32 pipe), correction solved
+ * with the low-precision factor, x += d in FP64, until every column's
+ * normwise backward error <= tol or max_iter corrections were applied
+ * (LAPACK dsposv semantics).  X is output
  * only.  Synchronises the stream once per refinement step to read the error.
  * Returns 0, GB300_EDOM (low-precision factor not positive definite) or
  * GB300_ETIMEDOUT (no convergence); *info (may be NULL) gets the details. */
@@ -62,8 +64,9 @@ int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda,
 /* Persistent solver context: owns a stream and device buffers for systems up
  * to n_max x n_max with up to nrhs_max right-hand sides, so that repeated
  * solves allocate nothing.  _dsposv_host takes HOST buffers (pinned for full
- * copy bandwidth), copies A and B in, solves as starpu_gb300_dsposv, copies X
- * out and synchronises. */
+ * copy bandwidth), copies the lower triangle of A (the only part the solve
+ * reads) and B in, solves as starpu_gb300_dsposv, copies X out and
+ * synchronises. */
 typedef struct starpu_gb300_solver starpu_gb300_solver;
 starpu_gb300_solver *starpu_gb300_solver_create(int n_max, int nrhs_max, int nb, int nterms);
 int starpu_gb300_solver_destroy(starpu_gb300_solver *solver);

@@ -1,6 +1,7 @@
 // Mixed-precision SPD solve with FP64 iterative refinement (LAPACK dsposv
-// semantics, no reference counterpart: the reference Cholesky is FP32
-// factorisation only, examples/cholesky/cholesky_kernels.c:53-55).
+// semantics with uplo = L: only the lower triangle of A is read; no reference
+// counterpart: the reference Cholesky is FP32 factorisation only,
+// examples/cholesky/cholesky_kernels.c:53-55).
 //
 //   W = fp32(A)                       (lower triangle, fused with ||A||_inf)
 //   W = L L^T                         tensor-core tiled Cholesky (split-BF16)
@@ -47,6 +48,63 @@ __global__ void convert_lower_norm_kernel(int n, const double *__restrict__ A, l
         s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if (threadIdx.x == 0) atomicMax(anorm_bits, (unsigned long long)__double_as_longlong(s));
+    }
+}
+
+// The same from the lower triangle only (A symmetric, the upper part never
+// read): one CTA per block of SYM_BW rows/columns I = [i0, i0 + bw).
+//   row sum_i = sum_{k < i} |A_ik|   (row i left of the diagonal: columns
+//               k < i, read as column segments of the block's rows)
+//             + sum_{k >= i} |A_ki|  (column i from the diagonal down)
+// Columns j in I are written to W (rows i >= j) while they are reduced.
+// Every CTA reads SYM_BW * n elements; max over rows is order-independent.
+constexpr int SYM_BW = 128;
+__global__ void __launch_bounds__(256) convert_lower_symnorm_kernel(int n, const double *__restrict__ A, long lda,
+                                                                    float *__restrict__ W, long ldw,
+                                                                    unsigned long long *anorm_bits)
+{
+    const int i0 = blockIdx.x * SYM_BW;
+    const int bw = min(SYM_BW, n - i0);
+    const int tid = threadIdx.x;
+    __shared__ double left[2][SYM_BW];
+    __shared__ double down[SYM_BW];
+    __shared__ double red[8];
+    // row parts: thread (t = tid % 128, h = tid / 128) sums columns k = h, h+2, ... < i0 + t of row i0 + t
+    {
+        const int t = tid & (SYM_BW - 1), h = tid >> 7;
+        double s = 0.0;
+        if (t < bw) {
+            const double *a = A + i0 + t;
+            for (int k = h; k < i0 + t; k += 2) s += fabs(a[(long)k * lda]);
+        }
+        left[h][t] = s;
+    }
+    // column parts: column j = i0 + c, rows j .. n-1, by the whole CTA
+    for (int c = 0; c < bw; ++c) {
+        const int j = i0 + c;
+        const double *a = A + (long)j * lda;
+        float *w = W + (long)j * ldw;
+        double s = 0.0;
+        for (int i = j + tid; i < n; i += blockDim.x) {
+            const double v = a[i];
+            s += fabs(v);
+            w[i] = (float)v;
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((tid & 31) == 0) red[tid >> 5] = s;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int q = 0; q < 8; ++q) t += red[q];
+            down[c] = t;
+        }
+        __syncthreads();
+    }
+    if (tid < 32) {
+        double m = 0.0;
+        for (int t = tid; t < bw; t += 32) m = fmax(m, left[0][t] + left[1][t] + down[t]);
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+        if (tid == 0) atomicMax(anorm_bits, (unsigned long long)__double_as_longlong(m));
     }
 }
 
@@ -285,7 +343,8 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
 static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws)
 {
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
-    gb300_count_launch(), convert_lower_norm_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits);
+    gb300_count_launch(), convert_lower_symnorm_kernel<<<(n + SYM_BW - 1) / SYM_BW, 256, 0, s>>>(n, A, lda, ws.W, n,
+                                                                                                 ws.anorm_bits);
     int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err);
     if (rc) return rc;
     potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
@@ -459,6 +518,9 @@ int starpu_gb300_solver_destroy(starpu_gb300_solver *h)
 
 void *starpu_gb300_solver_stream(starpu_gb300_solver *h) { return h ? (void *)h->stream : nullptr; }
 
+// column panel width of the host-to-device copy of A's lower triangle
+static constexpr int HOST_PANEL = 512;
+
 int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, const double *A, int lda,
                                     const double *B, int ldb, double *X, int ldx, double tol, int max_iter,
                                     starpu_gb300_ir_info *info)
@@ -468,26 +530,36 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
     if (!n || !nrhs) return GB300_OK;
     cudaStream_t s = h->stream;
     int rc;
-    // one linear copy when the host matrix is contiguous (lda == n): a pitched
-    // copy of n rows moves far less than the link bandwidth
-    if ((rc = gb300_record_cuda_error(
-             lda == n ? cudaMemcpyAsync(h->A, A, sizeof(double) * (size_t)n * n, cudaMemcpyHostToDevice, s)
-                      : cudaMemcpy2DAsync(h->A, sizeof(double) * n, A, sizeof(double) * lda, sizeof(double) * n, n,
-                                          cudaMemcpyHostToDevice, s))))
-        return rc;
+    int slot = gb300_prof_begin(s, GB300_PROF_TRANSFER);
+    // only the lower triangle is read by the solve: copy it as trapezoidal
+    // column panels (rows j0..n-1 of columns j0..j0+w-1), each one pitched
+    // copy of whole column segments -- n^2/2 + n w/2 elements instead of n^2
+    double abytes = 0.0;
+    for (int j0 = 0; j0 < n; j0 += HOST_PANEL) {
+        const int w = std::min(HOST_PANEL, n - j0);
+        const size_t rows = (size_t)(n - j0);
+        if ((rc = gb300_record_cuda_error(cudaMemcpy2DAsync(h->A + j0 + (size_t)j0 * n, sizeof(double) * n,
+                                                            A + j0 + (size_t)j0 * lda, sizeof(double) * lda,
+                                                            sizeof(double) * rows, w, cudaMemcpyHostToDevice, s))))
+            return rc;
+        abytes += 8.0 * rows * w;
+    }
     if ((rc = gb300_record_cuda_error(
              ldb == n ? cudaMemcpyAsync(h->B, B, sizeof(double) * (size_t)n * nrhs, cudaMemcpyHostToDevice, s)
                       : cudaMemcpy2DAsync(h->B, sizeof(double) * n, B, sizeof(double) * ldb, sizeof(double) * n,
                                           nrhs, cudaMemcpyHostToDevice, s))))
         return rc;
+    gb300_prof_end(s, slot, 0.0, abytes + 8.0 * n * (double)nrhs);
     int status = starpu_gb300_dsposv(s, n, nrhs, h->A, n, h->B, n, h->X, n, h->nb, h->nterms, tol, max_iter, h->work,
                                      h->lwork, info);
     if (status != GB300_OK && status != GB300_ETIMEDOUT) return status;
+    slot = gb300_prof_begin(s, GB300_PROF_TRANSFER);
     if ((rc = gb300_record_cuda_error(
              ldx == n ? cudaMemcpyAsync(X, h->X, sizeof(double) * (size_t)n * nrhs, cudaMemcpyDeviceToHost, s)
                       : cudaMemcpy2DAsync(X, sizeof(double) * ldx, h->X, sizeof(double) * n, sizeof(double) * n,
                                           nrhs, cudaMemcpyDeviceToHost, s))))
         return rc;
+    gb300_prof_end(s, slot, 0.0, 8.0 * n * (double)nrhs);
     if ((rc = gb300_record_cuda_error(cudaStreamSynchronize(s)))) return rc;
     return status;
 }

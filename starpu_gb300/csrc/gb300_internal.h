@@ -50,6 +50,6 @@ extern "C" void gb300_count_launch(void);
 // prof_begin/prof_end bracket one launch with CUDA events on its stream when
 // profiling is enabled; both are no-ops otherwise.
 enum gb300_prof_kind { GB300_PROF_TC_UPDATE = 0, GB300_PROF_PANEL = 1, GB300_PROF_RESIDUAL = 2, GB300_PROF_SOLVE = 3,
-                       GB300_PROF_BATCHED = 4, GB300_PROF_KINDS = 5 };
+                       GB300_PROF_BATCHED = 4, GB300_PROF_TRANSFER = 5, GB300_PROF_KINDS = 6 };
 extern "C" int gb300_prof_begin(cudaStream_t s, int kind);
 extern "C" void gb300_prof_end(cudaStream_t s, int slot, double algorithmic_flops, double algorithmic_bytes);

@@ -1,5 +1,5 @@
-// Residual r = b - A x of the refinement loop on the FP32 pipe in double-float
-// arithmetic.  GB300 issues FP64 FMAs at ~1/60 of its FP32 rate, so the FP64
+// Residual r = b - A x of the refinement loop (A symmetric, lower triangle
+// read) on the FP32 pipe in double-float arithmetic.  GB300 issues FP64 FMAs at ~1/60 of its FP32 rate, so the FP64
 // residual (2 n^2 nrhs flops) is compute-bound at the FP64 peak; the same sum
 // is formed here from FP32 pairs (hi + lo, 48 significant bits):
 //
@@ -102,18 +102,43 @@ __global__ void __launch_bounds__(256) df_split_x_kernel(int n, const double *__
     }
 }
 
+// Stage layout of a 128-row x 32-column block of the symmetric A read from
+// its lower triangle only: blocks strictly below the diagonal are read as
+// they are (threads along rows: coalesced), blocks strictly above as the
+// transpose of the mirror block (threads along k: coalesced), blocks that
+// cross the diagonal element by element.
+enum { RDF_LOWER = 0, RDF_UPPER = 1, RDF_DIAG = 2 };
+__device__ __forceinline__ int rdf_mode(int i0, int k0)
+{
+    if (k0 + RDF_BK <= i0) return RDF_LOWER;
+    if (k0 >= i0 + RDF_BM) return RDF_UPPER;
+    return RDF_DIAG;
+}
+// element e (0 .. 4095) of a stage -> (row, kk)
+__device__ __forceinline__ void rdf_coords(int mode, int e, int &row, int &kk)
+{
+    if (mode == RDF_UPPER) {
+        kk = e & (RDF_BK - 1);
+        row = e >> 5;
+    } else {
+        row = e & (RDF_BM - 1);
+        kk = e >> 7;
+    }
+}
+
 // P[z n nrhs + i + j n] = -(A[i, kz] X[kz, j]) over the K chunk z = blockIdx.z
 // (kchunk a multiple of RDF_BK), rows i of the 128-row block blockIdx.x,
-// columns j of the group of 16 blockIdx.y.  256 threads: thread
-// (r = tid % 64, g = tid / 64) owns rows r, r + 64 and columns 4g .. 4g+3.
-// The next stage's A block is loaded into registers while the current one is
-// multiplied from shared memory.
+// columns j of the group of 16 blockIdx.y.  A is symmetric and only its lower
+// triangle is read.  256 threads: thread (r = tid % 64, g = tid / 64) owns
+// rows r, r + 64 and columns 4g .. 4g+3.  The next stage's A block is loaded
+// into registers while the current one is multiplied from shared memory.
 __global__ void __launch_bounds__(256, 2) residual_df_kernel(int n, int nrhs, const double *__restrict__ A, long lda,
                                                              const float2 *__restrict__ Xs, const int *__restrict__ sx,
                                                              const unsigned long long *__restrict__ anorm_bits,
                                                              int kchunk, double *__restrict__ P)
 {
-    __shared__ float2 As[RDF_BK][RDF_BM];
+    // one float2 of padding per row: the transposed (upper) stages store along k
+    __shared__ float2 As[RDF_BK][RDF_BM + 1];
     __shared__ __align__(16) float2 Xt[RDF_BK][16];
     const int tid = threadIdx.x;
     const int i0 = blockIdx.x * RDF_BM;
@@ -129,11 +154,18 @@ __global__ void __launch_bounds__(256, 2) residual_df_kernel(int n, int nrhs, co
     double ra[16];
     float4 rx;
     auto load_stage = [&](int k0) {
+        const int mode = rdf_mode(i0, k0);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-            const int e = tid + 256 * q;
-            const int row = e & (RDF_BM - 1), k = k0 + (e >> 7);
-            ra[q] = (i0 + row < n && k < kz1) ? __ldg(&A[(long)(i0 + row) + (long)k * lda]) : 0.0;
+            int row, kk;
+            rdf_coords(mode, tid + 256 * q, row, kk);
+            const int i = i0 + row, k = k0 + kk;
+            double v = 0.0;
+            if (i < n && k < kz1) {
+                const bool mirror = mode == RDF_UPPER || (mode == RDF_DIAG && k > i);
+                v = __ldg(mirror ? &A[(long)k + (long)i * lda] : &A[(long)i + (long)k * lda]);
+            }
+            ra[q] = v;
         }
         const int k = k0 + (tid >> 3), c = (tid & 7) * 2;
         float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -156,10 +188,12 @@ __global__ void __launch_bounds__(256, 2) residual_df_kernel(int n, int nrhs, co
     int stage = 0;
     for (int k0 = kz0; k0 < kz1; k0 += RDF_BK) {
         __syncthreads();  // the previous stage's reads of As / Xt are done
+        const int mode = rdf_mode(i0, k0);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-            const int e = tid + 256 * q;
-            As[e >> 7][e & (RDF_BM - 1)] = df_split_scaled(ra[q], ea);
+            int row, kk;
+            rdf_coords(mode, tid + 256 * q, row, kk);
+            As[kk][row] = df_split_scaled(ra[q], ea);
         }
         reinterpret_cast<float4 *>(&Xt[0][0])[tid] = rx;
         __syncthreads();

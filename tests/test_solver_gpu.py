@@ -68,6 +68,22 @@ def test_dsposv_scaled_matrix_residual(gpu, oracle, scale):
     assert abs(be - info.backward_error) <= 1e-13 + 0.01 * be
 
 
+@pytest.mark.parametrize("n,nb", [(1000, 256), (640, 128)])
+def test_dsposv_reads_only_the_lower_triangle(gpu, oracle, n, nb):
+    """LAPACK uplo = 'L': the strict upper triangle of A is never read, so
+    filling it with NaN leaves the solution bit-identical."""
+    nrhs = 5
+    A = oracle.spd_gram(n, 45, oracle.alpha_for_kappa(1e3))
+    B = oracle.uniform_rhs(n, nrhs, 46)
+    rc, info, X = solve(gpu, A, B, nb, 3)
+    assert rc == 0
+    An = np.array(A, order="F")
+    An[np.triu_indices(n, 1)] = np.nan
+    rc2, info2, X2 = solve(gpu, An, B, nb, 3)
+    assert rc2 == 0 and info2.iterations == info.iterations
+    np.testing.assert_array_equal(X2, X)
+
+
 def test_dsposv_ill_conditioned_reports_status(gpu, oracle):
     n, nb, nrhs = 768, 256, 2
     A = oracle.spd_gram(n, 33, oracle.alpha_for_kappa(1e6))
