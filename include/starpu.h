@@ -362,6 +362,7 @@ struct starpu_task {
     double predicted_transfer;
     unsigned long magic;
     void *sched_data;
+    unsigned color;        /* display colour of the task in traces */
     void *starpu_private;  /* runtime job */
 };
 
@@ -482,6 +483,9 @@ void starpu_perfmodel_update_history(struct starpu_perfmodel *model, struct star
 unsigned starpu_worker_get_count(void);
 unsigned starpu_cpu_worker_get_count(void);
 unsigned starpu_cuda_worker_get_count(void);
+/* workers driving MPI / TCP-IP server-client sinks: none in this runtime */
+unsigned starpu_mpi_sc_worker_get_count(void);
+unsigned starpu_tcpip_sc_worker_get_count(void);
 unsigned starpu_hip_worker_get_count(void);
 unsigned starpu_opencl_worker_get_count(void);
 int starpu_worker_get_id(void);
@@ -563,8 +567,17 @@ void starpu_bound_compute(double *res, double *integer_res, int integer);
 void starpu_bound_print_lp(FILE *output);
 void starpu_bound_print_mps(FILE *output);
 void starpu_bound_print(FILE *output, int integer);
+#define STARPU_PROFILING_DISABLE 0
+#define STARPU_PROFILING_ENABLE 1
 int starpu_profiling_status_set(int status);
 int starpu_profiling_status_get(void);
+/* prints the runtime's host<->device transfer totals (starpu_profiling.h) */
+void starpu_profiling_bus_helper_display_summary(void);
+void starpu_bound_print_dot(FILE *output);
+
+/* ================================================= random numbers (starpu_rand.h) */
+#define starpu_srand48(seed) srand48(seed)
+#define starpu_drand48() drand48()
 
 /* ============================================================ GB300 extras
  * Statistics of the runtime's CUDA execution (no StarPU counterpart). */

@@ -194,6 +194,8 @@ int starpu_asynchronous_copy_disabled(void) { return 0; }
 unsigned starpu_worker_get_count(void) { return (unsigned)rt.nworkers; }
 unsigned starpu_cpu_worker_get_count(void) { return (unsigned)rt.ncpu; }
 unsigned starpu_cuda_worker_get_count(void) { return (unsigned)rt.ncuda; }
+unsigned starpu_mpi_sc_worker_get_count(void) { return 0; }
+unsigned starpu_tcpip_sc_worker_get_count(void) { return 0; }
 unsigned starpu_hip_worker_get_count(void) { return 0; }
 unsigned starpu_opencl_worker_get_count(void) { return 0; }
 int starpu_worker_get_id(void) { return tls_worker; }
@@ -361,6 +363,22 @@ void starpu_bound_print(FILE *output, int integer)
 {
     (void)integer;
     if (output) fprintf(output, "bound not provided by the GB300 runtime\n");
+}
+
+void starpu_bound_print_dot(FILE *output)
+{
+    if (output) fprintf(output, "/* task graph bound not provided by the GB300 runtime */\ndigraph G {}\n");
+}
+
+void starpu_profiling_bus_helper_display_summary(void)
+{
+    rt_lock();
+    const unsigned long h2d = rt.stats.h2d_bytes, d2h = rt.stats.d2h_bytes;
+    rt_unlock();
+    fprintf(stderr, "\n#---------------------\nData transfer stats:\n");
+    fprintf(stderr, "\tNUMA 0 -> CUDA 0\t%.4f MB\n", h2d / 1048576.0);
+    fprintf(stderr, "\tCUDA 0 -> NUMA 0\t%.4f MB\n", d2h / 1048576.0);
+    fprintf(stderr, "Total transfers: %.4f MB\n#---------------------\n", (h2d + d2h) / 1048576.0);
 }
 
 static int profiling_status = 0;

@@ -119,3 +119,22 @@ def test_gb300_driver_without_gpu_reports_skipped():
     r = subprocess.run([os.path.join(libdir, "chol_implicit_gb300"), "-size", "256", "-nblocks", "2"],
                        env=_env(STARPU_NCUDA=0, STARPU_NCPU=2), capture_output=True, text=True, timeout=120)
     assert r.returncode == 77, r.stdout + r.stderr
+
+
+# The reference's unchanged LU drivers (examples/lu: lu_example.c with the
+# implicit-dependency and the tag-based DAGs, xlu_implicit*.c / xlu*.c) and its
+# CPU codelets on this runtime's CPU workers: each must pass its own check
+# ||PA - LU|| / (||A|| N) <= PIVOT_THRESHHOLD (lu_example.c, check_result).
+@pytest.mark.parametrize("prog", ["lu_implicit_float", "lu_tag_float", "lu_implicit_double", "lu_tag_double"])
+@pytest.mark.parametrize("mode", [[], ["-piv"], ["-piv", "-no-stride"]])
+def test_unchanged_reference_lu_drivers_on_cpu_workers(prog, mode):
+    if not os.path.isdir(os.path.join(REF, "examples", "lu")):
+        pytest.skip("reference tree not available on this machine")
+    _lib()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}", "_ref/" + prog], check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", prog)
+    r = subprocess.run([exe, "-size", "768", "-nblocks", "4", "-check", *mode], env=_env(STARPU_NCUDA=0, STARPU_NCPU=4),
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    m = re.search(r"\|\|P?A-LU\|\| / \(\|\|A\|\|\*N\) : ([0-9.e+-]+)", r.stderr)
+    assert m and float(m.group(1)) <= 1e-6, r.stderr
