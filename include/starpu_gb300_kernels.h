@@ -67,6 +67,55 @@ int starpu_gb300_dsyrk_ln_tile(void *stream, int n, int k, double alpha, const d
 int starpu_gb300_sgemm_nt_tile(void *stream, int m, int n, int k, float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc);
 int starpu_gb300_dgemm_nt_tile(void *stream, int m, int n, int k, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc);
 
+/* ---------------- LU tile codelet bodies (examples/lu, FP32 / FP64) -------
+ * The reference LU keeps the pivot in L: A = L U with L lower non-unit and U
+ * unit upper (examples/lu/xlu_kernels.c:369-380). */
+
+/* In-place LU of the n x n tile A, no pivoting.  Replaces the GETRF codelet
+ * (cusolverDnSgetrf, or the host loop of cublasSscal / cublasSger with one
+ * synchronisation per column, examples/lu/xlu_kernels.c:385-433).  A zero
+ * pivot writes info = k + 1 to *d_info (may be NULL) without trapping. */
+int starpu_gb300_sgetrf_tile(void *stream, int n, float *A, int lda, int *d_info);
+int starpu_gb300_dgetrf_tile(void *stream, int n, double *A, int lda, int *d_info);
+
+/* The GETRF_PIVOT codelet (xlu_kernels.c:491-657): as above, except that a
+ * step whose pivot has magnitude below `threshold` takes the largest entry of
+ * its row (first on ties) and swaps those two whole columns.  d_ipiv (device,
+ * n ints) receives, per step, the column swapped in (the step itself when it
+ * pivoted in place) or -1 when the step did not pivot.  `work` (device,
+ * >= _workspace(n) bytes) holds a copy of the tile: the blocked factorisation
+ * runs first and, if a step needed a pivot, the tile is restored and factored
+ * again with pivoting. */
+size_t starpu_gb300_sgetrf_pivot_tile_workspace(int n);
+size_t starpu_gb300_dgetrf_pivot_tile_workspace(int n);
+int starpu_gb300_sgetrf_pivot_tile(void *stream, int n, float *A, int lda, float threshold, int *d_ipiv, void *work,
+                                   size_t lwork, int *d_info);
+int starpu_gb300_dgetrf_pivot_tile(void *stream, int n, double *A, int lda, double threshold, int *d_ipiv, void *work,
+                                   size_t lwork, int *d_info);
+
+/* B[m x n] <- L^{-1} B, L m x m lower non-unit.  Replaces cublasStrsm(LEFT,
+ * LOWER, N, NON_UNIT) of the TRSM_LL codelet, xlu_kernels.c:192-199. */
+int starpu_gb300_strsm_llnn_tile(void *stream, int m, int n, const float *L, int ldl, float *B, int ldb);
+int starpu_gb300_dtrsm_llnn_tile(void *stream, int m, int n, const double *L, int ldl, double *B, int ldb);
+
+/* B[m x n] <- B U^{-1}, U n x n unit upper.  Replaces cublasStrsm(RIGHT,
+ * UPPER, N, UNIT) of the TRSM_RU codelet, xlu_kernels.c:281-289. */
+int starpu_gb300_strsm_runu_tile(void *stream, int m, int n, const float *U, int ldu, float *B, int ldb);
+int starpu_gb300_dtrsm_runu_tile(void *stream, int m, int n, const double *U, int ldu, double *B, int ldb);
+
+/* C[m x n] <- alpha * A * B + beta * C, A m x k, B k x n.  Replaces
+ * cublasSgemm(N, N) of the LU GEMM codelet, xlu_kernels.c:74-78. */
+int starpu_gb300_sgemm_nn_tile(void *stream, int m, int n, int k, float alpha, const float *A, int lda, const float *B,
+                               int ldb, float beta, float *C, int ldc);
+int starpu_gb300_dgemm_nn_tile(void *stream, int m, int n, int k, double alpha, const double *A, int lda,
+                               const double *B, int ldb, double beta, double *C, int ldc);
+
+/* Swap columns pairs[2s] and pairs[2s+1] of the m-row tile A, for s = 0 ..
+ * npairs-1 in that order (pairs is a HOST array).  Replaces the cublasSswap
+ * loop of the PIVOT codelet, xlu_kernels.c:696-708. */
+int starpu_gb300_sswap_columns_tile(void *stream, int m, float *A, int lda, const int *pairs, int npairs);
+int starpu_gb300_dswap_columns_tile(void *stream, int m, double *A, int lda, const int *pairs, int npairs);
+
 /* ---------------- whole matrix, plain precision --------------------------- */
 
 /* Tiled right-looking Cholesky of the whole n x n matrix with tile nb (0 =
