@@ -37,7 +37,7 @@ def lib() -> C.CDLL:
     global _o
     if _o is None:
         if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-                os.path.getmtime(os.path.join(HERE, f)) for f in ("chol_oracle.c", "cpu_chol.c")):
+                os.path.getmtime(os.path.join(HERE, f)) for f in ("chol_oracle.c", "cpu_chol.c", "lu_oracle.c")):
             build(with_ref=False)
         o = C.CDLL(LIB)
         o.oracle_hilbert_f32.argtypes = [ci, vp, ci]
@@ -62,6 +62,12 @@ def lib() -> C.CDLL:
         o.cpu_chol_potrf_tiled_f64.argtypes = [ci, vp, ci, ci, ci]
         o.cpu_chol_potrs_f64.argtypes = [ci, ci, vp, ci, vp, ci, ci]
         o.cpu_chol_set_blas_threads.argtypes = [ci]
+        for p, t in (("s", C.c_float), ("d", C.c_double)):
+            getattr(o, f"oracle_{p}lu_getrf").argtypes = [ci, vp, ci, t, vp, ci]
+            getattr(o, f"oracle_{p}lu_trsm_ll").argtypes = [ci, ci, vp, ci, vp, ci]
+            getattr(o, f"oracle_{p}lu_trsm_ru").argtypes = [ci, ci, vp, ci, vp, ci]
+            getattr(o, f"oracle_{p}lu_gemm").argtypes = [ci, ci, ci, vp, ci, vp, ci, vp, ci]
+            getattr(o, f"oracle_{p}lu_pivot").argtypes = [ci, vp, ci, vp]
         _o = o
     return _o
 
@@ -222,3 +228,39 @@ def cpu_potrf_tiled(A: np.ndarray, nblocks: int, nthreads: int) -> int:
 def cpu_potrs(L: np.ndarray, B: np.ndarray, nthreads: int) -> int:
     assert cpu_init()
     return lib().cpu_chol_potrs_f64(L.shape[0], B.shape[1], _p(L), L.shape[0], _p(B), B.shape[0], nthreads)
+
+
+# ------------------------------------------------------------------ LU (examples/lu)
+def _lu_prefix(a: np.ndarray) -> str:
+    return "s" if a.dtype == np.float32 else "d"
+
+
+def lu_getrf(A: np.ndarray, thr: float = 0.0, iamax_shift: int = 0):
+    """In-place LU of a Fortran-ordered tile (L non-unit, U unit); returns
+    (info, ipiv) with ipiv[z] = the column swapped in at step z, -1 if none.
+    iamax_shift = 1 reproduces the reference CPU branch built against a
+    Fortran-interface BLAS (1-based ISAMAX used as 0-based)."""
+    assert A.flags.f_contiguous and A.shape[0] == A.shape[1]
+    n = A.shape[0]
+    ipiv = np.full(n, -1, dtype=np.int32)
+    info = getattr(lib(), f"oracle_{_lu_prefix(A)}lu_getrf")(n, _p(A), n, thr, _p(ipiv), iamax_shift)
+    return info, ipiv
+
+
+def lu_trsm_ll(L: np.ndarray, B: np.ndarray) -> None:
+    getattr(lib(), f"oracle_{_lu_prefix(B)}lu_trsm_ll")(B.shape[0], B.shape[1], _p(L), L.shape[0], _p(B), B.shape[0])
+
+
+def lu_trsm_ru(U: np.ndarray, B: np.ndarray) -> None:
+    getattr(lib(), f"oracle_{_lu_prefix(B)}lu_trsm_ru")(B.shape[0], B.shape[1], _p(U), U.shape[0], _p(B), B.shape[0])
+
+
+def lu_gemm(A: np.ndarray, B: np.ndarray, Cm: np.ndarray) -> None:
+    getattr(lib(), f"oracle_{_lu_prefix(Cm)}lu_gemm")(Cm.shape[0], Cm.shape[1], A.shape[1], _p(A), A.shape[0], _p(B),
+                                                       B.shape[0], _p(Cm), Cm.shape[0])
+
+
+def lu_pivot(T: np.ndarray, ipiv_tile: np.ndarray) -> None:
+    """Column swaps of the PIVOT codelet; ipiv_tile[r] = tile-local column (r = no swap)."""
+    p = np.ascontiguousarray(ipiv_tile, dtype=np.int32)
+    getattr(lib(), f"oracle_{_lu_prefix(T)}lu_pivot")(T.shape[0], _p(T), T.shape[0], _p(p))
