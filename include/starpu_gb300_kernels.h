@@ -110,11 +110,12 @@ int starpu_gb300_sgemm_nn_tile(void *stream, int m, int n, int k, float alpha, c
 int starpu_gb300_dgemm_nn_tile(void *stream, int m, int n, int k, double alpha, const double *A, int lda,
                                const double *B, int ldb, double beta, double *C, int ldc);
 
-/* Swap columns pairs[2s] and pairs[2s+1] of the m-row tile A, for s = 0 ..
- * npairs-1 in that order (pairs is a HOST array).  Replaces the cublasSswap
- * loop of the PIVOT codelet, xlu_kernels.c:696-708. */
-int starpu_gb300_sswap_columns_tile(void *stream, int m, float *A, int lda, const int *pairs, int npairs);
-int starpu_gb300_dswap_columns_tile(void *stream, int m, double *A, int lda, const int *pairs, int npairs);
+/* Swap columns pairs[2s] and pairs[2s+1] of the m x n tile A, for s = 0 ..
+ * npairs-1 in that order (pairs is a HOST array; an index outside [0, n) is
+ * GB300_EINVAL).  Replaces the cublasSswap loop of the PIVOT codelet,
+ * xlu_kernels.c:696-708. */
+int starpu_gb300_sswap_columns_tile(void *stream, int m, int n, float *A, int lda, const int *pairs, int npairs);
+int starpu_gb300_dswap_columns_tile(void *stream, int m, int n, double *A, int lda, const int *pairs, int npairs);
 
 /* ---------------- whole matrix, plain precision --------------------------- */
 

@@ -121,9 +121,11 @@ static int getrf_pivot_tile(void *stream, int n, T *A, int lda, T threshold, int
 }
 
 template <typename T>
-static int swap_columns(void *stream, int m, T *A, int lda, const int *pairs, int npairs)
+static int swap_columns(void *stream, int m, int n, T *A, int lda, const int *pairs, int npairs)
 {
-    if (m < 0 || lda < (m > 1 ? m : 1) || npairs < 0 || (npairs && !pairs)) return GB300_EINVAL;
+    if (m < 0 || n < 0 || lda < (m > 1 ? m : 1) || npairs < 0 || (npairs && !pairs)) return GB300_EINVAL;
+    for (int k = 0; k < 2 * npairs; ++k)
+        if (pairs[k] < 0 || pairs[k] >= n) return GB300_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
     if (!m || !npairs) return GB300_OK;
     LuSwapList list;
@@ -219,13 +221,13 @@ int starpu_gb300_dgemm_nn_tile(void *stream, int m, int n, int k, double alpha, 
     return gemm_nn_tile<double>(stream, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
-int starpu_gb300_sswap_columns_tile(void *stream, int m, float *A, int lda, const int *pairs, int npairs)
+int starpu_gb300_sswap_columns_tile(void *stream, int m, int n, float *A, int lda, const int *pairs, int npairs)
 {
-    return swap_columns<float>(stream, m, A, lda, pairs, npairs);
+    return swap_columns<float>(stream, m, n, A, lda, pairs, npairs);
 }
-int starpu_gb300_dswap_columns_tile(void *stream, int m, double *A, int lda, const int *pairs, int npairs)
+int starpu_gb300_dswap_columns_tile(void *stream, int m, int n, double *A, int lda, const int *pairs, int npairs)
 {
-    return swap_columns<double>(stream, m, A, lda, pairs, npairs);
+    return swap_columns<double>(stream, m, n, A, lda, pairs, npairs);
 }
 
 } // extern "C"
