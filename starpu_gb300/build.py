@@ -54,7 +54,8 @@ def _run(cmd: list[str]) -> None:
 
 
 CHOL_LIBNAME = "libstarpu_gb300_chol.so"
-EXAMPLES = ["chol_implicit_gb300"]
+LU_LIBNAME = "libstarpu_gb300_lu.so"
+EXAMPLES = {"chol_implicit_gb300": CHOL_LIBNAME, "lu_gb300": LU_LIBNAME}
 
 
 def chol_lib_path() -> str:
@@ -77,18 +78,21 @@ def _build_codelets_and_examples(main_changed: bool) -> None:
     inc = ["-I" + INCLUDE, "-I" + os.path.join(CUDA_HOME, "include")]
     rpath = "-Wl,-rpath," + LIBDIR + ":" + os.path.join(CUDA_HOME, "lib64")
     deps = max([os.path.getmtime(h) for h in _headers()] + [os.path.getmtime(lib_path())])
-    csrcs = sorted(glob.glob(os.path.join(CSRC, "codelets", "*.c")))
-    out = chol_lib_path()
-    if main_changed or not os.path.exists(out) or any(_stale(out, s, deps) for s in csrcs):
-        _run(["gcc", "-O2", "-g", "-fPIC", "-std=gnu11", "-Wall", "-shared", "-o", out + ".tmp", *csrcs, *inc,
-              "-L" + LIBDIR, "-lstarpu_gb300", rpath])
-        os.replace(out + ".tmp", out)
-    for ex in EXAMPLES:
+    # codelet libraries: the Cholesky codelets (codelets/) and the LU codelets (codelets_lu/)
+    for sub, name in (("codelets", CHOL_LIBNAME), ("codelets_lu", LU_LIBNAME)):
+        csrcs = sorted(glob.glob(os.path.join(CSRC, sub, "*.c")))
+        out = os.path.join(LIBDIR, name)
+        if main_changed or not os.path.exists(out) or any(_stale(out, s, deps) for s in csrcs):
+            _run(["gcc", "-O2", "-g", "-fPIC", "-std=gnu11", "-Wall", "-shared", "-o", out + ".tmp", *csrcs, *inc,
+                  "-L" + LIBDIR, "-lstarpu_gb300", rpath])
+            os.replace(out + ".tmp", out)
+    for ex, codelet_lib in EXAMPLES.items():
         src = os.path.join(CSRC, "examples", ex + ".c")
         exe = example_path(ex)
-        if main_changed or _stale(exe, src, max(deps, os.path.getmtime(out))):
+        lib = os.path.join(LIBDIR, codelet_lib)
+        if main_changed or _stale(exe, src, max(deps, os.path.getmtime(lib))):
             _run(["gcc", "-O2", "-g", "-std=gnu11", "-Wall", "-o", exe + ".tmp", src, *inc, "-L" + LIBDIR,
-                  "-lstarpu_gb300_chol", "-lstarpu_gb300", rpath, "-lm", "-lpthread"])
+                  "-l" + codelet_lib[3:-3], "-lstarpu_gb300", rpath, "-lm", "-lpthread"])
             os.replace(exe + ".tmp", exe)
 
 
