@@ -70,26 +70,45 @@ __global__ void __launch_bounds__(256) convert_lower_symnorm_kernel(int n, const
     __shared__ double down[SYM_BW];
     __shared__ double red[8];
     // row parts: thread (t = tid % 128, h = tid / 128) sums columns k = h, h+2, ... < i0 + t of row i0 + t
+    // (four independent partial sums: GB300 issues few FP64 adds per clock, a
+    // single dependent chain would leave the pipe waiting on its latency)
     {
         const int t = tid & (SYM_BW - 1), h = tid >> 7;
-        double s = 0.0;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
         if (t < bw) {
             const double *a = A + i0 + t;
-            for (int k = h; k < i0 + t; k += 2) s += fabs(a[(long)k * lda]);
+            const int kend = i0 + t;
+            int k = h;
+            for (; k + 6 < kend; k += 8) {
+                s0 += fabs(a[(long)k * lda]);
+                s1 += fabs(a[(long)(k + 2) * lda]);
+                s2 += fabs(a[(long)(k + 4) * lda]);
+                s3 += fabs(a[(long)(k + 6) * lda]);
+            }
+            for (; k < kend; k += 2) s0 += fabs(a[(long)k * lda]);
         }
-        left[h][t] = s;
+        left[h][t] = (s0 + s1) + (s2 + s3);
     }
     // column parts: column j = i0 + c, rows j .. n-1, by the whole CTA
     for (int c = 0; c < bw; ++c) {
         const int j = i0 + c;
         const double *a = A + (long)j * lda;
         float *w = W + (long)j * ldw;
-        double s = 0.0;
-        for (int i = j + tid; i < n; i += blockDim.x) {
+        double s0 = 0.0, s1 = 0.0;
+        int i = j + tid;
+        for (; i + (int)blockDim.x < n; i += 2 * blockDim.x) {
+            const double v0 = a[i], v1 = a[i + blockDim.x];
+            s0 += fabs(v0);
+            s1 += fabs(v1);
+            w[i] = (float)v0;
+            w[i + blockDim.x] = (float)v1;
+        }
+        if (i < n) {
             const double v = a[i];
-            s += fabs(v);
+            s0 += fabs(v);
             w[i] = (float)v;
         }
+        double s = s0 + s1;
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if ((tid & 31) == 0) red[tid >> 5] = s;
         __syncthreads();
@@ -521,6 +540,43 @@ void *starpu_gb300_solver_stream(starpu_gb300_solver *h) { return h ? (void *)h-
 // column panel width of the host-to-device copy of A's lower triangle
 static constexpr int HOST_PANEL = 512;
 
+// Column j of the lower triangle (rows j..n-1) from host memory the device
+// can read (pinned, mapped) into D (ld ldd): one CTA per column, four loads
+// in flight per thread so the host link stays busy.
+__global__ void __launch_bounds__(256) gather_lower_kernel(int n, const double *__restrict__ H, long ldh,
+                                                           double *__restrict__ D, long ldd)
+{
+    const long j = blockIdx.x;
+    const double *src = H + j * ldh;
+    double *dst = D + j * ldd;
+    for (long i = j + threadIdx.x; i < n; i += 4L * blockDim.x) {
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long r = i + (long)u * blockDim.x;
+            v[u] = r < n ? src[r] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long r = i + (long)u * blockDim.x;
+            if (r < n) dst[r] = v[u];
+        }
+    }
+}
+
+// Device address of a pinned (page-locked, mapped) host buffer, or NULL when
+// `p` is not one -- ordinary pageable memory takes the copy path.
+static const double *device_view_of_pinned(const double *p)
+{
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (pa.type != cudaMemoryTypeHost || !pa.devicePointer) return nullptr;
+    return (const double *)pa.devicePointer;
+}
+
 int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, const double *A, int lda,
                                     const double *B, int ldb, double *X, int ldx, double tol, int max_iter,
                                     starpu_gb300_ir_info *info)
@@ -535,14 +591,25 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
     // column panels (rows j0..n-1 of columns j0..j0+w-1), each one pitched
     // copy of whole column segments -- n^2/2 + n w/2 elements instead of n^2
     double abytes = 0.0;
-    for (int j0 = 0; j0 < n; j0 += HOST_PANEL) {
-        const int w = std::min(HOST_PANEL, n - j0);
-        const size_t rows = (size_t)(n - j0);
-        if ((rc = gb300_record_cuda_error(cudaMemcpy2DAsync(h->A + j0 + (size_t)j0 * n, sizeof(double) * n,
-                                                            A + j0 + (size_t)j0 * lda, sizeof(double) * lda,
-                                                            sizeof(double) * rows, w, cudaMemcpyHostToDevice, s))))
-            return rc;
-        abytes += 8.0 * rows * w;
+    const double *mapped = device_view_of_pinned(A);
+    if (mapped) {
+        // pinned host memory the GPU can read: one kernel pulls exactly the
+        // lower triangle over the host link (pitched copies of column
+        // segments run far below the link rate)
+        gb300_count_launch(), gather_lower_kernel<<<n, 256, 0, s>>>(n, mapped, lda, h->A, n);
+        if ((rc = gb300_last_launch_status())) return rc;
+        abytes = 8.0 * n * (n + 1.0) / 2.0;
+    } else {
+        for (int j0 = 0; j0 < n; j0 += HOST_PANEL) {
+            const int w = std::min(HOST_PANEL, n - j0);
+            const size_t rows = (size_t)(n - j0);
+            if ((rc = gb300_record_cuda_error(cudaMemcpy2DAsync(h->A + j0 + (size_t)j0 * n, sizeof(double) * n,
+                                                                A + j0 + (size_t)j0 * lda, sizeof(double) * lda,
+                                                                sizeof(double) * rows, w, cudaMemcpyHostToDevice,
+                                                                s))))
+                return rc;
+            abytes += 8.0 * rows * w;
+        }
     }
     if ((rc = gb300_record_cuda_error(
              ldb == n ? cudaMemcpyAsync(h->B, B, sizeof(double) * (size_t)n * nrhs, cudaMemcpyHostToDevice, s)
