@@ -144,7 +144,8 @@ starpu_gb300_server *starpu_gb300_server_create(size_t hbm_budget_bytes, int exe
                                                 int mode);
 /* Queue a request (the struct must stay valid until it is done).  0 or GB300_EINVAL. */
 int starpu_gb300_server_submit(starpu_gb300_server *server, starpu_gb300_request *req);
-/* Block until req is done; returns req->status. */
+/* Block until req is done; returns req->status (GB300_EINVAL for a NULL server
+ * or a request that was not queued). */
 int starpu_gb300_server_wait(starpu_gb300_server *server, starpu_gb300_request *req);
 /* Block until every submitted request is done. */
 int starpu_gb300_server_drain(starpu_gb300_server *server);

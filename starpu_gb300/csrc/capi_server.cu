@@ -377,13 +377,17 @@ int starpu_gb300_server_submit(starpu_gb300_server *sv, starpu_gb300_request *r)
 
 int starpu_gb300_server_wait(starpu_gb300_server *sv, starpu_gb300_request *r)
 {
+    if (!sv || !r) return GB300_EINVAL;
+    // a request that was never queued is not waited for: with nothing in
+    // flight and r not done, submit refused it (or it was never submitted)
     std::unique_lock<std::mutex> lk(sv->mu);
-    sv->cv_done.wait(lk, [&] { return r->done != 0; });
-    return r->status;
+    sv->cv_done.wait(lk, [&] { return r->done != 0 || sv->inflight == 0; });
+    return r->done ? r->status : GB300_EINVAL;
 }
 
 int starpu_gb300_server_drain(starpu_gb300_server *sv)
 {
+    if (!sv) return GB300_EINVAL;
     std::unique_lock<std::mutex> lk(sv->mu);
     sv->cv_done.wait(lk, [&] { return sv->inflight == 0; });
     return GB300_OK;

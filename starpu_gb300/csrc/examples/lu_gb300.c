@@ -11,8 +11,11 @@
  *   lu_gb300 [-size n] [-nblocks b] [-double] [-piv] [-check] [-seed s] [-niter k] [-small-pivots]
  *
  * Input as the reference driver (lu_example.c:221-233): a_ij uniform [0, 1),
- * a_ii = (a_ii + 1) * n; -small-pivots zeroes some diagonal entries so that
- * pivoting triggers.  -check: || A P v - L (U v) || / (||A|| ||v|| n) for
+ * a_ii = (a_ii + 1) * n.  -small-pivots zeroes row i up to and including the
+ * diagonal for i = 5, 102, 199, ... (i mod 97 = 5): every term of that step's
+ * eliminated pivot is then a product with an exact zero, so the pivot is
+ * exactly 0 in either precision and the step must pivot (a zero diagonal
+ * entry alone leaves a pivot near -0.8 / n, above both thresholds).  -check: || A P v - L (U v) || / (||A|| ||v|| n) for
  * random v (P the recorded column swaps), must be <= 1e-4 (the reference's
  * PIVOT_THRESHHOLD bound on ||PA - LU|| / (||A|| n)).  Prints "n ms GFlop/s"
  * (flops 2 n^3 / 3).  Exit 77 without a CUDA worker, 1 on a failed check.
@@ -187,7 +190,7 @@ int main(int argc, char **argv)
             for (unsigned i = 0; i < n; ++i) {
                 double v = drand48();
                 if (i == j) v = (v + 1.0) * n;
-                if (small_pivots && i == j && (i % 97 == 5)) v = 0.0;
+                if (small_pivots && j <= i && (i % 97 == 5)) v = 0.0;
                 if (is_double) ((double *)A)[(size_t)i + (size_t)j * n] = v;
                 else ((float *)A)[(size_t)i + (size_t)j * n] = (float)v;
             }

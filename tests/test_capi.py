@@ -58,6 +58,27 @@ def test_codelet_library_defines_the_reference_symbols(libs):
         assert hasattr(chol, sym), sym
 
 
+def test_lu_codelet_library_defines_the_reference_symbols(libs):
+    lu = C.CDLL(os.path.join(ROOT, "starpu_gb300", "lib", "libstarpu_gb300_lu.so"))
+    for sym in ("cl_getrf", "cl_getrf_pivot", "cl_trsm_ll", "cl_trsm_ru", "cl_gemm", "cl_pivot", "scratch",
+                "devInfo", "lu_kernel_init", "lu_kernel_fini"):
+        assert hasattr(lu, sym), sym
+
+
+def test_tests_keep_device_buffers_alive():
+    """A DeviceBuffer frees its memory when its last reference goes, so the
+    pointer read off a buffer made inside a call's arguments is already freed
+    when the kernel runs.  No test may pass one."""
+    bad = []
+    here = os.path.dirname(os.path.abspath(__file__))
+    for name in sorted(os.listdir(here)):
+        if name.endswith(".py"):
+            for no, line in enumerate(open(os.path.join(here, name)), 1):
+                if re.search(r"\)\.ptr\b", line.split("#")[0]):
+                    bad.append(f"{name}:{no}: {line.strip()}")
+    assert not bad, bad
+
+
 def test_invalid_arguments_are_rejected_without_a_gpu(libs):
     main, _ = libs
     EINVAL = -22
@@ -66,4 +87,7 @@ def test_invalid_arguments_are_rejected_without_a_gpu(libs):
     assert main.starpu_gb300_spotrs_noalloc(None, 16385, 1, None, 16385, None, 16385, None) == EINVAL
     assert main.starpu_gb300_dsposv(None, 10, 1, None, 10, None, 10, None, 10, 0, 2, 1e-12, 10, None, 0, None) == EINVAL
     assert main.starpu_gb300_dsposv_workspace(32768, 16, 1024) > 4 * 32768 * 32768
+    assert main.starpu_gb300_server_wait(None, None) == EINVAL
+    assert main.starpu_gb300_server_drain(None) == EINVAL
+    assert main.starpu_gb300_server_submit(None, None) == EINVAL
     assert main.starpu_gb300_launch_count() == 0

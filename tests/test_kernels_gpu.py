@@ -179,7 +179,10 @@ def test_not_spd_sets_info_without_fault(gpu):
     gpu.starpu_gb300_stream_sync(None)
     assert info.download((1,), np.int32)[0] == 151
     # the context is still usable
-    check(gpu.starpu_gb300_dpotrf_tile(None, 4, up(np.eye(4)).ptr, 4, None))
+    d4 = up(np.eye(4))
+    check(gpu.starpu_gb300_dpotrf_tile(None, 4, d4.ptr, 4, None))
+    gpu.starpu_gb300_stream_sync(None)
+    np.testing.assert_array_equal(d4.download((4, 4), np.float64), np.eye(4))
 
 
 def test_device_generator_matches_oracle(gpu, oracle):

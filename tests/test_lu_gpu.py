@@ -106,8 +106,9 @@ def test_triangular_solves_ragged_vs_oracle(gpu, oracle, p, m, n):
     oracle.lu_trsm_ll(Lm, r1)
     oracle.lu_trsm_ru(Un, r2)
     b1, b2 = up(B), up(B)
-    check(getattr(gpu, f"starpu_gb300_{p}trsm_llnn_tile")(None, m, n, up(Lm).ptr, m, b1.ptr, m))
-    check(getattr(gpu, f"starpu_gb300_{p}trsm_runu_tile")(None, m, n, up(Un).ptr, n, b2.ptr, m))
+    dl, du = up(Lm), up(Un)  # held until the kernels have run: a dropped buffer is freed at once
+    check(getattr(gpu, f"starpu_gb300_{p}trsm_llnn_tile")(None, m, n, dl.ptr, m, b1.ptr, m))
+    check(getattr(gpu, f"starpu_gb300_{p}trsm_runu_tile")(None, m, n, du.ptr, n, b2.ptr, m))
     assert rel(down(b1, B), r1) <= 10 * TOL[p]
     assert rel(down(b2, B), r2) <= 10 * TOL[p]
 

@@ -83,10 +83,11 @@ def test_repeat_rhs_reuses_the_device_factor(gpu, oracle, problems):
     r1, X1 = request(A, B, 777)
     r2, X2 = request(None, B2, 777)  # matrix not resent: the cached factor is used
     sv = gpu.starpu_gb300_server_create(24 * GB, 2, 2048, 16, 0)
+    assert sv, gpu.starpu_gb300_last_error()
     try:
-        gpu.starpu_gb300_server_submit(sv, C.byref(r1))
+        assert gpu.starpu_gb300_server_submit(sv, C.byref(r1)) == 0
         assert gpu.starpu_gb300_server_wait(sv, C.byref(r1)) == 0
-        gpu.starpu_gb300_server_submit(sv, C.byref(r2))
+        assert gpu.starpu_gb300_server_submit(sv, C.byref(r2)) == 0
         assert gpu.starpu_gb300_server_wait(sv, C.byref(r2)) == 0
     finally:
         gpu.starpu_gb300_server_destroy(sv)
