@@ -577,6 +577,18 @@ static const double *device_view_of_pinned(const double *p)
     return (const double *)pa.devicePointer;
 }
 
+// The device view of a whole column-major n x n host matrix (ld lda): both
+// its first and its last element must be pinned and mapped at the same
+// offset, else the copy path is taken.
+static const double *device_view_of_pinned_matrix(const double *A, int n, int lda)
+{
+    const double *d0 = device_view_of_pinned(A);
+    if (!d0) return nullptr;
+    const size_t last = (size_t)(n - 1) + (size_t)(n - 1) * lda;
+    const double *d1 = device_view_of_pinned(A + last);
+    return d1 == d0 + last ? d0 : nullptr;
+}
+
 int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, const double *A, int lda,
                                     const double *B, int ldb, double *X, int ldx, double tol, int max_iter,
                                     starpu_gb300_ir_info *info)
@@ -591,7 +603,7 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
     // column panels (rows j0..n-1 of columns j0..j0+w-1), each one pitched
     // copy of whole column segments -- n^2/2 + n w/2 elements instead of n^2
     double abytes = 0.0;
-    const double *mapped = device_view_of_pinned(A);
+    const double *mapped = device_view_of_pinned_matrix(A, n, lda);
     if (mapped) {
         // pinned host memory the GPU can read: one kernel pulls exactly the
         // lower triangle over the host link (pitched copies of column
