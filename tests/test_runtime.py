@@ -138,3 +138,20 @@ def test_unchanged_reference_lu_drivers_on_cpu_workers(prog, mode):
     assert r.returncode == 0, r.stdout + r.stderr
     m = re.search(r"\|\|P?A-LU\|\| / \(\|\|A\|\|\*N\) : ([0-9.e+-]+)", r.stderr)
     assert m and float(m.group(1)) <= 1e-6, r.stderr
+
+
+@pytest.mark.parametrize("prog", ["lu_implicit_gb300_float", "lu_implicit_gb300_double"])
+@pytest.mark.parametrize("mode", [[], ["-piv"]])
+def test_unchanged_reference_lu_driver_links_gb300_lu_codelets(prog, mode):
+    """The unchanged LU drivers link libstarpu_gb300_lu.so in place of
+    xlu_kernels.c (every codelet, handle and init/fini symbol resolves).  Its
+    codelets are CUDA-only, so without a CUDA worker every submit returns
+    -ENODEV and the driver exits 77 (lu_example.c:537)."""
+    if not os.path.isdir(os.path.join(REF, "examples", "lu")):
+        pytest.skip("reference tree not available on this machine")
+    _lib()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}", "_ref/" + prog], check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", prog)
+    r = subprocess.run([exe, "-size", "256", "-nblocks", "2", *mode], env=_env(STARPU_NCUDA=0, STARPU_NCPU=2),
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 77, r.stdout + r.stderr
