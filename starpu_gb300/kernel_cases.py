@@ -7,6 +7,7 @@
     python -m starpu_gb300.kernel_cases dsposv    --n 8192  --nb 1024 --nrhs 16 --reps 2
     python -m starpu_gb300.kernel_cases spotrf_tc --n 8192  --nb 1024 --nterms 3 --reps 2
     python -m starpu_gb300.kernel_cases dpotrf    --n 8192  --nb 512 --reps 2
+    python -m starpu_gb300.kernel_cases tile_ops  --n 1024 --reps 200
 
 Each case allocates its operands once, runs `--reps` launches of the same
 shape and prints the mean time per launch measured with CUDA events.
@@ -39,7 +40,8 @@ def _timed(L, fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv"])
+    ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv",
+                                     "tile_ops"])
     ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--n", type=int, default=8192)
@@ -114,6 +116,40 @@ def main(argv=None):
             check(L.starpu_gb300_spotrf_tc(None, n, F.ptr, n, nb, a.nterms, Wk.ptr, ws, info.ptr, err.ptr))
         ms = _timed(L, run, a.reps)
         out.update(ms_including_upload=ms)
+    elif a.case == "tile_ops":
+        # the FP32 pieces of the mixed solve's diagonal-tile factorisation: the
+        # 64 x 64 leaf, the whole n x n tile, and one step's panel TRSM and SYRK
+        # at their largest shape (n - 64 rows, 64 columns)
+        n = a.n
+        i = np.arange(n, dtype=np.float32)
+        Ah = np.asfortranarray(1.0 / (1.0 + i[:, None] + i[None, :]), dtype=np.float32)
+        Ah[np.diag_indices(n)] += n
+        A0, Aw = DeviceBuffer.from_array(Ah), DeviceBuffer(4 * n * n)
+        info = DeviceBuffer(4)
+        nbytes = 4 * n * n
+
+        def restore():
+            check(L.starpu_gb300_memcpy_d2d(None, Aw.ptr, A0.ptr, nbytes))
+        ms_copy = _timed(L, restore, a.reps)
+
+        def potrf(k):
+            def f():
+                restore()
+                check(L.starpu_gb300_spotrf_tile(None, k, Aw.ptr, n, info.ptr))
+            return f
+        m, w = n - 64, 64
+        ms_leaf = _timed(L, potrf(64), a.reps) - ms_copy
+        ms_tile = _timed(L, potrf(n), a.reps) - ms_copy
+        restore()
+        check(L.starpu_gb300_spotrf_tile(None, n, Aw.ptr, n, info.ptr))
+        Lw = DeviceBuffer.from_array(np.zeros((n, n), np.float32))
+        check(L.starpu_gb300_memcpy_d2d(None, Lw.ptr, Aw.ptr, nbytes))
+        ms_trsm = _timed(L, lambda: check(L.starpu_gb300_strsm_rltn_tile(None, m, w, 1.0, Lw.ptr, n, Aw.ptr + 4 * 64,
+                                                                          n)), a.reps)
+        ms_syrk = _timed(L, lambda: check(L.starpu_gb300_ssyrk_ln_tile(None, m, w, -1.0, Lw.ptr + 4 * 64, n, 1.0,
+                                                                        Aw.ptr + 4 * (64 + 64 * n), n)), a.reps)
+        out.update(n=n, ms_leaf64=ms_leaf, ms_tile=ms_tile, ms_trsm=ms_trsm, ms_syrk=ms_syrk, ms_restore=ms_copy,
+                   tile_gflops=n ** 3 / 3 / ms_tile / 1e6)
     elif a.case == "dpotrf":
         n, nb = a.n, a.nb
         A = DeviceBuffer(8 * n * n)
