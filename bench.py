@@ -33,6 +33,10 @@ sys.path.insert(0, ROOT)
 METRIC = "SPD solve GFLOP/s @1e-12 backward err, mixed vs FP64; solves/s + p99 latency"
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one tc_update_kernel launch,
+# m = 8192, k = 1024, 3 split-BF16 products (ncu, GB300)
+TC_TRAFFIC_M8192 = 249.5e6
+
 def solve_flops(n: int, nrhs: int) -> float:
     return n ** 3 / 3.0 + 2.0 * n * n * nrhs
 
@@ -428,9 +432,25 @@ def run_ours(args):
         v["share"] = v["ms_per_step"] / ms if ms else None
     tc = prof["tc_update"]
     peak_tc = peaks["bf16_tflops_sustained"]
+    traffic, traffic_src = args.tc_traffic, "given on the command line"
+    if traffic is None:
+        # DRAM bytes per launch: the ncu capture of one m = 8192, k = 1024
+        # launch (dram__bytes_read.sum + dram__bytes_write.sum) scaled to each
+        # trailing update of the factorisation (m = n - (k+1) nb) by its
+        # algorithmic bytes (FP32 C lower triangle read + written, two BF16
+        # K-major panels), averaged over the launches like `achieved`
+        def tc_bytes(m, kb=nb):
+            ldk = (kb + 63) // 64 * 64
+            return 8.0 * m * (m + 1) / 2 + 2.0 * m * ldk * 2
+        ms_list = [n - (k + 1) * nb for k in range((n + nb - 1) // nb - 1)]
+        if ms_list:
+            traffic = sum(TC_TRAFFIC_M8192 * tc_bytes(m) / tc_bytes(8192, 1024) for m in ms_list) / len(ms_list)
+            traffic_src = (f"ncu capture of an m=8192 k=1024 launch ({TC_TRAFFIC_M8192 / 1e6:.1f} MB) scaled by "
+                           f"algorithmic bytes to the {len(ms_list)} launches of one factorisation, mean per launch")
     roofline = {"bound": "tensor", "achieved": tc["tflops"], "peak": peak_tc, "unit": "TFLOP/s",
                 "frac": (tc["tflops"] / peak_tc) if tc["tflops"] else None,
-                "traffic": args.tc_traffic, "kernel": "tc_update_kernel (split-BF16 tcgen05 trailing update)",
+                "traffic": traffic, "traffic_source": traffic_src,
+                "kernel": "tc_update_kernel (split-BF16 tcgen05 trailing update)",
                 "peak_source": f"{peaks['source']} bf16 sustained (kernel timed inside a long step)",
                 "algorithmic": "flops = nterms * kb * m*(m+1) per launch (lower triangle of an m x m rank-kb update)"}
 
@@ -596,7 +616,8 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=8192)
     ap.add_argument("--cpu-nb", type=int, default=512)
     ap.add_argument("--tc-traffic", type=float, default=None,
-                    help="ncu dram bytes of one trailing-update launch scaled to a full launch (profiles/)")
+                    help="DRAM bytes per trailing-update launch (default: the ncu capture of an m = 8192 launch "
+                         "scaled to the factorisation's launches)")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-fp64-same-n", action="store_true")
