@@ -9,6 +9,7 @@
 #include <stdio.h>
 
 #include "gb300_internal.h"
+#include "kernels/diag_coop.cuh"
 #include "kernels/tc_update.cuh"
 #include "starpu_gb300_kernels.h"
 #include "starpu_gb300_solver.h"
@@ -143,11 +144,13 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
 
 // Workspace of potrf_tc for order n and tile nb (ldk = nb rounded up to 64):
 // the split panel (hi, lo: n x ldk BF16 each), the inverse of the diagonal
-// tile (ldk x ldk FP32) and its split (hi, lo), and the doubling scratch of
-// the triangular inverse (ldk * ldk / 4 FP32).
+// tile (ldk x ldk FP32) and its split (hi, lo), the doubling scratch of the
+// triangular inverse (ldk x ldk FP32) and the diagonal-tile kernel's barrier
+// counter.
 struct TcWs {
     __nv_bfloat16 *hi, *lo, *ihi, *ilo;
     float *linv, *scratch;
+    unsigned *bar;  // grid-barrier counter of the diagonal-tile kernel
 };
 static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
 {
@@ -161,8 +164,49 @@ static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
         w->ihi = (__nv_bfloat16 *)(w->linv + inv);
         w->ilo = w->ihi + inv;
         w->scratch = (float *)(w->ilo + inv);
+        w->bar = (unsigned *)(w->scratch + inv);
     }
-    return 2 * panel + inv * 4 + 2 * inv * 2 + inv;  // scratch: inv / 4 floats
+    return 2 * panel + inv * 4 + 2 * inv * 2 + inv * 4 + 256;
+}
+
+// Factor the FP32 diagonal tile (n <= DC_MAXN) in place and, when `invert`,
+// write its lower-triangular inverse to Linv (ld ldi): one cooperative launch
+// of diag_coop_kernel, the grid sized to the widest phase and to what can be
+// resident at once.
+static int diag_factor_inverse(cudaStream_t s, int n, float *A, long lda, float *Linv, long ldi, float *T,
+                               unsigned *bar, int *info, int info_base, int *err, bool invert)
+{
+    static int occ = -1;
+    if (occ < 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, diag_coop_kernel, DC_T, 0) != cudaSuccess) {
+        cudaGetLastError();
+        occ = 1;
+    }
+    const int nblk = (n + DC_B - 1) / DC_B;
+    int work = std::max(nblk, nblk * (nblk - 1) / 2);
+    for (int h = DC_B; invert && h < n; h *= 2) {
+        int tiles = 0;
+        for (int o = 0; o + h < n; o += 2 * h) tiles += ((std::min(h, n - o - h) + DC_B - 1) / DC_B) * (h / DC_B);
+        work = std::max(work, tiles);
+    }
+    const int grid = std::max(1, std::min(work, num_sms() * std::max(occ, 1)));
+    if (invert) cudaMemset2DAsync(Linv, ldi * sizeof(float), 0, n * sizeof(float), n, s);
+    cudaMemsetAsync(bar, 0, sizeof(unsigned), s);
+    DiagCoopArgs a;
+    a.n = n;
+    a.A = A;
+    a.lda = lda;
+    a.Linv = Linv;
+    a.ldi = ldi;
+    a.T = T;
+    a.info = info;
+    a.info_base = info_base;
+    a.bar = bar;
+    a.err = err;
+    a.invert = invert ? 1 : 0;
+    void *args[] = {&a};
+    gb300_count_launch();
+    return gb300_record_cuda_error(
+        cudaLaunchCooperativeKernel((const void *)diag_coop_kernel, dim3(grid), dim3(DC_T), args, 0, s));
 }
 
 // Tiled right-looking Cholesky of an FP32 matrix on the tensor cores
@@ -181,14 +225,20 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
         float *Akk = A + k0 + (long)k0 * lda;
         const int m = n - k0 - kb;
         int slot = gb300_prof_begin(s, GB300_PROF_PANEL);
-        potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
+        int rc = 0;
+        if (kb <= DC_MAXN) {
+            rc = diag_factor_inverse(s, kb, Akk, lda, w.linv, ldk, w.scratch, w.bar, d_info, k0, d_err, m > 0);
+        } else {
+            potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
+            if (m > 0) trtri_lower<float>(s, kb, Akk, lda, w.linv, ldk, w.scratch);
+        }
+        if (rc) return rc;
         if (m <= 0) {
             gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0, 4.0 * kb * kb);
             break;
         }
         float *P = A + (k0 + kb) + (long)k0 * lda;
-        trtri_lower<float>(s, kb, Akk, lda, w.linv, ldk, w.scratch);
-        int rc = split_bf16(s, kb, kb, w.linv, ldk, w.ihi, w.ilo, ldk);
+        rc = split_bf16(s, kb, kb, w.linv, ldk, w.ihi, w.ilo, ldk);
         if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, w.lo, ldk);
         if (!rc) rc = tc_update(s, m, kb, kb, w.hi, w.lo, ldk, w.ihi, w.ilo, ldk, 3, 0, P, lda, d_err, 1);
         if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, np > 1 ? w.lo : nullptr, ldk);

@@ -129,3 +129,39 @@ def test_spotrf_tc_gram_residual(gpu, oracle):
         res[nterms] = oracle.llt_residual(A, L)
     assert res[1] < 1e-2
     assert res[3] < 1e-5
+
+
+@pytest.mark.parametrize("n,nb", [(2000, 1000), (700, 333), (1088, 1024), (130, 64), (1024, 1024)])
+def test_spotrf_tc_diagonal_tile_shapes(gpu, oracle, n, nb):
+    """The diagonal tile is factored and inverted by one cooperative launch in
+    64 x 64 blocks: ragged last blocks (1000 = 15 x 64 + 40, 333), a ragged
+    last doubling pair, a 64 tail, a tile with no panel below it.  The factor
+    meets the split-BF16 residual bound, the strict upper triangle is never
+    written, and no barrier wait runs out."""
+    A = oracle.spd_gram(n, 7, 1.0).astype(np.float32)
+    A[np.triu_indices(n, 1)] = -3.0  # never read, never written
+    d = DeviceBuffer.from_array(A)
+    ws = gpu.starpu_gb300_spotrf_tc_workspace(n, nb)
+    W = DeviceBuffer(ws)
+    info, err = zeros_err(), zeros_err()
+    check(gpu.starpu_gb300_spotrf_tc(None, n, d.ptr, n, nb, 3, W.ptr, ws, info.ptr, err.ptr))
+    out = d.download((n, n), np.float32)
+    assert info.download((1,), np.int32)[0] == 0
+    assert err.download((1,), np.int32)[0] == 0
+    np.testing.assert_array_equal(out[np.triu_indices(n, 1)], -3.0)
+    Af = np.tril(A.astype(np.float64)) + np.tril(A.astype(np.float64), -1).T
+    assert oracle.llt_residual(Af, np.tril(out)) < 1e-5
+
+
+def test_spotrf_tc_reports_the_first_non_positive_pivot(gpu):
+    n, nb = 700, 333
+    A = np.eye(n, dtype=np.float32) * 2
+    A[450, 450] = -1.0  # tile 1 (333..665), 64-block 1 of that tile, row 53 of it
+    d = DeviceBuffer.from_array(A)
+    ws = gpu.starpu_gb300_spotrf_tc_workspace(n, nb)
+    W = DeviceBuffer(ws)
+    info, err = zeros_err(), zeros_err()
+    check(gpu.starpu_gb300_spotrf_tc(None, n, d.ptr, n, nb, 3, W.ptr, ws, info.ptr, err.ptr))
+    assert info.download((1,), np.int32)[0] == 451
+    assert err.download((1,), np.int32)[0] == 0
+
