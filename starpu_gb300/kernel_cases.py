@@ -8,6 +8,7 @@
     python -m starpu_gb300.kernel_cases spotrf_tc --n 8192  --nb 1024 --nterms 3 --reps 2
     python -m starpu_gb300.kernel_cases dpotrf    --n 8192  --nb 512 --reps 2
     python -m starpu_gb300.kernel_cases tile_ops  --n 1024 --reps 200
+    python -m starpu_gb300.kernel_cases diag      --n 1024 --reps 50
 
 Each case allocates its operands once, runs `--reps` launches of the same
 shape and prints the mean time per launch measured with CUDA events.
@@ -38,10 +39,18 @@ def _timed(L, fn, reps):
     return ms
 
 
+def oracle_free_spd(n):
+    """FP32 SPD test matrix: 1 / (1 + i + j) plus n on the diagonal."""
+    i = np.arange(n, dtype=np.float32)
+    A = 1.0 / (1.0 + i[:, None] + i[None, :])
+    A[np.diag_indices(n)] += n
+    return A.astype(np.float32)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv",
-                                     "tile_ops"])
+                                     "tile_ops", "diag"])
     ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--n", type=int, default=8192)
@@ -150,6 +159,28 @@ def main(argv=None):
                                                                         Aw.ptr + 4 * (64 + 64 * n), n)), a.reps)
         out.update(n=n, ms_leaf64=ms_leaf, ms_tile=ms_tile, ms_trsm=ms_trsm, ms_syrk=ms_syrk, ms_restore=ms_copy,
                    tile_gflops=n ** 3 / 3 / ms_tile / 1e6)
+    elif a.case == "diag":
+        # the tensor-core Cholesky's diagonal-tile step alone: spotrf_tc of an
+        # n x n matrix with nb = n (factor only), and of n + 64 with nb = n
+        # (factor + inverse of the n x n tile, then a 64-row panel and update)
+        n = a.n
+        out.update(n=n)
+        for tag, N in (("factor", n), ("factor_inverse_plus_64", n + 64)):
+            Ah = np.asfortranarray(oracle_free_spd(N))
+            A0, Aw = DeviceBuffer.from_array(Ah), DeviceBuffer(4 * N * N)
+            ws = L.starpu_gb300_spotrf_tc_workspace(N, n)
+            Wk = DeviceBuffer(ws)
+            info, err = DeviceBuffer(4), DeviceBuffer.from_array(np.zeros(1, np.int32))
+
+            def restore():
+                check(L.starpu_gb300_memcpy_d2d(None, Aw.ptr, A0.ptr, 4 * N * N))
+
+            def run():
+                restore()
+                check(L.starpu_gb300_spotrf_tc(None, N, Aw.ptr, N, n, 3, Wk.ptr, ws, info.ptr, err.ptr))
+            ms_copy = _timed(L, restore, a.reps)
+            out["ms_" + tag] = _timed(L, run, a.reps) - ms_copy
+            out["err_" + tag] = int(DeviceBuffer.download(err, (1,), np.int32)[0])
     elif a.case == "dpotrf":
         n, nb = a.n, a.nb
         A = DeviceBuffer(8 * n * n)
