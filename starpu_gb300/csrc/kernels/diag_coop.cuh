@@ -101,133 +101,146 @@ __device__ __forceinline__ void dc_load(float *s, const float *g, long ld, int r
     }
 }
 
-// Unblocked Cholesky of the bk x bk lower block in D (shared), in place.
-// Thread (ti = row, tc = tid / 64) keeps row ti, columns tc, tc + 4, ... in
-// registers; column z is published through a double-buffered shared vector,
-// one barrier per step.  A non-positive pivot sets info (first wins) when
-// `report`.  invd[j] = 1 / l_jj on return.
-__device__ __forceinline__ void dc_potf2(float *D, int bk, float *colbuf, float *invd, int *info, int info_base,
-                                         bool report)
+// Cholesky of the nb x nb (nb <= 32) lower block of D at offset `off`, in
+// place, by one warp: lane i holds row i in registers, the step loop is
+// unrolled (static register indices) and column values travel by shuffles,
+// so no CTA barrier sits on the chain.  Lanes i >= nb hold identity rows.
+// 1/l_zz comes from rsqrtf: this factor is the mixed solve's FP32 working
+// factor, refined afterwards, so the last ulp of the pivots does not matter.
+// invd[i] = 1 / l_ii.  The first non-positive pivot sets *info (first wins).
+__device__ __noinline__ void dc_potf2_32(float *D, int off, int nb, float *invd, int *info, int info_base,
+                                            bool report)
 {
-    const int tid = threadIdx.x, ti = tid & 63, tc = tid >> 6;
-    float a[16];
+    const unsigned FULL = 0xffffffffu;
+    const int i = threadIdx.x & 31;
+    float a[32];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-        const int c = tc + 4 * q;
-        a[q] = (ti < bk && c <= ti) ? D[c * DC_LD + ti] : 0.0f;
+    for (int c = 0; c < 32; ++c) a[c] = (i < nb) ? ((c <= i) ? D[off + c * DC_LD + i] : 0.0f) : (c == i ? 1.0f : 0.0f);
+    int badz = -1;
+    float myinv = 1.0f;
+#pragma unroll
+    for (int z = 0; z < 32; ++z) {
+        const float d = __shfl_sync(FULL, a[z], z);
+        if (!(d > 0.0f) && badz < 0) badz = z;
+        const float inv = rsqrtf(d);
+        const float li = a[z] * inv;
+        if (i == z) {
+            a[z] = d * inv;
+            myinv = inv;
+        } else if (i > z) {
+            a[z] = li;
+        }
+#pragma unroll
+        for (int c = z + 1; c < 32; ++c) {
+            const float lc = __shfl_sync(FULL, li, c);
+            if (i >= c) a[c] = fmaf(-li, lc, a[c]);
+        }
     }
-    bool bad = false;
-    for (int z = 0; z < bk; ++z) {
-        float *cz = colbuf + (z & 1) * DC_B;
-        const int qz = z >> 2;
-        if (tc == (z & 3)) {
-            float v = a[0];
+    if (i < nb) {
 #pragma unroll
-            for (int q = 1; q < 16; ++q)
-                if (q == qz) v = a[q];
-            cz[ti] = v;
-        }
-        __syncthreads();
-        const float d = cz[z];
-        if (!(d > 0.0f) && !bad) {
-            bad = true;
-            if (report && tid == 0 && info) atomicCAS(info, 0, info_base + z + 1);
-        }
-        const float lzz = sqrtf(d);
-        const float inv = 1.0f / lzz;
-        const float li = cz[ti] * inv;
-        if (tc == (z & 3) && ti >= z) {
-            const float nv = (ti == z) ? lzz : li;
+        for (int c = 0; c < 32; ++c)
+            if (c <= i) D[off + c * DC_LD + i] = a[c];
+    }
+    invd[i] = myinv;
+    if (report && i == 0 && badz >= 0 && badz < nb && info) atomicCAS(info, 0, info_base + badz + 1);
+}
+
+// Cholesky of the bk x bk (bk <= 64) lower block in D (shared), in place:
+// 32 x 32 blocks -- warp 0 factors L11, warp 1 solves L21 = A21 L11^-T (lane
+// = row, unrolled column-oriented substitution), the CTA updates
+// A22 -= L21 L21^T, warp 0 factors L22.  invd[j] = 1 / l_jj (1 for j >= bk).
+__device__ __forceinline__ void dc_potf2(float *D, int bk, float *invd, int *info, int info_base, bool report)
+{
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) dc_potf2_32(D, 0, min(bk, 32), invd, info, info_base, report);
+    __syncthreads();
+    if (bk > 32) {
+        if (warp == 1) {
+            const int r = 32 + lane;
+            float x[32];
 #pragma unroll
-            for (int q = 0; q < 16; ++q)
-                if (q == qz) a[q] = nv;
-        }
-        if (ti > z) {
+            for (int c = 0; c < 32; ++c) x[c] = D[c * DC_LD + r];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int c = tc + 4 * q;
-                if (c > z && c <= ti) a[q] = fmaf(-li, cz[c] * inv, a[q]);
+            for (int j = 0; j < 32; ++j) {
+                x[j] *= invd[j];
+#pragma unroll
+                for (int c = j + 1; c < 32; ++c) x[c] = fmaf(-D[j * DC_LD + c], x[j], x[c]);
+            }
+            if (r < bk) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c) D[c * DC_LD + r] = x[c];
             }
         }
+        __syncthreads();
+        for (int e = tid; e < 32 * 32; e += DC_T) {
+            const int r = 32 + (e & 31), c = 32 + (e >> 5);
+            if (c <= r && r < bk) {
+                float acc = D[c * DC_LD + r];
+#pragma unroll 8
+                for (int p = 0; p < 32; ++p) acc = fmaf(-D[p * DC_LD + r], D[p * DC_LD + c], acc);
+                D[c * DC_LD + r] = acc;
+            }
+        }
+        __syncthreads();
+        if (warp == 0) dc_potf2_32(D, 32 * DC_LD + 32, bk - 32, invd + 32, info, info_base + 32, report);
+    } else if (tid >= 32 && tid < 64) {
+        invd[tid] = 1.0f;
     }
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-        const int c = tc + 4 * q;
-        if (ti < bk && c <= ti) D[c * DC_LD + ti] = a[q];
-    }
-    __syncthreads();
-    if (tid < bk) invd[tid] = 1.0f / D[tid * DC_LD + tid];
     __syncthreads();
 }
 
-// Bs (rows x bk, shared) <- Bs L^-T, L the factored block in D: every row is
-// an independent forward substitution, column-oriented like reference BLAS
-// strsm (x_j *= 1/l_jj, then x_c -= l_cj x_j for c > j).  Four lanes per row,
-// lane l holding columns l, l + 4, ...; x_j is passed within the lane group.
-__device__ __forceinline__ void dc_trsm(const float *D, float *Bs, int bk, const float *invd)
+// Forward substitution with the factored 64 x 64 block L in D, one system
+// per group of four lanes: lane l of the group holds entries 16 l .. 16 l + 15
+// of the group's vector x, which on return is L^-1 x (column-oriented:
+// x_j *= 1/l_jj, then x_c -= l_cj x_j for c > j).  The owner of x_j is lane
+// j / 16, its register j % 16 (a static index: j runs as 4 rolled groups of
+// 16 unrolled steps); x_j reaches the other lanes by a shuffle.
+__device__ __forceinline__ void dc_fwd_subst(const float *D, const float *invd, float x[16])
 {
-    const int tid = threadIdx.x, r = tid >> 2, l = tid & 3, src0 = tid & 28;
+    const int l = threadIdx.x & 3, src0 = threadIdx.x & 28;
+#pragma unroll 1
+    for (int G = 0; G < 4; ++G) {
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+            const int j = 16 * G + jj;
+            const float xo = x[jj] * invd[j];
+            if (l == G) x[jj] = xo;
+            const float xj = __shfl_sync(0xffffffffu, xo, src0 | G);
+            const float *Dj = D + j * DC_LD + 16 * l;
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                if (l > G || (l == G && q > jj)) x[q] = fmaf(-Dj[q], xj, x[q]);
+        }
+    }
+}
+
+// Bs (64 rows, bk columns, shared) <- Bs L^-T with L the factored block in D:
+// row r of Bs is the system of lane group r (threads 4r .. 4r + 3).
+__device__ __forceinline__ void dc_trsm(const float *D, float *Bs, const float *invd)
+{
+    const int r = threadIdx.x >> 2, l = threadIdx.x & 3;
     float x[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) x[q] = Bs[(l + 4 * q) * DC_LD + r];
-    for (int j = 0; j < bk; ++j) {
-        const int qj = j >> 2;
-        float xj = 0.0f;
-        if (l == (j & 3)) {
-            xj = x[0];
+    for (int q = 0; q < 16; ++q) x[q] = Bs[(16 * l + q) * DC_LD + r];
+    dc_fwd_subst(D, invd, x);
 #pragma unroll
-            for (int q = 1; q < 16; ++q)
-                if (q == qj) xj = x[q];
-            xj *= invd[j];
-#pragma unroll
-            for (int q = 0; q < 16; ++q)
-                if (q == qj) x[q] = xj;
-        }
-        xj = __shfl_sync(0xffffffffu, xj, src0 | (j & 3));
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int c = l + 4 * q;
-            if (c > j) x[q] = fmaf(-D[j * DC_LD + c], xj, x[q]);
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < 16; ++q) Bs[(l + 4 * q) * DC_LD + r] = x[q];
+    for (int q = 0; q < 16; ++q) Bs[(16 * l + q) * DC_LD + r] = x[q];
     __syncthreads();
 }
 
-// Lower-triangular inverse X = L^-1 of the factored bk x bk block in D,
-// written to the global block g (ld ldg, lower part only): column c of X is
-// the forward substitution L x = e_c, four lanes per column.
+// X = L^-1 of the factored bk x bk block in D, written to the global block g
+// (ld ldg, lower part only): column c of X solves L x = e_c in lane group c.
 __device__ __forceinline__ void dc_trtri(const float *D, int bk, const float *invd, float *g, long ldg)
 {
-    const int tid = threadIdx.x, c = tid >> 2, l = tid & 3, src0 = tid & 28;
-    float y[16];
+    const int c = threadIdx.x >> 2, l = threadIdx.x & 3;
+    float x[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) y[q] = (l + 4 * q == c) ? 1.0f : 0.0f;
-    for (int p = 0; p < bk; ++p) {
-        const int qp = p >> 2;
-        float xp = 0.0f;
-        if (l == (p & 3)) {
-            xp = y[0];
-#pragma unroll
-            for (int q = 1; q < 16; ++q)
-                if (q == qp) xp = y[q];
-            xp *= invd[p];
-#pragma unroll
-            for (int q = 0; q < 16; ++q)
-                if (q == qp) y[q] = xp;
-        }
-        xp = __shfl_sync(0xffffffffu, xp, src0 | (p & 3));
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int r = l + 4 * q;
-            if (r > p) y[q] = fmaf(-D[p * DC_LD + r], xp, y[q]);
-        }
-    }
+    for (int q = 0; q < 16; ++q) x[q] = (16 * l + q == c) ? 1.0f : 0.0f;
+    dc_fwd_subst(D, invd, x);
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-        const int r = l + 4 * q;
-        if (r < bk && c < bk && r >= c) g[r + (long)c * ldg] = y[q];
+        const int r = 16 * l + q;
+        if (r < bk && c < bk && r >= c) g[r + (long)c * ldg] = x[q];
     }
 }
 
@@ -266,7 +279,7 @@ __device__ __forceinline__ void dc_tri_index(int t, int &ii, int &jj)
 __global__ void __launch_bounds__(DC_T) diag_coop_kernel(DiagCoopArgs a)
 {
     __shared__ float s0[DC_B * DC_LD], s1[DC_B * DC_LD];
-    __shared__ float colbuf[2 * DC_B], invd[DC_B];
+    __shared__ float invd[DC_B];
     __shared__ int s_ok;
     const int n = a.n, nblk = (n + DC_B - 1) / DC_B;
     const int tid = threadIdx.x, tr = tid & 15, tn = tid >> 4;
@@ -279,7 +292,7 @@ __global__ void __launch_bounds__(DC_T) diag_coop_kernel(DiagCoopArgs a)
             float *Akk = a.A + k0 + (long)k0 * a.lda;
             dc_load(s0, Akk, a.lda, bk, bk);
             __syncthreads();
-            dc_potf2(s0, bk, colbuf, invd, a.info, a.info_base + k0, blockIdx.x == 0);
+            dc_potf2(s0, bk, invd, a.info, a.info_base + k0, blockIdx.x == 0);
             for (int i = k + (int)blockIdx.x; i < nblk; i += gridDim.x) {
                 if (i == k) {
                     for (int e = tid; e < DC_B * DC_B; e += DC_T) {
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(DC_T) diag_coop_kernel(DiagCoopArgs a)
                     __syncthreads();  // s1 of the previous block row has been stored
                     dc_load(s1, Aik, a.lda, ri, bk);
                     __syncthreads();
-                    dc_trsm(s0, s1, bk, invd);
+                    dc_trsm(s0, s1, invd);
                     for (int e = tid; e < DC_B * DC_B; e += DC_T) {
                         const int r = e & 63, c = e >> 6;
                         if (r < ri && c < bk) Aik[r + (long)c * a.lda] = s1[c * DC_LD + r];
