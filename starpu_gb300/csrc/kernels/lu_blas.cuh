@@ -41,19 +41,11 @@ __global__ void __launch_bounds__(256) getf2_small_kernel(int n, T *__restrict__
         a[q] = (ti < n && c < n) ? A[(long)ti + (long)c * lda] : T(0);
     }
     bool flagged = false;
-    // rolled step loop (an unrolled one stalls on instruction fetch); column
-    // z's register is picked by a select chain
-#pragma unroll 1
-    for (int z = 0; z < n; ++z) {
-        T *cz = col[z & 1], *rz = row[z & 1];
-        if (tc == z % CL) {
-            const int qz = z / CL;
-            T v = a[0];
 #pragma unroll
-            for (int q = 1; q < NC; ++q)
-                if (q == qz) v = a[q];
-            cz[ti] = v;
-        }
+    for (int z = 0; z < NMAX; ++z) {
+        if (z >= n) break;
+        T *cz = col[z & 1], *rz = row[z & 1];
+        if (tc == z % CL) cz[ti] = a[z / CL];
         if (ti == z) {
 #pragma unroll
             for (int q = 0; q < NC; ++q) rz[tc + q * CL] = a[q];

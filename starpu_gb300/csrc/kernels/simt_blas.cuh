@@ -193,12 +193,10 @@ template <typename T, int NMAX>
 __global__ void __launch_bounds__(256) potf2_small_kernel(int n, T *__restrict__ A, long lda, int *info, int info_base)
 {
     // 256 threads as NMAX rows x CL column lanes; thread (ti, tc) keeps row ti,
-    // columns tc, tc + CL, ... in registers.  The owners publish column z
-    // through a double-buffered shared vector (one barrier per step), every
-    // thread scales its two factors by 1/sqrt(a_zz) itself.  The step loop
-    // stays rolled (a fully unrolled one is NMAX copies of the update and
-    // stalls on instruction fetch); column z's register is picked by a
-    // select chain.
+    // columns tc, tc + CL, ... in registers.  The step loop is unrolled so
+    // that column z lives in a fixed register of its owners; the owners
+    // publish column z through a double-buffered shared vector (one barrier
+    // per step), every thread scales its two factors by 1/sqrt(a_zz) itself.
     constexpr int CL = 256 / NMAX, NC = NMAX / CL;
     __shared__ T col[2][NMAX];
     const int tid = threadIdx.x;
@@ -210,17 +208,11 @@ __global__ void __launch_bounds__(256) potf2_small_kernel(int n, T *__restrict__
         a[q] = (ti < n && c <= ti) ? A[(long)ti + (long)c * lda] : T(0);
     }
     bool bad = false;
-#pragma unroll 1
-    for (int z = 0; z < n; ++z) {
-        T *cz = col[z & 1];
-        const int qz = z / CL;
-        if (tc == z % CL) {  // owners of column z publish it (rows < z hold 0)
-            T v = a[0];
 #pragma unroll
-            for (int q = 1; q < NC; ++q)
-                if (q == qz) v = a[q];
-            cz[ti] = v;
-        }
+    for (int z = 0; z < NMAX; ++z) {
+        if (z >= n) break;
+        T *cz = col[z & 1];
+        if (tc == z % CL) cz[ti] = a[z / CL];  // owners of column z publish it (rows < z hold 0)
         __syncthreads();
         const T d = cz[z];
         if (!(d > T(0)) && !bad) {
@@ -230,12 +222,7 @@ __global__ void __launch_bounds__(256) potf2_small_kernel(int n, T *__restrict__
         const T lzz = sqrt(d);
         const T inv = T(1) / lzz;
         const T li = cz[ti] * inv;
-        if (tc == z % CL && ti >= z) {
-            const T nv = (ti == z) ? lzz : li;
-#pragma unroll
-            for (int q = 0; q < NC; ++q)
-                if (q == qz) a[q] = nv;
-        }
+        if (tc == z % CL) a[z / CL] = (ti == z) ? lzz : (ti > z ? li : a[z / CL]);
         if (ti > z) {
 #pragma unroll
             for (int q = 0; q < NC; ++q) {
