@@ -181,13 +181,16 @@ static int diag_factor_inverse(cudaStream_t s, int n, float *A, long lda, float 
         cudaGetLastError();
         occ = 1;
     }
+    // widest phase: block rows + inverse combines (A), tile updates +
+    // inverse products (B), the last row's products
     const int nblk = (n + DC_B - 1) / DC_B;
-    int work = std::max(nblk, nblk * (nblk - 1) / 2);
-    for (int h = DC_B; invert && h < n; h *= 2) {
-        int tiles = 0;
-        for (int o = 0; o + h < n; o += 2 * h) tiles += ((std::min(h, n - o - h) + DC_B - 1) / DC_B) * (h / DC_B);
-        work = std::max(work, tiles);
+    int work = 1;
+    for (int k = 0; k < nblk; ++k) {
+        const int m = nblk - k - 1;
+        work = std::max(work, nblk - k + (invert && k >= 2 ? k - 1 : 0));
+        if (m > 0) work = std::max(work, m * (m + 1) / 2 + (invert && k >= 1 ? k * (k + 1) / 2 : 0));
     }
+    if (invert) work = std::max(work, nblk * (nblk - 1) / 2);
     const int grid = std::max(1, std::min(work, num_sms() * std::max(occ, 1)));
     if (invert) cudaMemset2DAsync(Linv, ldi * sizeof(float), 0, n * sizeof(float), n, s);
     cudaMemsetAsync(bar, 0, sizeof(unsigned), s);

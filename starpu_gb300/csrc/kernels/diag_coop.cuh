@@ -5,17 +5,19 @@
 //
 // The tile is handled in 64 x 64 blocks, right-looking, as the tile loop of
 // examples/cholesky/cholesky_implicit.c:244-318 with the POTRF/TRSM/SYRK/GEMM
-// codelet arithmetic of cholesky_kernels.c (unblocked POTRF leaf: sqrt, scale
-// by 1/l_zz, rank-1 update; column-oriented TRSM; GEMM updates).  Step k:
-//   A  every CTA of block row i >= k loads the diagonal block, factors it in
-//      shared memory (the same instructions in every CTA, so every copy is
-//      bit-identical), then the CTA of row k stores it and inverts it while
-//      the others solve their block L_ik = A_ik L_kk^-T;
+// codelet arithmetic of cholesky_kernels.c (unblocked POTRF leaf: scale by
+// 1/l_zz, rank-1 update; column-oriented TRSM; GEMM updates).  Step k:
+//   A  every CTA with a block row i >= k loads the diagonal block and factors
+//      it in shared memory (the same instructions in every CTA, so every copy
+//      is bit-identical); the CTA of row k stores it and inverts it, the
+//      others solve their block L_ik = A_ik L_kk^-T;
 //   B  the trailing blocks A_ij -= L_ik L_jk^T (k < j <= i) are spread over
 //      the grid.
-// Then the inverse of the whole tile by doubling: for h = 64, 128, ...,
-// [L11 0; L21 L22]^-1 = [I11 0; -I22 L21 I11  I22] on pairs of order-h
-// diagonal blocks, T = L21 I11 into scratch, then X21 = -I22 T.
+// The inverse X = L^-1 is built on the way, block row by block row from
+// L X = I:  X_kj = -X_kk sum_{p=j}^{k-1} L_kp X_pj.  The products of row k
+// run in phase B of step k, their sums and the X_kk multiply in phase A of
+// step k+1, both in CTAs the factorisation leaves idle; only the last block
+// row follows the factorisation.
 //
 // Phases are separated by grid barriers: a launch counter that each CTA
 // bumps, waited on with acquire loads.  The launch is cooperative (every CTA
@@ -37,7 +39,7 @@ __device__ __forceinline__ uint64_t dc_timer()
 
 constexpr int DC_B = 64;         // block order
 constexpr int DC_T = 256;        // threads per CTA
-constexpr int DC_LD = DC_B + 1;  // pitch of a shared tile (column-major: s[c * DC_LD + r])
+constexpr int DC_LD = DC_B + 4;  // pitch of a shared tile (column-major: s[c * DC_LD + r]); float4-aligned
 constexpr int DC_MAXN = 1024;
 constexpr int DC_ERR_TIMEOUT = 4;  // *err code of a barrier wait that ran out
 constexpr uint64_t DC_WAIT_NS = 1000000000ull;
@@ -48,7 +50,7 @@ struct DiagCoopArgs {
     long lda;
     float *Linv;  // n x n, strict upper part zeroed by the caller
     long ldi;
-    float *T;  // scratch of the doubling products: n * n floats
+    float *T;  // scratch of the inverse's block products: n * n floats
     int *info;
     int info_base;
     unsigned *bar;  // barrier counter, zero at launch
@@ -244,24 +246,34 @@ __device__ __forceinline__ void dc_trtri(const float *D, int bk, const float *in
     }
 }
 
-// acc (thread's 4 x 4 of a 64 x 64 tile) += As * op(Bs): As 64 x 64, Bs
-// 64 x 64 read as B (NN) or B^T (NT).  Thread (tr = tid % 16, tn = tid / 16)
-// owns rows tr + 16 a and columns tn + 16 b.
-template <bool NT>
+// acc += As * Bs for 64 x 64 shared tiles: As column-major (As[p * DC_LD + r]
+// = A(r, p)), Bs stored p-major (Bs[p * DC_LD + c] = B(p, c)) -- which is how
+// dc_load stores a tile whose transpose is the operand (NT products).
+// Thread (tr = tid % 16, tn = tid / 16) owns rows 4 tr .. 4 tr + 3 and
+// columns 4 tn .. 4 tn + 3: two float4 shared loads per 16 FMAs.
 __device__ __forceinline__ void dc_mma(const float *As, const float *Bs, float acc[4][4])
 {
     const int tr = threadIdx.x & 15, tn = threadIdx.x >> 4;
-#pragma unroll 4
+#pragma unroll 8
     for (int p = 0; p < DC_B; ++p) {
-        float av[4], bv[4];
+        const float4 av = *reinterpret_cast<const float4 *>(As + p * DC_LD + 4 * tr);
+        const float4 bv = *reinterpret_cast<const float4 *>(Bs + p * DC_LD + 4 * tn);
+        const float ar[4] = {av.x, av.y, av.z, av.w}, br[4] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
-        for (int a = 0; a < 4; ++a) av[a] = As[p * DC_LD + tr + 16 * a];
+        for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) bv[b] = NT ? Bs[p * DC_LD + tn + 16 * b] : Bs[(tn + 16 * b) * DC_LD + p];
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(ar[i], br[j], acc[i][j]);
+    }
+}
+
+// rows x cols block of a column-major global matrix into a shared tile
+// stored p-major (s[r * DC_LD + c] = g(r, c)), zero outside: the B operand
+// of an NN product.
+__device__ __forceinline__ void dc_load_t(float *s, const float *g, long ld, int rows, int cols)
+{
+    for (int e = threadIdx.x; e < DC_B * DC_B; e += DC_T) {
+        const int r = e & (DC_B - 1), c = e >> 6;
+        s[r * DC_LD + c] = (r < rows && c < cols) ? __ldcg(g + r + (long)c * ld) : 0.0f;
     }
 }
 
@@ -276,24 +288,114 @@ __device__ __forceinline__ void dc_tri_index(int t, int &ii, int &jj)
     jj = t - i * (i + 1) / 2;
 }
 
+// C (rows x cols of a column-major global matrix) -= acc, where the mask
+// `lower` keeps only elements on or below the diagonal.  vec: C and ld allow
+// float4 accesses along the thread's four rows.
+__device__ __forceinline__ void dc_sub_store(float *C, long ld, int rows, int cols, bool lower, bool vec,
+                                             const float acc[4][4])
+{
+    const int tr = threadIdx.x & 15, tn = threadIdx.x >> 4, r0 = 4 * tr;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c = 4 * tn + j;
+        if (c >= cols) continue;
+        float *p = C + r0 + (long)c * ld;
+        if (vec && r0 + 3 < rows && (!lower || c <= r0)) {
+            float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+            v.x -= acc[0][j];
+            v.y -= acc[1][j];
+            v.z -= acc[2][j];
+            v.w -= acc[3][j];
+            *reinterpret_cast<float4 *>(p) = v;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (r0 + i < rows && (!lower || c <= r0 + i)) p[i] = __ldcg(p + i) - acc[i][j];
+        }
+    }
+}
+
+// The slot of the product L_kp X_pj (64 x 64, ld 64) in the scratch area.
+__device__ __forceinline__ float *dc_slot(const DiagCoopArgs &a, int j, int p)
+{
+    return a.T + (long)(p * (p + 1) / 2 + j) * (DC_B * DC_B);
+}
+
+// slot(j, p) = L_kp X_pj (rows of block row k: rk), X_pj the inverse block
+__device__ __forceinline__ void dc_inv_product(const DiagCoopArgs &a, int k, int j, int p, float *s0, float *s1)
+{
+    const int rk = min(DC_B, a.n - k * DC_B);
+    __syncthreads();  // shared tiles free
+    dc_load(s0, a.A + k * DC_B + (long)(p * DC_B) * a.lda, a.lda, rk, DC_B);
+    dc_load_t(s1, a.Linv + p * DC_B + (long)(j * DC_B) * a.ldi, a.ldi, DC_B, DC_B);
+    __syncthreads();
+    float acc[4][4] = {};
+    dc_mma(s0, s1, acc);
+    const int tr = threadIdx.x & 15, tn = threadIdx.x >> 4;
+    float *S = dc_slot(a, j, p);
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj)
+        *reinterpret_cast<float4 *>(S + 4 * tr + (4 * tn + jj) * DC_B) =
+            make_float4(acc[0][jj], acc[1][jj], acc[2][jj], acc[3][jj]);
+}
+
+// X_kj = -X_kk (sum_{p = j}^{k-1} slot(j, p)), summed in p order
+__device__ __forceinline__ void dc_inv_combine(const DiagCoopArgs &a, int k, int j, float *s0, float *s1)
+{
+    const int rk = min(DC_B, a.n - k * DC_B);
+    __syncthreads();  // shared tiles free
+    for (int e = threadIdx.x; e < DC_B * DC_B; e += DC_T) {
+        float v = 0.0f;
+        for (int p = j; p < k; ++p) v += __ldcg(dc_slot(a, j, p) + e);
+        s1[(e & (DC_B - 1)) * DC_LD + (e >> 6)] = v;
+    }
+    dc_load(s0, a.Linv + k * DC_B + (long)(k * DC_B) * a.ldi, a.ldi, rk, rk);
+    __syncthreads();
+    float acc[4][4] = {};
+    dc_mma(s0, s1, acc);
+    const int tr = threadIdx.x & 15, tn = threadIdx.x >> 4;
+    float *X = a.Linv + k * DC_B + (long)(j * DC_B) * a.ldi;
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (4 * tr + i < rk) X[4 * tr + i + (long)(4 * tn + jj) * a.ldi] = -acc[i][jj];
+}
+
+// ---------------------------------------------------------------------------
+// The kernel.  Step k, phase A: the tasks t = blockIdx.x, + gridDim.x, ...
+// of [factor block rows k .. nblk-1 | combine row k-1 of the inverse];
+// phase B: [trailing tile updates | products of row k of the inverse].  The
+// inverse is built row by row as X_kj = -X_kk sum_{p=j}^{k-1} L_kp X_pj
+// (L X = I, block row k), in CTAs the factorisation leaves idle; only the
+// last row runs after the factorisation.
+// ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(DC_T) diag_coop_kernel(DiagCoopArgs a)
 {
-    __shared__ float s0[DC_B * DC_LD], s1[DC_B * DC_LD];
+    __shared__ __align__(16) float s0[DC_B * DC_LD];
+    __shared__ __align__(16) float s1[DC_B * DC_LD];
     __shared__ float invd[DC_B];
     __shared__ int s_ok;
-    const int n = a.n, nblk = (n + DC_B - 1) / DC_B;
-    const int tid = threadIdx.x, tr = tid & 15, tn = tid >> 4;
+    const int n = a.n, nblk = (n + DC_B - 1) / DC_B, G = gridDim.x, b = blockIdx.x;
+    const int tid = threadIdx.x;
+    const bool vec = ((reinterpret_cast<uintptr_t>(a.A) & 15) == 0) && ((a.lda & 3) == 0);
     unsigned phase = 0;
 
     for (int k = 0; k < nblk; ++k) {
         const int k0 = k * DC_B, bk = min(DC_B, n - k0);
-        // ---- A: diagonal block and the block rows i = k + blockIdx.x, + gridDim.x, ... below it
-        if (k + (int)blockIdx.x < nblk) {
-            float *Akk = a.A + k0 + (long)k0 * a.lda;
-            dc_load(s0, Akk, a.lda, bk, bk);
-            __syncthreads();
-            dc_potf2(s0, bk, invd, a.info, a.info_base + k0, blockIdx.x == 0);
-            for (int i = k + (int)blockIdx.x; i < nblk; i += gridDim.x) {
+        float *Akk = a.A + k0 + (long)k0 * a.lda;
+        // ---- phase A
+        const int nf = nblk - k, nc = (a.invert && k >= 2) ? k - 1 : 0;
+        bool factored = false;
+        for (int t = b; t < nf + nc; t += G) {
+            if (t < nf) {
+                if (!factored) {
+                    dc_load(s0, Akk, a.lda, bk, bk);
+                    __syncthreads();
+                    dc_potf2(s0, bk, invd, a.info, a.info_base + k0, b == 0);
+                    factored = true;
+                }
+                const int i = k + t;
                 if (i == k) {
                     for (int e = tid; e < DC_B * DC_B; e += DC_T) {
                         const int r = e & 63, c = e >> 6;
@@ -312,106 +414,47 @@ __global__ void __launch_bounds__(DC_T) diag_coop_kernel(DiagCoopArgs a)
                         if (r < ri && c < bk) Aik[r + (long)c * a.lda] = s1[c * DC_LD + r];
                     }
                 }
+            } else {
+                dc_inv_combine(a, k - 1, t - nf, s0, s1);  // factor tasks come first: s0 is free
             }
         }
         if (!dc_sync(a, ++phase, &s_ok)) return;
         if (k == nblk - 1) break;
-        // ---- B: trailing update of the blocks (i, j), k < j <= i
-        const int m = nblk - k - 1, ntiles = m * (m + 1) / 2;
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            int ii, jj;
-            dc_tri_index(t, ii, jj);
-            const int bi = k + 1 + ii, bj = k + 1 + jj;
-            const int i0 = bi * DC_B, j0 = bj * DC_B, ri = min(DC_B, n - i0), rj = min(DC_B, n - j0);
-            __syncthreads();  // the previous tile's shared operands are free
-            dc_load(s0, a.A + i0 + (long)k0 * a.lda, a.lda, ri, bk);
-            dc_load(s1, a.A + j0 + (long)k0 * a.lda, a.lda, rj, bk);
-            __syncthreads();
-            float acc[4][4] = {};
-            dc_mma<true>(s0, s1, acc);
-            float *Cij = a.A + i0 + (long)j0 * a.lda;
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int c = tn + 16 * b;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int r = tr + 16 * q;
-                    if (r < ri && c < rj && (bi != bj || c <= r)) {
-                        float *p = Cij + r + (long)c * a.lda;
-                        *p = __ldcg(p) - acc[q][b];
-                    }
-                }
+        // ---- phase B
+        const int m = nblk - k - 1, nu = m * (m + 1) / 2;
+        const int np = (a.invert && k >= 1) ? k * (k + 1) / 2 : 0;
+        for (int t = b; t < nu + np; t += G) {
+            if (t < nu) {
+                int ii, jj;
+                dc_tri_index(t, ii, jj);
+                const int bi = k + 1 + ii, bj = k + 1 + jj;
+                const int i0 = bi * DC_B, j0 = bj * DC_B, ri = min(DC_B, n - i0), rj = min(DC_B, n - j0);
+                __syncthreads();  // the previous task's shared operands are free
+                dc_load(s0, a.A + i0 + (long)k0 * a.lda, a.lda, ri, bk);
+                dc_load(s1, a.A + j0 + (long)k0 * a.lda, a.lda, rj, bk);
+                __syncthreads();
+                float acc[4][4] = {};
+                dc_mma(s0, s1, acc);
+                dc_sub_store(a.A + i0 + (long)j0 * a.lda, a.lda, ri, rj, bi == bj, vec, acc);
+            } else {
+                int p, j;
+                dc_tri_index(t - nu, p, j);
+                dc_inv_product(a, k, j, p, s0, s1);
             }
         }
         if (!dc_sync(a, ++phase, &s_ok)) return;
     }
 
-    // ---- inverse of the whole tile by doubling
-    for (int h = DC_B; a.invert && h < n; h *= 2) {
-        const int th = h / DC_B;
-        const int npairs = (n - h + 2 * h - 1) / (2 * h);  // pairs whose second half starts below n
-        // stage 1: T_p = L21 I11 (r2 x h), tiles (ta, tb); I11's block (c, tb) is zero for c < tb
-        int tiles = 0;
-        for (int p = 0; p < npairs; ++p) tiles += ((min(h, n - (2 * p + 1) * h) + DC_B - 1) / DC_B) * th;
-        for (int u = blockIdx.x; u < tiles; u += gridDim.x) {
-            int p = 0, rem = u, r2 = 0, tr2 = 0;
-            for (;; ++p) {
-                r2 = min(h, n - (2 * p + 1) * h);
-                tr2 = (r2 + DC_B - 1) / DC_B;
-                if (rem < tr2 * th) break;
-                rem -= tr2 * th;
-            }
-            const int ta = rem % tr2, tb = rem / tr2, o = 2 * p * h;
-            const int rows = min(DC_B, r2 - ta * DC_B);
-            float acc[4][4] = {};
-            for (int c = tb; c < th; ++c) {
-                __syncthreads();
-                dc_load(s0, a.A + (o + h + ta * DC_B) + (long)(o + c * DC_B) * a.lda, a.lda, rows, DC_B);
-                dc_load(s1, a.Linv + (o + c * DC_B) + (long)(o + tb * DC_B) * a.ldi, a.ldi, DC_B, DC_B);
-                __syncthreads();
-                dc_mma<false>(s0, s1, acc);
-            }
-            float *Tp = a.T + (long)p * h * h;  // r2 x h, ld h
-#pragma unroll
-            for (int b = 0; b < 4; ++b)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int r = ta * DC_B + tr + 16 * q, cc = tb * DC_B + tn + 16 * b;
-                    if (r < r2) Tp[r + (long)cc * h] = acc[q][b];
-                }
+    // ---- the last row of the inverse
+    if (a.invert && nblk >= 2) {
+        const int k = nblk - 1;
+        for (int t = b; t < k * (k + 1) / 2; t += G) {
+            int p, j;
+            dc_tri_index(t, p, j);
+            dc_inv_product(a, k, j, p, s0, s1);
         }
         if (!dc_sync(a, ++phase, &s_ok)) return;
-        // stage 2: X21 = -I22 T_p into Linv; I22's block (ta, c) is zero for c > ta
-        for (int u = blockIdx.x; u < tiles; u += gridDim.x) {
-            int p = 0, rem = u, r2 = 0, tr2 = 0;
-            for (;; ++p) {
-                r2 = min(h, n - (2 * p + 1) * h);
-                tr2 = (r2 + DC_B - 1) / DC_B;
-                if (rem < tr2 * th) break;
-                rem -= tr2 * th;
-            }
-            const int ta = rem % tr2, tb = rem / tr2, o = 2 * p * h;
-            const int rows = min(DC_B, r2 - ta * DC_B);
-            const float *Tp = a.T + (long)p * h * h;
-            float acc[4][4] = {};
-            for (int c = 0; c <= ta; ++c) {
-                const int kc = min(DC_B, r2 - c * DC_B);
-                __syncthreads();
-                dc_load(s0, a.Linv + (o + h + ta * DC_B) + (long)(o + h + c * DC_B) * a.ldi, a.ldi, rows, kc);
-                dc_load(s1, Tp + c * DC_B + (long)(tb * DC_B) * h, h, kc, DC_B);
-                __syncthreads();
-                dc_mma<false>(s0, s1, acc);
-            }
-            float *X = a.Linv + (o + h + ta * DC_B) + (long)(o + tb * DC_B) * a.ldi;
-#pragma unroll
-            for (int b = 0; b < 4; ++b)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int r = tr + 16 * q, cc = tn + 16 * b;
-                    if (r < rows) X[r + (long)cc * a.ldi] = -acc[q][b];
-                }
-        }
-        if (!dc_sync(a, ++phase, &s_ok)) return;
+        for (int t = b; t < k; t += G) dc_inv_combine(a, k, t, s0, s1);
     }
 }
 
