@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include "gb300_internal.h"
+#include "kernels/tile_sweep.cuh"
 #include "kernels/residual_df.cuh"
 #include "kernels/simt_blas.cuh"
 #include "starpu_gb300_kernels.h"
@@ -24,7 +25,8 @@
 
 namespace gb300 {
 
-int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err);
+int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err,
+             float *linv_band);
 
 // One CTA per column j of A: writes the lower part of column j to W in FP32
 // and folds sum_i |A_ij| (= row sum of the symmetric A) into *anorm.
@@ -299,7 +301,10 @@ struct SolverWs {
     void *panel;           // split-BF16 panels
     double *R;             // n x nrhs FP64 residual
     float *Y;              // n x nrhs FP32 right-hand side / correction
-    void *sweep;           // inverted diagonal blocks + flags of the POTRS sweeps
+    void *sweep;           // inverted 64 x 64 diagonal blocks + flags of the 64-row POTRS sweeps
+    float *band;           // inverses of the nb x nb diagonal tiles (tile T at band + T * ldk * ldk), or null
+    float *Z;              // n x 16 scratch of the tile-row sweeps
+    int *cnt;              // 2 * ntiles + 1 counters of the tile-row sweeps
     double *partials;      // K-split partials of the residual
     float2 *xs;            // double-float split of X (n x 16 per group of 16 columns)
     int *sx;               // per-column scale exponents of X
@@ -312,6 +317,48 @@ struct SolverWs {
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// The tile-row sweeps need the factorisation's diagonal-tile inverses (tiles
+// of order <= 1024 inverted by the cooperative diagonal kernel) and slabs of
+// 32 rows that tile each nb x nb tile.
+static bool tile_sweep_ok(int nb) { return nb > 0 && nb % TSW_SLAB == 0 && nb <= GB300_DIAG_TILE_MAX; }
+
+// L y = b then L^T x = y with the inverted nb x nb diagonal tiles in `band`
+// (ld ldk, tile T at band + T * ldk * ldk): one launch per sweep and group
+// of 16 right-hand sides.
+static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L, long ldl, const float *band, long ldk,
+                        float *Y, long ldy, float *Z, int *cnt, int *err)
+{
+    if (n <= 0 || nrhs <= 0) return;
+    TileSweepArgs a;
+    a.n = n;
+    a.nb = nb;
+    a.ntiles = (n + nb - 1) / nb;
+    a.nslabs = (a.ntiles - 1) * (nb / TSW_SLAB) + (n - (a.ntiles - 1) * nb + TSW_SLAB - 1) / TSW_SLAB;
+    a.L = L;
+    a.ldl = ldl;
+    a.Dinv = band;
+    a.ldd = ldk;
+    a.dstride = ldk * ldk;
+    a.ldb = ldy;
+    a.Z = Z;
+    a.zcount = cnt;
+    a.ycount = cnt + a.ntiles;
+    a.ticket = (unsigned *)(cnt + 2 * a.ntiles);
+    a.err = err;
+    a.budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
+    auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+    a.vec = al(L) && al(band) && al(Y) && al(Z) && ldl % 4 == 0 && ldk % 4 == 0 && ldy % 4 == 0 && n % 4 == 0;
+    for (int c0 = 0; c0 < nrhs; c0 += 16) {
+        a.nrhs = std::min(16, nrhs - c0);
+        a.B = Y + (long)c0 * ldy;
+        a.vec = a.vec && al(a.B);
+        cudaMemsetAsync(cnt, 0, (2 * a.ntiles + 1) * sizeof(int), s);
+        gb300_count_launch(), tile_sweep_kernel<false><<<a.nslabs, TSW_T, 0, s>>>(a);
+        cudaMemsetAsync(cnt, 0, (2 * a.ntiles + 1) * sizeof(int), s);
+        gb300_count_launch(), tile_sweep_kernel<true><<<a.nslabs, TSW_T, 0, s>>>(a);
+    }
+}
 
 static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
 {
@@ -328,6 +375,11 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t panel_bytes = starpu_gb300_spotrf_tc_workspace(n, nb);
     const size_t oP = take(panel_bytes);
     const size_t oT = take(potrs_sweep_workspace<float>(n));
+    const bool tiles = tile_sweep_ok(nb);
+    const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64, ntiles = nb > 0 ? ((size_t)n + nb - 1) / nb : 0;
+    const size_t oB = tiles ? take(ntiles * ldk * ldk * sizeof(float)) : 0;
+    const size_t oZ = tiles ? take((size_t)n * 16 * sizeof(float)) : 0;
+    const size_t oC = tiles ? take((2 * ntiles + 1) * sizeof(int)) : 0;
     const size_t oS = take(4 * sizeof(unsigned long long));
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
@@ -345,6 +397,9 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->R = (double *)(b + oR);
         ws->Y = (float *)(b + oY);
         ws->sweep = b + oT;
+        ws->band = tiles ? (float *)(b + oB) : nullptr;
+        ws->Z = tiles ? (float *)(b + oZ) : nullptr;
+        ws->cnt = tiles ? (int *)(b + oC) : nullptr;
         ws->partials = (double *)(b + oQ);
         ws->xs = (float2 *)(b + oX);
         ws->sx = (int *)(b + oI);
@@ -359,14 +414,23 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
 }
 
 
+// y <- L^-T L^-1 y with the FP32 factor W: tile-row sweeps when the
+// factorisation kept its diagonal-tile inverses, else 64-row sweeps.
+static void correction_solve(cudaStream_t s, int n, int nrhs, int nb, const SolverWs &ws)
+{
+    const long ldk = ((long)nb + 63) / 64 * 64;
+    if (ws.band) tile_sweeps(s, n, nrhs, nb, ws.W, n, ws.band, ldk, ws.Y, n, ws.Z, ws.cnt, ws.err);
+    else potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
+}
+
 static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws)
 {
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
     gb300_count_launch(), convert_lower_symnorm_kernel<<<(n + SYM_BW - 1) / SYM_BW, 256, 0, s>>>(n, A, lda, ws.W, n,
                                                                                                  ws.anorm_bits);
-    int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err);
+    int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
     if (rc) return rc;
-    potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
+    if (!ws.band) potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
     return gb300_last_launch_status();
 }
 
@@ -413,7 +477,7 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
     gb300_count_launch(), colmax_exp_kernel<<<nrhs, 256, 0, s>>>(n, B, ldb, ws.rexp);
     gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n, ws.rexp);
     int slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
-    potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
+    correction_solve(s, n, nrhs, nb, ws);
     gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
     gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 0, nullptr,
                                                                            ws.rexp);
@@ -440,7 +504,7 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
         if (it >= max_iter) break;
         gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.R, n, ws.Y, n, ws.rexp);
         slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
-        potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
+        correction_solve(s, n, nrhs, nb, ws);
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
         gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 1, ws.done,
                                                                                ws.rexp);

@@ -169,6 +169,8 @@ static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
     return 2 * panel + inv * 4 + 2 * inv * 2 + inv * 4 + 256;
 }
 
+static_assert(DC_MAXN == GB300_DIAG_TILE_MAX, "one limit for the diagonal-tile kernel");
+
 // Factor the FP32 diagonal tile (n <= DC_MAXN) in place and, when `invert`,
 // write its lower-triangular inverse to Linv (ld ldi): one cooperative launch
 // of diag_coop_kernel, the grid sized to the widest phase and to what can be
@@ -217,7 +219,8 @@ static int diag_factor_inverse(cudaStream_t s, int n, float *A, long lda, float 
 // diagonal tile (SIMT), its inverse (64 x 64 blocks + batched doubling), the
 // panel TRSM  P <- P L_kk^-T  as one split-BF16 product P * Linv^T (store
 // form, always 3 products), then the trailing update  A22 -= P P^T  (lower).
-int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err)
+int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err,
+             float *linv_band)
 {
     const long ldk = ((long)nb + 63) / 64 * 64;
     TcWs w;
@@ -229,11 +232,15 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
         const int m = n - k0 - kb;
         int slot = gb300_prof_begin(s, GB300_PROF_PANEL);
         int rc = 0;
+        // the inverse of the diagonal tile: step k's own block of the band
+        // when the caller keeps them all, else the one reused buffer
+        float *linv = linv_band ? linv_band + (size_t)(k0 / nb) * ldk * ldk : w.linv;
         if (kb <= DC_MAXN) {
-            rc = diag_factor_inverse(s, kb, Akk, lda, w.linv, ldk, w.scratch, w.bar, d_info, k0, d_err, m > 0);
+            rc = diag_factor_inverse(s, kb, Akk, lda, linv, ldk, w.scratch, w.bar, d_info, k0, d_err,
+                                     m > 0 || linv_band);
         } else {
             potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
-            if (m > 0) trtri_lower<float>(s, kb, Akk, lda, w.linv, ldk, w.scratch);
+            if (m > 0) trtri_lower<float>(s, kb, Akk, lda, linv, ldk, w.scratch);
         }
         if (rc) return rc;
         if (m <= 0) {
@@ -241,7 +248,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
             break;
         }
         float *P = A + (k0 + kb) + (long)k0 * lda;
-        rc = split_bf16(s, kb, kb, w.linv, ldk, w.ihi, w.ilo, ldk);
+        rc = split_bf16(s, kb, kb, linv, ldk, w.ihi, w.ilo, ldk);
         if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, w.lo, ldk);
         if (!rc) rc = tc_update(s, m, kb, kb, w.hi, w.lo, ldk, w.ihi, w.ilo, ldk, 3, 0, P, lda, d_err, 1);
         if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, np > 1 ? w.lo : nullptr, ldk);
@@ -292,7 +299,7 @@ int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int n
     cudaStream_t s = (cudaStream_t)stream;
     if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), s);
     if (!n) return GB300_OK;
-    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err);
+    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr);
 }
 
 } // extern "C"

@@ -7,6 +7,10 @@
 
 namespace gb300 {
 
+// largest diagonal tile the cooperative factor-and-invert kernel handles
+constexpr int GB300_DIAG_TILE_MAX = 1024;
+
+
 // the two phases of starpu_gb300_dsposv (capi_solver.cu)
 int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
                   starpu_gb300_ir_info *out);

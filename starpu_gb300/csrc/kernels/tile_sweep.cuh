@@ -1,0 +1,302 @@
+// Single-launch triangular sweeps of the mixed solve's FP32 correction solve
+// (POTRS with the factor L: L y = b, then L^T x = y) in tile rows of the
+// factorisation's tile order nb, with the explicitly inverted nb x nb
+// diagonal tiles the factorisation leaves behind.  The chain of dependent
+// steps is n / nb long (32 at n = 32768, nb = 1024) instead of n / 64.
+//
+// One CTA per 32-row slab; a CTA takes a ticket when it starts and solves the
+// slab of that rank in solve order.  Forward, slab of tile row T:
+//   z = b_slab - sum_{j<T} L_slab,j y_j   (each y_j as soon as tile row j is
+//                                          complete: ycount[j] slabs stored)
+//   z is published (Z rows, zcount[T]); once the whole tile row's z is there,
+//   y_slab = (L_TT^-1)_slab,0..slab z_T    (the lower-triangular inverse)
+//   y is stored in place of b and counted in ycount[T].
+// Backward, slab of tile row T (tile rows in reverse order):
+//   z = y_slab - sum_{j>T} (L_j,slab)^T x_j,   x_slab = ((L_TT^-1)^T)_slab z_T.
+// A CTA only waits on slabs with earlier tickets or on the other slabs of its
+// own tile row, whose tickets are consecutive: every CTA it waits for either
+// runs or starts once earlier tile rows finish, so the sweep cannot deadlock
+// however CTAs are scheduled.  Every wait is bounded by a %globaltimer budget;
+// on timeout the CTA records an error and carries on, so the launch ends.
+//
+// The products are register-blocked: the K range of every chunk (128 columns)
+// is split over the 8 warps, each lane keeps 4 rows x 4 right-hand sides, and
+// the next chunk is fetched into registers while the current one is used.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gb300 {
+
+constexpr int TSW_SLAB = 32;   // rows per CTA
+constexpr int TSW_KC = 128;    // K chunk
+constexpr int TSW_MP = 36;     // pitch of one K index of the operand chunk (32 rows + 4)
+constexpr int TSW_VP = 20;     // pitch of one K index of the right-hand-side chunk (16 + 4)
+constexpr int TSW_T = 256;
+
+struct TileSweepArgs {
+    int n, nrhs, nb;
+    int ntiles, nslabs;
+    const float *L;
+    long ldl;
+    const float *Dinv;  // tile T's inverse at Dinv + T * dstride, leading dimension ldd
+    long ldd, dstride;
+    float *B;  // right-hand sides in, solution out (n x nrhs, ld ldb)
+    long ldb;
+    float *Z;  // n x 16 scratch, ld n
+    unsigned *ticket;
+    int *zcount, *ycount;  // per tile row, zero at launch
+    int *err;
+    unsigned long long budget_ns;
+    int vec;  // L, Dinv, B, Z and their leading dimensions allow 16-byte loads
+};
+
+__device__ __forceinline__ int tsw_ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint64_t tsw_timer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait (thread 0, then the CTA) until *cnt >= target.  On timeout or an
+// error seen elsewhere the CTA stops waiting from then on (*skip).
+__device__ __forceinline__ void tsw_wait(const TileSweepArgs &a, const int *cnt, int target, int *skip)
+{
+    if (threadIdx.x == 0 && !*skip && tsw_ld_acquire(cnt) < target) {
+        const uint64_t t0 = tsw_timer();
+        while (tsw_ld_acquire(cnt) < target) {
+            if (*(volatile int *)a.err || tsw_timer() - t0 > a.budget_ns) {
+                atomicCAS(a.err, 0, 1);
+                *skip = 1;
+                break;
+            }
+            __nanosleep(64);
+        }
+    }
+    __syncthreads();
+}
+
+// Register-staged chunk of the operand M (32 x kc, element (r, p)) and of the
+// right-hand sides V (kc x 16, element (p, c)).
+//   TR = false: M(r, p) = M[r + p * ldm]  (rows of L or of the inverse)
+//   TR = true : M(r, p) = M[p + r * ldm]  (columns: the transposed operand)
+//   V(p, c) = V[p + c * ldv]
+struct TswStage {
+    float4 m[4];
+    float4 v[2];
+};
+
+template <bool TR>
+__device__ __forceinline__ void tsw_fetch(TswStage &st, const float *M, long ldm, int rows, const float *V, long ldv,
+                                          int kc, int nrhs, bool vec)
+{
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int e = tid + TSW_T * u;  // 1024 float4 of the 32 x 128 chunk
+        int r, p;
+        if (!TR) { r = (e & 7) * 4; p = e >> 3; }   // 4 consecutive rows of column p
+        else     { p = (e & 31) * 4; r = e >> 5; }  // 4 consecutive p of row r
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!TR) {
+            if (p < kc) {
+                const float *src = M + r + (long)p * ldm;
+                if (vec && r + 3 < rows) x = __ldcg(reinterpret_cast<const float4 *>(src));
+                else {
+                    if (r < rows) x.x = __ldcg(src);
+                    if (r + 1 < rows) x.y = __ldcg(src + 1);
+                    if (r + 2 < rows) x.z = __ldcg(src + 2);
+                    if (r + 3 < rows) x.w = __ldcg(src + 3);
+                }
+            }
+        } else {
+            if (r < rows) {
+                const float *src = M + p + (long)r * ldm;
+                if (vec && p + 3 < kc) x = __ldcg(reinterpret_cast<const float4 *>(src));
+                else {
+                    if (p < kc) x.x = __ldcg(src);
+                    if (p + 1 < kc) x.y = __ldcg(src + 1);
+                    if (p + 2 < kc) x.z = __ldcg(src + 2);
+                    if (p + 3 < kc) x.w = __ldcg(src + 3);
+                }
+            }
+        }
+        st.m[u] = x;
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const int e = tid + TSW_T * u;  // 512 float4: 16 columns x 32 groups of 4 K indices
+        const int p = (e & 31) * 4, c = e >> 5;
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c < nrhs) {
+            const float *src = V + p + (long)c * ldv;
+            if (vec && p + 3 < kc) x = __ldcg(reinterpret_cast<const float4 *>(src));
+            else {
+                if (p < kc) x.x = __ldcg(src);
+                if (p + 1 < kc) x.y = __ldcg(src + 1);
+                if (p + 2 < kc) x.z = __ldcg(src + 2);
+                if (p + 3 < kc) x.w = __ldcg(src + 3);
+            }
+        }
+        st.v[u] = x;
+    }
+}
+
+template <bool TR>
+__device__ __forceinline__ void tsw_put(const TswStage &st, float *Ms, float *Vs)
+{
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int e = tid + TSW_T * u;
+        if (!TR) {
+            const int r = (e & 7) * 4, p = e >> 3;
+            *reinterpret_cast<float4 *>(Ms + p * TSW_MP + r) = st.m[u];
+        } else {
+            const int p = (e & 31) * 4, r = e >> 5;
+            Ms[p * TSW_MP + r] = st.m[u].x;
+            Ms[(p + 1) * TSW_MP + r] = st.m[u].y;
+            Ms[(p + 2) * TSW_MP + r] = st.m[u].z;
+            Ms[(p + 3) * TSW_MP + r] = st.m[u].w;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const int e = tid + TSW_T * u;
+        const int p = (e & 31) * 4, c = e >> 5;
+        Vs[p * TSW_VP + c] = st.v[u].x;
+        Vs[(p + 1) * TSW_VP + c] = st.v[u].y;
+        Vs[(p + 2) * TSW_VP + c] = st.v[u].z;
+        Vs[(p + 3) * TSW_VP + c] = st.v[u].w;
+    }
+}
+
+// acc (this warp's share of the K range) += M(32 x K) V(K x 16).  Warp w
+// takes K indices 16 w .. 16 w + 15 of every chunk; lane (rr = lane % 8,
+// cc = lane / 8) keeps rows 4 rr .. 4 rr + 3 and right-hand sides
+// 4 cc .. 4 cc + 3.
+template <bool TR>
+__device__ __forceinline__ void tsw_product(float acc[4][4], const float *M, long ldm, int rows, const float *V,
+                                            long ldv, int K, int nrhs, bool vec, float *Ms, float *Vs)
+{
+    if (K <= 0) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane & 7, cc = lane >> 3;
+    TswStage st;
+    tsw_fetch<TR>(st, M, ldm, rows, V, ldv, min(TSW_KC, K), nrhs, vec);
+    for (int p0 = 0; p0 < K; p0 += TSW_KC) {
+        __syncthreads();  // the previous chunk has been used
+        tsw_put<TR>(st, Ms, Vs);
+        __syncthreads();
+        const int pn = p0 + TSW_KC;
+        if (pn < K) {
+            const float *Mn = TR ? M + pn : M + (long)pn * ldm;
+            tsw_fetch<TR>(st, Mn, ldm, rows, V + pn, ldv, min(TSW_KC, K - pn), nrhs, vec);
+        }
+#pragma unroll
+        for (int pp = 0; pp < 16; ++pp) {
+            const int p = warp * 16 + pp;
+            const float4 m4 = *reinterpret_cast<const float4 *>(Ms + p * TSW_MP + 4 * rr);
+            const float4 v4 = *reinterpret_cast<const float4 *>(Vs + p * TSW_VP + 4 * cc);
+            const float mv[4] = {m4.x, m4.y, m4.z, m4.w}, vv[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(mv[i], vv[j], acc[i][j]);
+        }
+    }
+}
+
+// Sum the 8 warps' partial products (plus `base` for warp 0's share, the
+// right-hand side) into out (32 x 16, shared, row-major with pitch 16).
+__device__ __forceinline__ void tsw_reduce(const float acc[4][4], float *red, float *out)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane & 7, cc = lane >> 3;
+    __syncthreads();  // red may alias the chunk buffers
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) red[warp * 512 + (4 * rr + i) * 16 + 4 * cc + j] = acc[i][j];
+    __syncthreads();
+    for (int e = threadIdx.x; e < 512; e += TSW_T) {
+        float s = 0.0f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += red[w * 512 + e];
+        out[e] = s;
+    }
+    __syncthreads();
+}
+
+template <bool TRANS>
+__global__ void __launch_bounds__(TSW_T) tile_sweep_kernel(TileSweepArgs a)
+{
+    __shared__ __align__(16) float Ms[TSW_KC * TSW_MP];
+    __shared__ __align__(16) float Vs[TSW_KC * TSW_VP];
+    __shared__ float zs[TSW_SLAB * 16];
+    __shared__ unsigned s_ticket;
+    __shared__ int s_skip;
+    float *red = Ms;  // 8 x 512 floats after the products
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        s_ticket = atomicAdd(a.ticket, 1u);
+        s_skip = 0;
+    }
+    __syncthreads();
+    const int t = (int)s_ticket;
+    if (t >= a.nslabs) return;
+    const int spt = a.nb / TSW_SLAB;
+    const int q = TRANS ? a.nslabs - 1 - t : t;
+    const int T = q / spt, s = q % spt;
+    const int t0 = T * a.nb, kbT = min(a.nb, a.n - t0);
+    const int nsT = (kbT + TSW_SLAB - 1) / TSW_SLAB;
+    const int r0 = t0 + s * TSW_SLAB, rows = min(TSW_SLAB, kbT - s * TSW_SLAB);
+    const bool vec = a.vec != 0;
+
+    // contributions of the other tile rows: acc = -sum (L_slab,j y_j) or -sum (L_j,slab^T x_j)
+    float acc[4][4] = {};
+    const int jbeg = TRANS ? a.ntiles - 1 : 0, jend = TRANS ? T : T, jstep = TRANS ? -1 : 1;
+    for (int j = jbeg; j != jend; j += jstep) {
+        const int j0 = j * a.nb, kbj = min(a.nb, a.n - j0);
+        tsw_wait(a, &a.ycount[j], (kbj + TSW_SLAB - 1) / TSW_SLAB, &s_skip);
+        if (!TRANS) tsw_product<false>(acc, a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
+        else tsw_product<true>(acc, a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
+    }
+    tsw_reduce(acc, red, zs);
+    // z = b_slab - sum: publish
+    for (int e = tid; e < TSW_SLAB * 16; e += TSW_T) {
+        const int r = e >> 4, c = e & 15;
+        if (r < rows && c < a.nrhs) a.Z[(long)(r0 + r) + (long)c * a.n] = __ldcg(&a.B[(long)(r0 + r) + (long)c * a.ldb]) - zs[e];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicAdd(&a.zcount[T], 1);
+    tsw_wait(a, &a.zcount[T], nsT, &s_skip);
+
+    // diagonal tile: forward y_slab = Dinv(slab rows, 0 .. slab end) z_T;
+    // backward x_slab = Dinv(slab start .. kbT, slab columns)^T z_T
+    float acc2[4][4] = {};
+    const float *D = a.Dinv + (long)T * a.dstride;
+    if (!TRANS) {
+        tsw_product<false>(acc2, D + s * TSW_SLAB, a.ldd, rows, a.Z + t0, a.n, s * TSW_SLAB + rows, a.nrhs, vec, Ms, Vs);
+    } else {
+        const int k0 = s * TSW_SLAB;
+        tsw_product<true>(acc2, D + k0 + (long)k0 * a.ldd, a.ldd, rows, a.Z + t0 + k0, a.n, kbT - k0, a.nrhs, vec, Ms,
+                          Vs);
+    }
+    tsw_reduce(acc2, red, zs);
+    for (int e = tid; e < TSW_SLAB * 16; e += TSW_T) {
+        const int r = e >> 4, c = e & 15;
+        if (r < rows && c < a.nrhs) a.B[(long)(r0 + r) + (long)c * a.ldb] = zs[e];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicAdd(&a.ycount[T], 1);
+}
+
+} // namespace gb300
