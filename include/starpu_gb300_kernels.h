@@ -141,6 +141,18 @@ size_t starpu_gb300_spotrs_sweep_workspace(int n);
 int starpu_gb300_spotrs_sweep(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb, void *work,
                               size_t lwork, int *d_err);
 
+/* Same LAPACK xPOTRS contract (min-dgels/base/SRC/dpotrs.c, uplo = L) when
+ * the factorisation kept the inverses of its nb x nb diagonal tiles: two
+ * single-launch sweeps per group of 16 right-hand sides over 32-row slabs,
+ * n / nb dependent steps each.  Tile T's inverse (lower triangular, zero
+ * above the diagonal) is at Dinv + T * ldd * ldd with leading dimension
+ * ldd >= nb; nb a multiple of 32, at most 1024.  `work` (device, >=
+ * _workspace(n, nb) bytes) holds the sweeps' scratch and counters; d_err is
+ * set non-zero if an internal wait timed out (the result is then invalid). */
+size_t starpu_gb300_spotrs_inv_tiles_workspace(int n, int nb);
+int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const float *L, int ldl, const float *Dinv,
+                                  int ldd, float *B, int ldb, void *work, size_t lwork, int *d_err);
+
 /* Allocation-free variant of starpu_gb300_spotrs_sweep.  It has no
  * counterpart in the reference.  For callers that must not allocate device
  * memory -- a codelet body running inside a runtime that owns all device

@@ -707,6 +707,26 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
     return status;
 }
 
+size_t starpu_gb300_spotrs_inv_tiles_workspace(int n, int nb)
+{
+    if (n < 0 || !tile_sweep_ok(nb)) return 0;
+    const size_t ntiles = ((size_t)n + nb - 1) / nb;
+    return align256((size_t)n * 16 * sizeof(float)) + align256((2 * ntiles + 1) * sizeof(int));
+}
+
+int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const float *L, int ldl, const float *Dinv,
+                                  int ldd, float *B, int ldb, void *work, size_t lwork, int *d_err)
+{
+    if (n < 0 || nrhs < 0 || !tile_sweep_ok(nb) || ldl < (n > 1 ? n : 1) || ldb < (n > 1 ? n : 1) || ldd < nb ||
+        (n && (!L || !Dinv || !B || !work || !d_err || lwork < starpu_gb300_spotrs_inv_tiles_workspace(n, nb))))
+        return GB300_EINVAL;
+    if (!n || !nrhs) return GB300_OK;
+    float *Z = (float *)work;
+    int *cnt = (int *)((char *)work + align256((size_t)n * 16 * sizeof(float)));
+    tile_sweeps((cudaStream_t)stream, n, nrhs, nb, L, ldl, Dinv, ldd, B, ldb, Z, cnt, d_err);
+    return gb300_last_launch_status();
+}
+
 size_t starpu_gb300_backward_error_workspace(int n, int nrhs)
 {
     return align256((size_t)n * nrhs * sizeof(double)) + align256((size_t)nrhs * (sizeof(double) + sizeof(int))) +

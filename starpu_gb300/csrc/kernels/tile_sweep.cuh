@@ -93,17 +93,41 @@ struct TswStage {
     float4 v[2];
 };
 
+// Element maps (1024 float4 of M, 512 of V per chunk), chosen so that the
+// transposing shared stores of tsw_put hit 32 distinct banks:
+//   M, TR = false: float4 = 4 consecutive rows r of column p (coalesced rows);
+//   M, TR = true : lane = row r, a thread's 4 float4 = 16 consecutive p (two
+//                  whole 32-byte sectors of column r);
+//   V: lane = (c = lane % 16, half-warp h), float4 f = 16 u + 2 w + h of
+//      column c (V is small and stays in L2).
+template <bool TR>
+__device__ __forceinline__ void tsw_map_m(int u, int &r, int &p)
+{
+    const int tid = threadIdx.x;
+    if (!TR) {
+        const int e = tid + TSW_T * u;
+        r = (e & 7) * 4;
+        p = e >> 3;
+    } else {
+        r = tid & 31;
+        p = ((tid >> 5) * 4 + u) * 4;
+    }
+}
+__device__ __forceinline__ void tsw_map_v(int u, int &p, int &c)
+{
+    const int tid = threadIdx.x;
+    c = tid & 15;
+    p = (16 * u + (tid >> 4)) * 4;
+}
+
 template <bool TR>
 __device__ __forceinline__ void tsw_fetch(TswStage &st, const float *M, long ldm, int rows, const float *V, long ldv,
                                           int kc, int nrhs, bool vec)
 {
-    const int tid = threadIdx.x;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        const int e = tid + TSW_T * u;  // 1024 float4 of the 32 x 128 chunk
         int r, p;
-        if (!TR) { r = (e & 7) * 4; p = e >> 3; }   // 4 consecutive rows of column p
-        else     { p = (e & 31) * 4; r = e >> 5; }  // 4 consecutive p of row r
+        tsw_map_m<TR>(u, r, p);
         float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
         if (!TR) {
             if (p < kc) {
@@ -132,8 +156,8 @@ __device__ __forceinline__ void tsw_fetch(TswStage &st, const float *M, long ldm
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-        const int e = tid + TSW_T * u;  // 512 float4: 16 columns x 32 groups of 4 K indices
-        const int p = (e & 31) * 4, c = e >> 5;
+        int p, c;
+        tsw_map_v(u, p, c);
         float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
         if (c < nrhs) {
             const float *src = V + p + (long)c * ldv;
@@ -152,15 +176,13 @@ __device__ __forceinline__ void tsw_fetch(TswStage &st, const float *M, long ldm
 template <bool TR>
 __device__ __forceinline__ void tsw_put(const TswStage &st, float *Ms, float *Vs)
 {
-    const int tid = threadIdx.x;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        const int e = tid + TSW_T * u;
+        int r, p;
+        tsw_map_m<TR>(u, r, p);
         if (!TR) {
-            const int r = (e & 7) * 4, p = e >> 3;
             *reinterpret_cast<float4 *>(Ms + p * TSW_MP + r) = st.m[u];
         } else {
-            const int p = (e & 31) * 4, r = e >> 5;
             Ms[p * TSW_MP + r] = st.m[u].x;
             Ms[(p + 1) * TSW_MP + r] = st.m[u].y;
             Ms[(p + 2) * TSW_MP + r] = st.m[u].z;
@@ -169,8 +191,8 @@ __device__ __forceinline__ void tsw_put(const TswStage &st, float *Ms, float *Vs
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-        const int e = tid + TSW_T * u;
-        const int p = (e & 31) * 4, c = e >> 5;
+        int p, c;
+        tsw_map_v(u, p, c);
         Vs[p * TSW_VP + c] = st.v[u].x;
         Vs[(p + 1) * TSW_VP + c] = st.v[u].y;
         Vs[(p + 2) * TSW_VP + c] = st.v[u].z;

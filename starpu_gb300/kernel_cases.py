@@ -9,6 +9,7 @@
     python -m starpu_gb300.kernel_cases dpotrf    --n 8192  --nb 512 --reps 2
     python -m starpu_gb300.kernel_cases tile_ops  --n 1024 --reps 200
     python -m starpu_gb300.kernel_cases diag      --n 1024 --reps 50
+    python -m starpu_gb300.kernel_cases tile_sweep --n 32768 --nb 1024 --nrhs 16 --reps 5
 
 Each case allocates its operands once, runs `--reps` launches of the same
 shape and prints the mean time per launch measured with CUDA events.
@@ -50,7 +51,7 @@ def oracle_free_spd(n):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv",
-                                     "tile_ops", "diag"])
+                                     "tile_ops", "diag", "tile_sweep"])
     ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--n", type=int, default=8192)
@@ -181,6 +182,30 @@ def main(argv=None):
             ms_copy = _timed(L, restore, a.reps)
             out["ms_" + tag] = _timed(L, run, a.reps) - ms_copy
             out["err_" + tag] = int(DeviceBuffer.download(err, (1,), np.int32)[0])
+    elif a.case == "tile_sweep":
+        # both tile-row sweeps of one FP32 correction solve (identity
+        # diagonal-tile inverses: the timing does not depend on the values)
+        n, nb, nrhs = a.n, a.nb, a.nrhs
+        i = np.arange(n, dtype=np.float32)
+        F = DeviceBuffer(4 * n * n)
+        for c0 in range(0, n, 2048):  # the factor column panel by column panel (host memory stays small)
+            w = min(2048, n - c0)
+            Lp = np.asfortranarray(1.0 / (1.0 + i[:, None] + i[None, c0:c0 + w]), dtype=np.float32)
+            Lp[np.arange(c0, c0 + w), np.arange(w)] += n
+            check(L.starpu_gb300_memcpy_h2d(None, F.ptr + 4 * n * c0, Lp.ctypes.data, Lp.nbytes))
+        ldd = (nb + 63) // 64 * 64
+        ntiles = (n + nb - 1) // nb
+        eye = np.asfortranarray(np.eye(ldd, dtype=np.float32))
+        D = DeviceBuffer(4 * ntiles * ldd * ldd)
+        for T in range(ntiles):
+            check(L.starpu_gb300_memcpy_h2d(None, D.ptr + 4 * T * ldd * ldd, eye.ctypes.data, eye.nbytes))
+        Y = DeviceBuffer.from_array(np.ones((n, nrhs), np.float32))
+        lw = L.starpu_gb300_spotrs_inv_tiles_workspace(n, nb)
+        Wk = DeviceBuffer(lw)
+        err = DeviceBuffer.from_array(np.zeros(1, np.int32))
+        ms = _timed(L, lambda: check(L.starpu_gb300_spotrs_inv_tiles(None, n, nrhs, nb, F.ptr, n, D.ptr, ldd, Y.ptr, n,
+                                                                      Wk.ptr, lw, err.ptr)), a.reps)
+        out.update(ms_two_sweeps=ms, gbs=4.0 * n * n / ms / 1e6, err=int(err.download((1,), np.int32)[0]))
     elif a.case == "dpotrf":
         n, nb = a.n, a.nb
         A = DeviceBuffer(8 * n * n)

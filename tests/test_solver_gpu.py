@@ -179,3 +179,50 @@ def test_profiling_counts_kernel_classes(gpu, oracle):
     assert launches.value == n // nb - 1 and ms.value > 0
     expected = sum(3 * nb * (n - (k + 1) * nb) * (n - (k + 1) * nb + 1.0) for k in range(n // nb - 1))
     assert abs(fl.value - expected) <= 1e-9 * expected
+
+
+def inv_tile_band(L32, nb):
+    """Inverses of the nb x nb diagonal tiles of L, tile T as an ldd x ldd
+    column-major block at T * ldd * ldd (zero above the diagonal)."""
+    n = L32.shape[0]
+    ldd = (nb + 63) // 64 * 64
+    ntiles = (n + nb - 1) // nb
+    band = np.zeros(ntiles * ldd * ldd, np.float32)
+    for T in range(ntiles):
+        t0 = T * nb
+        kb = min(nb, n - t0)
+        blk = np.zeros((ldd, ldd), np.float32, order="F")
+        blk[:kb, :kb] = np.tril(np.linalg.inv(L32[t0:t0 + kb, t0:t0 + kb].astype(np.float64)))
+        band[T * ldd * ldd:(T + 1) * ldd * ldd] = blk.ravel(order="F")
+    return band, ldd
+
+
+@pytest.mark.parametrize("n,nb,nrhs", [(2048, 1024, 16), (1000, 256, 5), (777, 96, 20), (64, 32, 1), (130, 64, 3)])
+def test_spotrs_inv_tiles_matches_fp64_triangular_solves(gpu, oracle, n, nb, nrhs):
+    """POTRS by tile-row sweeps with the diagonal-tile inverses supplied:
+    agrees with an FP64 solve by the same FP32 factor to FP32 accuracy, and
+    repeats bit-identically."""
+    A = oracle.spd_gram(n, 71, 1.0)
+    L32 = np.asfortranarray(np.tril(np.linalg.cholesky(A)).astype(np.float32))
+    band, ldd = inv_tile_band(L32, nb)
+    B = oracle.uniform_rhs(n, nrhs, 72).astype(np.float32)
+    dL, dD = DeviceBuffer.from_array(L32), DeviceBuffer.from_array(band)
+    lw = gpu.starpu_gb300_spotrs_inv_tiles_workspace(n, nb)
+    W, err = DeviceBuffer(lw), DeviceBuffer.from_array(np.zeros(1, np.int32))
+    outs = []
+    for _ in range(2):
+        dB = DeviceBuffer.from_array(B)
+        check(gpu.starpu_gb300_spotrs_inv_tiles(None, n, nrhs, nb, dL.ptr, n, dD.ptr, ldd, dB.ptr, n, W.ptr, lw,
+                                                 err.ptr))
+        outs.append(dB.download((n, nrhs), np.float32))
+    assert err.download((1,), np.int32)[0] == 0
+    np.testing.assert_array_equal(outs[0], outs[1])
+    L64 = L32.astype(np.float64)
+    ref = np.linalg.solve(L64.T, np.linalg.solve(L64, B.astype(np.float64)))
+    assert np.max(np.abs(outs[0] - ref)) / np.max(np.abs(ref)) < 2e-5
+
+
+def test_spotrs_inv_tiles_rejects_bad_tiles(gpu):
+    assert gpu.starpu_gb300_spotrs_inv_tiles_workspace(100, 48) == 0  # nb not a multiple of 32
+    assert gpu.starpu_gb300_spotrs_inv_tiles(None, 100, 1, 48, None, 100, None, 64, None, 100, None, 0, None) == -22
+    assert gpu.starpu_gb300_spotrs_inv_tiles(None, 100, 1, 2048, None, 100, None, 2048, None, 100, None, 0, None) == -22
