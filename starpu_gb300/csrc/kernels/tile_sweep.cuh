@@ -19,12 +19,9 @@
 // however CTAs are scheduled.  Every wait is bounded by a %globaltimer budget;
 // on timeout the CTA records an error and carries on, so the launch ends.
 //
-// The products are register-blocked: the K range of every chunk (64 columns)
-// is split over the 4 warps, each lane keeps 4 rows x 4 right-hand sides, and
+// The products are register-blocked: the K range of every chunk (128 columns)
+// is split over the 8 warps, each lane keeps 4 rows x 4 right-hand sides, and
 // the next chunk is fetched into registers while the current one is used.
-// A CTA is small (128 threads, <= 73 registers: 7 per SM, 16 KB of shared memory) so
-// that all slabs of a 32768-row solve are resident at once: each follows the
-// wavefront of finished tile rows instead of starting late with a backlog.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,10 +29,10 @@
 namespace gb300 {
 
 constexpr int TSW_SLAB = 32;   // rows per CTA
-constexpr int TSW_KC = 64;     // K chunk
+constexpr int TSW_KC = 128;    // K chunk
 constexpr int TSW_MP = 36;     // pitch of one K index of the operand chunk (32 rows + 4)
 constexpr int TSW_VP = 20;     // pitch of one K index of the right-hand-side chunk (16 + 4)
-constexpr int TSW_T = 128;     // 4 warps: small enough that every slab's CTA stays resident
+constexpr int TSW_T = 256;
 
 struct TileSweepArgs {
     int n, nrhs, nb;
@@ -96,12 +93,12 @@ struct TswStage {
     float4 v[2];
 };
 
-// Element maps (512 float4 of M, 256 of V per chunk), chosen so that the
+// Element maps (1024 float4 of M, 512 of V per chunk), chosen so that the
 // transposing shared stores of tsw_put hit 32 distinct banks:
 //   M, TR = false: float4 = 4 consecutive rows r of column p (coalesced rows);
 //   M, TR = true : lane = row r, a thread's 4 float4 = 16 consecutive p (two
 //                  whole 32-byte sectors of column r);
-//   V: lane = (c = lane % 16, half-warp h), float4 f = 8 u + 2 w + h of
+//   V: lane = (c = lane % 16, half-warp h), float4 f = 16 u + 2 w + h of
 //      column c (V is small and stays in L2).
 template <bool TR>
 __device__ __forceinline__ void tsw_map_m(int u, int &r, int &p)
@@ -120,7 +117,7 @@ __device__ __forceinline__ void tsw_map_v(int u, int &p, int &c)
 {
     const int tid = threadIdx.x;
     c = tid & 15;
-    p = (8 * u + (tid >> 4)) * 4;
+    p = (16 * u + (tid >> 4)) * 4;
 }
 
 template <bool TR>
@@ -204,7 +201,7 @@ __device__ __forceinline__ void tsw_put(const TswStage &st, float *Ms, float *Vs
 }
 
 // acc (this warp's share of the K range) += M(32 x K) V(K x 16).  Warp w
-// takes K indices 16 w .. 16 w + 15 of every 64-column chunk; lane (rr = lane % 8,
+// takes K indices 16 w .. 16 w + 15 of every chunk; lane (rr = lane % 8,
 // cc = lane / 8) keeps rows 4 rr .. 4 rr + 3 and right-hand sides
 // 4 cc .. 4 cc + 3.
 template <bool TR>
@@ -238,7 +235,7 @@ __device__ __forceinline__ void tsw_product(float acc[4][4], const float *M, lon
     }
 }
 
-// Sum the 4 warps' partial products (plus `base` for warp 0's share, the
+// Sum the 8 warps' partial products (plus `base` for warp 0's share, the
 // right-hand side) into out (32 x 16, shared, row-major with pitch 16).
 __device__ __forceinline__ void tsw_reduce(const float acc[4][4], float *red, float *out)
 {
@@ -252,21 +249,21 @@ __device__ __forceinline__ void tsw_reduce(const float acc[4][4], float *red, fl
     for (int e = threadIdx.x; e < 512; e += TSW_T) {
         float s = 0.0f;
 #pragma unroll
-        for (int w = 0; w < TSW_T / 32; ++w) s += red[w * 512 + e];
+        for (int w = 0; w < 8; ++w) s += red[w * 512 + e];
         out[e] = s;
     }
     __syncthreads();
 }
 
 template <bool TRANS>
-__global__ void __launch_bounds__(TSW_T, 7) tile_sweep_kernel(TileSweepArgs a)
+__global__ void __launch_bounds__(TSW_T) tile_sweep_kernel(TileSweepArgs a)
 {
     __shared__ __align__(16) float Ms[TSW_KC * TSW_MP];
     __shared__ __align__(16) float Vs[TSW_KC * TSW_VP];
     __shared__ float zs[TSW_SLAB * 16];
     __shared__ unsigned s_ticket;
     __shared__ int s_skip;
-    float *red = Ms;  // 4 x 512 floats after the products
+    float *red = Ms;  // 8 x 512 floats after the products
     const int tid = threadIdx.x;
     if (tid == 0) {
         s_ticket = atomicAdd(a.ticket, 1u);
