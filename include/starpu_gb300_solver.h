@@ -154,6 +154,16 @@ int starpu_gb300_server_stats(starpu_gb300_server *server, unsigned long long *s
                               unsigned long long *cache_hits, unsigned long long *evictions, size_t *bytes_in_use);
 int starpu_gb300_server_destroy(starpu_gb300_server *server);
 
+/* R = B - A X for symmetric A (n x n, only the lower triangle is read), X, B,
+ * R n x nrhs, all FP64, to ~2^-56 of ||A||_inf ||X||_inf: the refinement
+ * residual of starpu_gb300_dsposv.  The products run on the tensor cores as
+ * exact integer products of 7-bit slices of A and X (fixed point with a power-
+ * of-two scale per matrix and per column).  Deterministic.  `work` (device,
+ * >= _workspace bytes); d_err is set non-zero if an internal wait timed out. */
+size_t starpu_gb300_dsyresidual_workspace(int n, int nrhs);
+int starpu_gb300_dsyresidual(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
+                             const double *B, int ldb, double *R, int ldr, void *work, size_t lwork, int *d_err);
+
 /* Plain FP64 solve: dpotrf (tile nb) + dpotrs, A and B overwritten (LAPACK dposv). */
 int starpu_gb300_dposv(void *stream, int n, int nrhs, double *A, int lda, double *B, int ldb, int nb, int *d_info);
 

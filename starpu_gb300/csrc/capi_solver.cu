@@ -58,7 +58,7 @@ __global__ void convert_lower_norm_kernel(int n, const double *__restrict__ A, l
 //   row sum_i = sum_{k < i} |A_ik|   (row i left of the diagonal: columns
 //               k < i, read as column segments of the block's rows)
 //             + sum_{k >= i} |A_ki|  (column i from the diagonal down)
-// Columns j in I are written to W (rows i >= j) while they are reduced.
+// Columns j in I are written to W (rows i >= j, when W is given) while they are reduced.
 // Every CTA reads SYM_BW * n elements; max over rows is order-independent.
 constexpr int SYM_BW = 128;
 __global__ void __launch_bounds__(256) convert_lower_symnorm_kernel(int n, const double *__restrict__ A, long lda,
@@ -95,20 +95,22 @@ __global__ void __launch_bounds__(256) convert_lower_symnorm_kernel(int n, const
     for (int c = 0; c < bw; ++c) {
         const int j = i0 + c;
         const double *a = A + (long)j * lda;
-        float *w = W + (long)j * ldw;
+        float *w = W ? W + (long)j * ldw : nullptr;
         double s0 = 0.0, s1 = 0.0;
         int i = j + tid;
         for (; i + (int)blockDim.x < n; i += 2 * blockDim.x) {
             const double v0 = a[i], v1 = a[i + blockDim.x];
             s0 += fabs(v0);
             s1 += fabs(v1);
-            w[i] = (float)v0;
-            w[i + blockDim.x] = (float)v1;
+            if (w) {
+                w[i] = (float)v0;
+                w[i + blockDim.x] = (float)v1;
+            }
         }
         if (i < n) {
             const double v = a[i];
             s0 += fabs(v);
-            w[i] = (float)v;
+            if (w) w[i] = (float)v;
         }
         double s = s0 + s1;
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -255,6 +257,33 @@ static void residual_df(cudaStream_t s, int n, int nrhs, const double *A, long l
     gb300_count_launch(), residual_reduce_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, nz, B, ldb, partials, R, ldr);
 }
 
+// The refinement's residual R = B - A X: the products on the tensor cores in
+// exact fixed-point slices (residual_tc), or, with STARPU_GB300_RESIDUAL=df,
+// in double-float on the FP32 pipe (residual_df).  The partials are reduced
+// in FP64 in a fixed order either way.
+static int residual_mixed(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx,
+                          const double *B, long ldb, double *R, long ldr, double *partials, float2 *xs, int *sx,
+                          void *rtc_xs, const unsigned long long *anorm_bits, int *d_err)
+{
+    static const bool use_df = [] {
+        const char *e = getenv("STARPU_GB300_RESIDUAL");
+        return e && !strcmp(e, "df");
+    }();
+    if (use_df) {
+        residual_df(s, n, nrhs, A, lda, X, ldx, B, ldb, R, ldr, partials, xs, sx, anorm_bits);
+        return gb300_last_launch_status();
+    }
+    const long cap = (long)(residual_partials(n, nrhs) / ((size_t)n * nrhs));
+    const int kc = residual_tc_kchunk(n, nrhs, (int)cap);
+    gb300_count_launch(), df_split_x_kernel<<<nrhs, 256, 0, s>>>(n, X, ldx, xs, sx);
+    int rc = residual_tc(s, n, nrhs, A, lda, X, ldx, sx, anorm_bits, kc, rtc_xs, partials, d_err);
+    if (rc) return rc;
+    const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
+    gb300_count_launch(), residual_reduce_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, (n + kc - 1) / kc, B, ldb,
+                                                                                partials, R, ldr);
+    return gb300_last_launch_status();
+}
+
 // Per right-hand side j (one CTA): berr_j = ||r_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf);
 // done_j = berr_j <= tol.
 __global__ void backward_error_kernel(int n, const double *__restrict__ R, long ldr, const double *__restrict__ X,
@@ -308,6 +337,7 @@ struct SolverWs {
     double *partials;      // K-split partials of the residual
     float2 *xs;            // double-float split of X (n x 16 per group of 16 columns)
     int *sx;               // per-column scale exponents of X
+    void *rtc_xs;          // x digit slices of the tensor-core residual
     double *berr;          // nrhs
     int *done;             // nrhs
     int *rexp;             // nrhs: power-of-two scales of the FP32 right-hand sides
@@ -389,6 +419,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t oX = take((size_t)n * 16 * ((nrhs + 15) / 16) * sizeof(float2));
     const size_t oI = take((size_t)nrhs * sizeof(int));
     const size_t oJ = take((size_t)nrhs * sizeof(int));
+    const size_t oK = take(residual_tc_xs_bytes(n, nrhs));
     if (ws && base) {
         char *b = (char *)base;
         ws->W = (float *)(b + oW);
@@ -404,6 +435,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->xs = (float2 *)(b + oX);
         ws->sx = (int *)(b + oI);
         ws->rexp = (int *)(b + oJ);
+        ws->rtc_xs = b + oK;
         ws->berr = (double *)(b + oE);
         ws->done = (int *)(b + oD);
         ws->anorm_bits = (unsigned long long *)(b + oS);
@@ -487,14 +519,23 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
     double worst = INFINITY;
     for (;; ++it) {
         slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
-        residual_df(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx, ws.anorm_bits);
+        if ((rc = residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx, ws.rtc_xs,
+                                 ws.anorm_bits, ws.err)))
+            break;
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
         gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb, ws.anorm_bits, tol, ws.berr, ws.done,
                                                                      ws.rexp);
         if ((rc = gb300_record_cuda_error(
                  cudaMemcpyAsync(hberr, ws.berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s))))
             break;
+        int herr = 0;  // a wait that ran out in a sweep or a residual invalidates the iteration
+        if ((rc = gb300_record_cuda_error(cudaMemcpyAsync(&herr, ws.err, sizeof herr, cudaMemcpyDeviceToHost, s))))
+            break;
         if ((rc = gb300_record_cuda_error(cudaStreamSynchronize(s)))) break;
+        if (herr) {
+            status = GB300_ETIMEDOUT;
+            break;
+        }
         worst = 0;
         for (int j = 0; j < nrhs; ++j) worst = fmax(worst, hberr[j]);
         if (worst <= tol) {
@@ -725,6 +766,58 @@ int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const f
     int *cnt = (int *)((char *)work + align256((size_t)n * 16 * sizeof(float)));
     tile_sweeps((cudaStream_t)stream, n, nrhs, nb, L, ldl, Dinv, ldd, B, ldb, Z, cnt, d_err);
     return gb300_last_launch_status();
+}
+
+// ---- symmetric residual R = B - A X with the tensor-core slice products ----
+
+static size_t syres_layout(int n, int nrhs, char *base, double **partials, float2 **xs, int **sx, void **rxs,
+                           unsigned long long **an)
+{
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    const size_t oP = take(residual_partials(n, nrhs) * sizeof(double));
+    const size_t oX = take((size_t)n * 16 * ((nrhs + 15) / 16) * sizeof(float2));
+    const size_t oS = take((size_t)nrhs * sizeof(int));
+    const size_t oR = take(residual_tc_xs_bytes(n, nrhs));
+    const size_t oA = take(4 * sizeof(unsigned long long));
+    if (base) {
+        *partials = (double *)(base + oP);
+        *xs = (float2 *)(base + oX);
+        *sx = (int *)(base + oS);
+        *rxs = base + oR;
+        *an = (unsigned long long *)(base + oA);
+    }
+    return off;
+}
+
+size_t starpu_gb300_dsyresidual_workspace(int n, int nrhs)
+{
+    if (n <= 0 || nrhs <= 0) return 0;
+    return syres_layout(n, nrhs, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+int starpu_gb300_dsyresidual(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
+                             const double *B, int ldb, double *R, int ldr, void *work, size_t lwork, int *d_err)
+{
+    if (n <= 0 || nrhs <= 0) return n < 0 || nrhs < 0 ? GB300_EINVAL : GB300_OK;
+    if (lda < n || ldx < n || ldb < n || ldr < n || !A || !X || !B || !R || !work || !d_err ||
+        lwork < starpu_gb300_dsyresidual_workspace(n, nrhs))
+        return GB300_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    double *partials;
+    float2 *xs;
+    int *sx;
+    void *rxs;
+    unsigned long long *an;
+    syres_layout(n, nrhs, (char *)work, &partials, &xs, &sx, &rxs, &an);
+    cudaMemsetAsync(an, 0, sizeof *an, s);
+    gb300_count_launch(), convert_lower_symnorm_kernel<<<(n + SYM_BW - 1) / SYM_BW, 256, 0, s>>>(n, A, lda, nullptr, 0,
+                                                                                                 an);
+    return residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, R, ldr, partials, xs, sx, rxs, an, d_err);
 }
 
 size_t starpu_gb300_backward_error_workspace(int n, int nrhs)

@@ -10,6 +10,7 @@
 
 #include "gb300_internal.h"
 #include "kernels/diag_coop.cuh"
+#include "kernels/residual_tc.cuh"
 #include "kernels/tc_update.cuh"
 #include "starpu_gb300_kernels.h"
 #include "starpu_gb300_solver.h"
@@ -266,6 +267,73 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
                        8.0 * m * (m + 1.0) / 2.0 + 2.0 * m * ldk * np);
         if (rc) return rc;
     }
+    return gb300_last_launch_status();
+}
+
+// ---- residual partials on the tensor cores (sliced fixed-point products) ----
+
+static long rtc_ldk(int n) { return ((long)n + 63) / 64 * 64; }
+
+size_t residual_tc_xs_bytes(int n, int nrhs)
+{
+    const long groups = (nrhs + 15) / 16;
+    return (size_t)groups * RTC_XROWS * rtc_ldk(n) * 2;
+}
+
+// K chunk of the tensor-core residual: a multiple of the exact accumulation
+// block, with enough work items (128-row block x chunk x group of 16) for a
+// few per SM, and at most max_chunks chunks (the partials buffer).
+int residual_tc_kchunk(int n, int nrhs, int max_chunks)
+{
+    const long items = (long)((n + RTC_BM - 1) / RTC_BM) * ((nrhs + 15) / 16);
+    long nk = (4L * num_sms() + items - 1) / items;
+    nk = std::max(1L, std::min<long>(max_chunks, nk));
+    long kc = ((n + nk - 1) / nk + RTC_KBLK - 1) / RTC_KBLK * RTC_KBLK;
+    return (int)std::max<long>(kc, RTC_KBLK);
+}
+
+// P_z = -(A X) over the K chunks z of length kchunk (A symmetric, lower
+// triangle read).  sx: ilogb(max |x_j|) per column (device), anorm_bits:
+// ||A||_inf (device).  xs: residual_tc_xs_bytes(n, nrhs) bytes of scratch.
+int residual_tc(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx, const int *sx,
+                const unsigned long long *anorm_bits, int kchunk, void *xs, double *partials, int *d_err)
+{
+    if (n <= 0 || nrhs <= 0) return GB300_OK;
+    if (kchunk % RTC_KBLK || !d_err) return GB300_EINVAL;
+    const long ldk = rtc_ldk(n);
+    const int groups = (nrhs + 15) / 16;
+    uint16_t *Xs = (uint16_t *)xs;
+    cudaMemsetAsync(xs, 0, residual_tc_xs_bytes(n, nrhs), s);
+    for (int g = 0; g < groups; ++g) {
+        const int nc = std::min(16, nrhs - 16 * g);
+        gb300_count_launch(), rtc_x_slices_kernel<<<dim3((unsigned)((ldk + 255) / 256), 16), 256, 0, s>>>(
+            n, nc, X + (long)g * 16 * ldx, ldx, sx + 16 * g, Xs + (long)g * RTC_XROWS * ldk, ldk);
+    }
+    CUtensorMap tm;
+    int rc = make_kmajor_map(&tm, xs, groups * RTC_XROWS, (int)ldk, ldk, RTC_XROWS);
+    if (rc) return rc;
+    ResidualTcArgs a;
+    a.n = n;
+    a.nrhs = nrhs;
+    a.A = A;
+    a.lda = lda;
+    a.anorm_bits = anorm_bits;
+    a.sx = sx;
+    a.kchunk = kchunk;
+    a.nblocks = (n + RTC_BM - 1) / RTC_BM;
+    a.nchunks = (n + kchunk - 1) / kchunk;
+    a.ngroups = groups;
+    a.nitems = a.nblocks * a.nchunks * a.ngroups;
+    a.P = partials;
+    a.err = d_err;
+    a.wait_budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(residual_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, RTC_SMEM);
+        attr_set = true;
+    }
+    const int grid = std::min(a.nitems, num_sms());
+    gb300_count_launch(), residual_tc_kernel<<<grid, RTC_THREADS, RTC_SMEM, s>>>(tm, a);
     return gb300_last_launch_status();
 }
 

@@ -10,6 +10,12 @@ namespace gb300 {
 // largest diagonal tile the cooperative factor-and-invert kernel handles
 constexpr int GB300_DIAG_TILE_MAX = 1024;
 
+// residual partials P_z = -(A X) on the tensor cores (capi_tc.cu)
+size_t residual_tc_xs_bytes(int n, int nrhs);
+int residual_tc_kchunk(int n, int nrhs, int max_chunks);
+int residual_tc(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx, const int *sx,
+                const unsigned long long *anorm_bits, int kchunk, void *xs, double *partials, int *d_err);
+
 
 // the two phases of starpu_gb300_dsposv (capi_solver.cu)
 int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,

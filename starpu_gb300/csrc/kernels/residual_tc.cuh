@@ -1,0 +1,438 @@
+// Residual partials of the refinement, P = -(A x) over K chunks, on the
+// tensor cores in exact fixed-point arithmetic (A symmetric, lower triangle
+// read; x FP64).  The FP64 matrix-vector products of the refinement are the
+// dominant FP64 work of a mixed-precision solve, and GB300's FP64 rate is a
+// small fraction of its BF16 tensor rate; this forms them from 7-bit slices:
+//
+//   A = 2^alpha     sum_{t=1..8} a_t 2^{-7t}   (alpha: ||A||_inf < 2^alpha)
+//   x = 2^beta_j    sum_{u=1..8} b_u 2^{-7u}   (per right-hand side)
+//
+// a_t, b_u: unsigned 7-bit digits of the magnitude (56 bits, the last one
+// rounded) carrying the element's sign -- integers in [-127, 127], exact in
+// BF16.  A x = 2^{alpha+beta} sum_{d=2..9} 2^{-7d} S_d with
+// S_d = sum_{t+u=d} a_t b_u (the pairs with t + u > 9 are below the digits'
+// own rounding): every S_d over a K block of 128 is an integer below 2^24
+// (at most 8 pairs x 127^2 x 128), so the FP32 accumulation of the tensor
+// cores is exact.  Per K block the 8 scales land in one 128 x 128 TMEM
+// accumulator: the x slices are stored as 15 blocks of 16 rows (7 zero blocks,
+// then b_1 .. b_8), and A slice t multiplies the 128-row window starting at
+// block 8 - t, so accumulator column block d - 2 receives a_t b_{d-t}.  The
+// epilogue folds the 8 exact block sums into a double-float (FP32 pair) per
+// row and right-hand side; the final value is scaled by 2^{alpha+beta} in
+// FP64.  Error: ~2^-56 of ||A||_inf ||x||_inf per element product.
+//
+// CTA (one per SM, persistent over work items = (128-row block, K chunk,
+// group of 16 right-hand sides)):
+//   warps 0-7  producers: load the FP64 A tile (128 rows x 64 k, from the
+//              lower triangle, mirrored above the diagonal), cut it into the
+//              digits and write slices 1-4, then 5-8 (two half stages) in the
+//              128-byte-swizzled K-major layout; warp 0 also fetches the x
+//              slice window of the stage by TMA
+//   warp 8     MMA issuer + TMEM owner (256 columns: two accumulators)
+//   warps 9-12 epilogue: tcgen05.ld of the accumulator, double-float fold
+// Every mbarrier wait is bounded; on timeout the CTA records an error and
+// drains its own copies and MMAs before exiting.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "sm100_ptx.cuh"
+
+namespace gb300 {
+
+constexpr int RTC_BM = 128;                       // rows per tile (MMA M)
+constexpr int RTC_BK = 64;                        // k per stage: one 128-byte swizzle row of BF16
+constexpr int RTC_HALF = 4;                       // slices per half stage
+constexpr int RTC_N = 128;                        // MMA N: 8 scales x 16 right-hand sides
+constexpr int RTC_XROWS = 240;                    // x slice rows: (7 zero + 8 slice) blocks x 16
+constexpr int RTC_KBLK = 128;                     // k per exact accumulation block (2 stages)
+constexpr int RTC_SLICE_BYTES = RTC_BM * RTC_BK * 2;         // 16 KB
+constexpr int RTC_AH_BYTES = RTC_HALF * RTC_SLICE_BYTES;     // 64 KB
+constexpr int RTC_X_BYTES = RTC_XROWS * RTC_BK * 2;          // 30 KB
+constexpr int RTC_PWARPS = 8;
+constexpr int RTC_MMA_WARP = 8;
+constexpr int RTC_EPI_WARP0 = 9;
+constexpr int RTC_THREADS = 13 * 32;
+constexpr int RTC_SMEM = 2 * RTC_AH_BYTES + 2 * RTC_X_BYTES + 1024 + 256;
+constexpr uint32_t RTC_TMEM_COLS = 256;
+constexpr int RTC_ERR_TIMEOUT = 5;
+
+struct ResidualTcArgs {
+    int n, nrhs;
+    const double *A;
+    long lda;
+    const unsigned long long *anorm_bits;  // ||A||_inf as FP64 bits: alpha = ilogb + 1
+    const int *sx;       // per right-hand side: ilogb(max |x_j|); beta_j = sx[j] + 1
+    int kchunk;          // multiple of RTC_KBLK
+    int nblocks, nchunks, ngroups, nitems;
+    double *P;           // partials: P[z n nrhs + i + j n]
+    int *err;
+    unsigned long long wait_budget_ns;
+};
+
+// |v| 2^(56 - e) rounded to an integer < 2^56, as two 28-bit halves; the
+// sign of v rides in bit 31 of the high half.  v given as its two 32-bit words.
+__device__ __forceinline__ void rtc_fixed(uint32_t whi, uint32_t wlo, int e, uint32_t &fhi, uint32_t &flo)
+{
+    const int ex = (int)((whi >> 20) & 0x7FF);
+    // mantissa m = 53 bits: mh (21 bits incl. the implicit one) : wlo (32 bits)
+    const uint32_t mh = (whi & 0xFFFFFu) | (ex ? 0x100000u : 0u);
+    const int sh = ex - 1019 - e;  // F = m << sh (sh <= 3 since |v| < 2^e), or m >> -sh rounded
+    uint64_t m = ((uint64_t)mh << 32) | wlo;
+    uint64_t F;
+    if (ex == 0 || ex == 0x7FF) F = 0;
+    else if (sh >= 0) F = m << sh;
+    else if (sh >= -56) F = (m + (1ull << (-sh - 1))) >> (-sh);
+    else F = 0;
+    fhi = (uint32_t)(F >> 28) | (whi & 0x80000000u);
+    flo = (uint32_t)F & 0xFFFFFFFu;
+}
+
+// e with v < 2^e for v = max |.| (1 for v = 0 or non-finite)
+__device__ __forceinline__ int rtc_bound_exp(double v)
+{
+    if (!(v > 0.0) || !isfinite(v)) return 1;
+    return ilogb(v) + 1;
+}
+
+// BF16 bits of digit t (1..8) with the sign
+__device__ __forceinline__ uint32_t rtc_digit_bf16(uint32_t fhi, uint32_t flo, int t)
+{
+    const uint32_t dgt = t <= 4 ? (fhi >> (28 - 7 * t)) & 127u : (flo >> (56 - 7 * t)) & 127u;
+    // exact: at most 7 significant bits
+    return (__float_as_uint(__uint2float_rn(dgt)) >> 16) | ((fhi >> 16) & 0x8000u);
+}
+
+// x slices for one group of 16 right-hand sides: Xs[row * ldk + k], row =
+// 16 b + j, b = 7 + (t - 1) for digit t (rows 0..111 stay zero).
+__global__ void rtc_x_slices_kernel(int n, int ncols, const double *__restrict__ X, long ldx,
+                                    const int *__restrict__ sx, uint16_t *__restrict__ Xs, long ldk)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (k >= ldk) return;
+    uint32_t fhi = 0, flo = 0;
+    if (k < n && j < ncols) {
+        const double v = X[k + (long)j * ldx];
+        const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+        rtc_fixed((uint32_t)(u >> 32), (uint32_t)u, sx[j] + 1, fhi, flo);
+    }
+#pragma unroll
+    for (int t = 1; t <= 8; ++t) {
+        const uint32_t h = (k < n && j < ncols) ? rtc_digit_bf16(fhi, flo, t) : 0u;
+        Xs[(long)(16 * (6 + t) + j) * ldk + k] = (uint16_t)h;
+    }
+}
+
+// byte offset of the 16-byte chunk (row r, k chunk c of 8 BF16) in a
+// 128-byte-swizzled K-major tile (8-row atoms of 1024 bytes)
+__device__ __forceinline__ uint32_t rtc_sw128(int r, int c)
+{
+    return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
+}
+
+__device__ __forceinline__ void rtc_item(const ResidualTcArgs &a, int it, int &blk, int &z, int &g)
+{
+    blk = it % a.nblocks;
+    const int r = it / a.nblocks;
+    z = r % a.nchunks;
+    g = r / a.nchunks;
+}
+
+__global__ void __launch_bounds__(RTC_THREADS, 1)
+residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArgs args)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;                          // 2 half stages x 4 slices x 16 KB
+    uint8_t *sX = smem + 2 * RTC_AH_BYTES;       // 2 x 30 KB
+    uint64_t *bars = (uint64_t *)(sX + 2 * RTC_X_BYTES);
+    uint64_t *a_full = bars, *a_empty = bars + 2;
+    uint64_t *x_full = bars + 4, *x_empty = bars + 6;
+    uint64_t *d_full = bars + 8, *d_empty = bars + 10;
+    uint64_t *drain = bars + 12;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 13);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2; ++s) {
+            ptx::mbar_init(&a_full[s], RTC_PWARPS * 32);
+            ptx::mbar_init(&a_empty[s], 1);
+            ptx::mbar_init(&x_full[s], 1);
+            ptx::mbar_init(&x_empty[s], 1);
+            ptx::mbar_init(&d_full[s], 1);
+            ptx::mbar_init(&d_empty[s], 128);
+        }
+        ptx::mbar_init(drain, 1);
+        *abort_flag = 0;
+        ptx::fence_mbarrier_init();
+    }
+    if (warp == 0 && lane == 0) ptx::tma_prefetch_desc(&tm_x);
+    if (warp == RTC_MMA_WARP) {
+        ptx::tmem_alloc(tmem_slot, RTC_TMEM_COLS);
+        ptx::tmem_relinquish();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+    const int n = args.n;
+    const int alpha = rtc_bound_exp(__longlong_as_double((long long)*args.anorm_bits));
+
+    if (warp < RTC_PWARPS) {
+        // ------------------------------------------------------------ producers
+        const int tid = threadIdx.x;  // 0..255
+        int as = 0, xs = 0;
+        uint32_t aph = 0, xph = 0;
+        int x_issued = 0;
+        bool ok = true;
+        for (int it = blockIdx.x; it < args.nitems && ok; it += gridDim.x) {
+            int blk, z, g;
+            rtc_item(args, it, blk, z, g);
+            const int i0 = blk * RTC_BM;
+            const int kz0 = z * args.kchunk, kz1 = min(n, kz0 + args.kchunk);
+            for (int k0 = kz0; k0 < kz1 && ok; k0 += RTC_BK) {
+                // x slice window of this stage (TMA, one thread)
+                if (tid == 0) {
+                    if (!ptx::wait_parity(&x_empty[xs], xph ^ 1, abort_flag, args.wait_budget_ns)) ok = false;
+                    else {
+                        ptx::mbar_arrive_expect_tx(&x_full[xs], RTC_X_BYTES);
+                        ptx::tma_load_2d(sX + xs * RTC_X_BYTES, &tm_x, &x_full[xs], k0, g * RTC_XROWS);
+                        ++x_issued;
+                    }
+                }
+                if (++xs == 2) {
+                    xs = 0;
+                    xph ^= 1;
+                }
+                // this thread's 4 chunks: row r = tid % 128, k chunks c = tid / 128 + 2 q;
+                // the raw FP64 words stay in registers, the fixed-point form is
+                // recomputed per half stage
+                const int r = tid & 127, row = i0 + r;
+                unsigned long long raw[4][8];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = (tid >> 7) + 2 * q;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int col = k0 + 8 * c + e;
+                        unsigned long long u = 0;
+                        if (row < n && col < kz1) {
+                            const double *src = col <= row ? &args.A[(long)row + (long)col * args.lda]
+                                                           : &args.A[(long)col + (long)row * args.lda];
+                            u = (unsigned long long)__double_as_longlong(__ldg(src));
+                        }
+                        raw[q][e] = u;
+                    }
+                }
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (!ptx::wait_parity(&a_empty[as], aph ^ 1, abort_flag, args.wait_budget_ns)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *buf = sA + as * RTC_AH_BYTES;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int c = (tid >> 7) + 2 * q;
+                        uint32_t fhi[8], flo[8];
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            rtc_fixed((uint32_t)(raw[q][e] >> 32), (uint32_t)raw[q][e], alpha, fhi[e], flo[e]);
+#pragma unroll
+                        for (int tl = 0; tl < RTC_HALF; ++tl) {
+                            const int t = 4 * h + tl + 1;
+                            uint32_t w[4];
+#pragma unroll
+                            for (int p = 0; p < 4; ++p)
+                                w[p] = rtc_digit_bf16(fhi[2 * p], flo[2 * p], t) |
+                                       (rtc_digit_bf16(fhi[2 * p + 1], flo[2 * p + 1], t) << 16);
+                            *reinterpret_cast<uint4 *>(buf + tl * RTC_SLICE_BYTES + rtc_sw128(r, c)) =
+                                make_uint4(w[0], w[1], w[2], w[3]);
+                        }
+                    }
+                    ptx::fence_proxy_async_smem();  // generic-proxy stores -> visible to the tensor cores
+                    ptx::mbar_arrive(&a_full[as]);
+                    if (++as == 2) {
+                        as = 0;
+                        aph ^= 1;
+                    }
+                }
+            }
+        }
+        if (!ok) {
+            if (!*abort_flag) atomicCAS(args.err, 0, RTC_ERR_TIMEOUT);
+            *abort_flag = 1;
+        }
+        // drain the x copies this CTA issued (bounded; ignores the abort flag)
+        if (tid == 0) {
+            int s = xs;
+            uint32_t ph = xph;
+            const int back = x_issued < 2 ? x_issued : 2;
+            for (int i = 0; i < back; ++i) {
+                if (--s < 0) {
+                    s = 1;
+                    ph ^= 1;
+                }
+                volatile int never = 0;
+                ptx::wait_parity(&x_full[s], ph, &never, args.wait_budget_ns);
+            }
+        }
+    } else if (warp == RTC_MMA_WARP) {
+        // ----------------------------------------------------------- MMA issuer
+        if (ptx::elect_one()) {
+            constexpr uint32_t idesc = ptx::make_idesc(RTC_BM, RTC_N, ptx::FMT_BF16);
+            int as = 0, xs = 0, db = 0;
+            uint32_t aph = 0, xph = 0, dph = 0;
+            bool ok = true;
+            for (int it = blockIdx.x; it < args.nitems && ok; it += gridDim.x) {
+                int blk, z, g;
+                rtc_item(args, it, blk, z, g);
+                const int kz0 = z * args.kchunk, kz1 = min(n, kz0 + args.kchunk);
+                int kin = 0;  // k covered in the current accumulation block
+                for (int k0 = kz0; k0 < kz1 && ok; k0 += RTC_BK) {
+                    if (kin == 0) {
+                        if (!ptx::wait_parity(&d_empty[db], dph ^ 1, abort_flag, args.wait_budget_ns)) {
+                            ok = false;
+                            break;
+                        }
+                        ptx::tc_fence_after();
+                    }
+                    if (!ptx::wait_parity(&x_full[xs], xph, abort_flag, args.wait_budget_ns)) {
+                        ok = false;
+                        break;
+                    }
+                    ptx::tc_fence_after();
+                    const uint32_t d_tmem = tmem_base + (uint32_t)(db * RTC_N);
+                    const uint32_t x_addr = ptx::smem_u32(sX + xs * RTC_X_BYTES);
+                    for (int h = 0; h < 2 && ok; ++h) {
+                        if (!ptx::wait_parity(&a_full[as], aph, abort_flag, args.wait_budget_ns)) {
+                            ok = false;
+                            break;
+                        }
+                        ptx::tc_fence_after();
+                        const uint32_t a_addr = ptx::smem_u32(sA + as * RTC_AH_BYTES);
+#pragma unroll
+                        for (int tl = 0; tl < RTC_HALF; ++tl) {
+                            const int t = 4 * h + tl + 1;
+                            const uint32_t aa = a_addr + tl * RTC_SLICE_BYTES;
+                            const uint32_t xa = x_addr + (uint32_t)(8 - t) * 2048u;  // window from row block 8 - t
+#pragma unroll
+                            for (int k = 0; k < RTC_BK / 16; ++k) {
+                                const uint32_t accum = (kin > 0 || h > 0 || tl > 0 || k > 0) ? 1u : 0u;
+                                ptx::mma_f16_ss(d_tmem, ptx::make_sdesc_k128(aa + k * 32),
+                                                ptx::make_sdesc_k128(xa + k * 32), idesc, accum);
+                            }
+                        }
+                        ptx::mma_commit(&a_empty[as]);
+                        if (++as == 2) {
+                            as = 0;
+                            aph ^= 1;
+                        }
+                    }
+                    if (!ok) break;
+                    ptx::mma_commit(&x_empty[xs]);
+                    if (++xs == 2) {
+                        xs = 0;
+                        xph ^= 1;
+                    }
+                    kin += RTC_BK;
+                    if (kin == RTC_KBLK || k0 + RTC_BK >= kz1) {
+                        ptx::mma_commit(&d_full[db]);
+                        kin = 0;
+                        if (++db == 2) {
+                            db = 0;
+                            dph ^= 1;
+                        }
+                    }
+                }
+            }
+            if (!ok) {
+                if (!*abort_flag) atomicCAS(args.err, 0, RTC_ERR_TIMEOUT);
+                *abort_flag = 1;
+            }
+            ptx::mma_commit(drain);
+            volatile int never = 0;
+            ptx::wait_parity(drain, 0, &never, args.wait_budget_ns);
+        }
+    } else {
+        // ------------------------------------------------------------- epilogue
+        // a warp may access only the TMEM lane quarter warp % 4: warps 9-12
+        // take quarters 1, 2, 3, 0
+        const int quarter = warp & 3;
+        const int rloc = quarter * 32 + lane;
+        int db = 0;
+        uint32_t dph = 0;
+        bool ok = true;
+        for (int it = blockIdx.x; it < args.nitems && ok; it += gridDim.x) {
+            int blk, z, g;
+            rtc_item(args, it, blk, z, g);
+            const int kz0 = z * args.kchunk, kz1 = min(n, kz0 + args.kchunk);
+            const int nblk = (kz1 - kz0 + RTC_KBLK - 1) / RTC_KBLK;
+            float hi[16], lo[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) hi[j] = lo[j] = 0.0f;
+            for (int b = 0; b < nblk; ++b) {
+                if (!ptx::wait_parity(&d_full[db], dph, abort_flag, args.wait_budget_ns)) {
+                    ok = false;
+                    break;
+                }
+                ptx::tc_fence_after();
+                const uint32_t tb = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(db * RTC_N);
+                // column block d - 2 holds S_d for the 16 right-hand sides; smallest scale first
+#pragma unroll 1
+                for (int ch = 3; ch >= 0; --ch) {
+                    uint32_t v[32];
+                    ptx::tmem_ld_32x32b_x32(tb + ch * 32, v);
+                    ptx::tmem_ld_wait();
+                    if (ch == 0) {
+                        ptx::tc_fence_before();
+                        ptx::mbar_arrive(&d_empty[db]);
+                    }
+#pragma unroll
+                    for (int half = 1; half >= 0; --half) {
+                        const int d = 2 + 2 * ch + half;
+                        const float sc = __uint_as_float((uint32_t)(127 - 7 * d) << 23);  // 2^-7d
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const float x = __fmul_rn(__uint_as_float(v[16 * half + j]), sc);  // exact
+                            const float s = __fadd_rn(hi[j], x);
+                            const float bb = __fsub_rn(s, hi[j]);
+                            lo[j] = __fadd_rn(lo[j], __fadd_rn(__fsub_rn(hi[j], __fsub_rn(s, bb)), __fsub_rn(x, bb)));
+                            hi[j] = s;
+                        }
+                    }
+                }
+                if (++db == 2) {
+                    db = 0;
+                    dph ^= 1;
+                }
+            }
+            if (!ok) break;
+            const int i = blk * RTC_BM + rloc;
+            if (i < n) {
+                double *Pz = args.P + (long)z * n * args.nrhs;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int jj = g * 16 + j;
+                    if (jj < args.nrhs)
+                        Pz[(long)i + (long)jj * n] = -scalbn((double)hi[j] + (double)lo[j], alpha + args.sx[jj] + 1);
+                }
+            }
+        }
+        if (!ok) {
+            if (!*abort_flag) atomicCAS(args.err, 0, RTC_ERR_TIMEOUT);
+            *abort_flag = 1;
+        }
+    }
+
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    if (warp == RTC_MMA_WARP) ptx::tmem_dealloc(tmem_base, RTC_TMEM_COLS);
+}
+
+} // namespace gb300

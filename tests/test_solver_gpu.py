@@ -226,3 +226,62 @@ def test_spotrs_inv_tiles_rejects_bad_tiles(gpu):
     assert gpu.starpu_gb300_spotrs_inv_tiles_workspace(100, 48) == 0  # nb not a multiple of 32
     assert gpu.starpu_gb300_spotrs_inv_tiles(None, 100, 1, 48, None, 100, None, 64, None, 100, None, 0, None) == -22
     assert gpu.starpu_gb300_spotrs_inv_tiles(None, 100, 1, 2048, None, 100, None, 2048, None, 100, None, 0, None) == -22
+
+
+def exact_residual(A, X, B):
+    """B - A X to ~1 ulp: every product split exactly into 26-bit halves
+    (Veltkamp), all terms of a row summed with math.fsum."""
+    import math
+
+    def split(v):
+        c = v * 134217729.0  # 2^27 + 1
+        hi = c - (c - v)
+        return hi, v - hi
+    Ah, Al = split(np.asarray(A, np.float64))
+    R = np.empty_like(B)
+    for j in range(X.shape[1]):
+        xh, xl = split(X[:, j])
+        for i in range(A.shape[0]):
+            terms = np.concatenate([Ah[i] * xh, Ah[i] * xl, Al[i] * xh, Al[i] * xl])
+            R[i, j] = math.fsum(np.concatenate([[B[i, j]], -terms]))
+    return R
+
+
+def dsyresidual(gpu, A, X, B):
+    n, nrhs = X.shape
+    dA, dX, dB = DeviceBuffer.from_array(A), DeviceBuffer.from_array(X), DeviceBuffer.from_array(B)
+    dR = DeviceBuffer(8 * n * nrhs)
+    lw = gpu.starpu_gb300_dsyresidual_workspace(n, nrhs)
+    W, err = DeviceBuffer(lw), DeviceBuffer.from_array(np.zeros(1, np.int32))
+    check(gpu.starpu_gb300_dsyresidual(None, n, nrhs, dA.ptr, n, dX.ptr, n, dB.ptr, n, dR.ptr, n, W.ptr, lw, err.ptr))
+    R = dR.download((n, nrhs), np.float64)
+    assert err.download((1,), np.int32)[0] == 0
+    return R
+
+
+@pytest.mark.parametrize("n,nrhs", [(128, 1), (500, 5), (777, 20)])
+def test_dsyresidual_tensor_core_slices_are_fp64_accurate(gpu, oracle, n, nrhs):
+    """The refinement residual from exact products of 7-bit slices on the
+    tensor cores: within 2^-45 of ||A||_inf ||x_j||_inf of the exact residual
+    (columns of very different scale, a zero column, negative entries),
+    bit-identical on repeat, and the strict upper triangle is never read."""
+    rng = np.random.default_rng(n + nrhs)
+    A = oracle.spd_gram(n, n, 0.3)
+    A[:, :] = A - 0.2 * np.mean(A)  # negative entries too (the residual needs no definiteness)
+    A = np.asfortranarray(np.tril(A) + np.tril(A, -1).T)
+    X = np.asfortranarray(rng.standard_normal((n, nrhs)) * np.exp(rng.uniform(-30, 30, nrhs)))
+    X[:, nrhs // 2] = 0.0
+    B = np.asfortranarray(A @ X + 1e-9 * rng.standard_normal((n, nrhs)) * np.abs(X).max(0))
+    R = dsyresidual(gpu, A, X, B)
+    Rx = exact_residual(A, X, B)
+    anorm = np.abs(A).sum(1).max()
+    for j in range(nrhs):
+        scale = anorm * np.abs(X[:, j]).max()
+        if scale == 0:
+            np.testing.assert_array_equal(R[:, j], B[:, j])
+        else:
+            assert np.max(np.abs(R[:, j] - Rx[:, j])) <= 2.0 ** -45 * scale, j
+    np.testing.assert_array_equal(dsyresidual(gpu, A, X, B), R)
+    An = np.array(A, order="F")
+    An[np.triu_indices(n, 1)] = np.nan
+    np.testing.assert_array_equal(dsyresidual(gpu, An, X, B), R)
