@@ -17,9 +17,10 @@
 // accumulator: the x slices are stored as 15 blocks of 16 rows (7 zero blocks,
 // then b_1 .. b_8), and A slice t multiplies the 128-row window starting at
 // block 8 - t, so accumulator column block d - 2 receives a_t b_{d-t}.  The
-// epilogue folds the 8 exact block sums into a double-float (FP32 pair) per
-// row and right-hand side; the final value is scaled by 2^{alpha+beta} in
-// FP64.  Error: ~2^-56 of ||A||_inf ||x||_inf per element product.
+// epilogue adds the exact block sums as integers, sum_d S_d 2^(7 (9 - d)), in
+// 128 bits over the whole K chunk, and rounds once to FP64 at the end (scaled
+// by 2^{alpha+beta-63}).  Error: ~2^-56 of ||A||_inf ||x||_inf per element
+// product from the digits, plus one FP64 rounding of each partial.
 //
 // CTA (one per SM, persistent over work items = (128-row block, K chunk,
 // group of 16 right-hand sides)):
@@ -29,7 +30,7 @@
 //              128-byte-swizzled K-major layout; warp 0 also fetches the x
 //              slice window of the stage by TMA
 //   warp 8     MMA issuer + TMEM owner (256 columns: two accumulators)
-//   warps 9-12 epilogue: tcgen05.ld of the accumulator, double-float fold
+//   warps 9-12 epilogue: tcgen05.ld of the accumulator, exact integer sums
 // Every mbarrier wait is bounded; on timeout the CTA records an error and
 // drains its own copies and MMAs before exiting.
 #pragma once
@@ -101,8 +102,10 @@ __device__ __forceinline__ int rtc_bound_exp(double v)
 __device__ __forceinline__ uint32_t rtc_digit_bf16(uint32_t fhi, uint32_t flo, int t)
 {
     const uint32_t dgt = t <= 4 ? (fhi >> (28 - 7 * t)) & 127u : (flo >> (56 - 7 * t)) & 127u;
-    // exact: at most 7 significant bits
-    return (__float_as_uint(__uint2float_rn(dgt)) >> 16) | ((fhi >> 16) & 0x8000u);
+    // dgt as an FP32 by a full-rate add ((2^23 + dgt) - 2^23), then its top 16
+    // bits: exact, the digit has at most 7 significant bits
+    const float f = __fsub_rn(__uint_as_float(0x4B000000u | dgt), 8388608.0f);
+    return (__float_as_uint(f) >> 16) | ((fhi >> 16) & 0x8000u);
 }
 
 // x slices for one group of 16 right-hand sides: Xs[row * ldk + k], row =
@@ -372,9 +375,11 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
             rtc_item(args, it, blk, z, g);
             const int kz0 = z * args.kchunk, kz1 = min(n, kz0 + args.kchunk);
             const int nblk = (kz1 - kz0 + RTC_KBLK - 1) / RTC_KBLK;
-            float hi[16], lo[16];
+            // exact accumulation: V = sum_blocks sum_d S_d 2^(7 (9 - d)) (|V| < 2^82),
+            // the value is V 2^-63
+            __int128 acc[16];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) hi[j] = lo[j] = 0.0f;
+            for (int j = 0; j < 16; ++j) acc[j] = 0;
             for (int b = 0; b < nblk; ++b) {
                 if (!ptx::wait_parity(&d_full[db], dph, abort_flag, args.wait_budget_ns)) {
                     ok = false;
@@ -382,28 +387,22 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
                 }
                 ptx::tc_fence_after();
                 const uint32_t tb = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(db * RTC_N);
-                // column block d - 2 holds S_d for the 16 right-hand sides; smallest scale first
+                // column block d - 2 holds S_d for the 16 right-hand sides (exact integers < 2^24)
 #pragma unroll 1
-                for (int ch = 3; ch >= 0; --ch) {
+                for (int ch = 0; ch < 4; ++ch) {
                     uint32_t v[32];
                     ptx::tmem_ld_32x32b_x32(tb + ch * 32, v);
                     ptx::tmem_ld_wait();
-                    if (ch == 0) {
+                    if (ch == 3) {
                         ptx::tc_fence_before();
                         ptx::mbar_arrive(&d_empty[db]);
                     }
 #pragma unroll
-                    for (int half = 1; half >= 0; --half) {
+                    for (int half = 0; half < 2; ++half) {
                         const int d = 2 + 2 * ch + half;
-                        const float sc = __uint_as_float((uint32_t)(127 - 7 * d) << 23);  // 2^-7d
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const float x = __fmul_rn(__uint_as_float(v[16 * half + j]), sc);  // exact
-                            const float s = __fadd_rn(hi[j], x);
-                            const float bb = __fsub_rn(s, hi[j]);
-                            lo[j] = __fadd_rn(lo[j], __fadd_rn(__fsub_rn(hi[j], __fsub_rn(s, bb)), __fsub_rn(x, bb)));
-                            hi[j] = s;
-                        }
+                        for (int j = 0; j < 16; ++j)
+                            acc[j] += (__int128)__float2int_rn(__uint_as_float(v[16 * half + j])) << (7 * (9 - d));
                     }
                 }
                 if (++db == 2) {
@@ -418,8 +417,12 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int jj = g * 16 + j;
-                    if (jj < args.nrhs)
-                        Pz[(long)i + (long)jj * n] = -scalbn((double)hi[j] + (double)lo[j], alpha + args.sx[jj] + 1);
+                    if (jj < args.nrhs) {
+                        // V = hi 2^64 + lo; one rounding in the sum
+                        const double hi = (double)(long long)(acc[j] >> 64);
+                        const double lo = (double)(unsigned long long)acc[j];
+                        Pz[(long)i + (long)jj * n] = -scalbn(fma(hi, 18446744073709551616.0, lo), alpha + args.sx[jj] + 1 - 63);
+                    }
                 }
             }
         }

@@ -10,6 +10,7 @@
     python -m starpu_gb300.kernel_cases tile_ops  --n 1024 --reps 200
     python -m starpu_gb300.kernel_cases diag      --n 1024 --reps 50
     python -m starpu_gb300.kernel_cases tile_sweep --n 32768 --nb 1024 --nrhs 16 --reps 5
+    python -m starpu_gb300.kernel_cases syresidual --n 32768 --nrhs 16 --reps 3
 
 Each case allocates its operands once, runs `--reps` launches of the same
 shape and prints the mean time per launch measured with CUDA events.
@@ -51,7 +52,7 @@ def oracle_free_spd(n):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv",
-                                     "tile_ops", "diag", "tile_sweep"])
+                                     "tile_ops", "diag", "tile_sweep", "syresidual"])
     ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--n", type=int, default=8192)
@@ -206,6 +207,22 @@ def main(argv=None):
         ms = _timed(L, lambda: check(L.starpu_gb300_spotrs_inv_tiles(None, n, nrhs, nb, F.ptr, n, D.ptr, ldd, Y.ptr, n,
                                                                       Wk.ptr, lw, err.ptr)), a.reps)
         out.update(ms_two_sweeps=ms, gbs=4.0 * n * n / ms / 1e6, err=int(err.download((1,), np.int32)[0]))
+    elif a.case == "syresidual":
+        # the refinement residual R = B - A X on the tensor cores (symmetric A, lower triangle read)
+        n, nrhs = a.n, a.nrhs
+        A = DeviceBuffer(8 * n * n)
+        W = DeviceBuffer(8 * n * n)
+        check(L.starpu_gb300_gen_spd_gram(None, n, 3, 1.0, A.ptr, n, W.ptr))
+        del W
+        Bd, Xd, Rd = DeviceBuffer(8 * n * nrhs), DeviceBuffer(8 * n * nrhs), DeviceBuffer(8 * n * nrhs)
+        check(L.starpu_gb300_gen_uniform_rhs(None, n, nrhs, 4, Bd.ptr, n))
+        check(L.starpu_gb300_gen_uniform_rhs(None, n, nrhs, 5, Xd.ptr, n))
+        lw = L.starpu_gb300_dsyresidual_workspace(n, nrhs)
+        Wk = DeviceBuffer(lw)
+        err = DeviceBuffer.from_array(np.zeros(1, np.int32))
+        ms = _timed(L, lambda: check(L.starpu_gb300_dsyresidual(None, n, nrhs, A.ptr, n, Xd.ptr, n, Bd.ptr, n, Rd.ptr, n,
+                                                                 Wk.ptr, lw, err.ptr)), a.reps)
+        out.update(ms=ms, tflops_fp64_equiv=2.0 * n * n * nrhs / ms / 1e9, err=int(err.download((1,), np.int32)[0]))
     elif a.case == "dpotrf":
         n, nb = a.n, a.nb
         A = DeviceBuffer(8 * n * n)
