@@ -7,8 +7,8 @@
 //   A = 2^alpha     sum_{t=1..8} a_t 2^{-7t}   (alpha: ||A||_inf < 2^alpha)
 //   x = 2^beta_j    sum_{u=1..8} b_u 2^{-7u}   (per right-hand side)
 //
-// a_t, b_u: unsigned 7-bit digits of the magnitude (56 bits, the last one
-// rounded) carrying the element's sign -- integers in [-127, 127], exact in
+// a_t, b_u: unsigned 7-bit digits of the magnitude (56 bits, truncated)
+// carrying the element's sign -- integers in [-127, 127], exact in
 // BF16.  A x = 2^{alpha+beta} sum_{d=2..9} 2^{-7d} S_d with
 // S_d = sum_{t+u=d} a_t b_u (the pairs with t + u > 9 are below the digits'
 // own rounding): every S_d over a K block of 128 is an integer below 2^24
@@ -19,8 +19,8 @@
 // block 8 - t, so accumulator column block d - 2 receives a_t b_{d-t}.  The
 // epilogue adds the exact block sums as integers, sum_d S_d 2^(7 (9 - d)), in
 // 128 bits over the whole K chunk, and rounds once to FP64 at the end (scaled
-// by 2^{alpha+beta-63}).  Error: ~2^-56 of ||A||_inf ||x||_inf per element
-// product from the digits, plus one FP64 rounding of each partial.
+// by 2^{alpha+beta-63}).  Error: below 2^-55 of ||A||_inf ||x||_inf per
+// element product from the digits, plus one FP64 rounding of each partial.
 //
 // CTA (one per SM, persistent over work items = (128-row block, K chunk,
 // group of 16 right-hand sides)):
@@ -73,22 +73,35 @@ struct ResidualTcArgs {
     unsigned long long wait_budget_ns;
 };
 
-// |v| 2^(56 - e) rounded to an integer < 2^56, as two 28-bit halves; the
-// sign of v rides in bit 31 of the high half.  v given as its two 32-bit words.
+// |v| 2^(56 - e) truncated to an integer F < 2^56, as two 28-bit halves
+// F = fhi 2^28 + flo; the sign of v rides in bit 31 of fhi.  v given as its
+// two 32-bit words; |v| < 2^e.  32-bit funnel shifts only.
 __device__ __forceinline__ void rtc_fixed(uint32_t whi, uint32_t wlo, int e, uint32_t &fhi, uint32_t &flo)
 {
     const int ex = (int)((whi >> 20) & 0x7FF);
-    // mantissa m = 53 bits: mh (21 bits incl. the implicit one) : wlo (32 bits)
-    const uint32_t mh = (whi & 0xFFFFFu) | (ex ? 0x100000u : 0u);
-    const int sh = ex - 1019 - e;  // F = m << sh (sh <= 3 since |v| < 2^e), or m >> -sh rounded
-    uint64_t m = ((uint64_t)mh << 32) | wlo;
-    uint64_t F;
-    if (ex == 0 || ex == 0x7FF) F = 0;
-    else if (sh >= 0) F = m << sh;
-    else if (sh >= -56) F = (m + (1ull << (-sh - 1))) >> (-sh);
-    else F = 0;
-    fhi = (uint32_t)(F >> 28) | (whi & 0x80000000u);
-    flo = (uint32_t)F & 0xFFFFFFFu;
+    const uint32_t mh = (whi & 0xFFFFFu) | 0x100000u;  // m = mh 2^32 + wlo, 53 bits
+    const int sh = ex - 1019 - e;                        // F = m 2^sh, sh <= 3
+    const int kh = 28 - sh;                              // fhi = m >> kh, kh >= 25
+    const uint32_t h = kh < 32 ? __funnelshift_r(wlo, mh, kh) : (kh < 53 ? mh >> (kh - 32) : 0u);
+    const int kl = -sh;                                  // flo = (m >> kl) mod 2^28 (left shift when kl < 0)
+    const uint32_t l = kl <= 0 ? wlo << (-kl) : (kl < 32 ? __funnelshift_r(wlo, mh, kl) : (kl < 53 ? mh >> (kl - 32) : 0u));
+    const bool finite_normal = ex != 0 && ex != 0x7FF;
+    fhi = finite_normal ? (h & 0xFFFFFFFu) | (whi & 0x80000000u) : 0u;
+    flo = finite_normal ? l & 0xFFFFFFFu : 0u;
+}
+
+// BF16 pair of digit t (1..8) of two elements (element 0 in the low half),
+// with their signs: each digit becomes an exact FP32 by a full-rate add
+// ((2^23 + d) - 2^23), whose top 16 bits are its BF16 (at most 7 significant
+// bits), and one byte permute packs the pair.
+__device__ __forceinline__ uint32_t rtc_digit_pair(uint32_t fhi0, uint32_t flo0, uint32_t fhi1, uint32_t flo1, int t)
+{
+    const uint32_t d0 = t <= 4 ? (fhi0 >> (28 - 7 * t)) & 127u : (flo0 >> (56 - 7 * t)) & 127u;
+    const uint32_t d1 = t <= 4 ? (fhi1 >> (28 - 7 * t)) & 127u : (flo1 >> (56 - 7 * t)) & 127u;
+    const float f0 = __fsub_rn(__uint_as_float(0x4B000000u | d0), 8388608.0f);
+    const float f1 = __fsub_rn(__uint_as_float(0x4B000000u | d1), 8388608.0f);
+    const uint32_t signs = ((fhi0 >> 16) & 0x8000u) | (fhi1 & 0x80000000u);
+    return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632) | signs;
 }
 
 // e with v < 2^e for v = max |.| (1 for v = 0 or non-finite)
@@ -96,16 +109,6 @@ __device__ __forceinline__ int rtc_bound_exp(double v)
 {
     if (!(v > 0.0) || !isfinite(v)) return 1;
     return ilogb(v) + 1;
-}
-
-// BF16 bits of digit t (1..8) with the sign
-__device__ __forceinline__ uint32_t rtc_digit_bf16(uint32_t fhi, uint32_t flo, int t)
-{
-    const uint32_t dgt = t <= 4 ? (fhi >> (28 - 7 * t)) & 127u : (flo >> (56 - 7 * t)) & 127u;
-    // dgt as an FP32 by a full-rate add ((2^23 + dgt) - 2^23), then its top 16
-    // bits: exact, the digit has at most 7 significant bits
-    const float f = __fsub_rn(__uint_as_float(0x4B000000u | dgt), 8388608.0f);
-    return (__float_as_uint(f) >> 16) | ((fhi >> 16) & 0x8000u);
 }
 
 // x slices for one group of 16 right-hand sides: Xs[row * ldk + k], row =
@@ -124,7 +127,7 @@ __global__ void rtc_x_slices_kernel(int n, int ncols, const double *__restrict__
     }
 #pragma unroll
     for (int t = 1; t <= 8; ++t) {
-        const uint32_t h = (k < n && j < ncols) ? rtc_digit_bf16(fhi, flo, t) : 0u;
+        const uint32_t h = (k < n && j < ncols) ? rtc_digit_pair(fhi, flo, 0u, 0u, t) & 0xFFFFu : 0u;
         Xs[(long)(16 * (6 + t) + j) * ldk + k] = (uint16_t)h;
     }
 }
@@ -211,24 +214,36 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
                     xs = 0;
                     xph ^= 1;
                 }
-                // this thread's 4 chunks: row r = tid % 128, k chunks c = tid / 128 + 2 q;
-                // the raw FP64 words stay in registers, the fixed-point form is
-                // recomputed per half stage
-                const int r = tid & 127, row = i0 + r;
-                unsigned long long raw[4][8];
+                // this thread's 4 chunks (row r, 8 consecutive k at chunk c), converted
+                // once to the fixed-point form.  Below the diagonal lanes run
+                // along rows (coalesced columns), above it (the mirror of a lower
+                // block) 8 lanes share a row (coalesced rows); crossing tiles pick
+                // per element.
+                const int mode = (k0 + RTC_BK <= i0) ? 0 : (k0 >= i0 + RTC_BM ? 1 : 2);
+                int rq[4], cq[4];
+                uint32_t fhi[4][8], flo[4][8];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const int c = (tid >> 7) + 2 * q;
+                    if (mode == 1) {
+                        rq[q] = (tid >> 3) + 32 * q;
+                        cq[q] = tid & 7;
+                    } else {
+                        rq[q] = tid & 127;
+                        cq[q] = (tid >> 7) + 2 * q;
+                    }
+                    const int row = i0 + rq[q], col0 = k0 + 8 * cq[q];
+                    const bool rok = row < n;
 #pragma unroll
                     for (int e = 0; e < 8; ++e) {
-                        const int col = k0 + 8 * c + e;
+                        const int col = col0 + e;
                         unsigned long long u = 0;
-                        if (row < n && col < kz1) {
-                            const double *src = col <= row ? &args.A[(long)row + (long)col * args.lda]
-                                                           : &args.A[(long)col + (long)row * args.lda];
+                        if (rok && col < kz1) {
+                            const bool mirror = mode == 1 || (mode == 2 && col > row);
+                            const double *src = mirror ? &args.A[(long)col + (long)row * args.lda]
+                                                       : &args.A[(long)row + (long)col * args.lda];
                             u = (unsigned long long)__double_as_longlong(__ldg(src));
                         }
-                        raw[q][e] = u;
+                        rtc_fixed((uint32_t)(u >> 32), (uint32_t)u, alpha, fhi[q][e], flo[q][e]);
                     }
                 }
 #pragma unroll
@@ -240,21 +255,15 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
                     uint8_t *buf = sA + as * RTC_AH_BYTES;
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const int c = (tid >> 7) + 2 * q;
-                        uint32_t fhi[8], flo[8];
-#pragma unroll
-                        for (int e = 0; e < 8; ++e)
-                            rtc_fixed((uint32_t)(raw[q][e] >> 32), (uint32_t)raw[q][e], alpha, fhi[e], flo[e]);
+                        const uint32_t off = rtc_sw128(rq[q], cq[q]);
 #pragma unroll
                         for (int tl = 0; tl < RTC_HALF; ++tl) {
                             const int t = 4 * h + tl + 1;
                             uint32_t w[4];
 #pragma unroll
                             for (int p = 0; p < 4; ++p)
-                                w[p] = rtc_digit_bf16(fhi[2 * p], flo[2 * p], t) |
-                                       (rtc_digit_bf16(fhi[2 * p + 1], flo[2 * p + 1], t) << 16);
-                            *reinterpret_cast<uint4 *>(buf + tl * RTC_SLICE_BYTES + rtc_sw128(r, c)) =
-                                make_uint4(w[0], w[1], w[2], w[3]);
+                                w[p] = rtc_digit_pair(fhi[q][2 * p], flo[q][2 * p], fhi[q][2 * p + 1], flo[q][2 * p + 1], t);
+                            *reinterpret_cast<uint4 *>(buf + tl * RTC_SLICE_BYTES + off) = make_uint4(w[0], w[1], w[2], w[3]);
                         }
                     }
                     ptx::fence_proxy_async_smem();  // generic-proxy stores -> visible to the tensor cores
