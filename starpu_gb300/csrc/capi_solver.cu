@@ -263,7 +263,7 @@ static void residual_df(cudaStream_t s, int n, int nrhs, const double *A, long l
 // in FP64 in a fixed order either way.
 static int residual_mixed(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx,
                           const double *B, long ldb, double *R, long ldr, double *partials, float2 *xs, int *sx,
-                          void *rtc_xs, const unsigned long long *anorm_bits, int *d_err)
+                          const void *rtc_a, void *rtc_xs, const unsigned long long *anorm_bits, int *d_err)
 {
     static const bool use_df = [] {
         const char *e = getenv("STARPU_GB300_RESIDUAL");
@@ -276,7 +276,7 @@ static int residual_mixed(cudaStream_t s, int n, int nrhs, const double *A, long
     const long cap = (long)(residual_partials(n, nrhs) / ((size_t)n * nrhs));
     const int kc = residual_tc_kchunk(n, nrhs, (int)cap);
     gb300_count_launch(), df_split_x_kernel<<<nrhs, 256, 0, s>>>(n, X, ldx, xs, sx);
-    int rc = residual_tc(s, n, nrhs, A, lda, X, ldx, sx, anorm_bits, kc, rtc_xs, partials, d_err);
+    int rc = residual_tc(s, n, nrhs, rtc_a, X, ldx, sx, anorm_bits, kc, rtc_xs, partials, d_err);
     if (rc) return rc;
     const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
     gb300_count_launch(), residual_reduce_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, (n + kc - 1) / kc, B, ldb,
@@ -338,6 +338,7 @@ struct SolverWs {
     float2 *xs;            // double-float split of X (n x 16 per group of 16 columns)
     int *sx;               // per-column scale exponents of X
     void *rtc_xs;          // x digit slices of the tensor-core residual
+    void *rtc_a;           // the 8 digit slices of A (cut once per matrix, kept with the factor)
     double *berr;          // nrhs
     int *done;             // nrhs
     int *rexp;             // nrhs: power-of-two scales of the FP32 right-hand sides
@@ -410,6 +411,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t oB = tiles ? take(ntiles * ldk * ldk * sizeof(float)) : 0;
     const size_t oZ = tiles ? take((size_t)n * 16 * sizeof(float)) : 0;
     const size_t oC = tiles ? take((2 * ntiles + 1) * sizeof(int)) : 0;
+    const size_t oA = take(residual_tc_a_bytes(n));
     const size_t oS = take(4 * sizeof(unsigned long long));
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
@@ -431,6 +433,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->band = tiles ? (float *)(b + oB) : nullptr;
         ws->Z = tiles ? (float *)(b + oZ) : nullptr;
         ws->cnt = tiles ? (int *)(b + oC) : nullptr;
+        ws->rtc_a = b + oA;
         ws->partials = (double *)(b + oQ);
         ws->xs = (float2 *)(b + oX);
         ws->sx = (int *)(b + oI);
@@ -460,7 +463,8 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
     gb300_count_launch(), convert_lower_symnorm_kernel<<<(n + SYM_BW - 1) / SYM_BW, 256, 0, s>>>(n, A, lda, ws.W, n,
                                                                                                  ws.anorm_bits);
-    int rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
+    int rc = residual_tc_slice_a(s, n, A, lda, ws.anorm_bits, ws.rtc_a);  // the residuals' slices of A
+    if (!rc) rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
     if (rc) return rc;
     if (!ws.band) potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
     return gb300_last_launch_status();
@@ -519,8 +523,8 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
     double worst = INFINITY;
     for (;; ++it) {
         slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
-        if ((rc = residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx, ws.rtc_xs,
-                                 ws.anorm_bits, ws.err)))
+        if ((rc = residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx, ws.rtc_a,
+                                 ws.rtc_xs, ws.anorm_bits, ws.err)))
             break;
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
         gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb, ws.anorm_bits, tol, ws.berr, ws.done,
@@ -771,7 +775,7 @@ int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const f
 // ---- symmetric residual R = B - A X with the tensor-core slice products ----
 
 static size_t syres_layout(int n, int nrhs, char *base, double **partials, float2 **xs, int **sx, void **rxs,
-                           unsigned long long **an)
+                           unsigned long long **an, void **rta)
 {
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -784,12 +788,14 @@ static size_t syres_layout(int n, int nrhs, char *base, double **partials, float
     const size_t oS = take((size_t)nrhs * sizeof(int));
     const size_t oR = take(residual_tc_xs_bytes(n, nrhs));
     const size_t oA = take(4 * sizeof(unsigned long long));
+    const size_t oT = take(residual_tc_a_bytes(n));
     if (base) {
         *partials = (double *)(base + oP);
         *xs = (float2 *)(base + oX);
         *sx = (int *)(base + oS);
         *rxs = base + oR;
         *an = (unsigned long long *)(base + oA);
+        *rta = base + oT;
     }
     return off;
 }
@@ -797,7 +803,7 @@ static size_t syres_layout(int n, int nrhs, char *base, double **partials, float
 size_t starpu_gb300_dsyresidual_workspace(int n, int nrhs)
 {
     if (n <= 0 || nrhs <= 0) return 0;
-    return syres_layout(n, nrhs, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    return syres_layout(n, nrhs, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
 int starpu_gb300_dsyresidual(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
@@ -811,13 +817,15 @@ int starpu_gb300_dsyresidual(void *stream, int n, int nrhs, const double *A, int
     double *partials;
     float2 *xs;
     int *sx;
-    void *rxs;
+    void *rxs, *rta;
     unsigned long long *an;
-    syres_layout(n, nrhs, (char *)work, &partials, &xs, &sx, &rxs, &an);
+    syres_layout(n, nrhs, (char *)work, &partials, &xs, &sx, &rxs, &an, &rta);
     cudaMemsetAsync(an, 0, sizeof *an, s);
     gb300_count_launch(), convert_lower_symnorm_kernel<<<(n + SYM_BW - 1) / SYM_BW, 256, 0, s>>>(n, A, lda, nullptr, 0,
                                                                                                  an);
-    return residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, R, ldr, partials, xs, sx, rxs, an, d_err);
+    int rc = residual_tc_slice_a(s, n, A, lda, an, rta);
+    if (rc) return rc;
+    return residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, R, ldr, partials, xs, sx, rta, rxs, an, d_err);
 }
 
 size_t starpu_gb300_backward_error_workspace(int n, int nrhs)

@@ -274,6 +274,21 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
 
 static long rtc_ldk(int n) { return ((long)n + 63) / 64 * 64; }
 
+size_t residual_tc_a_bytes(int n) { return n > 0 ? (size_t)8 * n * rtc_ldk(n) * 2 : 0; }
+
+// The 8 digit slices of the symmetric A (lower triangle read), once per matrix.
+int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const unsigned long long *anorm_bits,
+                        void *slices)
+{
+    if (n <= 0) return GB300_OK;
+    const long ldk = rtc_ldk(n);
+    cudaMemsetAsync(slices, 0, residual_tc_a_bytes(n), s);
+    const unsigned nt = (unsigned)((n + 63) / 64);
+    gb300_count_launch(), rtc_a_slices_kernel<<<dim3(nt, nt), 256, 0, s>>>(n, A, lda, anorm_bits, (uint16_t *)slices,
+                                                                           ldk);
+    return gb300_last_launch_status();
+}
+
 size_t residual_tc_xs_bytes(int n, int nrhs)
 {
     const long groups = (nrhs + 15) / 16;
@@ -292,10 +307,11 @@ int residual_tc_kchunk(int n, int nrhs, int max_chunks)
     return (int)std::max<long>(kc, RTC_KBLK);
 }
 
-// P_z = -(A X) over the K chunks z of length kchunk (A symmetric, lower
-// triangle read).  sx: ilogb(max |x_j|) per column (device), anorm_bits:
-// ||A||_inf (device).  xs: residual_tc_xs_bytes(n, nrhs) bytes of scratch.
-int residual_tc(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx, const int *sx,
+// P_z = -(A X) over the K chunks z of length kchunk, with the slices of the
+// symmetric A from residual_tc_slice_a.  sx: ilogb(max |x_j|) per column
+// (device), anorm_bits: ||A||_inf (device, the slices' scale).  xs:
+// residual_tc_xs_bytes(n, nrhs) bytes of scratch.
+int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const double *X, long ldx, const int *sx,
                 const unsigned long long *anorm_bits, int kchunk, void *xs, double *partials, int *d_err)
 {
     if (n <= 0 || nrhs <= 0) return GB300_OK;
@@ -309,14 +325,13 @@ int residual_tc(cudaStream_t s, int n, int nrhs, const double *A, long lda, cons
         gb300_count_launch(), rtc_x_slices_kernel<<<dim3((unsigned)((ldk + 255) / 256), 16), 256, 0, s>>>(
             n, nc, X + (long)g * 16 * ldx, ldx, sx + 16 * g, Xs + (long)g * RTC_XROWS * ldk, ldk);
     }
-    CUtensorMap tm;
+    CUtensorMap tm, tma;
     int rc = make_kmajor_map(&tm, xs, groups * RTC_XROWS, (int)ldk, ldk, RTC_XROWS);
+    if (!rc) rc = make_kmajor_map(&tma, a_slices, 8 * n, (int)ldk, ldk, RTC_BM);
     if (rc) return rc;
     ResidualTcArgs a;
     a.n = n;
     a.nrhs = nrhs;
-    a.A = A;
-    a.lda = lda;
     a.anorm_bits = anorm_bits;
     a.sx = sx;
     a.kchunk = kchunk;
@@ -333,7 +348,7 @@ int residual_tc(cudaStream_t s, int n, int nrhs, const double *A, long lda, cons
         attr_set = true;
     }
     const int grid = std::min(a.nitems, num_sms());
-    gb300_count_launch(), residual_tc_kernel<<<grid, RTC_THREADS, RTC_SMEM, s>>>(tm, a);
+    gb300_count_launch(), residual_tc_kernel<<<grid, RTC_THREADS, RTC_SMEM, s>>>(tma, tm, a);
     return gb300_last_launch_status();
 }
 

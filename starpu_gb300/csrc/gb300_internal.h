@@ -11,9 +11,12 @@ namespace gb300 {
 constexpr int GB300_DIAG_TILE_MAX = 1024;
 
 // residual partials P_z = -(A X) on the tensor cores (capi_tc.cu)
+size_t residual_tc_a_bytes(int n);
+int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const unsigned long long *anorm_bits,
+                        void *slices);
 size_t residual_tc_xs_bytes(int n, int nrhs);
 int residual_tc_kchunk(int n, int nrhs, int max_chunks);
-int residual_tc(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx, const int *sx,
+int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const double *X, long ldx, const int *sx,
                 const unsigned long long *anorm_bits, int kchunk, void *xs, double *partials, int *d_err);
 
 

@@ -22,15 +22,16 @@
 // by 2^{alpha+beta-63}).  Error: below 2^-55 of ||A||_inf ||x||_inf per
 // element product from the digits, plus one FP64 rounding of each partial.
 //
+// The slices of A are cut once per matrix (rtc_a_slices_kernel: 8 K-major
+// BF16 matrices of the whole symmetric A, from its lower triangle) and reused
+// by every residual of the refinement; the slices of x are cut per residual.
+//
 // CTA (one per SM, persistent over work items = (128-row block, K chunk,
 // group of 16 right-hand sides)):
-//   warps 0-7  producers: load the FP64 A tile (128 rows x 64 k, from the
-//              lower triangle, mirrored above the diagonal), cut it into the
-//              digits and write slices 1-4, then 5-8 (two half stages) in the
-//              128-byte-swizzled K-major layout; warp 0 also fetches the x
-//              slice window of the stage by TMA
-//   warp 8     MMA issuer + TMEM owner (256 columns: two accumulators)
-//   warps 9-12 epilogue: tcgen05.ld of the accumulator, exact integer sums
+//   warp 0     TMA producer: per 64-k stage the x slice window and the A
+//              slices in two half stages (slices 1-4, then 5-8)
+//   warp 1     MMA issuer + TMEM owner (256 columns: two accumulators)
+//   warps 2-5  epilogue: tcgen05.ld of the accumulator, exact integer sums
 // Every mbarrier wait is bounded; on timeout the CTA records an error and
 // drains its own copies and MMAs before exiting.
 #pragma once
@@ -52,18 +53,14 @@ constexpr int RTC_KBLK = 128;                     // k per exact accumulation bl
 constexpr int RTC_SLICE_BYTES = RTC_BM * RTC_BK * 2;         // 16 KB
 constexpr int RTC_AH_BYTES = RTC_HALF * RTC_SLICE_BYTES;     // 64 KB
 constexpr int RTC_X_BYTES = RTC_XROWS * RTC_BK * 2;          // 30 KB
-constexpr int RTC_PWARPS = 8;
-constexpr int RTC_MMA_WARP = 8;
-constexpr int RTC_EPI_WARP0 = 9;
-constexpr int RTC_THREADS = 13 * 32;
+constexpr int RTC_MMA_WARP = 1;
+constexpr int RTC_THREADS = 6 * 32;               // TMA producer, MMA issuer, 4 epilogue warps
 constexpr int RTC_SMEM = 2 * RTC_AH_BYTES + 2 * RTC_X_BYTES + 1024 + 256;
 constexpr uint32_t RTC_TMEM_COLS = 256;
 constexpr int RTC_ERR_TIMEOUT = 5;
 
 struct ResidualTcArgs {
     int n, nrhs;
-    const double *A;
-    long lda;
     const unsigned long long *anorm_bits;  // ||A||_inf as FP64 bits: alpha = ilogb + 1
     const int *sx;       // per right-hand side: ilogb(max |x_j|); beta_j = sx[j] + 1
     int kchunk;          // multiple of RTC_KBLK
@@ -132,6 +129,59 @@ __global__ void rtc_x_slices_kernel(int n, int ncols, const double *__restrict__
     }
 }
 
+// The 8 digit slices of the whole symmetric A (read from its lower triangle)
+// as K-major BF16 matrices: slice t (1..8), element (i, k) at
+// S[((t - 1) n + i) ldk + k].  One CTA per 64 x 64 tile (grid n/64 x n/64):
+// the lower-triangle block the tile reads from is staged in shared memory
+// (coalesced along its columns), the tile is written along k (coalesced),
+// 8 consecutive k per thread and slice (16-byte stores).  Columns k >= n of
+// the slices stay as the caller zeroed them.
+__global__ void __launch_bounds__(256) rtc_a_slices_kernel(int n, const double *__restrict__ A, long lda,
+                                                           const unsigned long long *__restrict__ anorm_bits,
+                                                           uint16_t *__restrict__ S, long ldk)
+{
+    __shared__ double T[64][65];
+    const int bi = blockIdx.y, bk = blockIdx.x;
+    const int i0 = bi * 64, k0 = bk * 64;
+    const bool mirror = bk > bi;
+    // source block: rows s0.., columns c0.. of the lower triangle
+    const int s0 = mirror ? k0 : i0, c0 = mirror ? i0 : k0;
+    for (int e = threadIdx.x; e < 64 * 64; e += 256) {
+        const int a = e & 63, b = e >> 6;
+        const int sr = s0 + a, sc = c0 + b;
+        T[b][a] = (sr < n && sc < n && sc <= sr) ? A[(long)sr + (long)sc * lda] : 0.0;
+    }
+    __syncthreads();
+    const int alpha = rtc_bound_exp(__longlong_as_double((long long)*anorm_bits));
+    for (int u = threadIdx.x; u < 64 * 8; u += 256) {
+        const int r = u >> 3, ch = u & 7, i = i0 + r;
+        if (i >= n) continue;
+        uint32_t fhi[8], flo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int c = 8 * ch + e;
+            // target (i, k0 + c): the lower block element (r, c), or its mirror
+            double v;
+            if (mirror) v = T[r][c];                 // A[k0 + c, i0 + r]
+            else if (bk == bi && c > r) v = T[r][c]; // diagonal tile above the diagonal: (c, r) of the block
+            else v = T[c][r];                        // A[i0 + r, k0 + c]
+            const unsigned long long w = (unsigned long long)__double_as_longlong(v);
+            rtc_fixed((uint32_t)(w >> 32), (uint32_t)w, alpha, fhi[e], flo[e]);
+        }
+        const int kk = k0 + 8 * ch;
+        if (kk >= n) continue;
+#pragma unroll
+        for (int t = 1; t <= 8; ++t) {
+            uint4 q;
+            q.x = rtc_digit_pair(fhi[0], flo[0], fhi[1], flo[1], t);
+            q.y = rtc_digit_pair(fhi[2], flo[2], fhi[3], flo[3], t);
+            q.z = rtc_digit_pair(fhi[4], flo[4], fhi[5], flo[5], t);
+            q.w = rtc_digit_pair(fhi[6], flo[6], fhi[7], flo[7], t);
+            *reinterpret_cast<uint4 *>(S + ((long)(t - 1) * n + i) * ldk + kk) = q;
+        }
+    }
+}
+
 // byte offset of the 16-byte chunk (row r, k chunk c of 8 BF16) in a
 // 128-byte-swizzled K-major tile (8-row atoms of 1024 bytes)
 __device__ __forceinline__ uint32_t rtc_sw128(int r, int c)
@@ -148,7 +198,8 @@ __device__ __forceinline__ void rtc_item(const ResidualTcArgs &a, int it, int &b
 }
 
 __global__ void __launch_bounds__(RTC_THREADS, 1)
-residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArgs args)
+residual_tc_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_x,
+                   const ResidualTcArgs args)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -165,7 +216,7 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     if (threadIdx.x == 0) {
         for (int s = 0; s < 2; ++s) {
-            ptx::mbar_init(&a_full[s], RTC_PWARPS * 32);
+            ptx::mbar_init(&a_full[s], 1);
             ptx::mbar_init(&a_empty[s], 1);
             ptx::mbar_init(&x_full[s], 1);
             ptx::mbar_init(&x_empty[s], 1);
@@ -176,7 +227,10 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
         *abort_flag = 0;
         ptx::fence_mbarrier_init();
     }
-    if (warp == 0 && lane == 0) ptx::tma_prefetch_desc(&tm_x);
+    if (warp == 0 && lane == 0) {
+        ptx::tma_prefetch_desc(&tm_a);
+        ptx::tma_prefetch_desc(&tm_x);
+    }
     if (warp == RTC_MMA_WARP) {
         ptx::tmem_alloc(tmem_slot, RTC_TMEM_COLS);
         ptx::tmem_relinquish();
@@ -188,109 +242,68 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
     const int n = args.n;
     const int alpha = rtc_bound_exp(__longlong_as_double((long long)*args.anorm_bits));
 
-    if (warp < RTC_PWARPS) {
-        // ------------------------------------------------------------ producers
-        const int tid = threadIdx.x;  // 0..255
-        int as = 0, xs = 0;
-        uint32_t aph = 0, xph = 0;
-        int x_issued = 0;
-        bool ok = true;
-        for (int it = blockIdx.x; it < args.nitems && ok; it += gridDim.x) {
-            int blk, z, g;
-            rtc_item(args, it, blk, z, g);
-            const int i0 = blk * RTC_BM;
-            const int kz0 = z * args.kchunk, kz1 = min(n, kz0 + args.kchunk);
-            for (int k0 = kz0; k0 < kz1 && ok; k0 += RTC_BK) {
-                // x slice window of this stage (TMA, one thread)
-                if (tid == 0) {
-                    if (!ptx::wait_parity(&x_empty[xs], xph ^ 1, abort_flag, args.wait_budget_ns)) ok = false;
-                    else {
-                        ptx::mbar_arrive_expect_tx(&x_full[xs], RTC_X_BYTES);
-                        ptx::tma_load_2d(sX + xs * RTC_X_BYTES, &tm_x, &x_full[xs], k0, g * RTC_XROWS);
-                        ++x_issued;
-                    }
-                }
-                if (++xs == 2) {
-                    xs = 0;
-                    xph ^= 1;
-                }
-                // this thread's 4 chunks (row r, 8 consecutive k at chunk c), converted
-                // once to the fixed-point form.  Below the diagonal lanes run
-                // along rows (coalesced columns), above it (the mirror of a lower
-                // block) 8 lanes share a row (coalesced rows); crossing tiles pick
-                // per element.
-                const int mode = (k0 + RTC_BK <= i0) ? 0 : (k0 >= i0 + RTC_BM ? 1 : 2);
-                int rq[4], cq[4];
-                uint32_t fhi[4][8], flo[4][8];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (mode == 1) {
-                        rq[q] = (tid >> 3) + 32 * q;
-                        cq[q] = tid & 7;
-                    } else {
-                        rq[q] = tid & 127;
-                        cq[q] = (tid >> 7) + 2 * q;
-                    }
-                    const int row = i0 + rq[q], col0 = k0 + 8 * cq[q];
-                    const bool rok = row < n;
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        const int col = col0 + e;
-                        unsigned long long u = 0;
-                        if (rok && col < kz1) {
-                            const bool mirror = mode == 1 || (mode == 2 && col > row);
-                            const double *src = mirror ? &args.A[(long)col + (long)row * args.lda]
-                                                       : &args.A[(long)row + (long)col * args.lda];
-                            u = (unsigned long long)__double_as_longlong(__ldg(src));
-                        }
-                        rtc_fixed((uint32_t)(u >> 32), (uint32_t)u, alpha, fhi[q][e], flo[q][e]);
-                    }
-                }
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (!ptx::wait_parity(&a_empty[as], aph ^ 1, abort_flag, args.wait_budget_ns)) {
+    if (warp == 0) {
+        // --------------------------------------------------------- TMA producer
+        if (ptx::elect_one()) {
+            int as = 0, xs = 0;
+            uint32_t aph = 0, xph = 0;
+            int a_issued = 0, x_issued = 0;
+            bool ok = true;
+            for (int it = blockIdx.x; it < args.nitems && ok; it += gridDim.x) {
+                int blk, z, g;
+                rtc_item(args, it, blk, z, g);
+                const int i0 = blk * RTC_BM;
+                const int kz0 = z * args.kchunk, kz1 = min(n, kz0 + args.kchunk);
+                for (int k0 = kz0; k0 < kz1 && ok; k0 += RTC_BK) {
+                    if (!ptx::wait_parity(&x_empty[xs], xph ^ 1, abort_flag, args.wait_budget_ns)) {
                         ok = false;
                         break;
                     }
-                    uint8_t *buf = sA + as * RTC_AH_BYTES;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint32_t off = rtc_sw128(rq[q], cq[q]);
-#pragma unroll
+                    ptx::mbar_arrive_expect_tx(&x_full[xs], RTC_X_BYTES);
+                    ptx::tma_load_2d(sX + xs * RTC_X_BYTES, &tm_x, &x_full[xs], k0, g * RTC_XROWS);
+                    ++x_issued;
+                    if (++xs == 2) {
+                        xs = 0;
+                        xph ^= 1;
+                    }
+                    for (int h = 0; h < 2; ++h) {
+                        if (!ptx::wait_parity(&a_empty[as], aph ^ 1, abort_flag, args.wait_budget_ns)) {
+                            ok = false;
+                            break;
+                        }
+                        ptx::mbar_arrive_expect_tx(&a_full[as], RTC_AH_BYTES);
+                        uint8_t *buf = sA + as * RTC_AH_BYTES;
                         for (int tl = 0; tl < RTC_HALF; ++tl) {
                             const int t = 4 * h + tl + 1;
-                            uint32_t w[4];
-#pragma unroll
-                            for (int p = 0; p < 4; ++p)
-                                w[p] = rtc_digit_pair(fhi[q][2 * p], flo[q][2 * p], fhi[q][2 * p + 1], flo[q][2 * p + 1], t);
-                            *reinterpret_cast<uint4 *>(buf + tl * RTC_SLICE_BYTES + off) = make_uint4(w[0], w[1], w[2], w[3]);
+                            ptx::tma_load_2d(buf + tl * RTC_SLICE_BYTES, &tm_a, &a_full[as], k0, (t - 1) * n + i0);
                         }
-                    }
-                    ptx::fence_proxy_async_smem();  // generic-proxy stores -> visible to the tensor cores
-                    ptx::mbar_arrive(&a_full[as]);
-                    if (++as == 2) {
-                        as = 0;
-                        aph ^= 1;
+                        ++a_issued;
+                        if (++as == 2) {
+                            as = 0;
+                            aph ^= 1;
+                        }
                     }
                 }
             }
-        }
-        if (!ok) {
-            if (!*abort_flag) atomicCAS(args.err, 0, RTC_ERR_TIMEOUT);
-            *abort_flag = 1;
-        }
-        // drain the x copies this CTA issued (bounded; ignores the abort flag)
-        if (tid == 0) {
-            int s = xs;
-            uint32_t ph = xph;
-            const int back = x_issued < 2 ? x_issued : 2;
-            for (int i = 0; i < back; ++i) {
-                if (--s < 0) {
-                    s = 1;
-                    ph ^= 1;
+            if (!ok) {
+                if (!*abort_flag) atomicCAS(args.err, 0, RTC_ERR_TIMEOUT);
+                *abort_flag = 1;
+            }
+            // drain: every TMA write into shared memory has landed before the CTA exits
+            volatile int never = 0;
+            for (int ring = 0; ring < 2; ++ring) {
+                uint64_t *full = ring ? x_full : a_full;
+                int s = ring ? xs : as;
+                uint32_t ph = ring ? xph : aph;
+                const int issued = ring ? x_issued : a_issued;
+                const int back = issued < 2 ? issued : 2;
+                for (int i = 0; i < back; ++i) {
+                    if (--s < 0) {
+                        s = 1;
+                        ph ^= 1;
+                    }
+                    ptx::wait_parity(&full[s], ph, &never, args.wait_budget_ns);
                 }
-                volatile int never = 0;
-                ptx::wait_parity(&x_full[s], ph, &never, args.wait_budget_ns);
             }
         }
     } else if (warp == RTC_MMA_WARP) {
@@ -372,8 +385,8 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_x, const ResidualTcArg
         }
     } else {
         // ------------------------------------------------------------- epilogue
-        // a warp may access only the TMEM lane quarter warp % 4: warps 9-12
-        // take quarters 1, 2, 3, 0
+        // a warp may access only the TMEM lane quarter warp % 4: warps 2-5
+        // take quarters 2, 3, 0, 1
         const int quarter = warp & 3;
         const int rloc = quarter * 32 + lane;
         int db = 0;
