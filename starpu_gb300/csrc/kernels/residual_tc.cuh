@@ -9,17 +9,20 @@
 //
 // a_t, b_u: unsigned 7-bit digits of the magnitude (56 bits, truncated)
 // carrying the element's sign -- integers in [-127, 127], exact in
-// BF16.  A x = 2^{alpha+beta} sum_{d=2..9} 2^{-7d} S_d with
-// S_d = sum_{t+u=d} a_t b_u (the pairs with t + u > 9 are below the digits'
-// own rounding): every S_d over a K block of 128 is an integer below 2^24
-// (at most 8 pairs x 127^2 x 128), so the FP32 accumulation of the tensor
-// cores is exact.  Per K block the 8 scales land in one 128 x 128 TMEM
-// accumulator: the x slices are stored as 15 blocks of 16 rows (7 zero blocks,
-// then b_1 .. b_8), and A slice t multiplies the 128-row window starting at
-// block 8 - t, so accumulator column block d - 2 receives a_t b_{d-t}.  The
-// epilogue adds the exact block sums as integers, sum_d S_d 2^(7 (9 - d)), in
-// 128 bits over the whole K chunk, and rounds once to FP64 at the end (scaled
-// by 2^{alpha+beta-63}).  Error: below 2^-55 of ||A||_inf ||x||_inf per
+// BF16.  A x = 2^{alpha+beta} sum_{d=2..10} 2^{-7d} S_d with
+// S_d = sum_{t+u=d} a_t b_u.  The pairs dropped (t + u > 10) weigh below
+// 2^-60 of 2^{alpha+beta} per product; stopping at t + u = 9 would leave
+// 2^-53 per product, whose random sum over 32768 terms is ~1e-13 of
+// ||A|| ||x|| -- visible in a backward error of 1e-13.  Every S_d over a K
+// block of 128 is an integer below 2^24 (at most 8 pairs x 127^2 x 128), so
+// the FP32 accumulation of the tensor cores is exact.  Per K block the 9
+// scales land in one 128 x 144 TMEM accumulator: the x slices are stored as
+// 16 blocks of 16 rows (7 zero blocks, b_1 .. b_8, one zero block), and A
+// slice t multiplies the 144-row window starting at block 8 - t, so
+// accumulator column block d - 2 receives a_t b_{d-t}.  The epilogue adds the
+// exact block sums as integers, sum_d S_d 2^(7 (10 - d)), in 128 bits over
+// the whole K chunk, and rounds once to FP64 at the end (scaled by
+// 2^{alpha+beta-70}).  Error: below 2^-55 of ||A||_inf ||x||_inf per
 // element product from the digits, plus one FP64 rounding of each partial.
 //
 // The slices of A are cut once per matrix (rtc_a_slices_kernel: 8 K-major
@@ -30,7 +33,7 @@
 // group of 16 right-hand sides)):
 //   warp 0     TMA producer: per 64-k stage the x slice window and the A
 //              slices in two half stages (slices 1-4, then 5-8)
-//   warp 1     MMA issuer + TMEM owner (256 columns: two accumulators)
+//   warp 1     MMA issuer + TMEM owner (512 columns: two 144-column accumulators)
 //   warps 2-5  epilogue: tcgen05.ld of the accumulator, exact integer sums
 // Every mbarrier wait is bounded; on timeout the CTA records an error and
 // drains its own copies and MMAs before exiting.
@@ -47,16 +50,18 @@ namespace gb300 {
 constexpr int RTC_BM = 128;                       // rows per tile (MMA M)
 constexpr int RTC_BK = 64;                        // k per stage: one 128-byte swizzle row of BF16
 constexpr int RTC_HALF = 4;                       // slices per half stage
-constexpr int RTC_N = 128;                        // MMA N: 8 scales x 16 right-hand sides
-constexpr int RTC_XROWS = 240;                    // x slice rows: (7 zero + 8 slice) blocks x 16
+constexpr int RTC_ND = 9;                         // scales d = 2 .. 10
+constexpr int RTC_N = RTC_ND * 16;                // MMA N: 9 scales x 16 right-hand sides
+constexpr int RTC_XROWS = 256;                    // x slice rows: (7 zero + 8 slice + 1 zero) blocks x 16
+constexpr uint32_t RTC_ACC_STRIDE = 256;          // TMEM columns between the two accumulators
 constexpr int RTC_KBLK = 128;                     // k per exact accumulation block (2 stages)
 constexpr int RTC_SLICE_BYTES = RTC_BM * RTC_BK * 2;         // 16 KB
 constexpr int RTC_AH_BYTES = RTC_HALF * RTC_SLICE_BYTES;     // 64 KB
-constexpr int RTC_X_BYTES = RTC_XROWS * RTC_BK * 2;          // 30 KB
+constexpr int RTC_X_BYTES = RTC_XROWS * RTC_BK * 2;          // 32 KB
 constexpr int RTC_MMA_WARP = 1;
 constexpr int RTC_THREADS = 6 * 32;               // TMA producer, MMA issuer, 4 epilogue warps
 constexpr int RTC_SMEM = 2 * RTC_AH_BYTES + 2 * RTC_X_BYTES + 1024 + 256;
-constexpr uint32_t RTC_TMEM_COLS = 256;
+constexpr uint32_t RTC_TMEM_COLS = 512;
 constexpr int RTC_ERR_TIMEOUT = 5;
 
 struct ResidualTcArgs {
@@ -331,7 +336,7 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_consta
                         break;
                     }
                     ptx::tc_fence_after();
-                    const uint32_t d_tmem = tmem_base + (uint32_t)(db * RTC_N);
+                    const uint32_t d_tmem = tmem_base + (uint32_t)db * RTC_ACC_STRIDE;
                     const uint32_t x_addr = ptx::smem_u32(sX + xs * RTC_X_BYTES);
                     for (int h = 0; h < 2 && ok; ++h) {
                         if (!ptx::wait_parity(&a_full[as], aph, abort_flag, args.wait_budget_ns)) {
@@ -397,8 +402,8 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_consta
             rtc_item(args, it, blk, z, g);
             const int kz0 = z * args.kchunk, kz1 = min(n, kz0 + args.kchunk);
             const int nblk = (kz1 - kz0 + RTC_KBLK - 1) / RTC_KBLK;
-            // exact accumulation: V = sum_blocks sum_d S_d 2^(7 (9 - d)) (|V| < 2^82),
-            // the value is V 2^-63
+            // exact accumulation: V = sum_blocks sum_d S_d 2^(7 (10 - d)) (|V| < 2^90),
+            // the value is V 2^-70
             __int128 acc[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) acc[j] = 0;
@@ -408,23 +413,25 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_consta
                     break;
                 }
                 ptx::tc_fence_after();
-                const uint32_t tb = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(db * RTC_N);
-                // column block d - 2 holds S_d for the 16 right-hand sides (exact integers < 2^24)
+                const uint32_t tb = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)db * RTC_ACC_STRIDE;
+                // column block d - 2 holds S_d for the 16 right-hand sides (exact integers < 2^24);
+                // 5 loads of 32 columns, the last half of the fifth unused
 #pragma unroll 1
-                for (int ch = 0; ch < 4; ++ch) {
+                for (int ch = 0; ch < 5; ++ch) {
                     uint32_t v[32];
                     ptx::tmem_ld_32x32b_x32(tb + ch * 32, v);
                     ptx::tmem_ld_wait();
-                    if (ch == 3) {
+                    if (ch == 4) {
                         ptx::tc_fence_before();
                         ptx::mbar_arrive(&d_empty[db]);
                     }
 #pragma unroll
                     for (int half = 0; half < 2; ++half) {
                         const int d = 2 + 2 * ch + half;
+                        if (d > 10) continue;
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
-                            acc[j] += (__int128)__float2int_rn(__uint_as_float(v[16 * half + j])) << (7 * (9 - d));
+                            acc[j] += (__int128)__float2int_rn(__uint_as_float(v[16 * half + j])) << (7 * (10 - d));
                     }
                 }
                 if (++db == 2) {
@@ -443,7 +450,7 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_consta
                         // V = hi 2^64 + lo; one rounding in the sum
                         const double hi = (double)(long long)(acc[j] >> 64);
                         const double lo = (double)(unsigned long long)acc[j];
-                        Pz[(long)i + (long)jj * n] = -scalbn(fma(hi, 18446744073709551616.0, lo), alpha + args.sx[jj] + 1 - 63);
+                        Pz[(long)i + (long)jj * n] = -scalbn(fma(hi, 18446744073709551616.0, lo), alpha + args.sx[jj] + 1 - 70);
                     }
                 }
             }
