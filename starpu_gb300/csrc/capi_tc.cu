@@ -282,7 +282,10 @@ int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const 
 {
     if (n <= 0) return GB300_OK;
     const long ldk = rtc_ldk(n);
-    cudaMemsetAsync(slices, 0, residual_tc_a_bytes(n), s);
+    // the kernel writes every column below round8(n); only the padding beyond it needs zeros
+    const long kw = ((long)n + 7) / 8 * 8;
+    if (ldk > kw)
+        cudaMemset2DAsync((uint16_t *)slices + kw, ldk * 2, 0, (ldk - kw) * 2, (size_t)8 * n, s);
     const unsigned nt = (unsigned)((n + 63) / 64);
     gb300_count_launch(), rtc_a_slices_kernel<<<dim3(nt, nt), 256, 0, s>>>(n, A, lda, anorm_bits, (uint16_t *)slices,
                                                                            ldk);
