@@ -53,82 +53,60 @@ __global__ void convert_lower_norm_kernel(int n, const double *__restrict__ A, l
     }
 }
 
-// The same from the lower triangle only (A symmetric, the upper part never
-// read): one CTA per block of SYM_BW rows/columns I = [i0, i0 + bw).
-//   row sum_i = sum_{k < i} |A_ik|   (row i left of the diagonal: columns
-//               k < i, read as column segments of the block's rows)
-//             + sum_{k >= i} |A_ki|  (column i from the diagonal down)
-// Columns j in I are written to W (rows i >= j, when W is given) while they are reduced.
-// Every CTA reads SYM_BW * n elements; max over rows is order-independent.
-constexpr int SYM_BW = 128;
-__global__ void __launch_bounds__(256) convert_lower_symnorm_kernel(int n, const double *__restrict__ A, long lda,
-                                                                    float *__restrict__ W, long ldw,
-                                                                    unsigned long long *anorm_bits)
+// W = fp32(A) on and below the diagonal (W optional), one CTA per column j
+// (rows j .. n-1), and max |A_ij| over the lower triangle into *amax_bits as
+// FP64 bits (an integer max of the magnitudes' bit patterns: exact and
+// order-independent).  The scale of the residual's digit slices and of the
+// infinity norm below.
+__global__ void __launch_bounds__(256) convert_lower_max_kernel(int n, const double *__restrict__ A, long lda,
+                                                                float *__restrict__ W, long ldw,
+                                                                unsigned long long *amax_bits)
 {
-    const int i0 = blockIdx.x * SYM_BW;
-    const int bw = min(SYM_BW, n - i0);
-    const int tid = threadIdx.x;
-    __shared__ double left[2][SYM_BW];
-    __shared__ double down[SYM_BW];
-    __shared__ double red[8];
-    // row parts: thread (t = tid % 128, h = tid / 128) sums columns k = h, h+2, ... < i0 + t of row i0 + t
-    // (four independent partial sums: GB300 issues few FP64 adds per clock, a
-    // single dependent chain would leave the pipe waiting on its latency)
-    {
-        const int t = tid & (SYM_BW - 1), h = tid >> 7;
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-        if (t < bw) {
-            const double *a = A + i0 + t;
-            const int kend = i0 + t;
-            int k = h;
-            for (; k + 6 < kend; k += 8) {
-                s0 += fabs(a[(long)k * lda]);
-                s1 += fabs(a[(long)(k + 2) * lda]);
-                s2 += fabs(a[(long)(k + 4) * lda]);
-                s3 += fabs(a[(long)(k + 6) * lda]);
-            }
-            for (; k < kend; k += 2) s0 += fabs(a[(long)k * lda]);
+    const long j = blockIdx.x;
+    const double *a = A + j * lda;
+    float *w = W ? W + j * ldw : nullptr;
+    unsigned long long m = 0;
+    long i = j + threadIdx.x;
+    for (; i + 256 < n; i += 512) {
+        const double v0 = a[i], v1 = a[i + 256];
+        m = max(m, (unsigned long long)__double_as_longlong(v0) & 0x7FFFFFFFFFFFFFFFull);
+        m = max(m, (unsigned long long)__double_as_longlong(v1) & 0x7FFFFFFFFFFFFFFFull);
+        if (w) {
+            w[i] = (float)v0;
+            w[i + 256] = (float)v1;
         }
-        left[h][t] = (s0 + s1) + (s2 + s3);
     }
-    // column parts: column j = i0 + c, rows j .. n-1, by the whole CTA
-    for (int c = 0; c < bw; ++c) {
-        const int j = i0 + c;
-        const double *a = A + (long)j * lda;
-        float *w = W ? W + (long)j * ldw : nullptr;
-        double s0 = 0.0, s1 = 0.0;
-        int i = j + tid;
-        for (; i + (int)blockDim.x < n; i += 2 * blockDim.x) {
-            const double v0 = a[i], v1 = a[i + blockDim.x];
-            s0 += fabs(v0);
-            s1 += fabs(v1);
-            if (w) {
-                w[i] = (float)v0;
-                w[i + blockDim.x] = (float)v1;
-            }
-        }
-        if (i < n) {
-            const double v = a[i];
-            s0 += fabs(v);
-            if (w) w[i] = (float)v;
-        }
-        double s = s0 + s1;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if ((tid & 31) == 0) red[tid >> 5] = s;
-        __syncthreads();
-        if (tid == 0) {
-            double t = 0.0;
-            for (int q = 0; q < 8; ++q) t += red[q];
-            down[c] = t;
-        }
-        __syncthreads();
+    if (i < n) {
+        const double v = a[i];
+        m = max(m, (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull);
+        if (w) w[i] = (float)v;
     }
-    if (tid < 32) {
-        double m = 0.0;
-        for (int t = tid; t < bw; t += 32) m = fmax(m, left[0][t] + left[1][t] + down[t]);
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
-        if (tid == 0) atomicMax(anorm_bits, (unsigned long long)__double_as_longlong(m));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)m, o));
+    __shared__ unsigned long long red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < 8; ++q) m = max(m, red[q]);
+        atomicMax(amax_bits, m);
     }
+}
+
+// ||A||_inf of the symmetric A from the per-tile row sums of |A| 2^-alpha
+// (rowsum[bk n + i], written while A is cut into its digit slices): each row
+// summed in a fixed order in FP64, the maximum folded into *anorm_bits.
+__global__ void norm_from_rowsums_kernel(int n, int nbk, const float *__restrict__ rowsum,
+                                         const unsigned long long *__restrict__ amax_bits,
+                                         unsigned long long *anorm_bits)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double sum = 0.0;
+    if (i < n)
+        for (int bk = 0; bk < nbk; ++bk) sum += (double)rowsum[(long)bk * n + i];
+    const double amax = __longlong_as_double((long long)*amax_bits);
+    const int alpha = (amax > 0.0 && isfinite(amax)) ? ilogb(amax) + 1 : 1;
+    unsigned long long m = (unsigned long long)__double_as_longlong(ldexp(sum, alpha));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(anorm_bits, m);
 }
 
 // y (FP32, n x nrhs) = fp32(x_j * 2^-e_j); used for b and r.  The power-of-two
@@ -261,6 +239,7 @@ static void residual_df(cudaStream_t s, int n, int nrhs, const double *A, long l
 // exact fixed-point slices (residual_tc), or, with STARPU_GB300_RESIDUAL=df,
 // in double-float on the FP32 pipe (residual_df).  The partials are reduced
 // in FP64 in a fixed order either way.
+// anorm_bits: [0] ||A||_inf, [2] max |A_ij| (the slices' scale), as FP64 bits.
 static int residual_mixed(cudaStream_t s, int n, int nrhs, const double *A, long lda, const double *X, long ldx,
                           const double *B, long ldb, double *R, long ldr, double *partials, float2 *xs, int *sx,
                           const void *rtc_a, void *rtc_xs, const unsigned long long *anorm_bits, int *d_err)
@@ -276,7 +255,7 @@ static int residual_mixed(cudaStream_t s, int n, int nrhs, const double *A, long
     const long cap = (long)(residual_partials(n, nrhs) / ((size_t)n * nrhs));
     const int kc = residual_tc_kchunk(n, nrhs, (int)cap);
     gb300_count_launch(), df_split_x_kernel<<<nrhs, 256, 0, s>>>(n, X, ldx, xs, sx);
-    int rc = residual_tc(s, n, nrhs, rtc_a, X, ldx, sx, anorm_bits, kc, rtc_xs, partials, d_err);
+    int rc = residual_tc(s, n, nrhs, rtc_a, X, ldx, sx, anorm_bits + 2, kc, rtc_xs, partials, d_err);
     if (rc) return rc;
     const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
     gb300_count_launch(), residual_reduce_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, (n + kc - 1) / kc, B, ldb,
@@ -339,6 +318,7 @@ struct SolverWs {
     int *sx;               // per-column scale exponents of X
     void *rtc_xs;          // x digit slices of the tensor-core residual
     void *rtc_a;           // the 8 digit slices of A (cut once per matrix, kept with the factor)
+    float *rowsum;         // n/64 x n row sums of the slicing pass, for ||A||_inf
     double *berr;          // nrhs
     int *done;             // nrhs
     int *rexp;             // nrhs: power-of-two scales of the FP32 right-hand sides
@@ -412,6 +392,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t oZ = tiles ? take((size_t)n * 16 * sizeof(float)) : 0;
     const size_t oC = tiles ? take((2 * ntiles + 1) * sizeof(int)) : 0;
     const size_t oA = take(residual_tc_a_bytes(n));
+    const size_t oN = take((size_t)((n + 63) / 64) * n * sizeof(float));
     const size_t oS = take(4 * sizeof(unsigned long long));
     const size_t oR = take((size_t)n * nrhs * sizeof(double));
     const size_t oY = take((size_t)n * nrhs * sizeof(float));
@@ -434,6 +415,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->Z = tiles ? (float *)(b + oZ) : nullptr;
         ws->cnt = tiles ? (int *)(b + oC) : nullptr;
         ws->rtc_a = b + oA;
+        ws->rowsum = (float *)(b + oN);
         ws->partials = (double *)(b + oQ);
         ws->xs = (float2 *)(b + oX);
         ws->sx = (int *)(b + oI);
@@ -460,10 +442,12 @@ static void correction_solve(cudaStream_t s, int n, int nrhs, int nb, const Solv
 
 static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws)
 {
+    // anorm_bits[0] = ||A||_inf, [1] = info + err, [2] = max |A_ij|
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
-    gb300_count_launch(), convert_lower_symnorm_kernel<<<(n + SYM_BW - 1) / SYM_BW, 256, 0, s>>>(n, A, lda, ws.W, n,
-                                                                                                 ws.anorm_bits);
-    int rc = residual_tc_slice_a(s, n, A, lda, ws.anorm_bits, ws.rtc_a);  // the residuals' slices of A
+    gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
+    int rc = residual_tc_slice_a(s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum);  // the residuals' slices of A
+    gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, (n + 63) / 64, ws.rowsum,
+                                                                                   ws.anorm_bits + 2, ws.anorm_bits);
     if (!rc) rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
     if (rc) return rc;
     if (!ws.band) potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
@@ -775,7 +759,7 @@ int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const f
 // ---- symmetric residual R = B - A X with the tensor-core slice products ----
 
 static size_t syres_layout(int n, int nrhs, char *base, double **partials, float2 **xs, int **sx, void **rxs,
-                           unsigned long long **an, void **rta)
+                           unsigned long long **an, void **rta, float **rsum)
 {
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -789,6 +773,7 @@ static size_t syres_layout(int n, int nrhs, char *base, double **partials, float
     const size_t oR = take(residual_tc_xs_bytes(n, nrhs));
     const size_t oA = take(4 * sizeof(unsigned long long));
     const size_t oT = take(residual_tc_a_bytes(n));
+    const size_t oN = take((size_t)((n + 63) / 64) * n * sizeof(float));
     if (base) {
         *partials = (double *)(base + oP);
         *xs = (float2 *)(base + oX);
@@ -796,6 +781,7 @@ static size_t syres_layout(int n, int nrhs, char *base, double **partials, float
         *rxs = base + oR;
         *an = (unsigned long long *)(base + oA);
         *rta = base + oT;
+        *rsum = (float *)(base + oN);
     }
     return off;
 }
@@ -803,7 +789,7 @@ static size_t syres_layout(int n, int nrhs, char *base, double **partials, float
 size_t starpu_gb300_dsyresidual_workspace(int n, int nrhs)
 {
     if (n <= 0 || nrhs <= 0) return 0;
-    return syres_layout(n, nrhs, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    return syres_layout(n, nrhs, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
 int starpu_gb300_dsyresidual(void *stream, int n, int nrhs, const double *A, int lda, const double *X, int ldx,
@@ -819,12 +805,13 @@ int starpu_gb300_dsyresidual(void *stream, int n, int nrhs, const double *A, int
     int *sx;
     void *rxs, *rta;
     unsigned long long *an;
-    syres_layout(n, nrhs, (char *)work, &partials, &xs, &sx, &rxs, &an, &rta);
-    cudaMemsetAsync(an, 0, sizeof *an, s);
-    gb300_count_launch(), convert_lower_symnorm_kernel<<<(n + SYM_BW - 1) / SYM_BW, 256, 0, s>>>(n, A, lda, nullptr, 0,
-                                                                                                 an);
-    int rc = residual_tc_slice_a(s, n, A, lda, an, rta);
+    float *rsum;
+    syres_layout(n, nrhs, (char *)work, &partials, &xs, &sx, &rxs, &an, &rta, &rsum);
+    cudaMemsetAsync(an, 0, 4 * sizeof *an, s);
+    gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, nullptr, 0, an + 2);
+    int rc = residual_tc_slice_a(s, n, A, lda, an + 2, rta, rsum);
     if (rc) return rc;
+    gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, (n + 63) / 64, rsum, an + 2, an);
     return residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, R, ldr, partials, xs, sx, rta, rxs, an, d_err);
 }
 

@@ -276,9 +276,11 @@ static long rtc_ldk(int n) { return ((long)n + 63) / 64 * 64; }
 
 size_t residual_tc_a_bytes(int n) { return n > 0 ? (size_t)8 * n * rtc_ldk(n) * 2 : 0; }
 
-// The 8 digit slices of the symmetric A (lower triangle read), once per matrix.
-int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const unsigned long long *anorm_bits,
-                        void *slices)
+// The 8 digit slices of the symmetric A (lower triangle read), once per
+// matrix, scaled by 2^alpha with max |A_ij| < 2^alpha (amax_bits: that max as
+// FP64 bits).  rowsum (optional): the per-tile row sums for the norm.
+int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const unsigned long long *amax_bits,
+                        void *slices, float *rowsum)
 {
     if (n <= 0) return GB300_OK;
     const long ldk = rtc_ldk(n);
@@ -287,8 +289,8 @@ int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const 
     if (ldk > kw)
         cudaMemset2DAsync((uint16_t *)slices + kw, ldk * 2, 0, (ldk - kw) * 2, (size_t)8 * n, s);
     const unsigned nt = (unsigned)((n + 63) / 64);
-    gb300_count_launch(), rtc_a_slices_kernel<<<dim3(nt, nt), 256, 0, s>>>(n, A, lda, anorm_bits, (uint16_t *)slices,
-                                                                           ldk);
+    gb300_count_launch(), rtc_a_slices_kernel<<<dim3(nt, nt), 256, 0, s>>>(n, A, lda, amax_bits, (uint16_t *)slices,
+                                                                           ldk, rowsum);
     return gb300_last_launch_status();
 }
 
@@ -312,10 +314,10 @@ int residual_tc_kchunk(int n, int nrhs, int max_chunks)
 
 // P_z = -(A X) over the K chunks z of length kchunk, with the slices of the
 // symmetric A from residual_tc_slice_a.  sx: ilogb(max |x_j|) per column
-// (device), anorm_bits: ||A||_inf (device, the slices' scale).  xs:
+// (device), amax_bits: max |A_ij| (device, the slices' scale).  xs:
 // residual_tc_xs_bytes(n, nrhs) bytes of scratch.
 int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const double *X, long ldx, const int *sx,
-                const unsigned long long *anorm_bits, int kchunk, void *xs, double *partials, int *d_err)
+                const unsigned long long *amax_bits, int kchunk, void *xs, double *partials, int *d_err)
 {
     if (n <= 0 || nrhs <= 0) return GB300_OK;
     if (kchunk % RTC_KBLK || !d_err) return GB300_EINVAL;
@@ -335,7 +337,7 @@ int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const dou
     ResidualTcArgs a;
     a.n = n;
     a.nrhs = nrhs;
-    a.anorm_bits = anorm_bits;
+    a.amax_bits = amax_bits;
     a.sx = sx;
     a.kchunk = kchunk;
     a.nblocks = (n + RTC_BM - 1) / RTC_BM;

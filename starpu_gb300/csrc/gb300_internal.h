@@ -12,8 +12,8 @@ constexpr int GB300_DIAG_TILE_MAX = 1024;
 
 // residual partials P_z = -(A X) on the tensor cores (capi_tc.cu)
 size_t residual_tc_a_bytes(int n);
-int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const unsigned long long *anorm_bits,
-                        void *slices);
+int residual_tc_slice_a(cudaStream_t s, int n, const double *A, long lda, const unsigned long long *amax_bits,
+                        void *slices, float *rowsum);
 size_t residual_tc_xs_bytes(int n, int nrhs);
 int residual_tc_kchunk(int n, int nrhs, int max_chunks);
 int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const double *X, long ldx, const int *sx,

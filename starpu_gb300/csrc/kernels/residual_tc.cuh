@@ -4,7 +4,7 @@
 // dominant FP64 work of a mixed-precision solve, and GB300's FP64 rate is a
 // small fraction of its BF16 tensor rate; this forms them from 7-bit slices:
 //
-//   A = 2^alpha     sum_{t=1..8} a_t 2^{-7t}   (alpha: ||A||_inf < 2^alpha)
+//   A = 2^alpha     sum_{t=1..8} a_t 2^{-7t}   (alpha: max |A_ij| < 2^alpha)
 //   x = 2^beta_j    sum_{u=1..8} b_u 2^{-7u}   (per right-hand side)
 //
 // a_t, b_u: unsigned 7-bit digits of the magnitude (56 bits, truncated)
@@ -66,7 +66,7 @@ constexpr int RTC_ERR_TIMEOUT = 5;
 
 struct ResidualTcArgs {
     int n, nrhs;
-    const unsigned long long *anorm_bits;  // ||A||_inf as FP64 bits: alpha = ilogb + 1
+    const unsigned long long *amax_bits;   // max |A_ij| as FP64 bits: alpha = ilogb + 1
     const int *sx;       // per right-hand side: ilogb(max |x_j|); beta_j = sx[j] + 1
     int kchunk;          // multiple of RTC_KBLK
     int nblocks, nchunks, ngroups, nitems;
@@ -140,10 +140,13 @@ __global__ void rtc_x_slices_kernel(int n, int ncols, const double *__restrict__
 // the lower-triangle block the tile reads from is staged in shared memory
 // (coalesced along its columns), the tile is written along k (coalesced),
 // 8 consecutive k per thread and slice (16-byte stores).  Columns k >= n of
-// the slices stay as the caller zeroed them.
+// the slices stay as the caller zeroed them.  The scale is 2^alpha with
+// max |A_ij| < 2^alpha.  rowsum (optional, n/64 x n): the tile's row sums of
+// |A| 2^-alpha, rowsum[bk n + i], for the infinity norm.
 __global__ void __launch_bounds__(256) rtc_a_slices_kernel(int n, const double *__restrict__ A, long lda,
-                                                           const unsigned long long *__restrict__ anorm_bits,
-                                                           uint16_t *__restrict__ S, long ldk)
+                                                           const unsigned long long *__restrict__ amax_bits,
+                                                           uint16_t *__restrict__ S, long ldk,
+                                                           float *__restrict__ rowsum)
 {
     __shared__ double T[64][65];
     const int bi = blockIdx.y, bk = blockIdx.x;
@@ -157,10 +160,9 @@ __global__ void __launch_bounds__(256) rtc_a_slices_kernel(int n, const double *
         T[b][a] = (sr < n && sc < n && sc <= sr) ? A[(long)sr + (long)sc * lda] : 0.0;
     }
     __syncthreads();
-    const int alpha = rtc_bound_exp(__longlong_as_double((long long)*anorm_bits));
+    const int alpha = rtc_bound_exp(__longlong_as_double((long long)*amax_bits));
     for (int u = threadIdx.x; u < 64 * 8; u += 256) {
         const int r = u >> 3, ch = u & 7, i = i0 + r;
-        if (i >= n) continue;
         uint32_t fhi[8], flo[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
@@ -173,8 +175,19 @@ __global__ void __launch_bounds__(256) rtc_a_slices_kernel(int n, const double *
             const unsigned long long w = (unsigned long long)__double_as_longlong(v);
             rtc_fixed((uint32_t)(w >> 32), (uint32_t)w, alpha, fhi[e], flo[e]);
         }
+        // row sums of |A| 2^-alpha over this tile's 64 columns, from the top 28
+        // fixed-point bits (ample for a norm): the 8 lanes of row r add theirs
+        if (rowsum) {
+            float rs = 0.0f;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) rs += __uint2float_rn(fhi[e] & 0xFFFFFFFu);
+            rs += __shfl_xor_sync(0xffffffffu, rs, 1);
+            rs += __shfl_xor_sync(0xffffffffu, rs, 2);
+            rs += __shfl_xor_sync(0xffffffffu, rs, 4);
+            if (ch == 0 && i < n) rowsum[(long)bk * n + i] = rs * 3.7252902984619140625e-9f;  // 2^-28
+        }
         const int kk = k0 + 8 * ch;
-        if (kk >= n) continue;
+        if (i >= n || kk >= n) continue;
 #pragma unroll
         for (int t = 1; t <= 8; ++t) {
             uint4 q;
@@ -245,7 +258,7 @@ residual_tc_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_consta
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     const int n = args.n;
-    const int alpha = rtc_bound_exp(__longlong_as_double((long long)*args.anorm_bits));
+    const int alpha = rtc_bound_exp(__longlong_as_double((long long)*args.amax_bits));
 
     if (warp == 0) {
         // --------------------------------------------------------- TMA producer
