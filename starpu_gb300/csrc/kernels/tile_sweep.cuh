@@ -83,6 +83,25 @@ __device__ __forceinline__ void tsw_wait(const TileSweepArgs &a, const int *cnt,
     __syncthreads();
 }
 
+// Prefetch into L2 the 32 x K operand a slab is about to multiply (it does
+// not depend on the flag the slab waits for, so its HBM latency overlaps the
+// wait): TR = false, one 128-byte line of 32 rows per column; TR = true, the
+// K consecutive elements of each of the 32 columns.
+template <bool TR>
+__device__ __forceinline__ void tsw_prefetch_l2(const float *M, long ldm, int rows, int K)
+{
+    if (!TR) {
+        for (int p = threadIdx.x; p < K; p += TSW_T)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(M + (long)p * ldm));
+    } else {
+        const int lines = (K + 31) / 32;
+        for (int e = threadIdx.x; e < rows * lines; e += TSW_T) {
+            const int r = e / lines, l = e - r * lines;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(M + (long)r * ldm + 32 * l));
+        }
+    }
+}
+
 // Register-staged chunk of the operand M (32 x kc, element (r, p)) and of the
 // right-hand sides V (kc x 16, element (p, c)).
 //   TR = false: M(r, p) = M[r + p * ldm]  (rows of L or of the inverse)
@@ -280,11 +299,18 @@ __global__ void __launch_bounds__(TSW_T) tile_sweep_kernel(TileSweepArgs a)
     const int r0 = t0 + s * TSW_SLAB, rows = min(TSW_SLAB, kbT - s * TSW_SLAB);
     const bool vec = a.vec != 0;
 
-    // contributions of the other tile rows: acc = -sum (L_slab,j y_j) or -sum (L_j,slab^T x_j)
+    // the slab's rows (forward) or columns (backward) of the diagonal tile's inverse, needed last
+    const float *D = a.Dinv + (long)T * a.dstride;
+    if (!TRANS) tsw_prefetch_l2<false>(D + s * TSW_SLAB, a.ldd, rows, s * TSW_SLAB + rows);
+    else tsw_prefetch_l2<true>(D + s * TSW_SLAB + (long)(s * TSW_SLAB) * a.ldd, a.ldd, rows, kbT - s * TSW_SLAB);
+
+    // contributions of the other tile rows: acc = sum (L_slab,j y_j) or sum (L_j,slab^T x_j)
     float acc[4][4] = {};
     const int jbeg = TRANS ? a.ntiles - 1 : 0, jend = TRANS ? T : T, jstep = TRANS ? -1 : 1;
     for (int j = jbeg; j != jend; j += jstep) {
         const int j0 = j * a.nb, kbj = min(a.nb, a.n - j0);
+        if (!TRANS) tsw_prefetch_l2<false>(a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, kbj);
+        else tsw_prefetch_l2<true>(a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, kbj);
         tsw_wait(a, &a.ycount[j], (kbj + TSW_SLAB - 1) / TSW_SLAB, &s_skip);
         if (!TRANS) tsw_product<false>(acc, a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
         else tsw_product<true>(acc, a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
@@ -303,7 +329,6 @@ __global__ void __launch_bounds__(TSW_T) tile_sweep_kernel(TileSweepArgs a)
     // diagonal tile: forward y_slab = Dinv(slab rows, 0 .. slab end) z_T;
     // backward x_slab = Dinv(slab start .. kbT, slab columns)^T z_T
     float acc2[4][4] = {};
-    const float *D = a.Dinv + (long)T * a.dstride;
     if (!TRANS) {
         tsw_product<false>(acc2, D + s * TSW_SLAB, a.ldd, rows, a.Z + t0, a.n, s * TSW_SLAB + rows, a.nrhs, vec, Ms, Vs);
     } else {
