@@ -440,15 +440,54 @@ static void correction_solve(cudaStream_t s, int n, int nrhs, int nb, const Solv
     else potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
 }
 
+// A side stream and a fork / join event pair per host thread and device: the
+// factor phase runs the passes that only read A (the residual's digit slices,
+// the infinity norm) beside the factorisation of W, which leaves most of the
+// GPU idle while its diagonal tiles are factored.
+struct SideStream {
+    int dev = -1;
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~SideStream()
+    {
+        if (s) cudaStreamDestroy(s);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+    }
+};
+
+static SideStream *side_stream()
+{
+    thread_local SideStream ss[16];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return nullptr;
+    SideStream &x = ss[dev];
+    if (!x.s) {
+        if (cudaStreamCreateWithFlags(&x.s, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) != cudaSuccess)
+            return nullptr;
+        x.dev = dev;
+    }
+    return &x;
+}
+
 static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws)
 {
     // anorm_bits[0] = ||A||_inf, [1] = info + err, [2] = max |A_ij|
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
     gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
-    int rc = residual_tc_slice_a(s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum);  // the residuals' slices of A
-    gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, (n + 63) / 64, ws.rowsum,
-                                                                                   ws.anorm_bits + 2, ws.anorm_bits);
+    // the residuals' slices of A and ||A||_inf, beside the factorisation
+    SideStream *ss = side_stream();
+    if (!ss) return gb300_record_cuda_error(cudaGetLastError());
+    cudaEventRecord(ss->fork, s);
+    cudaStreamWaitEvent(ss->s, ss->fork, 0);
+    int rc = residual_tc_slice_a(ss->s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum);
+    gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, ss->s>>>(n, (n + 63) / 64, ws.rowsum,
+                                                                                       ws.anorm_bits + 2, ws.anorm_bits);
+    cudaEventRecord(ss->join, ss->s);
     if (!rc) rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
+    cudaStreamWaitEvent(s, ss->join, 0);  // joined before anything reads the slices or the norm
     if (rc) return rc;
     if (!ws.band) potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
     return gb300_last_launch_status();
