@@ -21,7 +21,9 @@
 //
 // The products are register-blocked: the K range of every chunk (128 columns)
 // is split over the 8 warps, each lane keeps 4 rows x 4 right-hand sides, and
-// the next chunk is fetched into registers while the current one is used.
+// the next two chunks are fetched into registers while the current one is
+// used; the operands of a slab's next tile row are prefetched into L2 while it
+// waits for that row.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -224,33 +226,52 @@ __device__ __forceinline__ void tsw_put(const TswStage &st, float *Ms, float *Vs
 // cc = lane / 8) keeps rows 4 rr .. 4 rr + 3 and right-hand sides
 // 4 cc .. 4 cc + 3.
 template <bool TR>
+__device__ __forceinline__ void tsw_chunk_mma(float acc[4][4], const float *Ms, const float *Vs)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane & 7, cc = lane >> 3;
+#pragma unroll
+    for (int pp = 0; pp < 16; ++pp) {
+        const int p = warp * 16 + pp;
+        const float4 m4 = *reinterpret_cast<const float4 *>(Ms + p * TSW_MP + 4 * rr);
+        const float4 v4 = *reinterpret_cast<const float4 *>(Vs + p * TSW_VP + 4 * cc);
+        const float mv[4] = {m4.x, m4.y, m4.z, m4.w}, vv[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(mv[i], vv[j], acc[i][j]);
+    }
+}
+
+// acc += M(32 x K) V(K x 16), chunks of 128 K, two chunks in flight: chunk
+// c + 2 is fetched into the register set chunk c just left while chunk c is
+// multiplied from shared memory (the loop is unrolled by two so that both
+// register sets stay statically indexed).
+template <bool TR>
 __device__ __forceinline__ void tsw_product(float acc[4][4], const float *M, long ldm, int rows, const float *V,
                                             long ldv, int K, int nrhs, bool vec, float *Ms, float *Vs)
 {
     if (K <= 0) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane & 7, cc = lane >> 3;
-    TswStage st;
-    tsw_fetch<TR>(st, M, ldm, rows, V, ldv, min(TSW_KC, K), nrhs, vec);
-    for (int p0 = 0; p0 < K; p0 += TSW_KC) {
+    auto fetch = [&](TswStage &st, int c) {
+        const int p0 = c * TSW_KC;
+        const float *Mc = TR ? M + p0 : M + (long)p0 * ldm;
+        tsw_fetch<TR>(st, Mc, ldm, rows, V + p0, ldv, min(TSW_KC, K - p0), nrhs, vec);
+    };
+    const int nch = (K + TSW_KC - 1) / TSW_KC;
+    TswStage s0, s1;
+    fetch(s0, 0);
+    if (nch > 1) fetch(s1, 1);
+    for (int c = 0; c < nch; c += 2) {
         __syncthreads();  // the previous chunk has been used
-        tsw_put<TR>(st, Ms, Vs);
+        tsw_put<TR>(s0, Ms, Vs);
         __syncthreads();
-        const int pn = p0 + TSW_KC;
-        if (pn < K) {
-            const float *Mn = TR ? M + pn : M + (long)pn * ldm;
-            tsw_fetch<TR>(st, Mn, ldm, rows, V + pn, ldv, min(TSW_KC, K - pn), nrhs, vec);
-        }
-#pragma unroll
-        for (int pp = 0; pp < 16; ++pp) {
-            const int p = warp * 16 + pp;
-            const float4 m4 = *reinterpret_cast<const float4 *>(Ms + p * TSW_MP + 4 * rr);
-            const float4 v4 = *reinterpret_cast<const float4 *>(Vs + p * TSW_VP + 4 * cc);
-            const float mv[4] = {m4.x, m4.y, m4.z, m4.w}, vv[4] = {v4.x, v4.y, v4.z, v4.w};
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(mv[i], vv[j], acc[i][j]);
-        }
+        if (c + 2 < nch) fetch(s0, c + 2);
+        tsw_chunk_mma<TR>(acc, Ms, Vs);
+        if (c + 1 >= nch) break;
+        __syncthreads();
+        tsw_put<TR>(s1, Ms, Vs);
+        __syncthreads();
+        if (c + 3 < nch) fetch(s1, c + 3);
+        tsw_chunk_mma<TR>(acc, Ms, Vs);
     }
 }
 
