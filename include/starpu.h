@@ -471,13 +471,51 @@ double starpu_task_expected_length(struct starpu_task *task, struct starpu_perfm
 double starpu_task_expected_data_transfer_time(unsigned memory_node, struct starpu_task *task);
 uint32_t starpu_task_footprint(struct starpu_perfmodel *model, struct starpu_task *task,
                                struct starpu_perfmodel_arch *arch, unsigned nimpl);
+void starpu_perfmodel_init(struct starpu_perfmodel *model);
+int starpu_perfmodel_deinit(struct starpu_perfmodel *model);
+/* 0 on success, 1 when no file exists for the symbol or it is malformed */
+int starpu_perfmodel_load_file(const char *filename, struct starpu_perfmodel *model);
 int starpu_perfmodel_load_symbol(const char *symbol, struct starpu_perfmodel *model);
 int starpu_perfmodel_unload_model(struct starpu_perfmodel *model);
+/* the existing model file for `symbol`, "" when there is none */
 void starpu_perfmodel_get_model_path(const char *symbol, char *path, size_t maxlen);
+/* where the model file for `symbol` is written (its directory is created) */
+void starpu_perfmodel_get_model_path_default_location(const char *symbol, char *path, size_t maxlen);
 int starpu_save_history_based_model(struct starpu_perfmodel *model);
 void starpu_perfmodel_update_history(struct starpu_perfmodel *model, struct starpu_task *task,
                                      struct starpu_perfmodel_arch *arch, unsigned cpuid, unsigned nimpl,
                                      double measured);
+void starpu_perfmodel_update_history_n(struct starpu_perfmodel *model, struct starpu_task *task,
+                                       struct starpu_perfmodel_arch *arch, unsigned cpuid, unsigned nimpl,
+                                       double average_measured, unsigned number);
+double starpu_perfmodel_history_based_expected_perf(struct starpu_perfmodel *model, struct starpu_perfmodel_arch *arch,
+                                                    uint32_t footprint);
+
+/* perfmodel tooling (tools/starpu_perfmodel_display.c, tools/starpu_perfmodel_plot.c) */
+void starpu_drivers_preinit(void);
+void starpu_perfmodel_initialize(void);
+void starpu_perfmodel_free_sampling(void);
+int starpu_perfmodel_list(FILE *output);
+void starpu_perfmodel_directory(FILE *output);
+void starpu_perfmodel_dump_xml(FILE *output, struct starpu_perfmodel *model);
+void starpu_perfmodel_print(struct starpu_perfmodel *model, struct starpu_perfmodel_arch *arch, unsigned nimpl,
+                            char *parameter, uint32_t *footprint, FILE *output);
+int starpu_perfmodel_print_all(struct starpu_perfmodel *model, char *arch, char *parameter, uint32_t *footprint,
+                               FILE *output);
+int starpu_perfmodel_print_estimations(struct starpu_perfmodel *model, uint32_t footprint, FILE *output);
+int starpu_perfmodel_list_combs(FILE *output, struct starpu_perfmodel *model);
+int starpu_perfmodel_get_narch_combs(void);
+int starpu_perfmodel_arch_comb_add(int ndevices, struct starpu_perfmodel_device *devices);
+int starpu_perfmodel_arch_comb_get(int ndevices, struct starpu_perfmodel_device *devices);
+struct starpu_perfmodel_arch *starpu_perfmodel_arch_comb_fetch(int comb);
+const char *starpu_perfmodel_get_archtype_name(enum starpu_worker_archtype archtype);
+void starpu_perfmodel_get_arch_name(struct starpu_perfmodel_arch *arch, char *archname, size_t maxlen, unsigned nimpl);
+/* GB300 addition behind the plot tool: writes the gnuplot script `gp_path`
+ * and its averages file `avg_path` for a loaded model (only_comb < 0: every
+ * combination); 0 or -errno */
+int starpu_gb300_perfmodel_plot(struct starpu_perfmodel *model, struct starpu_perfmodel *energy_model,
+                                const char *symbol, const char *energy_symbol, int only_comb, int gflops, int energy,
+                                const char *gp_path, const char *avg_path);
 
 /* =================================================================== workers */
 unsigned starpu_worker_get_count(void);

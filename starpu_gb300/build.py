@@ -56,6 +56,8 @@ def _run(cmd: list[str]) -> None:
 CHOL_LIBNAME = "libstarpu_gb300_chol.so"
 LU_LIBNAME = "libstarpu_gb300_lu.so"
 EXAMPLES = {"chol_implicit_gb300": CHOL_LIBNAME, "lu_gb300": LU_LIBNAME}
+# perfmodel tools (csrc/tools/<name>.c), linked against libstarpu_gb300.so only
+TOOLS = ("starpu_perfmodel_display", "starpu_perfmodel_plot")
 
 
 def chol_lib_path() -> str:
@@ -93,6 +95,13 @@ def _build_codelets_and_examples(main_changed: bool) -> None:
         if main_changed or _stale(exe, src, max(deps, os.path.getmtime(lib))):
             _run(["gcc", "-O2", "-g", "-std=gnu11", "-Wall", "-o", exe + ".tmp", src, *inc, "-L" + LIBDIR,
                   "-l" + codelet_lib[3:-3], "-lstarpu_gb300", rpath, "-lm", "-lpthread"])
+            os.replace(exe + ".tmp", exe)
+    for tool in TOOLS:
+        src = os.path.join(CSRC, "tools", tool + ".c")
+        exe = example_path(tool)
+        if main_changed or _stale(exe, src, deps):
+            _run(["gcc", "-O2", "-g", "-std=gnu11", "-Wall", "-o", exe + ".tmp", src, *inc, "-L" + LIBDIR,
+                  "-lstarpu_gb300", rpath, "-lm", "-lpthread"])
             os.replace(exe + ".tmp", exe)
 
 

@@ -29,7 +29,12 @@ static std::mutex g_table_mu;
 
 static size_t smem_bytes() { return (size_t)(64 * 65 + 2 * 64 * BAT_TILE) * sizeof(float); }
 
-static void tuning_path(char *path, size_t len) { starpu_perfmodel_get_model_path("gb300_chol_tuning", path, len); }
+// the existing table file, else where a new one is written
+static void tuning_path(char *path, size_t len)
+{
+    starpu_perfmodel_get_model_path("gb300_chol_tuning", path, len);
+    if (!path[0]) starpu_perfmodel_get_model_path_default_location("gb300_chol_tuning", path, len);
+}
 
 static void load_table_locked()
 {

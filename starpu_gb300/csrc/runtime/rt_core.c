@@ -94,6 +94,7 @@ int starpu_initialize(struct starpu_conf *user_conf, int *argc, char ***argv)
     rt.max_prio = INT_MAX;
     rt.calibrate = (unsigned)env_int("STARPU_CALIBRATE", c.calibrate == (unsigned)-1 ? 0 : (int)c.calibrate);
     rt.transfer_us_per_byte = 1.0 / 50000.0; /* ~50 GB/s host <-> GPU */
+    rt_perfmodel_init();
 
     int ndev = 0;
     int want_cuda = c.ncuda >= 0 ? c.ncuda : -1;
@@ -149,6 +150,10 @@ int starpu_initialize(struct starpu_conf *user_conf, int *argc, char ***argv)
 }
 
 int starpu_is_initialized(void) { return rt.initialized > 0; }
+
+/* Driver pre-initialisation before starpu_init (src/core/workers.c:1614-1625):
+ * the CPU and CUDA drivers of this runtime need none. */
+void starpu_drivers_preinit(void) {}
 
 void starpu_shutdown(void)
 {

@@ -17,8 +17,9 @@
  *    pool of streams, one event per task for the edges) and launches it;
  *  - scheduling: dmda-style (expected finish time = worker availability +
  *    transfer + history-model length), priority-ordered worker queues;
- *  - history perfmodels per (symbol, arch, footprint), persisted in the
- *    version-45 text layout under $STARPU_PERF_MODEL_DIR/codelets/45/.
+ *  - history perfmodels per (symbol, architecture combination,
+ *    implementation, footprint), persisted in the version-45 text layout
+ *    under $STARPU_PERF_MODEL_DIR/codelets/45/ (rt_perfmodel.c).
  */
 #ifndef RT_INTERNAL_H
 #define RT_INTERNAL_H
@@ -140,8 +141,9 @@ void rt_flush_and_wait(void);
 /* rt_sched.c */
 void rt_sched_push(struct rt_job *j);
 struct rt_job *rt_sched_pop(struct rt_worker *w);
-double rt_expected_length(struct starpu_task *t, enum starpu_worker_archtype type);
-void rt_perfmodel_feedback(struct starpu_task *t, enum starpu_worker_archtype type, double us);
+double rt_expected_length(struct starpu_task *t, struct starpu_perfmodel_arch *arch);
+void rt_perfmodel_feedback(struct starpu_task *t, struct starpu_perfmodel_arch *arch, double us);
+void rt_perfmodel_init(void);
 void rt_perfmodel_save_all(void);
 
 /* rt_cuda.c */

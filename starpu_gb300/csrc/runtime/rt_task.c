@@ -301,7 +301,7 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
     struct starpu_task *t = j->task;
     if (t->cl && t->cl->model && measured_us > 0) {
         int w = j->worker;
-        rt_perfmodel_feedback(t, w >= 0 ? rt.workers[w].type : STARPU_CUDA_WORKER, measured_us);
+        rt_perfmodel_feedback(t, &rt.workers[w >= 0 ? w : 0].arch, measured_us);
     }
     if (t->callback_func) t->callback_func(t->callback_arg);
     rt_lock();

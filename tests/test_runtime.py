@@ -42,8 +42,10 @@ def runtime_test_binary(tmp_path_factory):
 
 @pytest.mark.parametrize("ncpu", [1, 4])
 def test_runtime_c_suite(runtime_test_binary, tmp_path, ncpu):
+    # the tile task runs for about a microsecond: timer noise alone breaks the
+    # 50 % outlier rule, so the rule is widened for the calibration check
     r = subprocess.run([runtime_test_binary], env=_env(STARPU_NCUDA=0, STARPU_NCPU=ncpu, STARPU_PERF_MODEL_DIR=tmp_path,
-                                                         STARPU_HOSTNAME="testhost"),
+                                                         STARPU_HOSTNAME="testhost", STARPU_HISTORY_MAX_ERROR=100000),
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and "ALL OK" in r.stdout, r.stdout + r.stderr
     assert (tmp_path / "codelets" / "45" / "gb300_test_tile_inc.testhost").exists()
