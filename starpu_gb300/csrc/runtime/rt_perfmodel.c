@@ -214,6 +214,7 @@ static pthread_mutex_t dir_mu = PTHREAD_MUTEX_INITIALIZER;
 static char *model_dirs[PM_MAXDIRS + 1];
 static int nmodel_dirs;
 static int model_dir_from_env;
+static char dirs_signature[4 * PM_DIRLEN];
 
 static void add_dir(const char *dir, int only_if_exists)
 {
@@ -232,10 +233,26 @@ static void add_dir(const char *dir, int only_if_exists)
     model_dirs[nmodel_dirs] = NULL;
 }
 
-static void set_dirs(void)
+/* The list is rebuilt whenever the variables it comes from change, so that a
+ * process may point successive calls at other model directories. */
+
+/* called with dir_mu held */
+static void set_dirs_locked(void)
 {
-    pthread_mutex_lock(&dir_mu);
+    char sig[sizeof dirs_signature];
+    const char *v[4] = {getenv("STARPU_PERF_MODEL_DIR"), getenv("STARPU_HOME"), getenv("HOME"),
+                        getenv("STARPU_PERF_MODEL_PATH")};
+    snprintf(sig, sizeof sig, "%s\n%s\n%s\n%s", v[0] ? v[0] : "", v[1] ? v[1] : "", v[2] ? v[2] : "",
+             v[3] ? v[3] : "");
+    if (nmodel_dirs != 0 && strcmp(sig, dirs_signature) != 0) {
+        for (int i = 0; i < nmodel_dirs; ++i) {
+            free(model_dirs[i]);
+            model_dirs[i] = NULL;
+        }
+        nmodel_dirs = 0;
+    }
     if (nmodel_dirs == 0) {
+        snprintf(dirs_signature, sizeof dirs_signature, "%s", sig);
         const char *env = getenv("STARPU_PERF_MODEL_DIR");
         model_dir_from_env = env && *env;
         if (model_dir_from_env) add_dir(env, 0);
@@ -252,7 +269,6 @@ static void set_dirs(void)
             free(copy);
         }
     }
-    pthread_mutex_unlock(&dir_mu);
 }
 
 /* STARPU_HOSTNAME, else the host name up to its first dot (src/common/utils.c:539-590) */
@@ -292,36 +308,49 @@ static void mkdir_p(const char *path)
 /* the first existing file among the directories, "" when none */
 void starpu_perfmodel_get_model_path(const char *symbol, char *path, size_t maxlen)
 {
-    set_dirs();
+    pthread_mutex_lock(&dir_mu);
+    set_dirs_locked();
     for (int i = 0; i < nmodel_dirs; ++i) {
         codelet_file(model_dirs[i], symbol, path, maxlen);
-        if (access(path, F_OK) == 0) return;
+        if (access(path, F_OK) == 0) {
+            pthread_mutex_unlock(&dir_mu);
+            return;
+        }
     }
+    pthread_mutex_unlock(&dir_mu);
     if (maxlen) path[0] = 0;
 }
 
 /* where a model is written: the first directory (its codelets/45/ is created) */
 void starpu_perfmodel_get_model_path_default_location(const char *symbol, char *path, size_t maxlen)
 {
-    set_dirs();
+    pthread_mutex_lock(&dir_mu);
+    set_dirs_locked();
     codelet_file(model_dirs[0], symbol, path, maxlen);
+    pthread_mutex_unlock(&dir_mu);
     mkdir_p(path);
 }
 
 void starpu_perfmodel_directory(FILE *output)
 {
-    set_dirs();
+    pthread_mutex_lock(&dir_mu);
+    set_dirs_locked();
     for (int i = 0; i < nmodel_dirs; ++i) fprintf(output, "directory: <%scodelets/%d/>\n", model_dirs[i], PM_VERSION);
+    pthread_mutex_unlock(&dir_mu);
 }
 
 static int name_cmp(const struct dirent **a, const struct dirent **b) { return strcmp((*a)->d_name, (*b)->d_name); }
 
 int starpu_perfmodel_list(FILE *output)
 {
-    set_dirs();
-    for (int i = 0; i < nmodel_dirs; ++i) {
-        char dir[PM_DIRLEN + 32];
-        snprintf(dir, sizeof dir, "%scodelets/%d/", model_dirs[i], PM_VERSION);
+    pthread_mutex_lock(&dir_mu);
+    set_dirs_locked();
+    char dirs[PM_MAXDIRS][PM_DIRLEN + 32];
+    const int ndirs = nmodel_dirs;
+    for (int i = 0; i < ndirs; ++i) snprintf(dirs[i], sizeof dirs[i], "%scodelets/%d/", model_dirs[i], PM_VERSION);
+    pthread_mutex_unlock(&dir_mu);
+    for (int i = 0; i < ndirs; ++i) {
+        const char *dir = dirs[i];
         struct dirent **list;
         int n = scandir(dir, &list, NULL, name_cmp);
         if (n < 0) {
@@ -922,7 +951,12 @@ void rt_perfmodel_save_all(void)
 
 /* ------------------------------------------------------- tooling: loading */
 
-void starpu_perfmodel_initialize(void) { set_dirs(); }
+void starpu_perfmodel_initialize(void)
+{
+    pthread_mutex_lock(&dir_mu);
+    set_dirs_locked();
+    pthread_mutex_unlock(&dir_mu);
+}
 
 void starpu_perfmodel_init(struct starpu_perfmodel *model) { ensure_model(model); }
 

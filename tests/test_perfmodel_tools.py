@@ -203,3 +203,28 @@ def test_reference_sample_models(tools, tmp_path):
     # coefficient count in one combination; every other file reads back
     assert malformed and all(n.startswith("starpu_dlu_lu_model_gemm") and n.endswith(".idgraf") for n in malformed)
     assert len(files) - len(malformed) >= 200
+
+
+def test_model_directory_follows_environment(native, tmp_path):
+    """A process may point successive calls at other model directories (the
+    batched autotuner's table lives there too): the search list is rebuilt
+    when STARPU_PERF_MODEL_DIR / STARPU_HOME / STARPU_PERF_MODEL_PATH change."""
+    import ctypes
+    f = native.starpu_perfmodel_get_model_path_default_location
+    f.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+    f.restype = None
+    saved = {k: os.environ.get(k) for k in ("STARPU_PERF_MODEL_DIR", "STARPU_HOSTNAME")}
+    try:
+        os.environ["STARPU_HOSTNAME"] = "envhost"
+        for sub in ("a", "b"):
+            os.environ["STARPU_PERF_MODEL_DIR"] = str(tmp_path / sub)
+            buf = ctypes.create_string_buffer(4096)
+            f(b"gb300_env_probe", buf, 4096)
+            assert buf.value.decode() == f"{tmp_path / sub}/codelets/45/gb300_env_probe.envhost"
+            assert (tmp_path / sub / "codelets" / "45").is_dir()
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
