@@ -430,29 +430,54 @@ def run_ours(args):
                       "gbs": (by.value / (tms.value * 1e-3) / 1e9) if tms.value else None}
     for v in prof.values():
         v["share"] = v["ms_per_step"] / ms if ms else None
+    # the trailing updates share the GPU with the next panel by design (the
+    # panel and update classes overlap in time, so shares may sum above 1)
+    sm_share = C.c_double(1.0)
+    L.starpu_gb300_profiling_sm_share(0, C.byref(sm_share))
+    prof["tc_update"]["sm_share"] = sm_share.value
     tc = prof["tc_update"]
     peak_tc = peaks["bf16_tflops_sustained"]
     traffic, traffic_src = args.tc_traffic, "given on the command line"
     if traffic is None:
         # DRAM bytes per launch: the ncu capture of one m = 8192, k = 1024
-        # launch (dram__bytes_read.sum + dram__bytes_write.sum) scaled to each
-        # trailing update of the factorisation (m = n - (k+1) nb) by its
-        # algorithmic bytes (FP32 C lower triangle read + written, two BF16
-        # K-major panels), averaged over the launches like `achieved`
-        def tc_bytes(m, kb=nb):
-            ldk = (kb + 63) // 64 * 64
+        # lower launch (dram__bytes_read.sum + dram__bytes_write.sum) scaled
+        # to each update launch of the factorisation by its algorithmic bytes
+        # (FP32 C read + written, two BF16 K-major panels), averaged over the
+        # launches like `achieved`.  Per step (m = n - (k+1) nb rows below the
+        # diagonal tile): the next column block (its kb1 x kb1 lower tile and
+        # the m2 x kb1 rectangle below, m2 = m - kb1), then the trailing m2 x m2
+        # lower triangle.
+        ldk = (nb + 63) // 64 * 64
+
+        def tc_bytes(m):
             return 8.0 * m * (m + 1) / 2 + 2.0 * m * ldk * 2
-        ms_list = [n - (k + 1) * nb for k in range((n + nb - 1) // nb - 1)]
-        if ms_list:
-            traffic = sum(TC_TRAFFIC_M8192 * tc_bytes(m) / tc_bytes(8192, 1024) for m in ms_list) / len(ms_list)
+
+        launch_bytes = []
+        for k in range((n + nb - 1) // nb - 1):
+            m = n - (k + 1) * nb
+            kb1 = min(nb, m)
+            m2 = m - kb1
+            launch_bytes.append(8.0 * (kb1 * (kb1 + 1) / 2 + m2 * kb1) + 2.0 * m * ldk * 2)
+            if m2 > 0:
+                launch_bytes.append(tc_bytes(m2))
+        if launch_bytes:
+            traffic = sum(TC_TRAFFIC_M8192 * b / tc_bytes(8192) for b in launch_bytes) / len(launch_bytes)
             traffic_src = (f"ncu capture of an m=8192 k=1024 launch ({TC_TRAFFIC_M8192 / 1e6:.1f} MB) scaled by "
-                           f"algorithmic bytes to the {len(ms_list)} launches of one factorisation, mean per launch")
+                           f"algorithmic bytes to the {len(launch_bytes)} update launches of one factorisation "
+                           "(next column block + trailing triangle per step), mean per launch")
     roofline = {"bound": "tensor", "achieved": tc["tflops"], "peak": peak_tc, "unit": "TFLOP/s",
                 "frac": (tc["tflops"] / peak_tc) if tc["tflops"] else None,
+                # the updates run on the SMs the concurrent panel leaves free:
+                # their time-weighted mean share of the SMs, and the fraction
+                # of the peak of that share they reach
+                "sm_share": sm_share.value,
+                "frac_of_sm_share": (tc["tflops"] / (peak_tc * sm_share.value)) if tc["tflops"] else None,
                 "traffic": traffic, "traffic_source": traffic_src,
                 "kernel": "tc_update_kernel (split-BF16 tcgen05 trailing update)",
                 "peak_source": f"{peaks['source']} bf16 sustained (kernel timed inside a long step)",
-                "algorithmic": "flops = nterms * kb * m*(m+1) per launch (lower triangle of an m x m rank-kb update)"}
+                "algorithmic": "flops = nterms * kb * 2 * (cells updated) per launch: per step the next column block "
+                               "(kb1 lower tile + m2 x kb1 rectangle) and the m2 x m2 lower triangle beyond it; "
+                               "summed over a step, nterms * kb * m*(m+1)"}
 
     # ---- kappa sweep (same Gram matrix, shifted diagonal)
     sweep = []

@@ -232,6 +232,10 @@ unsigned long long starpu_gb300_launch_count(void);
 void starpu_gb300_profiling_enable(int on);
 void starpu_gb300_profiling_reset(void);
 int starpu_gb300_profiling_get(int kind, unsigned long long *launches, double *total_ms, double *flops, double *bytes);
+/* The time-weighted mean fraction of the SMs a class's launches were limited
+ * to (1 unless a launch shared the GPU by design: the trailing updates that
+ * run beside the next panel leave that panel's SMs free). */
+int starpu_gb300_profiling_sm_share(int kind, double *share);
 
 #ifdef __cplusplus
 }

@@ -96,8 +96,11 @@ int split_bf16(cudaStream_t s, int m, int k, const float *P, long ldp, void *hi,
     return gb300_last_launch_status();
 }
 
+// max_grid > 0 caps the persistent grid (CTAs, one per SM): the trailing
+// update that runs beside the next panel leaves that panel's SMs free.
 int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void *a_lo, long lda, const void *b_hi,
-              const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0)
+              const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
+              int max_grid = 0)
 {
     if (m <= 0 || n <= 0 || K <= 0) return GB300_OK;
     if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!a_lo || !b_lo)) || (lower && m != n) || !d_err)
@@ -138,18 +141,19 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
         cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TCU_SMEM);
         attr_set = true;
     }
-    const int grid = std::min(a.num_tiles, num_sms());
+    const int grid = std::min(a.num_tiles, max_grid > 0 ? std::min(max_grid, num_sms()) : num_sms());
     gb300_count_launch(), tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, a);
     return gb300_last_launch_status();
 }
 
 // Workspace of potrf_tc for order n and tile nb (ldk = nb rounded up to 64):
-// the split panel (hi, lo: n x ldk BF16 each), the inverse of the diagonal
+// two split panels (hi, lo: n x ldk BF16 each; step k's panel is read by its
+// trailing update while step k+1's is written), the inverse of the diagonal
 // tile (ldk x ldk FP32) and its split (hi, lo), the doubling scratch of the
 // triangular inverse (ldk x ldk FP32) and the diagonal-tile kernel's barrier
 // counter.
 struct TcWs {
-    __nv_bfloat16 *hi, *lo, *ihi, *ilo;
+    __nv_bfloat16 *hi[2], *lo[2], *ihi, *ilo;
     float *linv, *scratch;
     unsigned *bar;  // grid-barrier counter of the diagonal-tile kernel
 };
@@ -159,15 +163,17 @@ static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
     const size_t panel = (size_t)n * ldk * 2, inv = ldk * ldk;
     if (w && base) {
         char *b = (char *)base;
-        w->hi = (__nv_bfloat16 *)b;
-        w->lo = w->hi + (size_t)n * ldk;
-        w->linv = (float *)(b + 2 * panel);
+        for (int i = 0; i < 2; ++i) {
+            w->hi[i] = (__nv_bfloat16 *)(b + 2 * i * panel);
+            w->lo[i] = (__nv_bfloat16 *)(b + (2 * i + 1) * panel);
+        }
+        w->linv = (float *)(b + 4 * panel);
         w->ihi = (__nv_bfloat16 *)(w->linv + inv);
         w->ilo = w->ihi + inv;
         w->scratch = (float *)(w->ilo + inv);
         w->bar = (unsigned *)(w->scratch + inv);
     }
-    return 2 * panel + inv * 4 + 2 * inv * 2 + inv * 4 + 256;
+    return 4 * panel + inv * 4 + 2 * inv * 2 + inv * 4 + 256;
 }
 
 static_assert(DC_MAXN == GB300_DIAG_TILE_MAX, "one limit for the diagonal-tile kernel");
@@ -177,7 +183,7 @@ static_assert(DC_MAXN == GB300_DIAG_TILE_MAX, "one limit for the diagonal-tile k
 // of diag_coop_kernel, the grid sized to the widest phase and to what can be
 // resident at once.
 static int diag_factor_inverse(cudaStream_t s, int n, float *A, long lda, float *Linv, long ldi, float *T,
-                               unsigned *bar, int *info, int info_base, int *err, bool invert)
+                               unsigned *bar, int *info, int info_base, int *err, bool invert, int max_sms = 0)
 {
     static int occ = -1;
     if (occ < 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, diag_coop_kernel, DC_T, 0) != cudaSuccess) {
@@ -194,7 +200,8 @@ static int diag_factor_inverse(cudaStream_t s, int n, float *A, long lda, float 
         if (m > 0) work = std::max(work, m * (m + 1) / 2 + (invert && k >= 1 ? k * (k + 1) / 2 : 0));
     }
     if (invert) work = std::max(work, nblk * (nblk - 1) / 2);
-    const int grid = std::max(1, std::min(work, num_sms() * std::max(occ, 1)));
+    const int sms = max_sms > 0 ? std::min(max_sms, num_sms()) : num_sms();
+    const int grid = std::max(1, std::min(work, sms * std::max(occ, 1)));
     if (invert) cudaMemset2DAsync(Linv, ldi * sizeof(float), 0, n * sizeof(float), n, s);
     cudaMemsetAsync(bar, 0, sizeof(unsigned), s);
     DiagCoopArgs a;
@@ -215,11 +222,120 @@ static int diag_factor_inverse(cudaStream_t s, int n, float *A, long lda, float 
         cudaLaunchCooperativeKernel((const void *)diag_coop_kernel, dim3(grid), dim3(DC_T), args, 0, s));
 }
 
+// A high-priority stream and a fork / join event pair per host thread and
+// device for the trailing updates that run beside the next panel.  The
+// priority lets the update's CTAs take their SMs before the panel's kernels
+// spread over the GPU.
+struct LookaheadStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~LookaheadStream()
+    {
+        if (s) cudaStreamDestroy(s);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+    }
+};
+
+static LookaheadStream *lookahead_stream()
+{
+    thread_local LookaheadStream ls[16];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return nullptr;
+    LookaheadStream &x = ls[dev];
+    if (!x.s) {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (cudaStreamCreateWithPriority(&x.s, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+            cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
+    return &x;
+}
+
+// SMs the panel of step k+1 keeps while step k's trailing update runs on the
+// others.  GB300_LOOKAHEAD_SMS fixes the count (0 runs the steps one after the
+// other); by default it is chosen per step to balance the two: the update's
+// 3 m2^2 kb flops on the remaining SMs against the panel's latency-bound
+// diagonal tile (about 0.75 ms) plus its 6 m2 kb^2 TRSM flops, both at the
+// split-BF16 tensor rate measured for this kernel (1.45 PFLOP/s on the whole GPU).
+static int lookahead_sms(int m2, int kb)
+{
+    static int fixed = -2;
+    if (fixed == -2) {
+        const char *e = getenv("GB300_LOOKAHEAD_SMS");
+        fixed = e && *e ? std::max(0, atoi(e)) : -1;
+    }
+    const int S = num_sms();
+    if (fixed >= 0) return fixed >= S ? 0 : fixed;
+    if (S < 32 || m2 <= 0) return 0;
+    const double R = 1.45e15 / S, t_diag = 0.75e-3;
+    const double f_upd = 3.0 * m2 * (double)m2 * kb, f_trsm = 6.0 * m2 * (double)kb * kb;
+    // below about a quarter of the GPU the diagonal-tile kernel itself slows down
+    int best = S / 4;
+    double best_t = 1e30;
+    for (int L = S / 4; L <= S - 16; L += 8) {
+        const double t = std::max(f_upd / (R * (S - L)), t_diag + f_trsm / (R * L));
+        if (t < best_t) {
+            best_t = t;
+            best = L;
+        }
+    }
+    return best;
+}
+
+// Panel of the step at column k0 (width kb): FP32 POTRF of the diagonal tile
+// (SIMT), its inverse, the panel TRSM  P <- P L_kk^-T  as one split-BF16
+// product P * Linv^T (store form, always 3 products), and the split of the
+// solved panel into (hi, lo) for the trailing update.  sms > 0 keeps its
+// kernels to that many SMs' worth of CTAs.
+static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb, int nb, int np, const TcWs &w,
+                      int buf, float *linv_band, int *d_info, int *d_err, int sms)
+{
+    const long ldk = ((long)nb + 63) / 64 * 64;
+    float *Akk = A + k0 + (long)k0 * lda;
+    const int m = n - k0 - kb;
+    const int slot = gb300_prof_begin(s, GB300_PROF_PANEL);
+    int rc = 0;
+    // the inverse of the diagonal tile: step k's own block of the band when
+    // the caller keeps them all, else the one reused buffer
+    float *linv = linv_band ? linv_band + (size_t)(k0 / nb) * ldk * ldk : w.linv;
+    if (kb <= DC_MAXN) {
+        rc = diag_factor_inverse(s, kb, Akk, lda, linv, ldk, w.scratch, w.bar, d_info, k0, d_err, m > 0 || linv_band,
+                                 sms);
+    } else {
+        potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
+        if (m > 0) trtri_lower<float>(s, kb, Akk, lda, linv, ldk, w.scratch);
+    }
+    if (rc || m <= 0) {
+        gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0, 4.0 * kb * kb);
+        return rc;
+    }
+    float *P = A + (k0 + kb) + (long)k0 * lda;
+    rc = split_bf16(s, kb, kb, linv, ldk, w.ihi, w.ilo, ldk);
+    if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi[buf], w.lo[buf], ldk);
+    if (!rc) rc = tc_update(s, m, kb, kb, w.hi[buf], w.lo[buf], ldk, w.ihi, w.ilo, ldk, 3, 0, P, lda, d_err, 1, sms);
+    if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi[buf], np > 1 ? w.lo[buf] : nullptr, ldk);
+    // algorithmic work of the panel: POTRF kb^3/3 + TRSM m kb^2; bytes: the
+    // tile and the panel read and written once, the BF16 panel written
+    gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0 + (double)m * kb * kb,
+                   8.0 * kb * kb + 8.0 * m * kb + 2.0 * m * ldk * np);
+    return rc;
+}
+
 // Tiled right-looking Cholesky of an FP32 matrix on the tensor cores
-// (split-BF16 products when nterms == 3).  Step k: FP32 POTRF of the
-// diagonal tile (SIMT), its inverse (64 x 64 blocks + batched doubling), the
-// panel TRSM  P <- P L_kk^-T  as one split-BF16 product P * Linv^T (store
-// form, always 3 products), then the trailing update  A22 -= P P^T  (lower).
+// (split-BF16 products when nterms == 3) with a lookahead of one panel.
+// After step k's panel, its rank-kb update is applied first to the next
+// column block (its lower diagonal tile and the rectangle below), then step
+// k+1's panel -- which needs nothing else -- runs on a few SMs while the rest
+// of step k's update (the trailing triangle beyond the next tile) runs on the
+// other SMs, from a high-priority stream.  The two write disjoint parts of A
+// and read different panel buffers; the streams join before step k+1's
+// update.  The diagonal-tile factorisation, latency-bound on a few SMs, thus
+// hides behind the trailing update.
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err,
              float *linv_band)
 {
@@ -227,46 +343,58 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
     TcWs w;
     tc_ws_layout(n, nb, work, &w);
     const int np = nterms == 3 ? 2 : 1;
-    for (int k0 = 0; k0 < n; k0 += nb) {
+    // a step has a trailing triangle beyond its next column block only when n > 2 nb
+    LookaheadStream *la = n > 2 * nb ? lookahead_stream() : nullptr;
+    int buf = 0;
+    int rc = panel_step(s, n, A, lda, 0, std::min(nb, n), nb, np, w, buf, linv_band, d_info, d_err, 0);
+    for (int k0 = 0; k0 < n && !rc; k0 += nb) {
         const int kb = std::min(nb, n - k0);
-        float *Akk = A + k0 + (long)k0 * lda;
         const int m = n - k0 - kb;
-        int slot = gb300_prof_begin(s, GB300_PROF_PANEL);
-        int rc = 0;
-        // the inverse of the diagonal tile: step k's own block of the band
-        // when the caller keeps them all, else the one reused buffer
-        float *linv = linv_band ? linv_band + (size_t)(k0 / nb) * ldk * ldk : w.linv;
-        if (kb <= DC_MAXN) {
-            rc = diag_factor_inverse(s, kb, Akk, lda, linv, ldk, w.scratch, w.bar, d_info, k0, d_err,
-                                     m > 0 || linv_band);
+        if (m <= 0) break;
+        const __nv_bfloat16 *hi = w.hi[buf], *lo = w.lo[buf];
+        const int kb1 = std::min(nb, m);  // width of the next column block
+        const int m2 = m - kb1;           // rows and columns beyond it
+        float *C11 = A + (k0 + kb) + (long)(k0 + kb) * lda;
+        // the next column block: its diagonal tile (lower) and the rectangle below
+        int slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
+        rc = tc_update(s, kb1, kb1, kb, hi, lo, ldk, hi, lo, ldk, nterms, 1, C11, lda, d_err);
+        if (!rc && m2 > 0)
+            rc = tc_update(s, m2, kb1, kb, hi + (size_t)kb1 * ldk, lo + (size_t)kb1 * ldk, ldk, hi, lo, ldk, nterms, 0,
+                           C11 + kb1, lda, d_err);
+        // algorithmic work: the lower triangle of the kb1 tile and the m2 x kb1
+        // rectangle, per term; bytes: C read + written in FP32, the panels read
+        gb300_prof_end(s, slot, (double)nterms * kb * ((double)kb1 * (kb1 + 1.0) + 2.0 * m2 * kb1),
+                       8.0 * ((double)kb1 * (kb1 + 1.0) / 2.0 + (double)m2 * kb1) + 2.0 * m * ldk * np);
+        if (rc) break;
+        const int nbuf = buf ^ 1;
+        float *C22 = C11 + kb1 + (long)kb1 * lda;
+        const __nv_bfloat16 *hi2 = hi + (size_t)kb1 * ldk, *lo2 = lo + (size_t)kb1 * ldk;
+        // algorithmic work of the trailing triangle, as for one lower update
+        const double f2 = (double)nterms * kb * (double)m2 * (m2 + 1.0);
+        const double b2 = 8.0 * m2 * (m2 + 1.0) / 2.0 + 2.0 * m2 * ldk * np;
+        const int la_sms = lookahead_sms(m2, kb);
+        if (m2 > 0 && la && la_sms > 0) {
+            cudaEventRecord(la->fork, s);
+            cudaStreamWaitEvent(la->s, la->fork, 0);
+            slot = gb300_prof_begin(la->s, GB300_PROF_TC_UPDATE);
+            gb300_prof_set_share(slot, (double)(num_sms() - la_sms) / num_sms());
+            rc = tc_update(la->s, m2, m2, kb, hi2, lo2, ldk, hi2, lo2, ldk, nterms, 1, C22, lda, d_err, 0,
+                           num_sms() - la_sms);
+            gb300_prof_end(la->s, slot, f2, b2);
+            cudaEventRecord(la->join, la->s);
+            if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, la_sms);
+            cudaStreamWaitEvent(s, la->join, 0);  // joined before step k+1's update
         } else {
-            potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
-            if (m > 0) trtri_lower<float>(s, kb, Akk, lda, linv, ldk, w.scratch);
+            if (m2 > 0) {
+                slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
+                rc = tc_update(s, m2, m2, kb, hi2, lo2, ldk, hi2, lo2, ldk, nterms, 1, C22, lda, d_err);
+                gb300_prof_end(s, slot, f2, b2);
+            }
+            if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, 0);
         }
-        if (rc) return rc;
-        if (m <= 0) {
-            gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0, 4.0 * kb * kb);
-            break;
-        }
-        float *P = A + (k0 + kb) + (long)k0 * lda;
-        rc = split_bf16(s, kb, kb, linv, ldk, w.ihi, w.ilo, ldk);
-        if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, w.lo, ldk);
-        if (!rc) rc = tc_update(s, m, kb, kb, w.hi, w.lo, ldk, w.ihi, w.ilo, ldk, 3, 0, P, lda, d_err, 1);
-        if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi, np > 1 ? w.lo : nullptr, ldk);
-        // algorithmic work of the panel: POTRF kb^3/3 + TRSM m kb^2; bytes: the
-        // tile and the panel read and written once, the BF16 panel written
-        gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0 + (double)m * kb * kb,
-                       8.0 * kb * kb + 8.0 * m * kb + 2.0 * m * ldk * np);
-        if (rc) return rc;
-        slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
-        rc = tc_update(s, m, m, kb, w.hi, w.lo, ldk, w.hi, w.lo, ldk, nterms, 1, A + (k0 + kb) + (long)(k0 + kb) * lda,
-                       lda, d_err);
-        // algorithmic work: the lower triangle (incl. diagonal) of an m x m rank-kb update per term;
-        // bytes: C lower read + write in FP32 plus one read of each BF16 panel
-        gb300_prof_end(s, slot, (double)nterms * kb * (double)m * (m + 1.0),
-                       8.0 * m * (m + 1.0) / 2.0 + 2.0 * m * ldk * np);
-        if (rc) return rc;
+        buf = nbuf;
     }
+    if (rc) return rc;
     return gb300_last_launch_status();
 }
 

@@ -17,6 +17,7 @@ struct ProfRec {
     cudaEvent_t e0, e1;
     int kind;
     double flops, bytes;
+    double sm_share;  // fraction of the SMs the launch's grid was limited to
 };
 std::mutex g_prof_mu;
 bool g_prof_on = false;
@@ -25,6 +26,7 @@ std::vector<cudaEvent_t> g_event_pool;
 struct ProfAgg {
     unsigned long long launches = 0;
     double ms = 0, flops = 0, bytes = 0;
+    double share_ms = 0;  // sum of time x SM share
 } g_prof_agg[GB300_PROF_KINDS];
 
 cudaEvent_t pool_get()
@@ -50,6 +52,7 @@ void resolve_locked()
         a.ms += ms;
         a.flops += r.flops;
         a.bytes += r.bytes;
+        a.share_ms += ms * r.sm_share;
         g_event_pool.push_back(r.e0);
         g_event_pool.push_back(r.e1);
     }
@@ -66,6 +69,7 @@ extern "C" int gb300_prof_begin(cudaStream_t s, int kind)
     r.e1 = pool_get();
     r.kind = kind;
     r.flops = r.bytes = 0;
+    r.sm_share = 1.0;
     cudaEventRecord(r.e0, s);
     g_prof_pending.push_back(r);
     return (int)g_prof_pending.size() - 1;
@@ -79,6 +83,13 @@ extern "C" void gb300_prof_end(cudaStream_t s, int slot, double flops, double by
     r.flops = flops;
     r.bytes = bytes;
     cudaEventRecord(r.e1, s);
+}
+
+extern "C" void gb300_prof_set_share(int slot, double sm_share)
+{
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    if (slot < 0 || slot >= (int)g_prof_pending.size()) return;
+    g_prof_pending[slot].sm_share = sm_share;
 }
 
 extern "C" int gb300_record_cuda_error(cudaError_t e)
@@ -168,6 +179,16 @@ int starpu_gb300_profiling_get(int kind, unsigned long long *launches, double *t
     if (total_ms) *total_ms = g_prof_agg[kind].ms;
     if (flops) *flops = g_prof_agg[kind].flops;
     if (bytes) *bytes = g_prof_agg[kind].bytes;
+    return GB300_OK;
+}
+
+int starpu_gb300_profiling_sm_share(int kind, double *share)
+{
+    if (kind < 0 || kind >= GB300_PROF_KINDS || !share) return GB300_EINVAL;
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    resolve_locked();
+    const ProfAgg &a = g_prof_agg[kind];
+    *share = a.ms > 0 ? a.share_ms / a.ms : 1.0;
     return GB300_OK;
 }
 

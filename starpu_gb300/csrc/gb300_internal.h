@@ -66,3 +66,5 @@ enum gb300_prof_kind { GB300_PROF_TC_UPDATE = 0, GB300_PROF_PANEL = 1, GB300_PRO
                        GB300_PROF_BATCHED = 4, GB300_PROF_TRANSFER = 5, GB300_PROF_KINDS = 6 };
 extern "C" int gb300_prof_begin(cudaStream_t s, int kind);
 extern "C" void gb300_prof_end(cudaStream_t s, int slot, double algorithmic_flops, double algorithmic_bytes);
+// the fraction of the SMs a profiled launch was limited to (default 1)
+extern "C" void gb300_prof_set_share(int slot, double sm_share);

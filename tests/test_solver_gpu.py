@@ -176,8 +176,11 @@ def test_profiling_counts_kernel_classes(gpu, oracle):
     assert gpu.starpu_gb300_launch_count() > c0
     launches, ms, fl = C.c_ulonglong(), C.c_double(), C.c_double()
     gpu.starpu_gb300_profiling_get(0, C.byref(launches), C.byref(ms), C.byref(fl), None)
-    assert launches.value == n // nb - 1 and ms.value > 0
-    expected = sum(3 * nb * (n - (k + 1) * nb) * (n - (k + 1) * nb + 1.0) for k in range(n // nb - 1))
+    # per step with rows below the diagonal tile: the next column block, then
+    # (when rows remain beyond it) the trailing triangle
+    steps = n // nb - 1
+    assert launches.value == steps + (steps - 1) and ms.value > 0
+    expected = sum(3 * nb * (n - (k + 1) * nb) * (n - (k + 1) * nb + 1.0) for k in range(steps))
     assert abs(fl.value - expected) <= 1e-9 * expected
 
 
