@@ -180,6 +180,33 @@ def cpu_sample(n: int, nb: int, nrhs: int, reps: int, seed: int = 7):
             "backward_error": berr, "seconds_per_solve": t}
 
 
+def cpu_config1(reps: int = 3):
+    """The reference's CPU-runnable configuration: plain FP32 tiled Cholesky,
+    N=2048, 8x8 tiles of 256, A_ij = 1/(i+j+1) + N delta_ij (the input of
+    examples/cholesky/cholesky_implicit.c:477-484), through the port of the CPU
+    codelets on all host cores; GFLOP/s with FLOPS_SPOTRF (cholesky.h:95) and
+    the reference's reconstruction check (max relative error <= 1e-4)."""
+    from oracle import oracle as O
+    if not O.cpu_init():
+        return None
+    n, nblocks = 2048, 8
+    cores = len(os.sched_getaffinity(0))
+    O.lib().cpu_chol_set_blas_threads(cores)
+    A = O.hilbert_f32(n)
+    times, ok, err = [], None, None
+    for _ in range(reps):
+        L = A.copy(order="F")
+        t0 = time.perf_counter()
+        info = O.cpu_potrf_tiled(L, nblocks, cores)
+        times.append(time.perf_counter() - t0)
+        assert info == 0
+        ok, err = O.check_hilbert(L)
+    t = min(times)
+    return {"workload": "plain FP32 tiled Cholesky, N=2048, 8x8 tiles of 256, Hilbert + N*I", "cores": cores,
+            "kind": "port", "gflops": O.flops_potrf(n) / t / 1e9, "ms": t * 1e3, "check_ok": bool(ok == 0),
+            "max_rel_err": err, "best_of": reps}
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -601,6 +628,8 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(args.cpu_n, args.cpu_nb, nrhs, 2)
+        if cpu is not None:
+            cpu["config1"] = cpu_config1()
 
     if rank == 0:
         fp64_same = next((f for f in fp64 if f["n"] == n), None)
