@@ -236,6 +236,12 @@ int starpu_gb300_profiling_get(int kind, unsigned long long *launches, double *t
  * to (1 unless a launch shared the GPU by design: the trailing updates that
  * run beside the next panel leave that panel's SMs free). */
 int starpu_gb300_profiling_sm_share(int kind, double *share);
+/* Per-launch start and end times (ms, relative to the first profiled launch
+ * after a reset; events on each launch's own stream, so overlapping launches
+ * show as overlapping spans), the counterpart of the start / end times of
+ * StarPU's per-task profiling information.  Fills up to `max` entries in
+ * profiling order and returns how many are recorded (at most 65536). */
+int starpu_gb300_profiling_timeline(int max, int *kinds, double *start_ms, double *end_ms);
 
 #ifdef __cplusplus
 }

@@ -440,10 +440,12 @@ static void correction_solve(cudaStream_t s, int n, int nrhs, int nb, const Solv
     else potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
 }
 
-// A side stream and a fork / join event pair per host thread and device: the
-// factor phase runs the passes that only read A (the residual's digit slices,
-// the infinity norm) beside the factorisation of W, which leaves most of the
-// GPU idle while its diagonal tiles are factored.
+// Streams and fork / join event pairs per host thread and device.  The
+// factor phase runs the factorisation of W on a high-priority stream and the
+// passes that only read A (the residual's digit slices, the infinity norm) on
+// a lowest-priority side stream: the side work then takes only the SMs the
+// factorisation leaves idle (its diagonal tiles are latency-bound) instead of
+// holding the GPU while the first diagonal tile waits.
 struct SideStream {
     int dev = -1;
     cudaStream_t s = nullptr;
@@ -456,17 +458,25 @@ struct SideStream {
     }
 };
 
-static SideStream *side_stream()
+// which = 0: the lowest-priority side stream; 1: the factorisation's stream,
+// one priority level below the top (the top is kept for the trailing updates
+// that run beside a panel)
+static SideStream *aux_stream(int which)
 {
-    thread_local SideStream ss[16];
+    thread_local SideStream ss[2][16];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return nullptr;
-    SideStream &x = ss[dev];
+    SideStream &x = ss[which][dev];
     if (!x.s) {
-        if (cudaStreamCreateWithFlags(&x.s, cudaStreamNonBlocking) != cudaSuccess ||
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        const int prio = which == 0 ? least : std::min(least, greatest + 1);
+        if (cudaStreamCreateWithPriority(&x.s, cudaStreamNonBlocking, prio) != cudaSuccess ||
             cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
             return nullptr;
+        }
         x.dev = dev;
     }
     return &x;
@@ -478,16 +488,19 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
     gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
     // the residuals' slices of A and ||A||_inf, beside the factorisation
-    SideStream *ss = side_stream();
-    if (!ss) return gb300_record_cuda_error(cudaGetLastError());
+    SideStream *ss = aux_stream(0), *fs = aux_stream(1);
+    if (!ss || !fs) return gb300_record_cuda_error(cudaGetLastError());
     cudaEventRecord(ss->fork, s);
     cudaStreamWaitEvent(ss->s, ss->fork, 0);
+    cudaStreamWaitEvent(fs->s, ss->fork, 0);
     int rc = residual_tc_slice_a(ss->s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum);
     gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, ss->s>>>(n, (n + 63) / 64, ws.rowsum,
                                                                                        ws.anorm_bits + 2, ws.anorm_bits);
     cudaEventRecord(ss->join, ss->s);
-    if (!rc) rc = potrf_tc(s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
-    cudaStreamWaitEvent(s, ss->join, 0);  // joined before anything reads the slices or the norm
+    if (!rc) rc = potrf_tc(fs->s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
+    cudaEventRecord(fs->join, fs->s);
+    cudaStreamWaitEvent(s, fs->join, 0);
+    cudaStreamWaitEvent(s, ss->join, 0);  // joined before anything reads the factor, the slices or the norm
     if (rc) return rc;
     if (!ws.band) potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
     return gb300_last_launch_status();

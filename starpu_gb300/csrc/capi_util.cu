@@ -1,5 +1,6 @@
 // Error reporting and device-memory helpers of the C-ABI.
 #include "gb300_internal.h"
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <stdio.h>
@@ -41,12 +42,31 @@ cudaEvent_t pool_get()
     return e;
 }
 
+// per-launch timeline (start / end relative to the first launch after a
+// reset), kept for the last kMaxTimeline launches
+struct ProfSpan {
+    int kind;
+    double start_ms, end_ms;
+};
+constexpr size_t kMaxTimeline = 1 << 16;
+std::vector<ProfSpan> g_prof_timeline;
+cudaEvent_t g_prof_origin = nullptr;  // e0 of the first launch after a reset (kept out of the pool)
+
 void resolve_locked()
 {
     for (auto &r : g_prof_pending) {
         cudaEventSynchronize(r.e1);
         float ms = 0;
         cudaEventElapsedTime(&ms, r.e0, r.e1);
+        if (!g_prof_origin) {
+            g_prof_origin = r.e0;
+            r.e0 = pool_get();  // the pool gets a fresh event in place of the kept one
+        }
+        if (g_prof_timeline.size() < kMaxTimeline) {
+            float t0 = 0;
+            if (r.e0 != nullptr) cudaEventElapsedTime(&t0, g_prof_origin, r.e1);
+            g_prof_timeline.push_back({r.kind, (double)t0 - ms, (double)t0});
+        }
         auto &a = g_prof_agg[r.kind];
         a.launches++;
         a.ms += ms;
@@ -168,6 +188,25 @@ void starpu_gb300_profiling_reset(void)
     std::lock_guard<std::mutex> g(g_prof_mu);
     resolve_locked();
     for (auto &a : g_prof_agg) a = ProfAgg();
+    g_prof_timeline.clear();
+    if (g_prof_origin) {
+        g_event_pool.push_back(g_prof_origin);
+        g_prof_origin = nullptr;
+    }
+}
+
+int starpu_gb300_profiling_timeline(int max, int *kinds, double *start_ms, double *end_ms)
+{
+    if (max < 0) return GB300_EINVAL;
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    resolve_locked();
+    const int n = (int)std::min((size_t)max, g_prof_timeline.size());
+    for (int i = 0; i < n; ++i) {
+        if (kinds) kinds[i] = g_prof_timeline[i].kind;
+        if (start_ms) start_ms[i] = g_prof_timeline[i].start_ms;
+        if (end_ms) end_ms[i] = g_prof_timeline[i].end_ms;
+    }
+    return (int)g_prof_timeline.size();
 }
 
 int starpu_gb300_profiling_get(int kind, unsigned long long *launches, double *total_ms, double *flops, double *bytes)

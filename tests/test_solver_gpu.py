@@ -182,6 +182,21 @@ def test_profiling_counts_kernel_classes(gpu, oracle):
     assert launches.value == steps + (steps - 1) and ms.value > 0
     expected = sum(3 * nb * (n - (k + 1) * nb) * (n - (k + 1) * nb + 1.0) for k in range(steps))
     assert abs(fl.value - expected) <= 1e-9 * expected
+    share = C.c_double()
+    check(gpu.starpu_gb300_profiling_sm_share(0, C.byref(share)))
+    assert 0.0 < share.value <= 1.0
+    # the per-launch timeline: one span per profiled launch of every class
+    total = 0
+    for kind in range(6):
+        la = C.c_ulonglong()
+        gpu.starpu_gb300_profiling_get(kind, C.byref(la), None, None, None)
+        total += la.value
+    cnt = gpu.starpu_gb300_profiling_timeline(0, None, None, None)
+    assert cnt == total
+    K, S, E = (C.c_int * cnt)(), (C.c_double * cnt)(), (C.c_double * cnt)()
+    assert gpu.starpu_gb300_profiling_timeline(cnt, K, S, E) == cnt
+    assert sum(1 for k in K if k == 0) == launches.value
+    assert all(e >= s for s, e in zip(S, E)) and min(S) > -0.01 and max(E) > 0
 
 
 def inv_tile_band(L32, nb):
