@@ -66,20 +66,39 @@ __global__ void __launch_bounds__(256) convert_lower_max_kernel(int n, const dou
     const double *a = A + j * lda;
     float *w = W ? W + j * ldw : nullptr;
     unsigned long long m = 0;
-    long i = j + threadIdx.x;
-    for (; i + 256 < n; i += 512) {
-        const double v0 = a[i], v1 = a[i + 256];
-        m = max(m, (unsigned long long)__double_as_longlong(v0) & 0x7FFFFFFFFFFFFFFFull);
-        m = max(m, (unsigned long long)__double_as_longlong(v1) & 0x7FFFFFFFFFFFFFFFull);
-        if (w) {
-            w[i] = (float)v0;
-            w[i + 256] = (float)v1;
-        }
-    }
-    if (i < n) {
-        const double v = a[i];
+    auto take = [&](long i, double v) {
         m = max(m, (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull);
         if (w) w[i] = (float)v;
+    };
+    long i0 = j;
+    // one element first when the column's lower part starts off a 16-byte boundary
+    if (i0 < n && ((uintptr_t)(a + i0) & 15)) {
+        if (threadIdx.x == 0) take(i0, a[i0]);
+        ++i0;
+    }
+    const bool vec = !((uintptr_t)(a + i0) & 15) && (!w || !((uintptr_t)(w + i0) & 7));
+    if (vec) {
+        // 16-byte loads, four in flight per thread: the conversion streams A at
+        // the HBM rate instead of waiting on one load at a time
+        const double2 *a2 = (const double2 *)(a + i0);
+        float2 *w2 = w ? (float2 *)(w + i0) : nullptr;
+        const long n2 = (n - i0) / 2;
+        for (long p = threadIdx.x; p < n2; p += 4 * 256) {
+            double2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (p + u * 256 < n2) v[u] = __ldcs(a2 + p + u * 256);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (p + u * 256 >= n2) break;
+                m = max(m, (unsigned long long)__double_as_longlong(v[u].x) & 0x7FFFFFFFFFFFFFFFull);
+                m = max(m, (unsigned long long)__double_as_longlong(v[u].y) & 0x7FFFFFFFFFFFFFFFull);
+                if (w2) w2[p + u * 256] = make_float2((float)v[u].x, (float)v[u].y);
+            }
+        }
+        if (((n - i0) & 1) && threadIdx.x == 0) take(n - 1, a[n - 1]);
+    } else {
+        for (long i = i0 + threadIdx.x; i < n; i += 256) take(i, a[i]);
     }
     for (int o = 16; o > 0; o >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)m, o));
     __shared__ unsigned long long red[8];
