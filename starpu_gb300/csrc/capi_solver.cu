@@ -11,6 +11,7 @@
 // until every right-hand side meets `tol` or `max_iter` corrections ran.
 // FP64 is used only for A, the residual and the solution accumulation.
 #include <algorithm>
+#include <functional>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -26,7 +27,7 @@
 namespace gb300 {
 
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err,
-             float *linv_band);
+             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows);
 
 // One CTA per column j of A: writes the lower part of column j to W in FP32
 // and folds sum_i |A_ij| (= row sum of the symmetric A) into *anorm.
@@ -501,22 +502,44 @@ static SideStream *aux_stream(int which)
     return &x;
 }
 
+// Rows of the trailing triangle below which the slicing of A starts beside
+// the factorisation (GB300_SLICE_ROWS; default n/2, measured at n = 32768:
+// from the first step 77.3 ms per solve, from 16384 rows 76.8, from 10240
+// 76.7, from 6144 78.1, after the factorisation 80.3).
+static int slice_rows(int n)
+{
+    static int v = -2;
+    if (v == -2) {
+        const char *e = getenv("GB300_SLICE_ROWS");
+        v = e && *e ? atoi(e) : -1;
+    }
+    return v < 0 ? n / 2 : v;
+}
+
 static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws)
 {
     // anorm_bits[0] = ||A||_inf, [1] = info + err, [2] = max |A_ij|
     cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
     gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
-    // the residuals' slices of A and ||A||_inf, beside the factorisation
+    // the residuals' slices of A and ||A||_inf, beside the factorisation: on
+    // the lowest-priority side stream, started once the factorisation's steps
+    // become bound by their diagonal tiles (trailing triangles of at most
+    // slice_rows rows) and leave most of the GPU idle
     SideStream *ss = aux_stream(0), *fs = aux_stream(1);
     if (!ss || !fs) return gb300_record_cuda_error(cudaGetLastError());
-    cudaEventRecord(ss->fork, s);
-    cudaStreamWaitEvent(ss->s, ss->fork, 0);
-    cudaStreamWaitEvent(fs->s, ss->fork, 0);
-    int rc = residual_tc_slice_a(ss->s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum);
-    gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, ss->s>>>(n, (n + 63) / 64, ws.rowsum,
-                                                                                       ws.anorm_bits + 2, ws.anorm_bits);
-    cudaEventRecord(ss->join, ss->s);
-    if (!rc) rc = potrf_tc(fs->s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band);
+    cudaEventRecord(fs->fork, s);
+    cudaStreamWaitEvent(fs->s, fs->fork, 0);
+    int side_rc = 0;
+    auto slice = [&](cudaStream_t from) {
+        cudaEventRecord(ss->fork, from);
+        cudaStreamWaitEvent(ss->s, ss->fork, 0);
+        side_rc = residual_tc_slice_a(ss->s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum);
+        gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, ss->s>>>(
+            n, (n + 63) / 64, ws.rowsum, ws.anorm_bits + 2, ws.anorm_bits);
+        cudaEventRecord(ss->join, ss->s);
+    };
+    int rc = potrf_tc(fs->s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band, slice, slice_rows(n));
+    if (!rc) rc = side_rc;
     cudaEventRecord(fs->join, fs->s);
     cudaStreamWaitEvent(s, fs->join, 0);
     cudaStreamWaitEvent(s, ss->join, 0);  // joined before anything reads the factor, the slices or the norm

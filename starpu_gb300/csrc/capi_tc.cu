@@ -5,6 +5,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <functional>
 #include <mutex>
 #include <stdio.h>
 
@@ -259,21 +260,27 @@ static LookaheadStream *lookahead_stream()
 // SMs the panel of step k+1 keeps while step k's trailing update runs on the
 // others.  GB300_LOOKAHEAD_SMS fixes the count (0 runs the steps one after the
 // other); by default it is chosen per step to balance the two: the update's
-// 3 m2^2 kb flops on the remaining SMs against the panel's latency-bound
-// diagonal tile (about 0.75 ms) plus its 6 m2 kb^2 TRSM flops, both at the
-// split-BF16 tensor rate measured for this kernel (1.45 PFLOP/s on the whole GPU).
+// 3 m2^2 kb flops on the remaining SMs, at the split-BF16 tensor rate measured
+// for this kernel (1.45 PFLOP/s on the whole GPU), against the panel's
+// latency-bound diagonal tile (about 0.75 ms) plus its 6 m2 kb^2 TRSM flops
+// and the panel splits, which together run at a fraction of that rate per SM
+// (GB300_PANEL_RATE, default 0.4: the per-step timeline of the n = 32768
+// solve gives 2.02 ms for a 27648-row panel on 38 SMs).
 static int lookahead_sms(int m2, int kb)
 {
     static int fixed = -2;
+    static double panel_rate = 0.4;
     if (fixed == -2) {
         const char *e = getenv("GB300_LOOKAHEAD_SMS");
         fixed = e && *e ? std::max(0, atoi(e)) : -1;
+        const char *r = getenv("GB300_PANEL_RATE");
+        if (r && *r && atof(r) > 0.0) panel_rate = atof(r);
     }
     const int S = num_sms();
     if (fixed >= 0) return fixed >= S ? 0 : fixed;
     if (S < 32 || m2 <= 0) return 0;
     const double R = 1.45e15 / S, t_diag = 0.75e-3;
-    const double f_upd = 3.0 * m2 * (double)m2 * kb, f_trsm = 6.0 * m2 * (double)kb * kb;
+    const double f_upd = 3.0 * m2 * (double)m2 * kb, f_trsm = 6.0 * m2 * (double)kb * kb / panel_rate;
     // below about a quarter of the GPU the diagonal-tile kernel itself slows down
     int best = S / 4;
     double best_t = 1e30;
@@ -336,9 +343,14 @@ static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb,
 // and read different panel buffers; the streams join before step k+1's
 // update.  The diagonal-tile factorisation, latency-bound on a few SMs, thus
 // hides behind the trailing update.
+// `side(s)`, when given, is called once, from the loop, when the step whose
+// trailing triangle first has at most `side_rows` rows has been enqueued: the
+// caller starts work that only needs the GPU's idle resources there (the
+// steps from then on are bound by their latency-bound diagonal tiles).
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err,
-             float *linv_band)
+             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows)
 {
+    bool side_done = !side;
     const long ldk = ((long)nb + 63) / 64 * 64;
     TcWs w;
     tc_ws_layout(n, nb, work, &w);
@@ -393,7 +405,12 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
             if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, 0);
         }
         buf = nbuf;
+        if (!side_done && m2 <= side_rows) {
+            side(s);
+            side_done = true;
+        }
     }
+    if (!side_done) side(s);
     if (rc) return rc;
     return gb300_last_launch_status();
 }
@@ -515,7 +532,7 @@ int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int n
     cudaStream_t s = (cudaStream_t)stream;
     if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), s);
     if (!n) return GB300_OK;
-    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr);
+    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr, {}, 0);
 }
 
 } // extern "C"
