@@ -27,7 +27,27 @@
 namespace gb300 {
 
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err,
-             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows);
+             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows,
+             const std::function<void(cudaStream_t, int, int)> &on_panel);
+
+// W(c, r) = W(r, c) for the rows r in [r0, n) below the column block
+// [c0, c0 + w): the strictly upper part of W then holds L^T outside the
+// diagonal tiles, which the backward sweeps read column by column like the
+// forward ones.  32 x 32 tiles transposed through shared memory.
+__global__ void mirror_block_kernel(int n, int c0, int w, int r0, float *W, long ldw)
+{
+    __shared__ float t[32][33];
+    const int rb = r0 + blockIdx.x * 32, cb = c0 + blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = rb + threadIdx.x, c = cb + y;
+        if (r < n && c < c0 + w) t[y][threadIdx.x] = W[r + (long)c * ldw];
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = rb + y, c = cb + threadIdx.x;
+        if (r < n && c < c0 + w) W[c + (long)r * ldw] = t[threadIdx.x][y];
+    }
+}
 
 // One CTA per column j of A: writes the lower part of column j to W in FP32
 // and folds sum_i |A_ij| (= row sum of the symmetric A) into *anorm.
@@ -358,7 +378,7 @@ static bool tile_sweep_ok(int nb) { return nb > 0 && nb % TSW_SLAB == 0 && nb <=
 // (ld ldk, tile T at band + T * ldk * ldk): one launch per sweep and group
 // of 16 right-hand sides.
 static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L, long ldl, const float *band, long ldk,
-                        float *Y, long ldy, float *Z, int *cnt, int *err)
+                        float *Y, long ldy, float *Z, int *cnt, int *err, int upper = 0)
 {
     if (n <= 0 || nrhs <= 0) return;
     TileSweepArgs a;
@@ -377,6 +397,7 @@ static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L,
     a.ycount = cnt + a.ntiles;
     a.ticket = (unsigned *)(cnt + 2 * a.ntiles);
     a.err = err;
+    a.upper = upper;
     a.budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
     a.vec = al(L) && al(band) && al(Y) && al(Z) && ldl % 4 == 0 && ldk % 4 == 0 && ldy % 4 == 0 && n % 4 == 0;
@@ -456,7 +477,8 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
 static void correction_solve(cudaStream_t s, int n, int nrhs, int nb, const SolverWs &ws)
 {
     const long ldk = ((long)nb + 63) / 64 * 64;
-    if (ws.band) tile_sweeps(s, n, nrhs, nb, ws.W, n, ws.band, ldk, ws.Y, n, ws.Z, ws.cnt, ws.err);
+    // the factor phase mirrors L^T into W's strictly upper part (outside the diagonal tiles)
+    if (ws.band) tile_sweeps(s, n, nrhs, nb, ws.W, n, ws.band, ldk, ws.Y, n, ws.Z, ws.cnt, ws.err, 1);
     else potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
 }
 
@@ -478,19 +500,20 @@ struct SideStream {
     }
 };
 
-// which = 0: the lowest-priority side stream; 1: the factorisation's stream,
-// one priority level below the top (the top is kept for the trailing updates
-// that run beside a panel)
+// which = 0: the lowest-priority side stream of the slicing; 1: the
+// factorisation's stream, one priority level below the top (the top is kept
+// for the trailing updates that run beside a panel); 2: the lowest-priority
+// stream that mirrors each finished column block of L into W's upper part
 static SideStream *aux_stream(int which)
 {
-    thread_local SideStream ss[2][16];
+    thread_local SideStream ss[3][16];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return nullptr;
     SideStream &x = ss[which][dev];
     if (!x.s) {
         int least = 0, greatest = 0;
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
-        const int prio = which == 0 ? least : std::min(least, greatest + 1);
+        const int prio = which == 1 ? std::min(least, greatest + 1) : least;
         if (cudaStreamCreateWithPriority(&x.s, cudaStreamNonBlocking, prio) != cudaSuccess ||
             cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming) != cudaSuccess) {
@@ -525,8 +548,8 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
     // the lowest-priority side stream, started once the factorisation's steps
     // become bound by their diagonal tiles (trailing triangles of at most
     // slice_rows rows) and leave most of the GPU idle
-    SideStream *ss = aux_stream(0), *fs = aux_stream(1);
-    if (!ss || !fs) return gb300_record_cuda_error(cudaGetLastError());
+    SideStream *ss = aux_stream(0), *fs = aux_stream(1), *ms = aux_stream(2);
+    if (!ss || !fs || !ms) return gb300_record_cuda_error(cudaGetLastError());
     cudaEventRecord(fs->fork, s);
     cudaStreamWaitEvent(fs->s, fs->fork, 0);
     int side_rc = 0;
@@ -538,8 +561,24 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
             n, (n + 63) / 64, ws.rowsum, ws.anorm_bits + 2, ws.anorm_bits);
         cudaEventRecord(ss->join, ss->s);
     };
-    int rc = potrf_tc(fs->s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band, slice, slice_rows(n));
+    // each finished column block of L mirrored into W's upper part, for the backward sweeps
+    bool mirrored = false;
+    auto mirror = [&](cudaStream_t from, int c0, int w) {
+        const int r0 = c0 + w;
+        if (!ws.band || r0 >= n) return;
+        cudaEventRecord(ms->fork, from);
+        cudaStreamWaitEvent(ms->s, ms->fork, 0);
+        const dim3 g((unsigned)((n - r0 + 31) / 32), (unsigned)((w + 31) / 32));
+        gb300_count_launch(), mirror_block_kernel<<<g, dim3(32, 8), 0, ms->s>>>(n, c0, w, r0, ws.W, n);
+        mirrored = true;
+    };
+    int rc = potrf_tc(fs->s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band, slice, slice_rows(n),
+                      mirror);
     if (!rc) rc = side_rc;
+    if (mirrored) {
+        cudaEventRecord(ms->join, ms->s);
+        cudaStreamWaitEvent(s, ms->join, 0);
+    }
     cudaEventRecord(fs->join, fs->s);
     cudaStreamWaitEvent(s, fs->join, 0);
     cudaStreamWaitEvent(s, ss->join, 0);  // joined before anything reads the factor, the slices or the norm

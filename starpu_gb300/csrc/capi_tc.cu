@@ -347,8 +347,12 @@ static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb,
 // trailing triangle first has at most `side_rows` rows has been enqueued: the
 // caller starts work that only needs the GPU's idle resources there (the
 // steps from then on are bound by their latency-bound diagonal tiles).
+// `on_panel(s, k0, kb)`, when given, is called after each panel whose
+// column block [k0, k0 + kb) has rows below its diagonal tile has been
+// enqueued: that block of the factor is final from then on.
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err,
-             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows)
+             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows,
+             const std::function<void(cudaStream_t, int, int)> &on_panel)
 {
     bool side_done = !side;
     const long ldk = ((long)nb + 63) / 64 * 64;
@@ -359,6 +363,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
     LookaheadStream *la = n > 2 * nb ? lookahead_stream() : nullptr;
     int buf = 0;
     int rc = panel_step(s, n, A, lda, 0, std::min(nb, n), nb, np, w, buf, linv_band, d_info, d_err, 0);
+    if (!rc && on_panel && n > nb) on_panel(s, 0, nb);
     for (int k0 = 0; k0 < n && !rc; k0 += nb) {
         const int kb = std::min(nb, n - k0);
         const int m = n - k0 - kb;
@@ -395,6 +400,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
             gb300_prof_end(la->s, slot, f2, b2);
             cudaEventRecord(la->join, la->s);
             if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, la_sms);
+            if (!rc && on_panel) on_panel(s, k0 + kb, kb1);
             cudaStreamWaitEvent(s, la->join, 0);  // joined before step k+1's update
         } else {
             if (m2 > 0) {
@@ -403,6 +409,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
                 gb300_prof_end(s, slot, f2, b2);
             }
             if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, 0);
+            if (!rc && on_panel && m2 > 0) on_panel(s, k0 + kb, kb1);
         }
         buf = nbuf;
         if (!side_done && m2 <= side_rows) {
@@ -532,7 +539,7 @@ int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int n
     cudaStream_t s = (cudaStream_t)stream;
     if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), s);
     if (!n) return GB300_OK;
-    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr, {}, 0);
+    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr, {}, 0, {});
 }
 
 } // extern "C"

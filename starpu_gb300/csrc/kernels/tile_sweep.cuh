@@ -51,6 +51,10 @@ struct TileSweepArgs {
     int *err;
     unsigned long long budget_ns;
     int vec;  // L, Dinv, B, Z and their leading dimensions allow 16-byte loads
+    // backward sweep: 1 when the strictly upper part of L's storage holds L^T
+    // outside the diagonal tiles (L(j, i) also at (i, j)), so the slab's rows
+    // of L^T are read column by column like the forward sweep's operands
+    int upper;
 };
 
 __device__ __forceinline__ int tsw_ld_acquire(const int *p)
@@ -330,10 +334,11 @@ __global__ void __launch_bounds__(TSW_T) tile_sweep_kernel(TileSweepArgs a)
     const int jbeg = TRANS ? a.ntiles - 1 : 0, jend = TRANS ? T : T, jstep = TRANS ? -1 : 1;
     for (int j = jbeg; j != jend; j += jstep) {
         const int j0 = j * a.nb, kbj = min(a.nb, a.n - j0);
-        if (!TRANS) tsw_prefetch_l2<false>(a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, kbj);
+        const bool direct = !TRANS || a.upper;  // operand read as rows of 32 per column
+        if (direct) tsw_prefetch_l2<false>(a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, kbj);
         else tsw_prefetch_l2<true>(a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, kbj);
         tsw_wait(a, &a.ycount[j], (kbj + TSW_SLAB - 1) / TSW_SLAB, &s_skip);
-        if (!TRANS) tsw_product<false>(acc, a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
+        if (direct) tsw_product<false>(acc, a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
         else tsw_product<true>(acc, a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
     }
     tsw_reduce(acc, red, zs);

@@ -31,6 +31,27 @@ def solve(gpu, A, B, nb, nterms, tol=1e-12, max_iter=30):
     return rc, info, X
 
 
+@pytest.mark.parametrize("n,nb", [(1000, 256), (2048, 512)])
+def test_factor_mirrors_lt_into_upper_part(gpu, oracle, n, nb):
+    """After the mixed solve the workspace's FP32 factor W (its first n x n
+    floats) holds L below the diagonal and, outside the diagonal tiles, L^T
+    above it: the backward sweeps read that copy."""
+    A = oracle.spd_gram(n, 41, oracle.alpha_for_kappa(1e3))
+    B = oracle.uniform_rhs(n, 2, 42)
+    dA, dB = DeviceBuffer.from_array(A), DeviceBuffer.from_array(B)
+    dX = DeviceBuffer(n * 2 * 8)
+    lw = gpu.starpu_gb300_dsposv_workspace(n, 2, nb)
+    W = DeviceBuffer(lw)
+    info = IrInfo()
+    rc = gpu.starpu_gb300_dsposv(None, n, 2, dA.ptr, n, dB.ptr, n, dX.ptr, n, nb, 3, 1e-12, 30, W.ptr, lw,
+                                 C.byref(info))
+    assert rc == 0
+    Wf = W.download((n * n,), np.float32).reshape((n, n), order="F")
+    tile = np.arange(n) // nb
+    below = tile[:, None] > tile[None, :]          # (r, c) strictly below the diagonal tiles
+    np.testing.assert_array_equal(Wf.T[below], Wf[below])
+
+
 # plain BF16 (nterms=1, u ~ 4e-3) only refines when kappa * u < 1: kappa = 1e2
 @pytest.mark.parametrize("kappa,nterms", [(1e2, 3), (1e4, 3), (1e2, 1)])
 def test_dsposv_reaches_fp64_backward_error(gpu, oracle, kappa, nterms):
