@@ -539,11 +539,16 @@ static int slice_rows(int n)
     return v < 0 ? n / 2 : v;
 }
 
-static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws)
+// prepared: W and max |A_ij| were written while A was gathered from the host
+// (gather_convert_kernel), the first pass is skipped
+static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws,
+                        bool prepared)
 {
     // anorm_bits[0] = ||A||_inf, [1] = info + err, [2] = max |A_ij|
-    cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
-    gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
+    if (!prepared) {
+        cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
+        gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
+    }
     // the residuals' slices of A and ||A||_inf, beside the factorisation: on
     // the lowest-priority side stream, started once the factorisation's steps
     // become bound by their diagonal tiles (trailing triangles of at most
@@ -592,12 +597,20 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
 // sweeps use.  Synchronises once to read the factorisation status.  The
 // workspace then holds everything a later refine phase needs, so a factor can
 // be kept on the device and reused for new right-hand sides.
-int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
-                  starpu_gb300_ir_info *out)
+void dsposv_prepared_targets(int n, int nrhs, int nb, void *work, float **W, unsigned long long **amax_block)
 {
     SolverWs ws;
     layout(n, nrhs, nb, work, &ws);
-    int rc = factor_phase(s, n, nb, nterms, A, lda, ws);
+    *W = ws.W;
+    *amax_block = ws.anorm_bits;
+}
+
+int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
+                  starpu_gb300_ir_info *out, bool prepared)
+{
+    SolverWs ws;
+    layout(n, nrhs, nb, work, &ws);
+    int rc = factor_phase(s, n, nb, nterms, A, lda, ws, prepared);
     int hinfo[2] = {0, 0};
     if (!rc) rc = gb300_record_cuda_error(cudaMemcpyAsync(hinfo, ws.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     if (!rc) rc = gb300_record_cuda_error(cudaStreamSynchronize(s));
@@ -767,26 +780,62 @@ void *starpu_gb300_solver_stream(starpu_gb300_solver *h) { return h ? (void *)h-
 static constexpr int HOST_PANEL = 512;
 
 // Column j of the lower triangle (rows j..n-1) from host memory the device
-// can read (pinned, mapped) into D (ld ldd): one CTA per column, four loads
-// in flight per thread so the host link stays busy.
-__global__ void __launch_bounds__(256) gather_lower_kernel(int n, const double *__restrict__ H, long ldh,
-                                                           double *__restrict__ D, long ldd)
+// can read (pinned, mapped), fused with the factor phase's first pass: into
+// D (FP64) and W (FP32), and
+// the integer max of |A_ij|'s bit patterns into *amax_bits -- what
+// convert_lower_max_kernel computes -- so the host path reads A over the link
+// once and the factor phase skips its own conversion.  16-byte loads, four in
+// flight per thread.
+__global__ void __launch_bounds__(256) gather_convert_kernel(int n, const double *__restrict__ H, long ldh,
+                                                             double *__restrict__ D, long ldd, float *__restrict__ W,
+                                                             long ldw, unsigned long long *amax_bits)
 {
     const long j = blockIdx.x;
     const double *src = H + j * ldh;
     double *dst = D + j * ldd;
-    for (long i = j + threadIdx.x; i < n; i += 4L * blockDim.x) {
-        double v[4];
+    float *w = W + j * ldw;
+    unsigned long long m = 0;
+    auto take = [&](long i, double v) {
+        m = max(m, (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull);
+        dst[i] = v;
+        w[i] = (float)v;
+    };
+    long i0 = j;
+    if (i0 < n && ((uintptr_t)(src + i0) & 15)) {
+        if (threadIdx.x == 0) take(i0, src[i0]);
+        ++i0;
+    }
+    const bool vec = !((uintptr_t)(src + i0) & 15) && !((uintptr_t)(dst + i0) & 15) && !((uintptr_t)(w + i0) & 7);
+    if (vec) {
+        const double2 *s2 = (const double2 *)(src + i0);
+        double2 *d2 = (double2 *)(dst + i0);
+        float2 *w2 = (float2 *)(w + i0);
+        const long n2 = (n - i0) / 2;
+        for (long p = threadIdx.x; p < n2; p += 4 * 256) {
+            double2 v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const long r = i + (long)u * blockDim.x;
-            v[u] = r < n ? src[r] : 0.0;
-        }
+            for (int u = 0; u < 4; ++u)
+                if (p + u * 256 < n2) v[u] = s2[p + u * 256];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const long r = i + (long)u * blockDim.x;
-            if (r < n) dst[r] = v[u];
+            for (int u = 0; u < 4; ++u) {
+                if (p + u * 256 >= n2) break;
+                m = max(m, (unsigned long long)__double_as_longlong(v[u].x) & 0x7FFFFFFFFFFFFFFFull);
+                m = max(m, (unsigned long long)__double_as_longlong(v[u].y) & 0x7FFFFFFFFFFFFFFFull);
+                d2[p + u * 256] = v[u];
+                w2[p + u * 256] = make_float2((float)v[u].x, (float)v[u].y);
+            }
         }
+        if (((n - i0) & 1) && threadIdx.x == 0) take(n - 1, src[n - 1]);
+    } else {
+        for (long i = i0 + threadIdx.x; i < n; i += 256) take(i, src[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)m, o));
+    __shared__ unsigned long long red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < 8; ++q) m = max(m, red[q]);
+        atomicMax(amax_bits, m);
     }
 }
 
@@ -830,11 +879,17 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
     // copy of whole column segments -- n^2/2 + n w/2 elements instead of n^2
     double abytes = 0.0;
     const double *mapped = device_view_of_pinned_matrix(A, n, lda);
+    const int nb_eff = h->nb > 0 ? h->nb : 1024;
     if (mapped) {
         // pinned host memory the GPU can read: one kernel pulls exactly the
         // lower triangle over the host link (pitched copies of column
-        // segments run far below the link rate)
-        gb300_count_launch(), gather_lower_kernel<<<n, 256, 0, s>>>(n, mapped, lda, h->A, n);
+        // segments run far below the link rate) and writes the factor
+        // phase's FP32 copy and max |A_ij| on the way
+        float *W = nullptr;
+        unsigned long long *amax = nullptr;
+        dsposv_prepared_targets(n, nrhs, nb_eff, h->work, &W, &amax);
+        cudaMemsetAsync(amax, 0, 4 * sizeof(unsigned long long), s);
+        gb300_count_launch(), gather_convert_kernel<<<n, 256, 0, s>>>(n, mapped, lda, h->A, n, W, n, amax + 2);
         if ((rc = gb300_last_launch_status())) return rc;
         abytes = 8.0 * n * (n + 1.0) / 2.0;
     } else {
@@ -855,8 +910,18 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
                                           nrhs, cudaMemcpyHostToDevice, s))))
         return rc;
     gb300_prof_end(s, slot, 0.0, abytes + 8.0 * n * (double)nrhs);
-    int status = starpu_gb300_dsposv(s, n, nrhs, h->A, n, h->B, n, h->X, n, h->nb, h->nterms, tol, max_iter, h->work,
+    int status;
+    if (mapped) {
+        // the factor phase's first pass was fused into the gather
+        if (info) memset(info, 0, sizeof *info);
+        if ((h->nterms != 1 && h->nterms != 3) || max_iter < 0 || !(tol >= 0)) return GB300_EINVAL;
+        status = dsposv_factor(s, n, nrhs, h->A, n, nb_eff, h->nterms, h->work, info, true);
+        if (status == GB300_OK)
+            status = dsposv_refine(s, n, nrhs, h->A, n, h->B, n, h->X, n, nb_eff, tol, max_iter, h->work, info);
+    } else {
+        status = starpu_gb300_dsposv(s, n, nrhs, h->A, n, h->B, n, h->X, n, h->nb, h->nterms, tol, max_iter, h->work,
                                      h->lwork, info);
+    }
     if (status != GB300_OK && status != GB300_ETIMEDOUT) return status;
     slot = gb300_prof_begin(s, GB300_PROF_TRANSFER);
     if ((rc = gb300_record_cuda_error(

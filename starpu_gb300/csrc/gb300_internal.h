@@ -21,8 +21,12 @@ int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const dou
 
 
 // the two phases of starpu_gb300_dsposv (capi_solver.cu)
+// prepared: W (FP32 lower A) and max |A_ij| are already in the workspace
 int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
-                  starpu_gb300_ir_info *out);
+                  starpu_gb300_ir_info *out, bool prepared = false);
+// the workspace regions the host path's fused gather writes: W (n x n FP32)
+// and the word that receives max |A_ij| (zeroed with its three neighbours)
+void dsposv_prepared_targets(int n, int nrhs, int nb, void *work, float **W, unsigned long long **amax_block);
 int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
                   int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out);
 

@@ -145,10 +145,13 @@ def test_solver_context_host_buffers_match_device_call(gpu, oracle):
         gpu.starpu_gb300_solver_destroy(h)
 
 
-def test_solver_context_pinned_host_buffers(gpu, oracle):
+@pytest.mark.parametrize("n", [900, 777])
+def test_solver_context_pinned_host_buffers(gpu, oracle, n):
     """Pinned host input: the context reads A's lower triangle with a gather
-    kernel instead of copies; the solution is bit-identical to the device call."""
-    n, nrhs, nb = 900, 4, 256
+    kernel instead of copies, writing the factor phase's FP32 copy and max
+    |A_ij| on the way (odd n: columns start off 16-byte boundaries); the
+    solution is bit-identical to the device call."""
+    nrhs, nb = 4, 256
     A = np.asfortranarray(oracle.spd_gram(n, 47, 0.5))
     B = np.asfortranarray(oracle.uniform_rhs(n, nrhs, 48))
     hA = gpu.starpu_gb300_host_malloc_pinned(8 * n * n)
