@@ -28,7 +28,7 @@ namespace gb300 {
 
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err,
              float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows,
-             const std::function<void(cudaStream_t, int, int)> &on_panel);
+             const std::function<void(cudaStream_t, int, int)> &on_panel, cudaEvent_t ready);
 
 // W(c, r) = W(r, c) for the rows r in [r0, n) below the column block
 // [c0, c0 + w): the strictly upper part of W then holds L^T outside the
@@ -81,9 +81,9 @@ __global__ void convert_lower_norm_kernel(int n, const double *__restrict__ A, l
 // infinity norm below.
 __global__ void __launch_bounds__(256) convert_lower_max_kernel(int n, const double *__restrict__ A, long lda,
                                                                 float *__restrict__ W, long ldw,
-                                                                unsigned long long *amax_bits)
+                                                                unsigned long long *amax_bits, int j0 = 0)
 {
-    const long j = blockIdx.x;
+    const long j = j0 + (long)blockIdx.x;
     const double *a = A + j * lda;
     float *w = W ? W + j * ldw : nullptr;
     unsigned long long m = 0;
@@ -545,9 +545,13 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
                         bool prepared)
 {
     // anorm_bits[0] = ||A||_inf, [1] = info + err, [2] = max |A_ij|
+    // the first column block is converted first; the rest converts beside the
+    // first panel, which reads nothing else, and the factorisation waits for
+    // it before its first update
+    const int first = std::min(n, nb);
     if (!prepared) {
         cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
-        gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
+        gb300_count_launch(), convert_lower_max_kernel<<<first, 256, 0, s>>>(n, A, lda, ws.W, n, ws.anorm_bits + 2);
     }
     // the residuals' slices of A and ||A||_inf, beside the factorisation: on
     // the lowest-priority side stream, started once the factorisation's steps
@@ -557,6 +561,14 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
     if (!ss || !fs || !ms) return gb300_record_cuda_error(cudaGetLastError());
     cudaEventRecord(fs->fork, s);
     cudaStreamWaitEvent(fs->s, fs->fork, 0);
+    cudaEvent_t converted = nullptr;
+    if (!prepared && n > first) {
+        cudaStreamWaitEvent(ss->s, fs->fork, 0);
+        gb300_count_launch(), convert_lower_max_kernel<<<n - first, 256, 0, ss->s>>>(n, A, lda, ws.W, n,
+                                                                                   ws.anorm_bits + 2, first);
+        cudaEventRecord(ss->join, ss->s);
+        converted = ss->join;
+    }
     int side_rc = 0;
     auto slice = [&](cudaStream_t from) {
         cudaEventRecord(ss->fork, from);
@@ -578,7 +590,7 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
         mirrored = true;
     };
     int rc = potrf_tc(fs->s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band, slice, slice_rows(n),
-                      mirror);
+                      mirror, converted);
     if (!rc) rc = side_rc;
     if (mirrored) {
         cudaEventRecord(ms->join, ms->s);

@@ -349,10 +349,12 @@ static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb,
 // steps from then on are bound by their latency-bound diagonal tiles).
 // `on_panel(s, k0, kb)`, when given, is called after each panel whose
 // column block [k0, k0 + kb) has rows below its diagonal tile has been
-// enqueued: that block of the factor is final from then on.
+// enqueued: that block of the factor is final from then on.  `ready`, when
+// given, is an event the first update waits for: the first panel reads only
+// the first column block, the rest of A may still be being written.
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err,
              float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows,
-             const std::function<void(cudaStream_t, int, int)> &on_panel)
+             const std::function<void(cudaStream_t, int, int)> &on_panel, cudaEvent_t ready)
 {
     bool side_done = !side;
     const long ldk = ((long)nb + 63) / 64 * 64;
@@ -363,6 +365,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
     LookaheadStream *la = n > 2 * nb ? lookahead_stream() : nullptr;
     int buf = 0;
     int rc = panel_step(s, n, A, lda, 0, std::min(nb, n), nb, np, w, buf, linv_band, d_info, d_err, 0);
+    if (ready) cudaStreamWaitEvent(s, ready, 0);
     if (!rc && on_panel && n > nb) on_panel(s, 0, nb);
     for (int k0 = 0; k0 < n && !rc; k0 += nb) {
         const int kb = std::min(nb, n - k0);
@@ -539,7 +542,7 @@ int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int n
     cudaStream_t s = (cudaStream_t)stream;
     if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), s);
     if (!n) return GB300_OK;
-    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr, {}, 0, {});
+    return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr, {}, 0, {}, nullptr);
 }
 
 } // extern "C"
