@@ -48,6 +48,12 @@ int main(void)
         const uint32_t fp = starpu_task_footprint(&model, t, arch, 0);
         const double mean = starpu_perfmodel_history_based_expected_perf(&model, arch, fp);
         CHECK(fabs(mean - (100.0 * (k + 1) + 0.5)) < 1e-9, "mean of the kept samples");
+        if (k == 0) {
+            /* one mean per worker (all CPU workers share the CPU combination) */
+            printf("ESTIMATIONS ");
+            starpu_perfmodel_print_estimations(&model, fp, stdout);
+            printf("\n");
+        }
         CHECK(fabs(starpu_task_expected_length(t, arch, 0) - mean) < 1e-9, "expected length = history mean");
         t->destroy = 0;
         starpu_task_destroy(t);

@@ -140,6 +140,8 @@ def test_runtime_written_model(perfmodel_binary, tools, tmp_path):
     assert sorted(round(e.mean, 6) for e in impl0.entries) == [100.5, 200.5, 300.5]
     assert sorted((e.nsample, e.mean) for e in impl1.entries) == [(4, 50.0), (4, 100.0), (4, 150.0)]
     assert sorted(e.flops for e in impl0.entries) == [2.0 * n ** 3 for n in (32, 64, 128)]
+    est = next(l for l in r.stdout.splitlines() if l.startswith("ESTIMATIONS "))
+    assert est.split()[1:] == ["1.005000e+02", "1.005000e+02"]  # STARPU_NCPU=2 workers
     # the in-process reload prints what the oracle reads from the file
     printed = r.stdout.split("BEGIN_PRINT\n")[1].split("END_PRINT\n")[0]
     assert printed == PO.print_all(m, reg)
