@@ -1098,7 +1098,9 @@ static int print_one(struct starpu_perfmodel *model, struct starpu_perfmodel_arc
 void starpu_perfmodel_print(struct starpu_perfmodel *model, struct starpu_perfmodel_arch *arch, unsigned nimpl,
                             char *parameter, uint32_t *footprint, FILE *output)
 {
+    pthread_mutex_lock(&model_mu);
     print_one(model, arch, nimpl, parameter, footprint, output);
+    pthread_mutex_unlock(&model_mu);
 }
 
 static void print_single(struct starpu_perfmodel *model, enum starpu_worker_archtype type, int devid, int ncores,
@@ -1112,10 +1114,23 @@ static void print_single(struct starpu_perfmodel *model, enum starpu_worker_arch
 }
 
 /* arch: NULL (every combination), "cpu", "cpu:<k>", "cuda", "cuda<d>" / "cuda_<d>" (perfmodel_print.c:166-285) */
+static int print_all_locked(struct starpu_perfmodel *model, char *arch, char *parameter, uint32_t *footprint,
+                            FILE *output);
+
+/* the model's lists are read under the model lock: workers may be recording */
 int starpu_perfmodel_print_all(struct starpu_perfmodel *model, char *arch, char *parameter, uint32_t *footprint,
                                FILE *output)
 {
     ensure_model(model);
+    pthread_mutex_lock(&model_mu);
+    const int rc = print_all_locked(model, arch, parameter, footprint, output);
+    pthread_mutex_unlock(&model_mu);
+    return rc;
+}
+
+static int print_all_locked(struct starpu_perfmodel *model, char *arch, char *parameter, uint32_t *footprint,
+                            FILE *output)
+{
     if (!arch) {
         const int n = starpu_perfmodel_get_narch_combs();
         for (int comb = 0; comb < n; ++comb) {
@@ -1162,8 +1177,11 @@ int starpu_perfmodel_print_estimations(struct starpu_perfmodel *model, uint32_t 
     for (unsigned w = 0; w < starpu_worker_get_count(); ++w) {
         struct starpu_perfmodel_arch *a = starpu_worker_get_perf_archtype((int)w, 0);
         const int comb = a ? starpu_perfmodel_arch_comb_get(a->ndevices, a->devices) : -1;
+        pthread_mutex_lock(&model_mu);
         struct pm_entry *e = find_entry(per_arch_if_any(model->state, comb, 0), footprint);
-        if (e) fprintf(output, "%s%e", w ? " " : "", e->mean);
+        const double mean = e ? e->mean : 0.0;
+        pthread_mutex_unlock(&model_mu);
+        if (e) fprintf(output, "%s%e", w ? " " : "", mean);
         else fprintf(output, "%sinf", w ? " " : "");
     }
     return 0;
