@@ -162,10 +162,28 @@ int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const f
  * Larger n is rejected with GB300_EINVAL.  It calls no allocator.  The first
  * call on a device (with it current) looks the array's address up once; make
  * it before any stream capture.  Calls share the array: calls that overlap on
- * the GPU race and must be serialised by the caller.  d_err may be NULL. */
+ * the GPU race and must be serialised by the caller.  d_err, when given, is
+ * used as starpu_gb300_spotrs_sweep uses it (set non-zero on a timeout, never
+ * cleared by the call: zero it before the first call).  d_err may be NULL:
+ * the call then waits for its stream and returns GB300_ETIMEDOUT if an
+ * internal wait timed out (B is then invalid). */
 #define STARPU_GB300_NOALLOC_MAX_N 16384
 int starpu_gb300_spotrs_noalloc(void *stream, int n, int nrhs, const float *L, int ldl, float *B, int ldb,
                                 int *d_err);
+
+/* Limit of every bounded wait of the sweeps (starpu_gb300_spotrs_sweep,
+ * _noalloc, _inv_tiles and the mixed solve's correction solves) on a flag
+ * that another CTA of the same launch publishes; a wait that runs out sets
+ * the call's error word and the launch still ends.  Default 2 s; 0 restores
+ * it.  Returns the previous limit.  The tensor-core kernels' pipeline waits
+ * keep their own fixed limit.  No counterpart in the reference (its CUDA
+ * path has no device-side waits). */
+unsigned long long starpu_gb300_set_wait_budget_ns(unsigned long long ns);
+
+/* Host-only self-check of the per-device bookkeeping of kernel attributes
+ * (dynamic shared memory limits are set once per function and device).
+ * Needs no GPU; returns 0 on success, else the number of the failing step. */
+int starpu_gb300_selftest_attr_book(void);
 
 /* ---------------- tensor-core trailing update (tcgen05, sm_103a) ---------- */
 

@@ -17,7 +17,23 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "lib", "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libref_lapack.so")
-REF_TREE = os.environ.get("STARPU_REFERENCE_TREE", "/root/reference")
+
+
+def _reference_tree() -> str:
+    """The reference checkout the build recipes compile from:
+    STARPU_REFERENCE_TREE, else the REF_DEFAULT location of oracle/Makefile (the
+    one recipe that names it).  An absent tree only skips the reference pins."""
+    env = os.environ.get("STARPU_REFERENCE_TREE")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REF_DEFAULT :="):
+                return line.split("=", 1)[1].strip()
+    return ""
+
+
+REF_TREE = _reference_tree()
 
 _o = None
 _r = None

@@ -16,7 +16,9 @@ Followed:
   * src/core/perfmodel/perfmodel_print.c:25-163 (starpu_perfmodel_print and
     the history lines), 166-285 (starpu_perfmodel_print_all);
   * src/core/perfmodel/perfmodel_history.c:1546-1560 (architecture names);
-  * tools/starpu_perfmodel_plot.c:330-470 (the averages file).
+  * tools/starpu_perfmodel_plot.c:330-470 (the averages file);
+  * src/core/perfmodel/perfmodel_history.c:1915-1990 (recording a measurement
+    into a history entry: HistoryRecord).
 """
 from __future__ import annotations
 
@@ -243,3 +245,46 @@ def plot_averages(m: Model) -> str:
                 row.append('\t""\t""')
         rows.append("".join(row) + "\n")
     return "".join(rows)
+
+
+class HistoryRecord:
+    """One history entry as StarPU's recording updates it
+    (src/core/perfmodel/perfmodel_history.c:1915-1990), for one footprint.
+
+    * A new entry of a history-based model does not keep a single first
+      measurement (1926-1933); a batch (number != 1) or another model type
+      keeps it.
+    * Later, a measurement whose ratio to the mean exceeds
+      1 + STARPU_HISTORY_MAX_ERROR/100 either way is an error, not a sample
+      (1947-1949); once the errors reach the sample count the entry is
+      flushed (1953-1964).
+    * Otherwise sum, sum2 and nsample grow, the mean is sum / n and the
+      deviation sqrt(|sum2 - sum^2 / n| / n) (1966-1973).
+    """
+
+    def __init__(self, history_based: bool = True, max_error: int = 50):
+        self.history_based, self.max_error = history_based, max_error
+        self.exists = False
+        self.sum = self.sum2 = self.mean = self.deviation = 0.0
+        self.nsample = self.nerror = 0
+
+    def record(self, measured: float, number: int = 1) -> None:
+        if not self.exists:
+            self.exists = True
+            if number != 1 or not self.history_based:
+                self.sum, self.sum2 = measured * number, measured * measured * number
+                self.nsample, self.mean = number, measured
+            return
+        ratio = measured / self.mean if self.mean else math.inf
+        if self.nsample and (100 * ratio > 100 + self.max_error or 100 / ratio > 100 + self.max_error):
+            self.nerror += number
+            if self.nerror >= self.nsample:
+                self.sum = self.sum2 = self.mean = self.deviation = 0.0
+                self.nsample = self.nerror = 0
+            return
+        self.sum += measured * number
+        self.sum2 += measured * measured * number
+        self.nsample += number
+        n = self.nsample
+        self.mean = self.sum / n
+        self.deviation = math.sqrt(abs(self.sum2 - self.sum * self.sum / n) / n)

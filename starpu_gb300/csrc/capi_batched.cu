@@ -56,18 +56,18 @@ static void load_table_locked()
     fclose(f);
 }
 
+// Persistent grid of the batched kernel on the current device: the SMs times
+// the CTAs resident per SM (the shared memory limit is set per device first).
 static int batched_grid()
 {
-    static int grid = 0;
-    if (!grid) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(batched_dposv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batched_dposv_kernel, BAT_THREADS, smem_bytes());
-        grid = std::max(1, sms) * std::max(1, per);
+    if (gb300_func_dyn_smem((const void *)batched_dposv_kernel, (int)smem_bytes())) return 0;
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batched_dposv_kernel, BAT_THREADS, smem_bytes()) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        per = 1;
     }
-    return grid;
+    return gb300_device_sms() * std::max(1, per);
 }
 
 struct BatWs {
@@ -164,7 +164,9 @@ static int run_batched(cudaStream_t s, int nsys, const int *n, const double *A, 
     a.berr = ws.berr;
     a.ticket = ws.ticket;
     a.nb_of_bucket = ws.nb;
-    const int grid = std::min(nsys, batched_grid());
+    const int bgrid = batched_grid();
+    if (bgrid <= 0) return GB300_ECUDA;  // the attribute set-up failed; its message is recorded
+    const int grid = std::min(nsys, bgrid);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (kernel_ms) {
         cudaEventCreate(&e0);
@@ -247,7 +249,7 @@ int starpu_gb300_batched_get_tuning(signed char *nb_per_bucket, int nbuckets)
 
 int starpu_gb300_batched_autotune(int systems_per_bucket, int reps)
 {
-    if (systems_per_bucket <= 0) systems_per_bucket = 2 * batched_grid();
+    if (systems_per_bucket <= 0) systems_per_bucket = 2 * std::max(1, batched_grid());
     if (reps <= 0) reps = 2;
     cudaStream_t s = nullptr;
     const int nrhs = 4;

@@ -182,11 +182,7 @@ static void trsv_block(cudaStream_t s, int w, int nrhs, const T *L, long ldl, T 
 {
     constexpr int W = potrs_w<T>::value;
     constexpr size_t smem = (size_t)(W * (W + 1) + W * 16) * sizeof(T);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(trsv_block_kernel<T, W, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
+    if (gb300_func_dyn_smem((const void *)trsv_block_kernel<T, W, TRANS>, (int)smem)) return;
     gb300_count_launch(), trsv_block_kernel<T, W, TRANS><<<cdiv(nrhs, 16), 128, smem, s>>>(w, nrhs, L, ldl, B, ldb);
 }
 
@@ -239,14 +235,11 @@ void potrs_sweep(cudaStream_t s, int n, int nrhs, const T *L, long ldl, void *ws
     const T *Linv = (const T *)ws;
     int *flags = (int *)((char *)ws + (((size_t)nblk * 64 * 64 * sizeof(T) + 255) & ~(size_t)255));
     unsigned *ticket = (unsigned *)(flags + nblk);
-    const unsigned long long budget = 2000000000ull;  // 2 s per wait: far above any legitimate stall
+    const unsigned long long budget = gb300_wait_budget_ns();
     static_assert(std::is_same<T, float>::value, "the single-launch sweeps are FP32");
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(trsv_sweep_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SWEEP_SMEM);
-        cudaFuncSetAttribute(trsv_sweep_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SWEEP_SMEM);
-        attr_set = true;
-    }
+    if (gb300_func_dyn_smem((const void *)trsv_sweep_kernel<false>, SWEEP_SMEM) ||
+        gb300_func_dyn_smem((const void *)trsv_sweep_kernel<true>, SWEEP_SMEM))
+        return;
     for (int c0 = 0; c0 < nrhs; c0 += 16) {
         const int nr = std::min(16, nrhs - c0);
         cudaMemsetAsync(flags, 0, (nblk + 1) * sizeof(int), s);

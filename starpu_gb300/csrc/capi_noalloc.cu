@@ -16,6 +16,8 @@
 // first call before any stream capture.  All calls share the one array and it
 // keeps the last call's contents: calls whose work overlaps on the GPU (for
 // instance on two streams) race on it and must be serialised by the caller.
+// Without a caller status word (d_err NULL) the call waits for its stream and
+// returns GB300_ETIMEDOUT if a sweep wait ran out.
 #include <mutex>
 #include <stdio.h>
 
@@ -72,10 +74,22 @@ extern "C" int starpu_gb300_spotrs_noalloc(void *stream, int n, int nrhs, const 
     if (rc) return rc;
     if (gb300::potrs_sweep_workspace<float>(n) > NOALLOC_SWEEP_BYTES) return GB300_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
+    // A caller's d_err is used as starpu_gb300_spotrs_sweep uses it: set on a
+    // timeout, never cleared here.  Without one the array's own error word is
+    // cleared (it keeps the previous call's value), and read back once the
+    // solve has run, so that a timeout still reaches the caller.
     int *err = d_err ? d_err : (int *)((char *)scratch + NOALLOC_ERR_OFFSET);
-    // the error word must start at zero; the sweeps clear their own flags
-    if ((rc = gb300_record_cuda_error(cudaMemsetAsync(err, 0, sizeof(int), s)))) return rc;
+    if (!d_err && (rc = gb300_record_cuda_error(cudaMemsetAsync(err, 0, sizeof(int), s)))) return rc;
     gb300::potrs_sweep_prepare<float>(s, n, L, ldl, scratch);
     gb300::potrs_sweep<float>(s, n, nrhs, L, ldl, scratch, B, ldb, err);
-    return gb300_last_launch_status();
+    if ((rc = gb300_last_launch_status()) || d_err) return rc;
+    int h_err = 0;
+    if ((rc = gb300_record_cuda_error(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s))) ||
+        (rc = gb300_record_cuda_error(cudaStreamSynchronize(s))))
+        return rc;
+    if (h_err) {
+        gb300_set_error("starpu_gb300_spotrs_noalloc: a sweep wait timed out; B is invalid");
+        return GB300_ETIMEDOUT;
+    }
+    return GB300_OK;
 }

@@ -398,7 +398,7 @@ static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L,
     a.ticket = (unsigned *)(cnt + 2 * a.ntiles);
     a.err = err;
     a.upper = upper;
-    a.budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
+    a.budget_ns = gb300_wait_budget_ns();
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
     a.vec = al(L) && al(band) && al(Y) && al(Z) && ldl % 4 == 0 && ldk % 4 == 0 && ldy % 4 == 0 && n % 4 == 0;
     for (int c0 = 0; c0 < nrhs; c0 += 16) {

@@ -53,17 +53,7 @@ static int make_kmajor_map(CUtensorMap *map, const void *base, int rows, int K, 
     return r == CUDA_SUCCESS ? GB300_OK : GB300_EINVAL;
 }
 
-static int num_sms()
-{
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
-}
+static int num_sms() { return gb300_device_sms(); }
 
 // P (m x k FP32, column-major, ldp) -> hi = bf16(P), lo = bf16(P - hi), both
 // K-major (row i holds P[i, 0..k)), row stride ldk; columns k..ldk-1 zeroed.
@@ -137,11 +127,7 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
     }
     a.err = d_err;
     a.wait_budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TCU_SMEM);
-        attr_set = true;
-    }
+    if (int rc = gb300_func_dyn_smem((const void *)tc_update_kernel, TCU_SMEM)) return rc;
     const int grid = std::min(a.num_tiles, max_grid > 0 ? std::min(max_grid, num_sms()) : num_sms());
     gb300_count_launch(), tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, a);
     return gb300_last_launch_status();
@@ -502,11 +488,7 @@ int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const dou
     a.P = partials;
     a.err = d_err;
     a.wait_budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(residual_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, RTC_SMEM);
-        attr_set = true;
-    }
+    if (int rc2 = gb300_func_dyn_smem((const void *)residual_tc_kernel, RTC_SMEM)) return rc2;
     const int grid = std::min(a.nitems, num_sms());
     gb300_count_launch(), residual_tc_kernel<<<grid, RTC_THREADS, RTC_SMEM, s>>>(tma, tm, a);
     return gb300_last_launch_status();

@@ -121,6 +121,77 @@ extern "C" int gb300_record_cuda_error(cudaError_t e)
 
 extern "C" void gb300_set_error(const char *msg) { snprintf(g_last_error, sizeof g_last_error, "%s", msg); }
 
+// ---- per-device launch set-up ----------------------------------------------
+// A kernel's dynamic shared memory limit is a property of the function on one
+// device: the first launch on every device needs its own cudaFuncSetAttribute.
+// The book keeps (function, device, bytes) triples under a mutex, so host
+// threads racing on a first call set the attribute once and never read a
+// half-written entry.
+namespace {
+std::mutex g_attr_mu;
+struct AttrRec {
+    const void *fn;
+    int dev, bytes;
+};
+std::vector<AttrRec> g_attr;
+
+// setter(fn, bytes) is called for (fn, dev) unless an entry with at least
+// `bytes` exists; the entry is recorded only when the setter succeeds.
+template <typename F> int attr_book_ensure(std::vector<AttrRec> &book, const void *fn, int dev, int bytes, F setter)
+{
+    for (const auto &r : book)
+        if (r.fn == fn && r.dev == dev && r.bytes >= bytes) return GB300_OK;
+    const int rc = setter(fn, bytes);
+    if (rc == GB300_OK) {
+        for (auto &r : book)
+            if (r.fn == fn && r.dev == dev) {
+                r.bytes = bytes;
+                return rc;
+            }
+        book.push_back({fn, dev, bytes});
+    }
+    return rc;
+}
+
+constexpr unsigned long long kDefaultWaitBudgetNs = 2000000000ull;  // 2 s: far above any legitimate stall
+std::atomic<unsigned long long> g_wait_budget_ns{kDefaultWaitBudgetNs};
+
+constexpr int kMaxDevices = 64;
+std::atomic<int> g_sms[kMaxDevices];
+} // namespace
+
+extern "C" int gb300_func_dyn_smem(const void *fn, int bytes)
+{
+    int dev = 0;
+    int rc = gb300_record_cuda_error(cudaGetDevice(&dev));
+    if (rc) return rc;
+    std::lock_guard<std::mutex> g(g_attr_mu);
+    return attr_book_ensure(g_attr, fn, dev, bytes, [](const void *f, int b) {
+        return gb300_record_cuda_error(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    });
+}
+
+extern "C" int gb300_device_sms(void)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev < 0 || dev >= kMaxDevices) dev = 0;
+    int n = g_sms[dev].load(std::memory_order_relaxed);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 1;
+        }
+        g_sms[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
+extern "C" unsigned long long gb300_wait_budget_ns(void) { return g_wait_budget_ns.load(std::memory_order_relaxed); }
+
 extern "C" int gb300_last_launch_status(void)
 {
     return gb300_record_cuda_error(cudaGetLastError());
@@ -129,6 +200,46 @@ extern "C" int gb300_last_launch_status(void)
 extern "C" {
 
 const char *starpu_gb300_last_error(void) { return g_last_error; }
+
+unsigned long long starpu_gb300_set_wait_budget_ns(unsigned long long ns)
+{
+    return g_wait_budget_ns.exchange(ns ? ns : kDefaultWaitBudgetNs);
+}
+
+int starpu_gb300_selftest_attr_book(void)
+{
+    std::vector<AttrRec> book;
+    int calls = 0, fail = 0;
+    auto setter = [&](const void *, int) {
+        ++calls;
+        return fail ? GB300_ECUDA : GB300_OK;
+    };
+    static const char f1 = 0, f2 = 0, f3 = 0;
+    struct Step {
+        const void *fn;
+        int dev, bytes, fail, calls_after, rc;
+    } steps[] = {
+        {&f1, 0, 54272, 0, 1, GB300_OK},     // first launch on device 0
+        {&f1, 0, 54272, 0, 1, GB300_OK},     // again on device 0: nothing to do
+        {&f1, 1, 54272, 0, 2, GB300_OK},     // first launch on device 1 sets it there too
+        {&f1, 0, 40000, 0, 2, GB300_OK},     // a smaller request is covered
+        {&f1, 0, 100000, 0, 3, GB300_OK},    // a larger one raises the limit
+        {&f1, 0, 100000, 0, 3, GB300_OK},
+        {&f1, 1, 100000, 0, 4, GB300_OK},    // ... separately per device
+        {&f2, 0, 54272, 0, 5, GB300_OK},     // another function
+        {&f3, 0, 1024, 1, 6, GB300_ECUDA},   // a failed set-up is not recorded
+        {&f3, 0, 1024, 0, 7, GB300_OK},      // and is retried on the next call
+        {&f3, 0, 1024, 0, 7, GB300_OK},
+    };
+    int i = 0;
+    for (const Step &st : steps) {
+        ++i;
+        fail = st.fail;
+        const int rc = attr_book_ensure(book, st.fn, st.dev, st.bytes, setter);
+        if (rc != st.rc || calls != st.calls_after) return i;
+    }
+    return book.size() == 4 ? 0 : i + 1;
+}
 
 void *starpu_gb300_device_malloc(size_t bytes)
 {

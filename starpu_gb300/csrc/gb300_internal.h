@@ -63,6 +63,15 @@ extern "C" void gb300_set_error(const char *msg);
 // starpu_gb300_launch_count()).
 extern "C" void gb300_count_launch(void);
 
+// Raise fn's dynamic shared memory limit to `bytes` on the current device,
+// once per (function, device); returns a GB300_* code.
+extern "C" int gb300_func_dyn_smem(const void *fn, int bytes);
+// Multiprocessor count of the current device (cached per device).
+extern "C" int gb300_device_sms(void);
+// Limit of one bounded wait on a flag or counter written by another CTA of
+// the same launch (starpu_gb300_set_wait_budget_ns; default 2 s).
+extern "C" unsigned long long gb300_wait_budget_ns(void);
+
 // Per-kernel-class timing (the profiling mode of starpu_gb300_profiling_*):
 // prof_begin/prof_end bracket one launch with CUDA events on its stream when
 // profiling is enabled; both are no-ops otherwise.

@@ -750,9 +750,11 @@ static int save_model(struct starpu_perfmodel *m)
 
 /* --------------------------------------------------- runtime model access */
 
+/* Double-checked initialisation: the fast path's acquire load pairs with the
+ * release store below, so a thread that sees is_init also sees m->state. */
 static void ensure_model(struct starpu_perfmodel *m)
 {
-    if (m->is_init) return;
+    if (__atomic_load_n(&m->is_init, __ATOMIC_ACQUIRE)) return;
     pthread_mutex_lock(&model_mu);
     if (!m->is_init) {
         m->state = calloc(1, sizeof *m->state);
@@ -767,7 +769,7 @@ static void ensure_model(struct starpu_perfmodel *m)
         }
         if (nmodels < MAX_MODELS) models[nmodels++] = m;
         m->is_loaded = 1;
-        m->is_init = 1;
+        __atomic_store_n(&m->is_init, 1, __ATOMIC_RELEASE);
     }
     pthread_mutex_unlock(&model_mu);
 }
@@ -843,12 +845,26 @@ static void record(struct starpu_perfmodel *m, struct starpu_task *t, struct sta
     struct pm_per_arch *pa = per_arch(m->state, comb, (int)nimpl);
     struct pm_entry *e = find_entry(pa, fp);
     if (!e) {
+        /* a new footprint (perfmodel_history.c:1915-1940): a history-based
+         * model does not keep a single first measurement, which is very often
+         * bogus (cold caches, lazy initialisation), and starts counting from
+         * the second; other models, and batches of several, keep it */
         e = calloc(1, sizeof *e);
         e->footprint = fp;
+        e->size = size;
+        e->flops = t->flops;
+        if (number != 1 || m->type != STARPU_HISTORY_BASED) {
+            e->sum = us * number;
+            e->sum2 = us * us * number;
+            e->nsample = number;
+            e->mean = us;
+        }
         e->next = pa->list;
         pa->list = e;
+        m->state->dirty = 1;
+        pthread_mutex_unlock(&model_mu);
+        return;
     }
-    e->size = size;
     const double ratio = e->mean > 0 ? us / e->mean : 1.0;
     if (e->nsample && (100 * ratio > 100 + history_max_error || 100 / ratio > 100 + history_max_error)) {
         e->nerror += number;

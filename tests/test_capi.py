@@ -91,3 +91,19 @@ def test_invalid_arguments_are_rejected_without_a_gpu(libs):
     assert main.starpu_gb300_server_drain(None) == EINVAL
     assert main.starpu_gb300_server_submit(None, None) == EINVAL
     assert main.starpu_gb300_launch_count() == 0
+
+
+def test_kernel_attributes_are_set_once_per_device(libs):
+    """The dynamic shared memory limit of a kernel is set per function and
+    device: the bookkeeping sets it again on a second device, on a larger
+    request and after a failed attempt, and never twice otherwise."""
+    main, _ = libs
+    assert main.starpu_gb300_selftest_attr_book() == 0
+
+
+def test_wait_budget_knob_without_a_gpu(libs):
+    main, _ = libs
+    default = main.starpu_gb300_set_wait_budget_ns(0)
+    assert default == 2_000_000_000
+    assert main.starpu_gb300_set_wait_budget_ns(123) == default
+    assert main.starpu_gb300_set_wait_budget_ns(0) == 123

@@ -10,12 +10,14 @@ import xml.etree.ElementTree as ET
 
 import pytest
 
+from oracle import oracle as O
+
 from oracle import perfmodel_oracle as PO
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FIXTURE_DIR = os.path.join(ROOT, "tests", "golden", "perfmodel")
 FIXTURE = "gb300_fixture_model.fixturehost"
-REF = os.environ.get("STARPU_REFERENCE_TREE", "/root/reference")
+REF = O.REF_TREE  # STARPU_REFERENCE_TREE, else the oracle recipe's location
 REF_SAMPLES = os.path.join(REF, "tools", "perfmodels", "sampling")
 
 
@@ -135,13 +137,23 @@ def test_runtime_written_model(perfmodel_binary, tools, tmp_path):
     m = PO.parse(text, reg)
     assert m.type == "history" and len(m.combs) == 1 and len(m.impls[m.combs[0]]) == 2
     impl0, impl1 = m.impls[m.combs[0]]
-    # 12 kept samples per size on impl 0 (the 10x outlier dropped), 4 on impl 1
-    assert sorted(e.nsample for e in impl0.entries) == [12, 12, 12]
-    assert sorted(round(e.mean, 6) for e in impl0.entries) == [100.5, 200.5, 300.5]
+    # impl 0: 12 calls per size, the first opens the entry and is not kept,
+    # the 10x outlier is an error -> 11 samples; impl 1: one batch of 4, kept
+    assert sorted(e.nsample for e in impl0.entries) == [11, 11, 11]
+    assert sorted(e.mean for e in impl0.entries) == [float(f"{100.0 * k + 6.0 / 11.0:e}") for k in (1, 2, 3)]
     assert sorted((e.nsample, e.mean) for e in impl1.entries) == [(4, 50.0), (4, 100.0), (4, 150.0)]
     assert sorted(e.flops for e in impl0.entries) == [2.0 * n ** 3 for n in (32, 64, 128)]
+    # the same sequence replayed through the oracle's restatement of the rule
+    for k, e in enumerate(sorted(impl0.entries, key=lambda e: e.mean)):
+        o = PO.HistoryRecord()
+        for i in range(12):
+            o.record(100.0 * (k + 1) + (i & 1))
+        o.record(1000.0 * (k + 1))
+        as_written = lambda x: float(f"{x:e}")  # noqa: E731  (the file holds %e values)
+        assert e.nsample == o.nsample
+        assert (e.mean, e.sum, e.sum2, e.deviation) == tuple(map(as_written, (o.mean, o.sum, o.sum2, o.deviation)))
     est = next(l for l in r.stdout.splitlines() if l.startswith("ESTIMATIONS "))
-    assert est.split()[1:] == ["1.005000e+02", "1.005000e+02"]  # STARPU_NCPU=2 workers
+    assert est.split()[1:] == ["1.005455e+02", "1.005455e+02"]  # STARPU_NCPU=2 workers
     # the in-process reload prints what the oracle reads from the file
     printed = r.stdout.split("BEGIN_PRINT\n")[1].split("END_PRINT\n")[0]
     assert printed == PO.print_all(m, reg)

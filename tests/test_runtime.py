@@ -14,8 +14,10 @@ import subprocess
 
 import pytest
 
+from oracle import oracle as O
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("STARPU_REFERENCE_TREE", "/root/reference")
+REF = O.REF_TREE  # STARPU_REFERENCE_TREE, else the oracle recipe's location
 
 
 def _lib():

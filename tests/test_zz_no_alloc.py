@@ -6,8 +6,11 @@ workspace.  This test checks, through the C-ABI, that the allocation-free
 entry point gives the same solution as the workspace entry point
 (starpu_gb300_spotrs_sweep) on two calls in a row -- the static scratch keeps
 the previous call's contents, so the second call also checks that everything
-that must start at zero is cleared -- and that sizes beyond the stated limit
-are rejected.  The file is named so that pytest collects it last.
+that must start at zero is cleared.  Both run the same kernels in the same
+order, so the solutions must be bit for bit the same.  It also checks that a
+wait that runs out is reported without a caller status word, and that sizes
+beyond the stated limit are rejected.  The file is named so that pytest
+collects it last.
 """
 import numpy as np
 import pytest
@@ -18,6 +21,7 @@ from starpu_gb300.native import check
 pytestmark = pytest.mark.gpu
 
 GB300_EINVAL = -22
+GB300_ETIMEDOUT = -110
 MAX_N = 16384
 
 
@@ -42,9 +46,44 @@ def test_noalloc_matches_workspace_entry_point(gpu, oracle, n, nrhs):
         check(gpu.starpu_gb300_stream_sync(None))
         X_ref = d_ref.download(Bm.shape, np.float32)
         X_new = d_new.download(Bm.shape, np.float32)
-        scale = np.max(np.abs(X_ref))
-        assert np.max(np.abs(X_new - X_ref)) <= 1e-4 * scale, f"call {call}"
+        assert np.array_equal(X_new, X_ref), f"call {call}"
         assert err.download((1,), np.int32)[0] == 0
+
+
+def test_noalloc_with_caller_status_word_keeps_it(gpu, oracle):
+    """A caller's d_err is set on a timeout and never cleared by the call."""
+    n, nrhs = 1000, 4
+    dL = DeviceBuffer.from_array(_factor(oracle, n))
+    Bm = oracle.uniform_rhs(n, nrhs, 7).astype(np.float32)
+    dB = DeviceBuffer.from_array(Bm)
+    err = DeviceBuffer.from_array(np.array([5], np.int32))
+    check(gpu.starpu_gb300_spotrs_noalloc(None, n, nrhs, dL.ptr, n, dB.ptr, n, err.ptr))
+    check(gpu.starpu_gb300_stream_sync(None))
+    assert err.download((1,), np.int32)[0] == 5
+
+
+def test_noalloc_without_status_word_reports_timeout(gpu, oracle):
+    """With d_err NULL a wait that runs out (1 ns limit) is returned as
+    GB300_ETIMEDOUT; with the default limit the next call succeeds."""
+    n, nrhs = 8192, 16
+    i = np.arange(n)
+    L = np.asfortranarray((np.tril(np.cos(i[:, None] * 0.37 + i[None, :]), -1) * (0.5 / n) + 2.0 * np.eye(n))
+                          .astype(np.float32))
+    dL = DeviceBuffer.from_array(L)
+    Bm = oracle.uniform_rhs(n, nrhs, 8).astype(np.float32)
+    dB = DeviceBuffer.from_array(Bm)
+    prev = gpu.starpu_gb300_set_wait_budget_ns(1)
+    try:
+        rc = gpu.starpu_gb300_spotrs_noalloc(None, n, nrhs, dL.ptr, n, dB.ptr, n, None)
+    finally:
+        gpu.starpu_gb300_set_wait_budget_ns(prev)
+    assert rc == GB300_ETIMEDOUT
+    assert b"timed out" in gpu.starpu_gb300_last_error()
+    dB.upload(Bm)
+    check(gpu.starpu_gb300_spotrs_noalloc(None, n, nrhs, dL.ptr, n, dB.ptr, n, None))
+    X = dB.download((n, nrhs), np.float32).astype(np.float64)
+    L64 = L.astype(np.float64)
+    assert np.max(np.abs(L64 @ (L64.T @ X) - Bm)) <= 1e-5 * np.max(np.abs(Bm))
 
 
 def test_noalloc_rejects_sizes_beyond_its_limit(gpu):
