@@ -150,36 +150,6 @@ class Dist:
 
 
 # ------------------------------------------------------------------ CPU path
-def cpu_sample(n: int, nb: int, nrhs: int, reps: int, seed: int = 7):
-    """StarPU's CPU path (port of its CPU codelets over OpenBLAS, FP64 tiles,
-    one BLAS thread per worker, all host cores) on one bounded sample."""
-    import numpy as np
-    from oracle import oracle as O
-    if not O.cpu_init():
-        return None
-    cores = len(os.sched_getaffinity(0))
-    Bn = O.normal_matrix(n, n, seed)
-    O.lib().cpu_chol_set_blas_threads(cores)
-    A = np.asfortranarray(Bn @ Bn.T / n)
-    A[np.diag_indices(n)] += O.alpha_for_kappa(1e4)
-    rhs = O.uniform_rhs(n, nrhs, seed + 1)
-    times, berr = [], None
-    for _ in range(reps):
-        L = np.array(A, order="F", copy=True)
-        X = np.array(rhs, order="F", copy=True)
-        t0 = time.perf_counter()
-        info = O.cpu_potrf_tiled(L, n // nb, cores)
-        info2 = O.cpu_potrs(L, X, cores)
-        times.append(time.perf_counter() - t0)
-        assert info == 0 and info2 == 0
-        berr, _ = O.backward_error(A, X, rhs)
-    t = min(times)
-    return {"value": solve_flops(n, nrhs) / t / 1e9, "unit": "GFLOP/s", "cores": cores, "kind": "port",
-            "sample": f"FP64 tiled Cholesky (StarPU CPU codelets port, OpenBLAS, {cores} workers) + dpotrs, "
-                      f"N={n}, tile {nb}, {nrhs} RHS, kappa=1e4; best of {reps}",
-            "backward_error": berr, "seconds_per_solve": t}
-
-
 def cpu_config1(reps: int = 3):
     """The reference's CPU-runnable configuration: plain FP32 tiled Cholesky,
     N=2048, 8x8 tiles of 256, A_ij = 1/(i+j+1) + N delta_ij (the input of
@@ -207,35 +177,116 @@ def cpu_config1(reps: int = 3):
             "max_rel_err": err, "best_of": reps}
 
 
+# ------------------------------------------- FP64 oracle: forward errors
+def host_backward_error(A, X, B):
+    """Normwise backward error max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf
+    + ||b_j||_inf) in FP64 on the host BLAS (A symmetric, full)."""
+    import numpy as np
+    R = B - A @ X
+    anorm = 0.0
+    for j0 in range(0, A.shape[1], 2048):  # column sums = row sums (symmetric A)
+        anorm = max(anorm, float(np.abs(A[:, j0:j0 + 2048]).sum(axis=0).max()))
+    num = np.abs(R).max(axis=0)
+    den = anorm * np.abs(X).max(axis=0) + np.abs(B).max(axis=0)
+    return float((num / den).max())
+
+
+def forward_error(X, Xo):
+    """max_j ||x_j - xo_j||_inf / ||xo_j||_inf against the oracle solution Xo."""
+    import numpy as np
+    return float((np.abs(X - Xo).max(axis=0) / np.abs(Xo).max(axis=0)).max())
+
+
+def oracle_solve(A, B, nb, cores, shift=0.0):
+    """FP64 oracle solution of (A + shift I) X = B: the port of StarPU's CPU
+    path (tiled FP64 Cholesky over OpenBLAS on all host cores, pinned to
+    CLAPACK dpotrf/dpotrs by the golden vectors), then dpotrs.  Returns
+    (X, seconds of the factor + solve)."""
+    import numpy as np
+    from oracle import oracle as O
+    n = A.shape[0]
+    L = np.array(A, order="F", copy=True)
+    if shift:
+        L[np.diag_indices(n)] += shift
+    X = np.array(B, order="F", copy=True)
+    t0 = time.perf_counter()
+    info = O.cpu_potrf_tiled(L, max(1, min(512, round(n / nb))), cores)
+    info2 = O.cpu_potrs(L, X, cores)
+    t = time.perf_counter() - t0
+    assert info == 0 and info2 == 0, (info, info2)
+    return X, t
+
+
+def accuracy_of(A, B, X, Xo, kappa, shift=0.0):
+    """Accuracy of one GPU result against the FP64 oracle solution."""
+    import numpy as np
+    As = A
+    if shift:
+        As = np.array(A, order="F", copy=True)
+        As[np.diag_indices(A.shape[0])] += shift
+    return {"kappa": kappa, "forward_error": forward_error(X, Xo), "backward_error_host": host_backward_error(As, X, B),
+            "oracle_backward_error": host_backward_error(As, Xo, B)}
+
+
 def run_reference(args):
+    """StarPU's CPU path (the port of its CPU codelets over OpenBLAS, FP64
+    tiles, priority DAG on all host cores) on the bench configuration itself:
+    N, tile, RHS and kappa of the GPU arm; one step = one factorisation +
+    solve of the same A = B B^T / N + alpha I (same PCG64 row streams as the
+    device generator), copied back from a pristine host copy before each step
+    (not timed)."""
+    import numpy as np
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    n, nb, nrhs = args.cpu_n, args.cpu_nb, args.nrhs
-    res = []
-    s = None
+    from oracle import oracle as O
+    if not O.cpu_init():
+        print(json.dumps({"impl": "reference", "unavailable": "scipy OpenBLAS not found on this host"}))
+        return 0
+    n, nb, nrhs = args.cpu_n or args.n, args.cpu_nb or args.nb, args.nrhs
+    cores = len(os.sched_getaffinity(0))
+    tg = time.perf_counter()
+    A = O.spd_gram_host_blas(n, 1234, alpha_for_kappa(args.kappa), cores)
+    rhs = O.uniform_rhs(n, nrhs, 99)
+    gen_s = time.perf_counter() - tg
+    L = np.empty_like(A, order="F")
+    nblocks = max(1, min(512, round(n / nb)))
+    times, X = [], None
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(n, nb, nrhs, 1, seed=7)
-        if r is None:
-            print(json.dumps({"impl": "reference", "unavailable": "scipy OpenBLAS not found on this host"}))
-            return 0
+        np.copyto(L, A)
+        X = np.array(rhs, order="F", copy=True)
+        t0 = time.perf_counter()
+        info = O.cpu_potrf_tiled(L, nblocks, cores)
+        info2 = O.cpu_potrs(L, X, cores)
+        t = time.perf_counter() - t0
+        assert info == 0 and info2 == 0
         if i >= args.warmup:
-            res.append(r)
-        s = r
-    t = statistics.median([r["seconds_per_solve"] for r in res])
+            times.append(t)
+    t = sum(times) / len(times)
     val = solve_flops(n, nrhs) / t / 1e9
+    berr = host_backward_error(A, X, rhs)
+    sample = (f"FP64 tiled Cholesky (StarPU CPU codelets port, OpenBLAS, {cores} workers) + dpotrs, N={n}, "
+              f"tile {n // nblocks}, {nrhs} RHS, kappa={args.kappa:g}: the full workload, every step")
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"StarPU CPU path (FP64 port of the tile codelets over OpenBLAS) SPD solve, "
-                                   f"N={n}, tile {nb}, {nrhs} RHS, kappa=1e4 (bounded sample of the N=32768 workload)",
-                       "n": n, "nb": nb, "nrhs": nrhs},
-            "backward_error": s["backward_error"],
-            "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": s["cores"], "kind": "port",
-                             "sample": s["sample"]},
+            "config": bench_config(args, world, n=n, nb=nb),
+            "backward_error": berr, "generation_s": gen_s, "step_s": times,
+            "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def bench_config(args, world, n=None, nb=None):
+    """The workload both arms name: the mixed-precision solve's configuration."""
+    n, nb = n or args.n, nb or args.nb
+    return {"workload": f"SPD solve, N={n}, tile {nb}, A=B*B^T/N+alpha*I (kappa={args.kappa:g}), {args.nrhs} RHS "
+                        f"U[-1,1], to backward error <= 1e-12 (GPU: split-BF16 tcgen05 factor + FP64 iterative "
+                        f"refinement)",
+            "n": n, "nb": nb, "nrhs": args.nrhs, "kappa": args.kappa,
+            "l2": "inputs larger than L2 (A is 8 GiB FP64 at N=32768; L2 129 MB)",
+            "parallelism": f"replicas x{world}"}
 
 
 # ------------------------------------------- config 4: batched uneven systems
@@ -280,10 +331,24 @@ def bench_batched(L, nsys=4096, nrhs=4, seed=2024):
     ms = min(ts)
     tune = (C.c_byte * 6)()
     L.starpu_gb300_batched_get_tuning(tune, 6)
+    # systems for the FP64 oracle: the 3 largest, the 2 smallest and 5 drawn at random
+    order = np.argsort(ns)
+    pick = sorted(set(order[-3:].tolist() + order[:2].tolist() +
+                      np.random.default_rng(seed + 1).choice(nsys, 5, replace=False).tolist()))
+    samples = []
+    for i in pick:
+        n = int(ns[i])
+        Ai = np.empty((n, n), np.float64, order="F")
+        Bi, Xi = np.empty((n, nrhs), np.float64, order="F"), np.empty((n, nrhs), np.float64, order="F")
+        check(L.starpu_gb300_memcpy_d2h(None, Ai.ctypes.data, dA.ptr + 8 * int(a_off[i]), Ai.nbytes))
+        check(L.starpu_gb300_memcpy_d2h(None, Bi.ctypes.data, dB.ptr + 8 * int(b_off[i]), Bi.nbytes))
+        check(L.starpu_gb300_memcpy_d2h(None, Xi.ctypes.data, dX.ptr + 8 * int(b_off[i]), Xi.nbytes))
+        check(L.starpu_gb300_stream_sync(None))
+        samples.append({"system": int(i), "n": n, "kappa": None, "A": Ai, "B": Bi, "X": Xi})
     return {"workload": f"{nsys} SPD systems, n log-uniform [32,1024], A=B*B^T/n+I, {nrhs} RHS, one persistent launch",
             "ms": ms, "gflops": flops / (ms * 1e-3) / 1e9, "systems_per_s": nsys / (ms * 1e-3),
             "max_backward_error": float(be.max()), "all_converged": bool((st >= 0).all()),
-            "corrections_max": int(st.max()), "tuning_nb_per_bucket": list(tune)}
+            "corrections_max": int(st.max()), "tuning_nb_per_bucket": list(tune), "_samples": samples}
 
 
 # --------------------------------------------------------- config 5: serving
@@ -325,7 +390,9 @@ def bench_serving(L, nreq=160, seed=5, repeat_frac=0.3, executors=4):
         trace.append((mi, nrhs, B))
     flops_new = lambda n, r: n ** 3 / 3 + 2 * n * n * r  # noqa: E731
 
-    def run(mode, nexec, arrivals=None):
+    kept = {}
+
+    def run(mode, nexec, arrivals=None, keep_results=False):
         sv = L.starpu_gb300_server_create(120 * (1 << 30), nexec, 8192, 16, mode)
         assert sv, L.starpu_gb300_last_error()
         reqs, keep = [], []
@@ -351,21 +418,40 @@ def bench_serving(L, nreq=160, seed=5, repeat_frac=0.3, executors=4):
         L.starpu_gb300_server_destroy(sv)
         lat = np.array([(r.end_us - r.submit_us) / 1e3 for r in reqs])
         ok = all(r.status == 0 for r in reqs)
-        berr = max(r.backward_error for r in reqs) if mode == 0 else None
+        berr = max(r.backward_error for r in reqs) if mode != 1 else None
+        if keep_results:
+            kept["X"] = keep
         return {"solves_per_s": len(reqs) / wall, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "all_ok": ok, "max_backward_error": berr,
                 "batched_launches": st[1].value, "cache_hits": st[2].value}
-    ours_sat = run(0, executors)
+    ours_sat = run(0, executors, keep_results=True)
     plain_sat = run(1, 1)
+    mixed_sat = run(2, 1)  # the same mixed solves, one at a time: no batching, overlap or cache
     rate = 0.7 * plain_sat["solves_per_s"]  # a load the plain baseline can sustain
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
     ours_lat = run(0, executors, arrivals)
     plain_lat = run(1, 1, arrivals)
+    mixed_lat = run(2, 1, arrivals)
+    # requests for the FP64 oracle: the largest new request, the largest repeat and 6 at random
+    new_q = [q for q in range(nreq) if trace[q][0] not in [trace[p][0] for p in range(q)]]
+    rep_q = [q for q in range(nreq) if q not in new_q]
+    big = lambda qs: max(qs, key=lambda q: mats[trace[q][0]][0]) if qs else None  # noqa: E731
+    pick = {big(new_q), big(rep_q)} | set(rng.choice(nreq, 6, replace=False).tolist())
+    samples = []
+    for q in sorted(p for p in pick if p is not None):
+        mi, nrhs, B = trace[q]
+        n, d = mats[mi]
+        samples.append({"request": int(q), "n": n, "kappa": float(kappas[mi]), "repeat": q in rep_q,
+                        "A": d.download((n, n), np.float64), "B": B, "X": kept["X"][q]})
     return {"workload": f"{nreq} requests, n log-uniform [64,8192], 1-16 RHS, kappa log-uniform [1e2,1e6], "
                         f"{int(repeat_frac * 100)}% repeat RHS, 120 GB budget, {executors} executors",
-            "saturation": {"ours": ours_sat, "plain_per_request": plain_sat,
-                           "speedup_solves_per_s": ours_sat["solves_per_s"] / plain_sat["solves_per_s"]},
-            "poisson_rate_per_s": rate, "at_rate": {"ours": ours_lat, "plain_per_request": plain_lat}}
+            "saturation": {"ours": ours_sat, "plain_per_request": plain_sat, "mixed_per_request": mixed_sat,
+                           "speedup_solves_per_s": ours_sat["solves_per_s"] / plain_sat["solves_per_s"],
+                           "speedup_vs_mixed_per_request": ours_sat["solves_per_s"] / mixed_sat["solves_per_s"],
+                           "speedup_mixed_per_request_vs_plain": mixed_sat["solves_per_s"] / plain_sat["solves_per_s"]},
+            "poisson_rate_per_s": rate,
+            "at_rate": {"ours": ours_lat, "plain_per_request": plain_lat, "mixed_per_request": mixed_lat},
+            "_samples": samples}
 
 
 # ------------------------------------------------------------------ GPU path
@@ -434,6 +520,8 @@ def run_ours(args):
     launches = L.starpu_gb300_launch_count() - launches0
     L.starpu_gb300_profiling_enable(0)
     clk = clocks.stop()
+    want_oracle = rank == 0 and world == 1 and not args.no_cpu
+    X_main = Xd.download((n, nrhs), np.float64) if want_oracle else None
     ms = L.starpu_gb300_event_elapsed_ms(e0, e1) / args.steps
     ms = dist.max(ms)
     flops = solve_flops(n, nrhs)
@@ -519,7 +607,8 @@ def run_ours(args):
                 tms = L.starpu_gb300_event_elapsed_ms(t0e, t1e)
                 sweep.append({"kappa": kap, "nterms": nt, "status": rc, "iterations": info.iterations,
                               "factor_terms": info.factor_terms, "backward_error": info.backward_error,
-                              "gflops": flops / (tms * 1e-3) / 1e9, "ms": tms})
+                              "gflops": flops / (tms * 1e-3) / 1e9, "ms": tms,
+                              "_X": Xd.download((n, nrhs), np.float64) if want_oracle else None})
         set_kappa(args.kappa)
 
     # ---- plain FP64 GPU solve (the baseline of the ">= 3x" target)
@@ -559,13 +648,16 @@ def run_ours(args):
             t_ms = min(ts)
             fp64.append({"n": fn, "nb": fnb, "nrhs": frhs, "ms": t_ms,
                          "gflops": solve_flops(fn, frhs) / (t_ms * 1e-3) / 1e9, "backward_error": float(be.max()),
-                         "kappa": args.kappa if same else "B B^T/N + 2I"})
+                         "kappa": args.kappa if same else "B B^T/N + 2I",
+                         "_X": Bf.download((fn, frhs), np.float64) if want_oracle else None,
+                         "_A": src_A.download((fn, fn), np.float64) if want_oracle and not same else None,
+                         "_B": src_B.download((fn, frhs), np.float64) if want_oracle and not same else None})
             if not same:
                 del src_A, src_B, tmp
     del with_work
 
     # ---- end to end: host buffers through the C-ABI solver context (H2D + solve + D2H per step)
-    e2e = None
+    e2e, X_e2e = None, None
     if not args.no_e2e:
         hA = L.starpu_gb300_host_malloc_pinned(8 * n * n)
         hB = L.starpu_gb300_host_malloc_pinned(8 * n * nrhs)
@@ -610,6 +702,9 @@ def run_ours(args):
                 "gbs": (by.value / (tms.value * 1e-3) / 1e9) if tms.value else None}
         # the host path moves A's lower triangle as 512-column trapezoidal panels
         h2d = sum(8 * (n - j0) * min(512, n - j0) for j0 in range(0, n, 512)) + 8 * n * nrhs
+        if want_oracle:
+            X_e2e = np.empty((n, nrhs), np.float64, order="F")
+            C.memmove(X_e2e.ctypes.data, hX, X_e2e.nbytes)
         e2e = {"value": world * flops / te / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 8 * n * nrhs, "ms_per_step": te * 1e3,
                "solves_per_s": world / te, "p50_ms": 1e3 * statistics.median(lat),
@@ -624,26 +719,78 @@ def run_ours(args):
     batched = bench_batched(L) if not args.no_batched else None
     serving = bench_serving(L) if not args.no_serving else None
 
-    # ---- CPU baseline (rank 0, N=1 only): StarPU CPU path port on a bounded sample
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_sample(args.cpu_n, args.cpu_nb, nrhs, 2)
-        if cpu is not None:
+    # ---- CPU baseline (rank 0, N=1 only): StarPU CPU path port on the bench
+    # system itself (one solve), whose FP64 solution is also the oracle for the
+    # forward errors of every GPU result of this run
+    cpu, accuracy = None, None
+    if want_oracle:
+        from oracle import oracle as O
+        if O.cpu_init():
+            cores = len(os.sched_getaffinity(0))
+            Ah = A.download((n, n), np.float64)  # kappa = args.kappa (the sweep restored it)
+            Bh = Bd.download((n, nrhs), np.float64)
+            cnb = args.cpu_nb or nb
+            Xo, t_cpu = oracle_solve(Ah, Bh, cnb, cores)
+            cpu = {"value": flops / t_cpu / 1e9, "unit": "GFLOP/s", "cores": cores, "kind": "port",
+                   "sample": f"FP64 tiled Cholesky (StarPU CPU codelets port, OpenBLAS, {cores} workers) + dpotrs, "
+                             f"the bench system itself: N={n}, tile {cnb}, {nrhs} RHS, kappa={args.kappa:g}; one solve",
+                   "seconds_per_solve": t_cpu, "backward_error": host_backward_error(Ah, Xo, Bh)}
             cpu["config1"] = cpu_config1()
+            oracle_note = ("FP64 oracle: the port of StarPU's CPU path (tiled FP64 Cholesky over OpenBLAS, pinned "
+                           "to CLAPACK dpotrf/dpotrs) on the same inputs; forward error = max_j ||x_j - xo_j||_inf "
+                           "/ ||xo_j||_inf; backward errors recomputed on the host in FP64")
+            accuracy = {"oracle": oracle_note, "dsposv": accuracy_of(Ah, Bh, X_main, Xo, args.kappa)}
+            if e2e is not None and X_e2e is not None:
+                accuracy["e2e"] = accuracy_of(Ah, Bh, X_e2e, Xo, args.kappa)
+            fp_same = next((f for f in fp64 if f["n"] == n), None)
+            if fp_same is not None and fp_same["_X"] is not None:
+                accuracy["fp64_plain_same_n"] = accuracy_of(Ah, Bh, fp_same["_X"], Xo, args.kappa)
+            ks = []
+            for sw in sweep:
+                if sw["_X"] is None:
+                    continue
+                if sw["kappa"] == args.kappa:
+                    ks.append(accuracy_of(Ah, Bh, sw["_X"], Xo, sw["kappa"]))
+                    continue
+                shift = alpha_for_kappa(sw["kappa"]) - alpha_for_kappa(args.kappa)
+                Xk, _ = oracle_solve(Ah, Bh, cnb, cores, shift)
+                ks.append(accuracy_of(Ah, Bh, sw["_X"], Xk, sw["kappa"], shift))
+            accuracy["kappa_sweep"] = ks
+            del Ah, Xo
+            cfg2 = next((f for f in fp64 if f["n"] != n), None)
+            if cfg2 is not None and cfg2["_A"] is not None:
+                X2, _ = oracle_solve(cfg2["_A"], cfg2["_B"], cfg2["nb"], cores)
+                accuracy["fp64_config2"] = accuracy_of(cfg2["_A"], cfg2["_B"], cfg2["_X"], X2, "B B^T/N + 2I")
+            for key, res in (("batched", batched), ("serving", serving)):
+                if res is None:
+                    continue
+                rows = []
+                for smp in res["_samples"]:
+                    Xs, _ = oracle_solve(smp["A"], smp["B"], 512, cores)
+                    r = accuracy_of(smp["A"], smp["B"], smp["X"], Xs, smp["kappa"])
+                    r.update({k: v for k, v in smp.items() if k not in ("A", "B", "X", "kappa")})
+                    rows.append(r)
+                accuracy[key] = {"samples": rows, "max_forward_error": max(r["forward_error"] for r in rows),
+                                 "max_backward_error_host": max(r["backward_error_host"] for r in rows)}
+
+    def public(x):
+        """The result without the host copies kept for the oracle (keys starting with _)."""
+        if isinstance(x, dict):
+            return {k: public(v) for k, v in x.items() if not k.startswith("_")}
+        if isinstance(x, list):
+            return [public(v) for v in x]
+        return x
 
     if rank == 0:
         fp64_same = next((f for f in fp64 if f["n"] == n), None)
+        fp64, sweep, batched, serving = public(fp64), public(sweep), public(batched), public(serving)
         line = {
             "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"mixed-precision SPD solve, N={n}, tile {nb}, A=B*B^T/N+alpha*I (kappa="
-                                   f"{args.kappa:g}), {nrhs} RHS U[-1,1], split-BF16 tcgen05 factor + FP64 "
-                                   f"iterative refinement to backward error <= 1e-12",
-                       "n": n, "nb": nb, "nrhs": nrhs, "kappa": args.kappa, "factor_terms": args.nterms,
-                       "l2": "inputs larger than L2 (A is 8 GiB FP64 at N=32768; L2 129 MB)",
-                       "parallelism": f"replicas x{world}", "generation_s": gen_s},
+            "config": bench_config(args, world), "factor_terms": args.nterms, "generation_s": gen_s,
             "backward_error": max(berrs), "backward_error_fp64_check": berr_fp64_check, "iterations": iters,
+            "forward_error": accuracy["dsposv"]["forward_error"] if accuracy else None, "accuracy": accuracy,
             "vs_fp64_plain_same_n": (value / world / fp64_same["gflops"]) if fp64_same else None,
             "fp64_plain": fp64, "kappa_sweep": sweep, "batched": batched, "serving": serving,
             "roofline": roofline, "kernels": prof,
@@ -924,8 +1071,8 @@ def main():
     ap.add_argument("--nterms", type=int, default=3)
     ap.add_argument("--max-iter", type=int, default=30)
     ap.add_argument("--fp64-n", type=int, default=16384)
-    ap.add_argument("--cpu-n", type=int, default=8192)
-    ap.add_argument("--cpu-nb", type=int, default=512)
+    ap.add_argument("--cpu-n", type=int, default=0, help="order of the reference arm's system (0: --n)")
+    ap.add_argument("--cpu-nb", type=int, default=0, help="tile of the CPU path (0: --nb)")
     ap.add_argument("--tc-traffic", type=float, default=None,
                     help="DRAM bytes per trailing-update launch (default: the ncu capture of an m = 8192 launch "
                          "scaled to the factorisation's launches)")

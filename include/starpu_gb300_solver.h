@@ -118,7 +118,9 @@ int starpu_gb300_batched_get_tuning(signed char *nb_per_bucket, int nbuckets);
  * Device memory (executor buffers + cached factors) stays within
  * hbm_budget_bytes; a request that cannot be cached is still served.
  * mode 0: mixed precision + refinement (the path above); mode 1: the plain
- * baseline -- every request alone, FP64 dposv, one at a time.
+ * baseline -- every request alone, FP64 dposv, one at a time; mode 2: every
+ * request alone as one mixed solve (factor + refinement, no batched launch,
+ * no factor cache), which isolates what batching and overlap add. 
  * A, B may be host or device pointers; X is written where it points. */
 typedef struct starpu_gb300_request {
     int n, nrhs;

@@ -69,6 +69,26 @@ static inline double u01(uint64_t x) { return (double)(x >> 11) * (1.0 / 9007199
 /* Row i of the N(0,1) matrix B comes from PCG64 stream (i + 1) of `seed`:
  * pairs of draws (u1, u2) give, by Box-Muller, z0 = r cos(2 pi u2) for an
  * even column and z1 = r sin(2 pi u2) for the next odd column. */
+/* Rows row0 .. row0 + rows - 1 of the matrix below, stored from B (row row0
+ * at B[0]): independent row streams, so callers may fill row ranges in
+ * parallel. */
+void oracle_normal_rows(int row0, int rows, int cols, uint64_t seed, double *B, int ldb)
+{
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int i = 0; i < rows; i++) {
+        pcg64_t r;
+        pcg64_seed(&r, seed, (uint64_t)(row0 + i) + 1);
+        for (int j = 0; j < cols; j += 2) {
+            double u1 = u01_open0(pcg64_next(&r));
+            double u2 = u01(pcg64_next(&r));
+            double rad = sqrt(-2.0 * log(u1));
+            double th = two_pi * u2;
+            B[IDX(i, j, ldb)] = rad * cos(th);
+            if (j + 1 < cols) B[IDX(i, j + 1, ldb)] = rad * sin(th);
+        }
+    }
+}
+
 void oracle_normal_matrix(int rows, int cols, uint64_t seed, double *B, int ldb)
 {
     const double two_pi = 6.283185307179586476925286766559;

@@ -58,6 +58,7 @@ def lib() -> C.CDLL:
         o = C.CDLL(LIB)
         o.oracle_hilbert_f32.argtypes = [ci, vp, ci]
         o.oracle_normal_matrix.argtypes = [ci, ci, cu64, vp, ci]
+        o.oracle_normal_rows.argtypes = [ci, ci, ci, cu64, vp, ci]
         o.oracle_uniform_rhs.argtypes = [ci, ci, cu64, vp, ci]
         o.oracle_spd_gram.argtypes = [ci, cu64, cd, vp, ci]
         o.oracle_chunk.argtypes = [ci, ci, ci, vp, vp]
@@ -111,6 +112,43 @@ def normal_matrix(rows: int, cols: int, seed: int) -> np.ndarray:
     B = np.empty((rows, cols), dtype=np.float64, order="F")
     lib().oracle_normal_matrix(rows, cols, seed, _p(B), rows)
     return B
+
+
+def normal_matrix_threaded(rows: int, cols: int, seed: int, threads: int) -> np.ndarray:
+    """normal_matrix, its row streams filled by `threads` host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+    B = np.empty((rows, cols), dtype=np.float64, order="F")
+    o = lib()
+    step = max(1, (rows + threads - 1) // max(1, threads))
+    base = B.ctypes.data
+
+    def fill(r0):
+        o.oracle_normal_rows(r0, min(step, rows - r0), cols, seed, C.c_void_p(base + 8 * r0), rows)
+    with ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        list(ex.map(fill, range(0, rows, step)))
+    return B
+
+
+def spd_gram_host_blas(n: int, seed: int, alpha: float, threads: int) -> np.ndarray:
+    """spd_gram for large n: B from the same row streams, A = B B^T / n + alpha I
+    through the host BLAS (scipy's dsyrk, lower), mirrored to the full matrix."""
+    from scipy.linalg import blas
+    assert cpu_init()
+    lib().cpu_chol_set_blas_threads(threads)
+    B = normal_matrix_threaded(n, n, seed, threads)
+    A = blas.dsyrk(1.0 / n, B, lower=1, trans=0)
+    del B
+    A = np.asfortranarray(A)
+    bs = 2048
+    for j0 in range(0, n, bs):
+        j1 = min(n, j0 + bs)
+        D = A[j0:j1, j0:j1]
+        A[j0:j1, j0:j1] = np.tril(D) + np.tril(D, -1).T
+        if j1 < n:
+            A[j0:j1, j1:] = A[j1:, j0:j1].T
+    A[np.diag_indices(n)] += alpha
+    lib().cpu_chol_set_blas_threads(1)
+    return A
 
 
 def uniform_rhs(n: int, nrhs: int, seed: int) -> np.ndarray:
@@ -175,6 +213,27 @@ def backward_error(A: np.ndarray, X: np.ndarray, B: np.ndarray) -> tuple[float, 
     w = lib().oracle_backward_error(A.shape[0], X.shape[1], _p(A), A.shape[0], _p(X), X.shape[0], _p(B),
                                     B.shape[0], _p(be))
     return w, be
+
+
+def llt_residual_blas(A: np.ndarray, L: np.ndarray) -> float:
+    """llt_residual (||A - L L^T||_F / ||A||_F over the symmetric A) through
+    numpy's BLAS, for orders where the plain-C loop is too slow."""
+    Lt = np.tril(np.asarray(L, dtype=np.float64))
+    R = np.asarray(A, dtype=np.float64) - Lt @ Lt.T
+    return float(np.linalg.norm(R) / np.linalg.norm(A))
+
+
+def cpu_solve(A: np.ndarray, B: np.ndarray, nb: int, nthreads: int) -> np.ndarray:
+    """FP64 solution of A X = B by the StarPU CPU path port (tiled FP64
+    Cholesky over OpenBLAS, pinned to CLAPACK dpotrf/dpotrs by the golden
+    vectors) and LAPACK dpotrs: the FP64 oracle for large orders."""
+    n = A.shape[0]
+    L = np.array(A, dtype=np.float64, order="F", copy=True)
+    X = np.array(B, dtype=np.float64, order="F", copy=True)
+    info = cpu_potrf_tiled(L, max(1, min(512, round(n / nb))), nthreads)
+    assert info == 0, info
+    assert cpu_potrs(L, X, nthreads) == 0
+    return X
 
 
 def flops_potrf(n: float) -> float:

@@ -135,7 +135,7 @@ static void serve_large(starpu_gb300_server *sv, Exec &e, starpu_gb300_request *
     const size_t ws_bytes = starpu_gb300_dsposv_workspace(n, sv->max_nrhs, NB);
     {
         std::lock_guard<std::mutex> g(sv->mu);
-        if (r->matrix_id) {
+        if (r->matrix_id && sv->mode == 0) {  // mode 2 keeps no factors
             auto it = sv->cache.find(r->matrix_id);
             if (it != sv->cache.end() && it->second->ready && it->second->n == n) {
                 entry = it->second;
@@ -313,7 +313,7 @@ extern "C" {
 starpu_gb300_server *starpu_gb300_server_create(size_t hbm_budget_bytes, int executors, int max_n, int max_nrhs,
                                                 int mode)
 {
-    if (executors < 1 || max_n < 1 || max_nrhs < 1 || (mode != 0 && mode != 1)) return nullptr;
+    if (executors < 1 || max_n < 1 || max_nrhs < 1 || mode < 0 || mode > 2) return nullptr;
     starpu_gb300_server *sv = new starpu_gb300_server();
     sv->budget = hbm_budget_bytes;
     sv->mode = mode;
@@ -328,6 +328,11 @@ starpu_gb300_server *starpu_gb300_server_create(size_t hbm_budget_bytes, int exe
         ok &= !gb300_record_cuda_error(cudaMalloc(&e.B, sizeof(double) * (size_t)max_n * max_nrhs));
         ok &= !gb300_record_cuda_error(cudaMalloc(&e.X, sizeof(double) * (size_t)max_n * max_nrhs));
         size_t bytes = sizeof(double) * ((size_t)max_n * max_n + 2 * (size_t)max_n * max_nrhs);
+        if (mode == 2) {  // per-request mixed solves: one solver workspace, no batch pools
+            e.lws = starpu_gb300_dsposv_workspace(max_n, max_nrhs, NB);
+            ok &= !gb300_record_cuda_error(cudaMalloc(&e.ws, e.lws));
+            bytes += e.lws;
+        }
         if (mode == 0) {
             e.lws = starpu_gb300_dsposv_workspace(max_n, max_nrhs, NB);
             ok &= !gb300_record_cuda_error(cudaMalloc(&e.ws, e.lws));
