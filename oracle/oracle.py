@@ -42,11 +42,26 @@ _blas_ready = False
 vp, ci, cd, cu64 = C.c_void_p, C.c_int, C.c_double, C.c_uint64
 
 
+# the reference driver sources staged for machines without the tree (git-ignored)
+STAGED_TREE = os.path.join(HERE, "_ref", "src")
+
+
 def build(with_ref: bool = True) -> None:
-    """Compile the restatement; also the reference CLAPACK when the tree is present."""
+    """Compile the restatement; also the reference CLAPACK when the tree is
+    present, and stage the unchanged drivers' sources for the GPU machine."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if with_ref and os.path.isdir(os.path.join(REF_TREE, "min-dgels")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-stage", f"REF={REF_TREE}"], check=True)
+
+
+def driver_tree() -> str | None:
+    """Where the unchanged reference drivers compile from: the reference tree,
+    else the staged copy of their sources, else None."""
+    for t in (REF_TREE, STAGED_TREE):
+        if t and os.path.isfile(os.path.join(t, "examples", "cholesky", "cholesky_implicit.c")):
+            return t
+    return None
 
 
 def lib() -> C.CDLL:

@@ -56,27 +56,30 @@ def test_sweep_wait_runs_out_then_next_call_succeeds(gpu):
     lw = gpu.starpu_gb300_spotrs_sweep_workspace(n)
     W = DeviceBuffer(lw)
 
-    prev = gpu.starpu_gb300_set_wait_budget_ns(1)
-    try:
+    def sweep():
         err = DeviceBuffer.from_array(np.zeros(1, np.int32))
         dB = DeviceBuffer.from_array(Bm)
         check(gpu.starpu_gb300_spotrs_sweep(None, n, nrhs, dL.ptr, n, dB.ptr, n, W.ptr, lw, err.ptr))
         check(gpu.starpu_gb300_stream_sync(None))
-        timed_out = int(err.download((1,), np.int32)[0])
+        return int(err.download((1,), np.int32)[0]), dB.download((n, nrhs), np.float32)
+
+    err0, X0 = sweep()  # the default limit: the reference result
+    assert err0 == 0
+    prev = gpu.starpu_gb300_set_wait_budget_ns(1)
+    try:
+        timed_out, _ = sweep()
     finally:
         gpu.starpu_gb300_set_wait_budget_ns(prev)
     assert timed_out != 0, "a 1 ns wait limit must run out in a 256-block sweep"
 
-    # the default limit again: the same call succeeds and solves L L^T X = B
-    err2 = DeviceBuffer.from_array(np.zeros(1, np.int32))
-    dB2 = DeviceBuffer.from_array(Bm)
-    check(gpu.starpu_gb300_spotrs_sweep(None, n, nrhs, dL.ptr, n, dB2.ptr, n, W.ptr, lw, err2.ptr))
-    check(gpu.starpu_gb300_stream_sync(None))
-    assert int(err2.download((1,), np.int32)[0]) == 0
-    X = dB2.download((n, nrhs), np.float32).astype(np.float64)
-    L64 = L.astype(np.float64)
+    # the default limit again: the same call succeeds, bit for bit as before,
+    # and solves L L^T X = B to FP32 accuracy
+    err2, X2 = sweep()
+    assert err2 == 0
+    np.testing.assert_array_equal(X2, X0)
+    L64, X = L.astype(np.float64), X2.astype(np.float64)
     R = L64 @ (L64.T @ X) - Bm
-    assert np.max(np.abs(R)) <= 1e-5 * np.max(np.abs(Bm))
+    assert np.max(np.abs(R)) <= 1e-4 * np.max(np.abs(Bm))
 
 
 def test_mixed_solve_reports_timeout_then_converges(gpu, oracle, short_budget):

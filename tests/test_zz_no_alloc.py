@@ -72,6 +72,9 @@ def test_noalloc_without_status_word_reports_timeout(gpu, oracle):
     dL = DeviceBuffer.from_array(L)
     Bm = oracle.uniform_rhs(n, nrhs, 8).astype(np.float32)
     dB = DeviceBuffer.from_array(Bm)
+    check(gpu.starpu_gb300_spotrs_noalloc(None, n, nrhs, dL.ptr, n, dB.ptr, n, None))
+    X0 = dB.download((n, nrhs), np.float32)
+    dB.upload(Bm)
     prev = gpu.starpu_gb300_set_wait_budget_ns(1)
     try:
         rc = gpu.starpu_gb300_spotrs_noalloc(None, n, nrhs, dL.ptr, n, dB.ptr, n, None)
@@ -81,9 +84,10 @@ def test_noalloc_without_status_word_reports_timeout(gpu, oracle):
     assert b"timed out" in gpu.starpu_gb300_last_error()
     dB.upload(Bm)
     check(gpu.starpu_gb300_spotrs_noalloc(None, n, nrhs, dL.ptr, n, dB.ptr, n, None))
-    X = dB.download((n, nrhs), np.float32).astype(np.float64)
-    L64 = L.astype(np.float64)
-    assert np.max(np.abs(L64 @ (L64.T @ X) - Bm)) <= 1e-5 * np.max(np.abs(Bm))
+    X = dB.download((n, nrhs), np.float32)
+    np.testing.assert_array_equal(X, X0)
+    L64, X = L.astype(np.float64), X.astype(np.float64)
+    assert np.max(np.abs(L64 @ (L64.T @ X) - Bm)) <= 1e-4 * np.max(np.abs(Bm))
 
 
 def test_noalloc_rejects_sizes_beyond_its_limit(gpu):
