@@ -72,16 +72,17 @@ def test_unchanged_cholesky_tag_on_gpu(drivers, mode):
     """cholesky_tag.c submits POTRF(0) last, after every task that waits for
     it by tag.  Its GEMM task passes the operands as (A_nk, A_mk)
     (examples/cholesky/cholesky_tag.h:145-146), so its factor misses the
-    reference's 1e-4 check by a hair on CPU workers too; the DAG must still
-    run to the end and print its timing line, and an element the check flags
-    must be off by that hair only."""
+    reference's 1e-4 check by a hair on CPU workers too, and the check's
+    assert then ends the process (its buffered timing line is lost).  The
+    DAG must still run to the end -- the check runs on the gathered factor --
+    and an element the check flags must be off by that hair only."""
     r = _run(os.path.join(drivers, "cholesky_tag_gb300"), ["-size", "1024", "-nblocks", "8", "-check"], mode)
-    assert re.search(r"^1024\t\d+\t[\d.]+", r.stdout, re.M), r.stdout[-2000:] + r.stderr[-2000:]
+    assert "comparing results" in r.stderr, r.stdout[-2000:] + r.stderr[-2000:]
     m = re.search(r"Error\[\d+, \d+\] --> [\d.]+ != [\d.]+ \(err ([\d.]+)\)", r.stderr)
     if m:
         assert float(m.group(1)) < 1e-3, r.stderr[-2000:]
     else:
-        assert r.returncode == 0, r.stderr[-2000:]
+        assert r.returncode == 0 and re.search(r"^1024\t\d+\t[\d.]+", r.stdout, re.M), r.stderr[-2000:]
 
 
 @pytest.mark.parametrize("mode", list(MODES))
