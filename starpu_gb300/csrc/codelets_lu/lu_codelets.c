@@ -39,6 +39,7 @@ starpu_data_handle_t devInfo = NULL;
 #define THRESHOLD_F32 10e-5
 #define THRESHOLD_F64 10e-10
 
+void lu_kernel_fini(void);
 static int *d_ipiv = NULL;     /* pivot record of one GETRF_PIVOT tile */
 static void *d_work = NULL;    /* copy of one tile for the pivoting fallback */
 static size_t work_bytes = 0;
@@ -72,8 +73,18 @@ static void lu_gb300_getrf_pivot(void *descr[], void *arg)
     const int f64 = IS_F64(descr[0]);
     void *s = starpu_cuda_get_local_stream();
     const size_t need = f64 ? starpu_gb300_dgetrf_pivot_tile_workspace(n) : starpu_gb300_sgetrf_pivot_tile_workspace(n);
-    STARPU_ASSERT_MSG(d_work && need <= work_bytes && n <= ipiv_cap,
-                      "LU tile of order %d exceeds the workspace sized by lu_kernel_init", n);
+    if (!d_work || need > work_bytes || n > ipiv_cap) {
+        /* xlu_implicit_pivot.c calls no lu_kernel_init (only xlu.c and
+         * xlu_implicit.c do), so the first pivoting tile sizes the workspace.
+         * This codelet synchronises its stream anyway (it fills the host pivot
+         * record), so no earlier use of the buffers is still in flight. */
+        lu_kernel_fini();
+        work_bytes = starpu_gb300_dgetrf_pivot_tile_workspace(n);
+        ipiv_cap = n;
+        d_work = starpu_gb300_device_malloc(work_bytes);
+        d_ipiv = starpu_gb300_device_malloc(sizeof(int) * (size_t)n);
+        STARPU_ASSERT_MSG(d_work && d_ipiv, "cannot allocate the LU pivoting workspace for tiles of order %d", n);
+    }
     if (f64)
         CHECK_LAUNCH(starpu_gb300_dgetrf_pivot_tile(s, n, a, ld, THRESHOLD_F64, d_ipiv, d_work, work_bytes, NULL));
     else
