@@ -152,7 +152,11 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                         ok = false;
                         break;
                     }
-                    const int term = kb / kblocks;
+                    // the two cross products first, A_hi B_hi^T last: while the
+                    // cross products accumulate, the accumulator holds only their
+                    // sum (about 2^-8 of the result), so the rounding of each of
+                    // their additions is 2^-8 smaller than on top of A_hi B_hi^T
+                    const int term = args.nterms == 3 ? (kb / kblocks + 1) % 3 : 0;
                     const int kx = (kb % kblocks) * TCU_BK;
                     const CUtensorMap *ma = (term == 2) ? &tm_a_lo : &tm_a_hi;
                     const CUtensorMap *mb = (term == 1) ? &tm_b_lo : &tm_b_hi;
