@@ -815,6 +815,9 @@ KERNEL_CASES_DOC = """Single-kernel cases for profiling (ncu) and quick timing, 
     python bench.py --case diag      --n 1024 --reps 50
     python bench.py --case tile_sweep --n 32768 --nb 1024 --nrhs 16 --reps 5
     python bench.py --case syresidual --n 32768 --nrhs 16 --reps 3
+    python bench.py --case batched --nsys 512 --reps 1
+    python bench.py --case lu_tile --n 1024 --reps 3
+    python bench.py --case dsposv_host --n 8192 --nb 1024 --nrhs 16 --reps 2
 
 Each case allocates its operands once, runs `--reps` launches of the same
 shape and prints the mean time per launch measured with CUDA events.
@@ -852,7 +855,9 @@ def run_case(argv):
     from starpu_gb300.native import check
     ap = argparse.ArgumentParser(prog="bench.py --case")
     ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv",
-                                     "tile_ops", "diag", "tile_sweep", "syresidual"])
+                                     "tile_ops", "diag", "tile_sweep", "syresidual", "batched", "lu_tile",
+                                     "dsposv_host"])
+    ap.add_argument("--nsys", type=int, default=512)
     ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--n", type=int, default=8192)
@@ -1050,6 +1055,50 @@ def run_case(argv):
                                                             1e-12, 30, Wk.ptr, lw, C.byref(info))), a.reps)
         out.update(ms=ms, gflops=(n ** 3 / 3 + 2.0 * n * n * nrhs) / ms / 1e6, iterations=info.iterations,
                    backward_error=info.backward_error)
+    elif a.case == "batched":
+        # the persistent batched solver on --nsys systems of the config's size distribution
+        r = bench_batched(L, nsys=a.nsys)
+        r.pop("_samples", None)
+        out.update(r)
+    elif a.case == "lu_tile":
+        # the LU tile codelet body (no pivoting) on an n x n diagonally dominant FP32 tile
+        n = a.n
+        i = np.arange(n, dtype=np.float32)
+        Ah = np.asfortranarray(1.0 / (1.0 + i[:, None] + i[None, :]), dtype=np.float32)
+        Ah[np.diag_indices(n)] += n
+        A0, Aw = DeviceBuffer.from_array(Ah), DeviceBuffer(4 * n * n)
+        info = DeviceBuffer(4)
+
+        def run():
+            check(L.starpu_gb300_memcpy_d2d(None, Aw.ptr, A0.ptr, 4 * n * n))
+            check(L.starpu_gb300_sgetrf_tile(None, n, Aw.ptr, n, info.ptr))
+        ms = _timed(L, run, a.reps)
+        out.update(n=n, ms_including_restore=ms, gflops=2.0 * n ** 3 / 3 / ms / 1e6)
+    elif a.case == "dsposv_host":
+        # the host-buffer solve of a solver context (gather over the host link with
+        # the fused FP32 conversion, the solve, X back)
+        from starpu_gb300.native import IrInfo
+        n, nb, nrhs = a.n, a.nb, a.nrhs
+        A = DeviceBuffer(8 * n * n)
+        W = DeviceBuffer(8 * n * n)
+        check(L.starpu_gb300_gen_spd_gram(None, n, 3, 4.0 / (a.kappa - 1.0), A.ptr, n, W.ptr))
+        del W
+        # pinned host A: the context's gather kernel reads it over the host link
+        hA = L.starpu_gb300_host_malloc_pinned(8 * n * n)
+        assert hA, L.starpu_gb300_last_error()
+        check(L.starpu_gb300_memcpy_d2h(None, hA, A.ptr, 8 * n * n))
+        check(L.starpu_gb300_stream_sync(None))
+        hB = np.asfortranarray(np.random.default_rng(4).uniform(-1, 1, (n, nrhs)))
+        hX = np.zeros((n, nrhs), order="F")
+        ctx = L.starpu_gb300_solver_create(n, nrhs, nb, a.nterms)
+        assert ctx, L.starpu_gb300_last_error()
+        info = IrInfo()
+        ms = _timed(L, lambda: check(L.starpu_gb300_solver_dsposv_host(ctx, n, nrhs, hA, n, hB.ctypes.data, n,
+                                                                        hX.ctypes.data, n, 1e-12, 30, C.byref(info))),
+                    a.reps)
+        L.starpu_gb300_solver_destroy(ctx)
+        L.starpu_gb300_host_free_pinned(hA)
+        out.update(ms=ms, iterations=info.iterations, backward_error=info.backward_error)
     print(json.dumps(out))
 
 

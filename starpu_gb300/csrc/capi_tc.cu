@@ -5,6 +5,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <functional>
 #include <mutex>
 #include <stdio.h>
@@ -87,27 +88,117 @@ int split_bf16(cudaStream_t s, int m, int k, const float *P, long ldp, void *hi,
     return gb300_last_launch_status();
 }
 
+// ---- scaled FP16 panels (the factorisation's operands) ---------------------
+//
+// Row i of P (m x k FP32, column-major) is scaled by 2^-e_i, the power of two
+// that brings max_k |P_ik| below 1 (rs[i] = 2^e_i; 1 for a zero row), and
+// split as x = P_ik 2^-e_i = h + 2^-11 l: h = fp16(x), l = fp16((x - h) 2^11),
+// H = 2^11 h (exact).  All three K-major (row i = k contiguous halves, row
+// stride ldk, columns k..ldk-1 zero).  About 22 significant bits of every
+// element reach the tensor cores, against 16 for the BF16 split.
+struct F16Panel {
+    __half *h, *l, *H;
+    float *rs;
+};
+
+// rs[i] = 2^e_i with max_k |P_ik| < 2^e_i (the largest |P_ik| is then below 1
+// after the scaling).  32 rows per CTA, the k loop split over 8 thread rows.
+__global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P, long ldp, float *__restrict__ rs)
+{
+    __shared__ float red[8][33];
+    const int r = blockIdx.x * 32 + threadIdx.x;
+    float mx = 0.0f;
+    if (r < m)
+        for (int c = threadIdx.y; c < k; c += 8) mx = fmaxf(mx, fabsf(P[r + (long)c * ldp]));
+    red[threadIdx.y][threadIdx.x] = mx;
+    __syncthreads();
+    if (threadIdx.y == 0 && r < m) {
+        for (int y = 1; y < 8; ++y) mx = fmaxf(mx, red[y][threadIdx.x]);
+        int e = 0;
+        if (mx > 0.0f && isfinite(mx)) frexpf(mx, &e);  // mx = f 2^e, 0.5 <= f < 1: mx < 2^e
+        rs[r] = ldexpf(1.0f, e);
+    }
+}
+
+__global__ void split_f16s_kmajor_kernel(int m, int k, const float *__restrict__ P, long ldp,
+                                         const float *__restrict__ rs, __half *__restrict__ h, __half *__restrict__ l,
+                                         __half *__restrict__ H, long ldk)
+{
+    __shared__ float t[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+        const int r = r0 + threadIdx.x, col = c0 + c;
+        t[c][threadIdx.x] = (r < m && col < k) ? P[r + (long)col * ldp] : 0.0f;
+    }
+    __syncthreads();
+    for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+        const int r = r0 + rr, col = c0 + threadIdx.x;
+        if (r < m && col < ldk) {
+            const float x = t[threadIdx.x][rr] / rs[r];  // exact: division by a power of two
+            const __half hh = __float2half_rn(x);
+            const float hf = __half2float(hh);
+            const long o = (long)r * ldk + col;
+            h[o] = hh;
+            l[o] = __float2half_rn((x - hf) * 2048.0f);
+            H[o] = __float2half_rn(hf * 2048.0f);
+        }
+    }
+}
+
+static int split_f16s(cudaStream_t s, int m, int k, const float *P, long ldp, const F16Panel &o, long ldk)
+{
+    if (m <= 0 || k <= 0) return GB300_OK;
+    gb300_count_launch(), panel_row_scale_kernel<<<(m + 31) / 32, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rs);
+    dim3 g((m + 31) / 32, (unsigned)((ldk + 31) / 32));
+    gb300_count_launch(), split_f16s_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rs, o.h, o.l, o.H, ldk);
+    return gb300_last_launch_status();
+}
+
+// rows [r, ...) of a split panel
+static F16Panel rows_of(const F16Panel &p, long r, long ldk)
+{
+    return {p.h + r * ldk, p.l + r * ldk, p.H + r * ldk, p.rs + r};
+}
+
+// One operand of the update: BF16 hi / lo, or the scaled FP16 split
+// (hi = h, lo = l, hh = H, rs = the row scales).
+struct TcOperand {
+    const void *hi, *lo, *hh;
+    const float *rs;
+};
+
 // max_grid > 0 caps the persistent grid (CTAs, one per SM): the trailing
 // update that runs beside the next panel leaves that panel's SMs free.
-int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void *a_lo, long lda, const void *b_hi,
-              const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
-              int max_grid = 0)
+// f16s: both operands are scaled FP16 panels.
+static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A, long lda, const TcOperand &B,
+                        long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store, int max_grid,
+                        bool f16s)
 {
     if (m <= 0 || n <= 0 || K <= 0) return GB300_OK;
-    if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!a_lo || !b_lo)) || (lower && m != n) || !d_err)
+    if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!A.lo || !B.lo)) || (lower && m != n) || !d_err ||
+        (f16s && (!A.hh || !A.rs || !B.rs)))
         return GB300_EINVAL;
-    CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
+    CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo, ta_hh;
     int rc;
-    if ((rc = make_kmajor_map(&ta_hi, a_hi, m, K, lda, TCU_BM))) return rc;
-    if ((rc = make_kmajor_map(&tb_hi, b_hi, n, K, ldb, TCU_BN))) return rc;
+    if ((rc = make_kmajor_map(&ta_hi, A.hi, m, K, lda, TCU_BM))) return rc;
+    if ((rc = make_kmajor_map(&tb_hi, B.hi, n, K, ldb, TCU_BN))) return rc;
     if (nterms == 3) {
-        if ((rc = make_kmajor_map(&ta_lo, a_lo, m, K, lda, TCU_BM))) return rc;
-        if ((rc = make_kmajor_map(&tb_lo, b_lo, n, K, ldb, TCU_BN))) return rc;
+        if ((rc = make_kmajor_map(&ta_lo, A.lo, m, K, lda, TCU_BM))) return rc;
+        if ((rc = make_kmajor_map(&tb_lo, B.lo, n, K, ldb, TCU_BN))) return rc;
     } else {
         ta_lo = ta_hi;
         tb_lo = tb_hi;
     }
+    if (f16s) {
+        if ((rc = make_kmajor_map(&ta_hh, A.hh, m, K, lda, TCU_BM))) return rc;
+    } else {
+        ta_hh = ta_hi;
+    }
     TcUpdateArgs a;
+    a.f16s = f16s ? 1 : 0;
+    a.rs_a = f16s ? A.rs : nullptr;
+    a.rs_b = f16s ? B.rs : nullptr;
+    a.gscale = 1.0f / 2048.0f;
     a.C = C;
     a.ldc = ldc;
     a.m = m;
@@ -129,38 +220,60 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
     a.wait_budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
     if (int rc = gb300_func_dyn_smem((const void *)tc_update_kernel, TCU_SMEM)) return rc;
     const int grid = std::min(a.num_tiles, max_grid > 0 ? std::min(max_grid, num_sms()) : num_sms());
-    gb300_count_launch(), tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, a);
+    gb300_count_launch(), tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, ta_hh, a);
     return gb300_last_launch_status();
 }
 
+// BF16 operands (the public C-ABI update)
+int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void *a_lo, long lda, const void *b_hi,
+              const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
+              int max_grid = 0)
+{
+    return tc_update_op(s, m, n, K, {a_hi, a_lo, nullptr, nullptr}, lda, {b_hi, b_lo, nullptr, nullptr}, ldb, nterms,
+                        lower, C, ldc, d_err, store, max_grid, false);
+}
+
+// scaled FP16 panels (the factorisation)
+static int tc_update_f16s(cudaStream_t s, int m, int n, int K, const F16Panel &A, long lda, const F16Panel &B,
+                          long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
+                          int max_grid = 0)
+{
+    return tc_update_op(s, m, n, K, {A.h, A.l, A.H, A.rs}, lda, {B.h, B.l, B.H, B.rs}, ldb, nterms, lower, C, ldc,
+                        d_err, store, max_grid, true);
+}
+
 // Workspace of potrf_tc for order n and tile nb (ldk = nb rounded up to 64):
-// two split panels (hi, lo: n x ldk BF16 each; step k's panel is read by its
-// trailing update while step k+1's is written), the inverse of the diagonal
-// tile (ldk x ldk FP32) and its split (hi, lo), the doubling scratch of the
-// triangular inverse (ldk x ldk FP32) and the diagonal-tile kernel's barrier
-// counter.
+// two split panels (scaled FP16 h, l, H: n x ldk each, and n row scales; step
+// k's panel is read by its trailing update while step k+1's is written), the
+// inverse of the diagonal tile (ldk x ldk FP32) and its split, the doubling
+// scratch of the triangular inverse (ldk x ldk FP32) and the diagonal-tile
+// kernel's barrier counter.
 struct TcWs {
-    __nv_bfloat16 *hi[2], *lo[2], *ihi, *ilo;
+    F16Panel pan[2], inv;
     float *linv, *scratch;
     unsigned *bar;  // grid-barrier counter of the diagonal-tile kernel
 };
 static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
 {
     const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64;
-    const size_t panel = (size_t)n * ldk * 2, inv = ldk * ldk;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t panel = al((size_t)n * ldk * 2), rsn = al((size_t)n * 4);
+    const size_t inv = ldk * ldk, invh = al(inv * 2), rsk = al(ldk * 4);
+    const size_t off_inv = 2 * (3 * panel + rsn);
+    const size_t off_linv = off_inv + 3 * invh + rsk;
     if (w && base) {
         char *b = (char *)base;
         for (int i = 0; i < 2; ++i) {
-            w->hi[i] = (__nv_bfloat16 *)(b + 2 * i * panel);
-            w->lo[i] = (__nv_bfloat16 *)(b + (2 * i + 1) * panel);
+            char *p = b + i * (3 * panel + rsn);
+            w->pan[i] = {(__half *)p, (__half *)(p + panel), (__half *)(p + 2 * panel), (float *)(p + 3 * panel)};
         }
-        w->linv = (float *)(b + 4 * panel);
-        w->ihi = (__nv_bfloat16 *)(w->linv + inv);
-        w->ilo = w->ihi + inv;
-        w->scratch = (float *)(w->ilo + inv);
+        char *q = b + off_inv;
+        w->inv = {(__half *)q, (__half *)(q + invh), (__half *)(q + 2 * invh), (float *)(q + 3 * invh)};
+        w->linv = (float *)(b + off_linv);
+        w->scratch = w->linv + inv;
         w->bar = (unsigned *)(w->scratch + inv);
     }
-    return 4 * panel + inv * 4 + 2 * inv * 2 + inv * 4 + 256;
+    return off_linv + 2 * inv * 4 + 256;
 }
 
 static_assert(DC_MAXN == GB300_DIAG_TILE_MAX, "one limit for the diagonal-tile kernel");
@@ -308,10 +421,10 @@ static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb,
         return rc;
     }
     float *P = A + (k0 + kb) + (long)k0 * lda;
-    rc = split_bf16(s, kb, kb, linv, ldk, w.ihi, w.ilo, ldk);
-    if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi[buf], w.lo[buf], ldk);
-    if (!rc) rc = tc_update(s, m, kb, kb, w.hi[buf], w.lo[buf], ldk, w.ihi, w.ilo, ldk, 3, 0, P, lda, d_err, 1, sms);
-    if (!rc) rc = split_bf16(s, m, kb, P, lda, w.hi[buf], np > 1 ? w.lo[buf] : nullptr, ldk);
+    rc = split_f16s(s, kb, kb, linv, ldk, w.inv, ldk);
+    if (!rc) rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk);
+    if (!rc) rc = tc_update_f16s(s, m, kb, kb, w.pan[buf], ldk, w.inv, ldk, 3, 0, P, lda, d_err, 1, sms);
+    if (!rc) rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk);
     // algorithmic work of the panel: POTRF kb^3/3 + TRSM m kb^2; bytes: the
     // tile and the panel read and written once, the BF16 panel written
     gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0 + (double)m * kb * kb,
@@ -346,7 +459,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
     const long ldk = ((long)nb + 63) / 64 * 64;
     TcWs w;
     tc_ws_layout(n, nb, work, &w);
-    const int np = nterms == 3 ? 2 : 1;
+    const int np = nterms == 3 ? 3 : 2;  // split panel arrays an update reads: h, l, H (or H, h)
     // a step has a trailing triangle beyond its next column block only when n > 2 nb
     LookaheadStream *la = n > 2 * nb ? lookahead_stream() : nullptr;
     int buf = 0;
@@ -357,16 +470,15 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
         const int kb = std::min(nb, n - k0);
         const int m = n - k0 - kb;
         if (m <= 0) break;
-        const __nv_bfloat16 *hi = w.hi[buf], *lo = w.lo[buf];
+        const F16Panel &pan = w.pan[buf];
         const int kb1 = std::min(nb, m);  // width of the next column block
         const int m2 = m - kb1;           // rows and columns beyond it
         float *C11 = A + (k0 + kb) + (long)(k0 + kb) * lda;
         // the next column block: its diagonal tile (lower) and the rectangle below
         int slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
-        rc = tc_update(s, kb1, kb1, kb, hi, lo, ldk, hi, lo, ldk, nterms, 1, C11, lda, d_err);
+        rc = tc_update_f16s(s, kb1, kb1, kb, pan, ldk, pan, ldk, nterms, 1, C11, lda, d_err);
         if (!rc && m2 > 0)
-            rc = tc_update(s, m2, kb1, kb, hi + (size_t)kb1 * ldk, lo + (size_t)kb1 * ldk, ldk, hi, lo, ldk, nterms, 0,
-                           C11 + kb1, lda, d_err);
+            rc = tc_update_f16s(s, m2, kb1, kb, rows_of(pan, kb1, ldk), ldk, pan, ldk, nterms, 0, C11 + kb1, lda, d_err);
         // algorithmic work: the lower triangle of the kb1 tile and the m2 x kb1
         // rectangle, per term; bytes: C read + written in FP32, the panels read
         gb300_prof_end(s, slot, (double)nterms * kb * ((double)kb1 * (kb1 + 1.0) + 2.0 * m2 * kb1),
@@ -374,7 +486,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
         if (rc) break;
         const int nbuf = buf ^ 1;
         float *C22 = C11 + kb1 + (long)kb1 * lda;
-        const __nv_bfloat16 *hi2 = hi + (size_t)kb1 * ldk, *lo2 = lo + (size_t)kb1 * ldk;
+        const F16Panel pan2 = rows_of(pan, kb1, ldk);
         // algorithmic work of the trailing triangle, as for one lower update
         const double f2 = (double)nterms * kb * (double)m2 * (m2 + 1.0);
         const double b2 = 8.0 * m2 * (m2 + 1.0) / 2.0 + 2.0 * m2 * ldk * np;
@@ -384,8 +496,8 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
             cudaStreamWaitEvent(la->s, la->fork, 0);
             slot = gb300_prof_begin(la->s, GB300_PROF_TC_UPDATE);
             gb300_prof_set_share(slot, (double)(num_sms() - la_sms) / num_sms());
-            rc = tc_update(la->s, m2, m2, kb, hi2, lo2, ldk, hi2, lo2, ldk, nterms, 1, C22, lda, d_err, 0,
-                           num_sms() - la_sms);
+            rc = tc_update_f16s(la->s, m2, m2, kb, pan2, ldk, pan2, ldk, nterms, 1, C22, lda, d_err, 0,
+                                num_sms() - la_sms);
             gb300_prof_end(la->s, slot, f2, b2);
             cudaEventRecord(la->join, la->s);
             if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, la_sms);
@@ -394,7 +506,7 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
         } else {
             if (m2 > 0) {
                 slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
-                rc = tc_update(s, m2, m2, kb, hi2, lo2, ldk, hi2, lo2, ldk, nterms, 1, C22, lda, d_err);
+                rc = tc_update_f16s(s, m2, m2, kb, pan2, ldk, pan2, ldk, nterms, 1, C22, lda, d_err);
                 gb300_prof_end(s, slot, f2, b2);
             }
             if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, 0);

@@ -205,7 +205,8 @@ __host__ __device__ constexpr uint32_t make_idesc(int M, int N, uint32_t ab_form
            ((uint32_t)(M >> 4) << 24);
 }
 
-constexpr uint32_t FMT_BF16 = 1;  // kind::f16
+constexpr uint32_t FMT_F16 = 0;   // kind::f16, FP16 operands
+constexpr uint32_t FMT_BF16 = 1;  // kind::f16, BF16 operands
 constexpr uint32_t FMT_TF32 = 2;  // kind::tf32
 
 } // namespace ptx

@@ -14,6 +14,16 @@
 // the FP32 panel into the product (the dropped A_lo B_lo^T term is ~2^-16
 // relative).
 //
+// Scaled FP16 operands (f16s = 1, the factorisation's panels): every row i of
+// a panel is scaled by a power of two 2^-e_i that brings its largest element
+// below 1, then split as x 2^-e_i = h + 2^-11 l with h = fp16(x 2^-e_i) and
+// l = fp16((x 2^-e_i - h) 2^11): about 22 significant bits (FP16 keeps 11,
+// and the split stays inside its normal range).  With H = 2^11 h (exact) the
+// three products H_A h_B^T + h_A l_B^T + l_A h_B^T accumulate 2^11 times the
+// scaled product in one accumulator; the epilogue multiplies by
+// 2^-11 2^e_i 2^e_j (rs_a[i] rs_b[j] gscale: powers of two, exact).  The
+// dropped l_A l_B^T term weighs 2^-22 of the product.
+//
 // CTA = 6 warps, one CTA per SM (persistent, static round-robin over tiles):
 //   warp 0  TMA producer     (one elected lane)
 //   warp 1  MMA issuer       (one elected lane) + TMEM owner (512 columns)
@@ -53,6 +63,9 @@ struct TcUpdateArgs {
     int nterms;        // 1 or 3
     int lower;         // 1: only elements with row >= col (square trailing matrix)
     int store;         // 1: C = sum (C is not read), 0: C -= sum
+    int f16s;          // 1: scaled FP16 operands (rs_a, rs_b, gscale below); 0: BF16
+    const float *rs_a, *rs_b;  // f16s: row scales 2^e of A (m) and B (n)
+    float gscale;              // f16s: 2^-11
     int tiles_m, tiles_n, num_tiles;
     int *err;
     unsigned long long wait_budget_ns;
@@ -84,7 +97,7 @@ __device__ __forceinline__ void tcu_tile_coords(const TcUpdateArgs &a, int t, in
 __global__ void __launch_bounds__(TCU_THREADS, 1)
 tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_constant__ CUtensorMap tm_a_lo,
                  const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
-                 const TcUpdateArgs args)
+                 const __grid_constant__ CUtensorMap tm_a_hh, const TcUpdateArgs args)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte aligned tile area (required by the 128B swizzle atoms)
@@ -123,6 +136,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
             ptx::tma_prefetch_desc(&tm_a_lo);
             ptx::tma_prefetch_desc(&tm_b_lo);
         }
+        if (args.f16s) ptx::tma_prefetch_desc(&tm_a_hh);
     }
     if (warp == 1) {
         ptx::tmem_alloc(tmem_slot, TCU_TMEM_COLS);
@@ -158,7 +172,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                     // their additions is 2^-8 smaller than on top of A_hi B_hi^T
                     const int term = args.nterms == 3 ? (kb / kblocks + 1) % 3 : 0;
                     const int kx = (kb % kblocks) * TCU_BK;
-                    const CUtensorMap *ma = (term == 2) ? &tm_a_lo : &tm_a_hi;
+                    // term 0: A_hi B_hi^T (scaled FP16: H_A h_B^T), 1: A_hi B_lo^T, 2: A_lo B_hi^T
+                    const CUtensorMap *ma = (term == 2) ? &tm_a_lo : (term == 0 && args.f16s) ? &tm_a_hh : &tm_a_hi;
                     const CUtensorMap *mb = (term == 1) ? &tm_b_lo : &tm_b_hi;
                     ptx::mbar_arrive_expect_tx(&full[stage], TCU_A_BYTES + TCU_B_BYTES);
                     ptx::tma_load_2d(sA + stage * TCU_A_BYTES, ma, &full[stage], kx, m0);
@@ -191,7 +206,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
     } else if (warp == 1) {
         // ------------------------------------------------------- MMA issuer
         if (ptx::elect_one()) {
-            constexpr uint32_t idesc = ptx::make_idesc(TCU_BM, TCU_BN, ptx::FMT_BF16);
+            const uint32_t idesc = args.f16s ? ptx::make_idesc(TCU_BM, TCU_BN, ptx::FMT_F16)
+                                             : ptx::make_idesc(TCU_BM, TCU_BN, ptx::FMT_BF16);
             int stage = 0;
             uint32_t phase = 0;
             int acc = 0;
@@ -261,6 +277,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
             const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TCU_BN);
             float *crow = args.C + row;
             const bool row_ok = row < args.m;
+            // scaled FP16: the row's factor 2^-11 2^e_i (the columns' 2^e_j below)
+            const float rsc = (args.f16s && row_ok) ? args.gscale * args.rs_a[row] : 1.0f;
 #pragma unroll 1
             for (int ch = 0; ch < TCU_BN / 32; ++ch) {
                 uint32_t r[32];
@@ -278,6 +296,16 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                         const int col = c0 + j;
                         const bool w = col < args.n && (!args.lower || row >= col);
                         cv[j] = (w && !args.store) ? crow[(long)col * args.ldc] : 0.0f;
+                    }
+                    if (args.f16s) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int col = c0 + j;
+                            const float cs = col < args.n ? args.rs_b[col] : 0.0f;
+                            // two exact power-of-two products, the first keeping the value
+                            // near its final size (no underflow for scales down to ~2^-60)
+                            r[j] = __float_as_uint((__uint_as_float(r[j]) * rsc) * cs);
+                        }
                     }
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
