@@ -818,6 +818,8 @@ KERNEL_CASES_DOC = """Single-kernel cases for profiling (ncu) and quick timing, 
     python bench.py --case batched --nsys 512 --reps 1
     python bench.py --case lu_tile --n 1024 --reps 3
     python bench.py --case dsposv_host --n 8192 --nb 1024 --nrhs 16 --reps 2
+    python bench.py --case factor_error --n 8192 --nb 1024 --kappa 1e4
+    python bench.py --case update_error --m 2048 --k 1024
 
 Each case allocates its operands once, runs `--reps` launches of the same
 shape and prints the mean time per launch measured with CUDA events.
@@ -856,7 +858,7 @@ def run_case(argv):
     ap = argparse.ArgumentParser(prog="bench.py --case")
     ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv",
                                      "tile_ops", "diag", "tile_sweep", "syresidual", "batched", "lu_tile",
-                                     "dsposv_host"])
+                                     "dsposv_host", "factor_error", "update_error"])
     ap.add_argument("--nsys", type=int, default=512)
     ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
@@ -1099,6 +1101,44 @@ def run_case(argv):
         L.starpu_gb300_solver_destroy(ctx)
         L.starpu_gb300_host_free_pinned(hA)
         out.update(ms=ms, iterations=info.iterations, backward_error=info.backward_error)
+    elif a.case == "factor_error":
+        # ||A - L L^T||_F / ||A||_F of the FP32 factor of A = B B^T / n + alpha I (kappa), mixed (tensor-core)
+        # factor with nterms 3 and 1, and the SIMT FP32 factor, FP64 on the host
+        n, nb = a.n, a.nb
+        dA, W0 = DeviceBuffer(8 * n * n), DeviceBuffer(8 * n * n)
+        check(L.starpu_gb300_gen_spd_gram(None, n, 5, alpha_for_kappa(a.kappa), dA.ptr, n, W0.ptr))
+        del W0
+        A = dA.download((n, n), np.float64)
+        del dA
+        A32 = np.asfortranarray(A.astype(np.float32))
+        for name, nt in (("mixed_nterms3", 3), ("mixed_nterms1", 1), ("simt_fp32", 0)):
+            d = DeviceBuffer.from_array(A32)
+            info, err = DeviceBuffer.from_array(np.zeros(1, np.int32)), DeviceBuffer.from_array(np.zeros(1, np.int32))
+            if nt:
+                ws = L.starpu_gb300_spotrf_tc_workspace(n, nb)
+                Wk = DeviceBuffer(ws)
+                check(L.starpu_gb300_spotrf_tc(None, n, d.ptr, n, nb, nt, Wk.ptr, ws, info.ptr, err.ptr))
+            else:
+                check(L.starpu_gb300_spotrf(None, n, d.ptr, n, nb, info.ptr))
+            check(L.starpu_gb300_stream_sync(None))
+            Lf = np.tril(d.download((n, n), np.float32).astype(np.float64))
+            out[name] = float(np.linalg.norm(Lf @ Lf.T - A) / np.linalg.norm(A))
+    elif a.case == "update_error":
+        # one BF16 split update C = -P P^T (m x K) against its FP64 product, rms relative error
+        m, k = a.m, a.k
+        rng = np.random.default_rng(1)
+        P = np.asfortranarray(rng.standard_normal((m, k)).astype(np.float32) / 32)
+        dP = DeviceBuffer.from_array(P)
+        hi, lo = DeviceBuffer(2 * m * k), DeviceBuffer(2 * m * k)
+        check(L.starpu_gb300_split_bf16(None, m, k, dP.ptr, m, hi.ptr, lo.ptr, k))
+        ex = P.astype(np.float64) @ P.astype(np.float64).T
+        for nt in (1, 3):
+            dC = DeviceBuffer.from_array(np.zeros((m, m), np.float32))
+            err = DeviceBuffer.from_array(np.zeros(1, np.int32))
+            check(L.starpu_gb300_tc_update(None, m, m, k, hi.ptr, lo.ptr, k, hi.ptr, lo.ptr, k, nt, 0, dC.ptr, m,
+                                           err.ptr))
+            Cg = -dC.download((m, m), np.float32).astype(np.float64)
+            out[f"bf16_nterms{nt}_rms"] = float(np.sqrt(((Cg - ex) ** 2).mean() / (ex ** 2).mean()))
     print(json.dumps(out))
 
 

@@ -90,20 +90,37 @@ int split_bf16(cudaStream_t s, int m, int k, const float *P, long ldp, void *hi,
 
 // ---- scaled FP16 panels (the factorisation's operands) ---------------------
 //
-// Row i of P (m x k FP32, column-major) is scaled by 2^-e_i, the power of two
-// that brings max_k |P_ik| below 1 (rs[i] = 2^e_i; 1 for a zero row), and
-// split as x = P_ik 2^-e_i = h + 2^-11 l: h = fp16(x), l = fp16((x - h) 2^11),
-// H = 2^11 h (exact).  All three K-major (row i = k contiguous halves, row
-// stride ldk, columns k..ldk-1 zero).  About 22 significant bits of every
-// element reach the tensor cores, against 16 for the BF16 split.
+// Row i of P (m x k FP32, column-major) is multiplied by 2^-k_i (rk[i] = k_i),
+// the power of two that brings a bound b_i of its elements below 2^15, and split as
+// x = h + l, h = fp16(x), l = fp16(x - h), both K-major (row i = k contiguous
+// halves, row stride ldk, columns k..ldk-1 zero).  About 22 significant bits
+// of every element above ~2^-18 b_i reach the tensor cores (16 with the BF16
+// split); elements up to about 4 b_i stay below FP16's largest value.
+//
+// The bounds need no pass over the panel: for the SPD matrix being factored,
+// the Schur complement S after any number of steps keeps |S_rj| <=
+// sqrt(S_rr S_jj) <= sqrt(A_rr A_jj), and a row of L keeps |L_rj| <= sqrt(A_rr)
+// (sum_j L_rj^2 = A_rr).  So with d = diag(A) saved before the factorisation:
+// b_r = sqrt(d_r f), f = max of d over the panel's columns for the panel
+// before its triangular solve, f = 1 for the solved panel.  A matrix that is
+// not SPD may break the bound; its factorisation then fails on a pivot.
 struct F16Panel {
-    __half *h, *l, *H;
-    float *rs;
+    __half *h, *l;
+    int *rk;
 };
 
-// rs[i] = 2^e_i with max_k |P_ik| < 2^e_i (the largest |P_ik| is then below 1
-// after the scaling).  32 rows per CTA, the k loop split over 8 thread rows.
-__global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P, long ldp, float *__restrict__ rs)
+// k with bound 2^-k < 2^15
+__device__ __forceinline__ int f16_row_exp(float bound)
+{
+    int e = 0;
+    if (bound > 0.0f && isfinite(bound)) frexpf(bound, &e);  // bound = f 2^e, 0.5 <= f < 1
+    return e - 15;
+}
+
+// rk[i] from the actual row maxima (the inverse of a diagonal tile, whose
+// elements have no bound from the matrix): 32 rows per CTA, the k loop split
+// over 8 thread rows.
+__global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P, long ldp, int *__restrict__ rk)
 {
     __shared__ float red[8][33];
     const int r = blockIdx.x * 32 + threadIdx.x;
@@ -114,71 +131,110 @@ __global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P
     __syncthreads();
     if (threadIdx.y == 0 && r < m) {
         for (int y = 1; y < 8; ++y) mx = fmaxf(mx, red[y][threadIdx.x]);
-        int e = 0;
-        if (mx > 0.0f && isfinite(mx)) frexpf(mx, &e);  // mx = f 2^e, 0.5 <= f < 1: mx < 2^e
-        rs[r] = ldexpf(1.0f, e);
+        rk[r] = f16_row_exp(mx);
     }
 }
 
-__global__ void split_f16s_kmajor_kernel(int m, int k, const float *__restrict__ P, long ldp,
-                                         const float *__restrict__ rs, __half *__restrict__ h, __half *__restrict__ l,
-                                         __half *__restrict__ H, long ldk)
+// d[r] = A_rr, and dtile[t] = max of d over the nb rows of column tile t
+__global__ void diag_bounds_kernel(int n, const float *__restrict__ A, long lda, int nb, float *__restrict__ d,
+                                   float *__restrict__ dtile)
+{
+    __shared__ float red[256];
+    const int t = blockIdx.x;
+    float mx = 0.0f;
+    for (int r = t * nb + threadIdx.x; r < min(n, (t + 1) * nb); r += blockDim.x) {
+        const float v = A[r + (long)r * lda];
+        d[r] = v;
+        mx = fmaxf(mx, fabsf(v));
+    }
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) dtile[t] = red[0];
+}
+
+// the split; rk given (from_bounds = 0) or computed from d / f (from_bounds = 1:
+// rows r0.. of the matrix, d indexed by matrix row, *f or 1 when f is NULL)
+__global__ void split_f16s_kmajor_kernel(int m, int k, const float *__restrict__ P, long ldp, int *__restrict__ rk,
+                                         int from_bounds, const float *__restrict__ d, int r0,
+                                         const float *__restrict__ f, __half *__restrict__ h, __half *__restrict__ l,
+                                         long ldk)
 {
     __shared__ float t[32][33];
-    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    __shared__ int sh[32];
+    const int rb = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    if (tid < 32 && rb + tid < m) {
+        int e;
+        if (from_bounds) {
+            // sqrt(d_r) sqrt(f): no underflow or overflow of the product for
+            // matrices scaled far from 1
+            e = f16_row_exp(sqrtf(fmaxf(d[r0 + rb + tid], 0.0f)) * (f ? sqrtf(*f) : 1.0f));
+            if (blockIdx.y == 0) rk[rb + tid] = e;
+        } else {
+            e = rk[rb + tid];
+        }
+        sh[tid] = -e;
+    }
     for (int c = threadIdx.y; c < 32; c += blockDim.y) {
-        const int r = r0 + threadIdx.x, col = c0 + c;
+        const int r = rb + threadIdx.x, col = c0 + c;
         t[c][threadIdx.x] = (r < m && col < k) ? P[r + (long)col * ldp] : 0.0f;
     }
     __syncthreads();
     for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
-        const int r = r0 + rr, col = c0 + threadIdx.x;
+        const int r = rb + rr, col = c0 + threadIdx.x;
         if (r < m && col < ldk) {
-            const float x = t[threadIdx.x][rr] / rs[r];  // exact: division by a power of two
+            const float x = ldexpf(t[threadIdx.x][rr], sh[rr]);  // exact (no scale factor to overflow)
             const __half hh = __float2half_rn(x);
-            const float hf = __half2float(hh);
             const long o = (long)r * ldk + col;
             h[o] = hh;
-            l[o] = __float2half_rn((x - hf) * 2048.0f);
-            H[o] = __float2half_rn(hf * 2048.0f);
+            l[o] = __float2half_rn(x - __half2float(hh));
         }
     }
 }
 
-static int split_f16s(cudaStream_t s, int m, int k, const float *P, long ldp, const F16Panel &o, long ldk)
+// from the actual row maxima (d == NULL) or from the diagonal bounds
+static int split_f16s(cudaStream_t s, int m, int k, const float *P, long ldp, const F16Panel &o, long ldk,
+                      const float *d = nullptr, int r0 = 0, const float *f = nullptr)
 {
     if (m <= 0 || k <= 0) return GB300_OK;
-    gb300_count_launch(), panel_row_scale_kernel<<<(m + 31) / 32, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rs);
+    if (!d) gb300_count_launch(), panel_row_scale_kernel<<<(m + 31) / 32, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rk);
     dim3 g((m + 31) / 32, (unsigned)((ldk + 31) / 32));
-    gb300_count_launch(), split_f16s_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rs, o.h, o.l, o.H, ldk);
+    gb300_count_launch(), split_f16s_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rk, d ? 1 : 0, d, r0, f,
+                                                                           o.h, o.l, ldk);
     return gb300_last_launch_status();
 }
 
 // rows [r, ...) of a split panel
 static F16Panel rows_of(const F16Panel &p, long r, long ldk)
 {
-    return {p.h + r * ldk, p.l + r * ldk, p.H + r * ldk, p.rs + r};
+    return {p.h + r * ldk, p.l + r * ldk, p.rk + r};
 }
 
 // One operand of the update: BF16 hi / lo, or the scaled FP16 split
-// (hi = h, lo = l, hh = H, rs = the row scales).
+// (hi = h, lo = l, rk = the row scale exponents).
 struct TcOperand {
-    const void *hi, *lo, *hh;
-    const float *rs;
+    const void *hi, *lo;
+    const int *rk;
 };
 
 // max_grid > 0 caps the persistent grid (CTAs, one per SM): the trailing
 // update that runs beside the next panel leaves that panel's SMs free.
-// f16s: both operands are scaled FP16 panels.
+// f16s: both operands are scaled FP16 panels.  [t0, t1) (t1 < 0: to the end)
+// restricts the launch to a range of the update's tiles, in the order
+// tcu_tile_coords gives them (lower: column by column from the diagonal).
 static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A, long lda, const TcOperand &B,
                         long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store, int max_grid,
-                        bool f16s)
+                        bool f16s, int t0 = 0, int t1 = -1)
 {
     if (m <= 0 || n <= 0 || K <= 0) return GB300_OK;
     if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!A.lo || !B.lo)) || (lower && m != n) || !d_err ||
-        (f16s && (!A.hh || !A.rs || !B.rs)))
+        (f16s && (!A.rk || !B.rk)))
         return GB300_EINVAL;
-    CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo, ta_hh;
+    CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
     int rc;
     if ((rc = make_kmajor_map(&ta_hi, A.hi, m, K, lda, TCU_BM))) return rc;
     if ((rc = make_kmajor_map(&tb_hi, B.hi, n, K, ldb, TCU_BN))) return rc;
@@ -189,16 +245,10 @@ static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A,
         ta_lo = ta_hi;
         tb_lo = tb_hi;
     }
-    if (f16s) {
-        if ((rc = make_kmajor_map(&ta_hh, A.hh, m, K, lda, TCU_BM))) return rc;
-    } else {
-        ta_hh = ta_hi;
-    }
     TcUpdateArgs a;
     a.f16s = f16s ? 1 : 0;
-    a.rs_a = f16s ? A.rs : nullptr;
-    a.rs_b = f16s ? B.rs : nullptr;
-    a.gscale = 1.0f / 2048.0f;
+    a.rk_a = f16s ? A.rk : nullptr;
+    a.rk_b = f16s ? B.rk : nullptr;
     a.C = C;
     a.ldc = ldc;
     a.m = m;
@@ -216,11 +266,15 @@ static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A,
     } else {
         a.num_tiles = a.tiles_m * a.tiles_n;
     }
+    a.tile_begin = std::max(0, std::min(t0, a.num_tiles));
+    a.tile_end = t1 < 0 ? a.num_tiles : std::max(a.tile_begin, std::min(t1, a.num_tiles));
+    if (a.tile_end <= a.tile_begin) return GB300_OK;
     a.err = d_err;
     a.wait_budget_ns = 2000000000ull;  // 2 s per wait: far above any legitimate stall
     if (int rc = gb300_func_dyn_smem((const void *)tc_update_kernel, TCU_SMEM)) return rc;
-    const int grid = std::min(a.num_tiles, max_grid > 0 ? std::min(max_grid, num_sms()) : num_sms());
-    gb300_count_launch(), tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, ta_hh, a);
+    const int ntl = a.tile_end - a.tile_begin;
+    const int grid = std::min(ntl, max_grid > 0 ? std::min(max_grid, num_sms()) : num_sms());
+    gb300_count_launch(), tc_update_kernel<<<grid, TCU_THREADS, TCU_SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, a);
     return gb300_last_launch_status();
 }
 
@@ -229,27 +283,31 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
               const void *b_lo, long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
               int max_grid = 0)
 {
-    return tc_update_op(s, m, n, K, {a_hi, a_lo, nullptr, nullptr}, lda, {b_hi, b_lo, nullptr, nullptr}, ldb, nterms,
+    return tc_update_op(s, m, n, K, {a_hi, a_lo, nullptr}, lda, {b_hi, b_lo, nullptr}, ldb, nterms,
                         lower, C, ldc, d_err, store, max_grid, false);
 }
 
 // scaled FP16 panels (the factorisation)
 static int tc_update_f16s(cudaStream_t s, int m, int n, int K, const F16Panel &A, long lda, const F16Panel &B,
                           long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
-                          int max_grid = 0)
+                          int max_grid = 0, int t0 = 0, int t1 = -1)
 {
-    return tc_update_op(s, m, n, K, {A.h, A.l, A.H, A.rs}, lda, {B.h, B.l, B.H, B.rs}, ldb, nterms, lower, C, ldc,
-                        d_err, store, max_grid, true);
+    return tc_update_op(s, m, n, K, {A.h, A.l, A.rk}, lda, {B.h, B.l, B.rk}, ldb, nterms, lower, C, ldc,
+                        d_err, store, max_grid, true, t0, t1);
 }
 
+
+
 // Workspace of potrf_tc for order n and tile nb (ldk = nb rounded up to 64):
-// two split panels (scaled FP16 h, l, H: n x ldk each, and n row scales; step
+// two split panels (scaled FP16 h, l: n x ldk each, and n row scales; step
 // k's panel is read by its trailing update while step k+1's is written), the
-// inverse of the diagonal tile (ldk x ldk FP32) and its split, the doubling
-// scratch of the triangular inverse (ldk x ldk FP32) and the diagonal-tile
-// kernel's barrier counter.
+// inverse of the diagonal tile (ldk x ldk FP32) and its split, the diagonal of
+// the matrix and its maximum per column tile (the panels' row bounds), the
+// doubling scratch of the triangular inverse (ldk x ldk FP32) and the
+// diagonal-tile kernel's barrier counter.
 struct TcWs {
     F16Panel pan[2], inv;
+    float *d, *dtile;
     float *linv, *scratch;
     unsigned *bar;  // grid-barrier counter of the diagonal-tile kernel
 };
@@ -259,16 +317,20 @@ static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t panel = al((size_t)n * ldk * 2), rsn = al((size_t)n * 4);
     const size_t inv = ldk * ldk, invh = al(inv * 2), rsk = al(ldk * 4);
-    const size_t off_inv = 2 * (3 * panel + rsn);
-    const size_t off_linv = off_inv + 3 * invh + rsk;
+    const size_t ntiles = nb > 0 ? ((size_t)n + nb - 1) / nb : 1;
+    const size_t off_inv = 2 * (2 * panel + rsn);
+    const size_t off_d = off_inv + 2 * invh + rsk;
+    const size_t off_linv = off_d + rsn + al(ntiles * 4);
     if (w && base) {
         char *b = (char *)base;
         for (int i = 0; i < 2; ++i) {
-            char *p = b + i * (3 * panel + rsn);
-            w->pan[i] = {(__half *)p, (__half *)(p + panel), (__half *)(p + 2 * panel), (float *)(p + 3 * panel)};
+            char *p = b + i * (2 * panel + rsn);
+            w->pan[i] = {(__half *)p, (__half *)(p + panel), (int *)(p + 2 * panel)};
         }
         char *q = b + off_inv;
-        w->inv = {(__half *)q, (__half *)(q + invh), (__half *)(q + 2 * invh), (float *)(q + 3 * invh)};
+        w->inv = {(__half *)q, (__half *)(q + invh), (int *)(q + 2 * invh)};
+        w->d = (float *)(b + off_d);
+        w->dtile = (float *)(b + off_d + rsn);
         w->linv = (float *)(b + off_linv);
         w->scratch = w->linv + inv;
         w->bar = (unsigned *)(w->scratch + inv);
@@ -393,13 +455,14 @@ static int lookahead_sms(int m2, int kb)
     return best;
 }
 
-// Panel of the step at column k0 (width kb): FP32 POTRF of the diagonal tile
-// (SIMT), its inverse, the panel TRSM  P <- P L_kk^-T  as one split-BF16
-// product P * Linv^T (store form, always 3 products), and the split of the
-// solved panel into (hi, lo) for the trailing update.  sms > 0 keeps its
+// Panel of the step at column k0 (width kb), in two parts.  panel_diag: the
+// FP32 POTRF of the diagonal tile (SIMT, one cooperative launch) and its
+// inverse, split for the tensor cores.  panel_solve: the panel TRSM
+// P <- P L_kk^-T  as one split-precision product P * Linv^T (store form,
+// always 3 products), with P split before and after.  sms > 0 keeps their
 // kernels to that many SMs' worth of CTAs.
-static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb, int nb, int np, const TcWs &w,
-                      int buf, float *linv_band, int *d_info, int *d_err, int sms)
+static int panel_diag(cudaStream_t s, int n, float *A, long lda, int k0, int kb, int nb, const TcWs &w,
+                      float *linv_band, int *d_info, int *d_err, int sms)
 {
     const long ldk = ((long)nb + 63) / 64 * 64;
     float *Akk = A + k0 + (long)k0 * lda;
@@ -416,24 +479,34 @@ static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb,
         potrf_tiled<float>(s, kb, Akk, lda, small_w<float>::value, d_info, k0);
         if (m > 0) trtri_lower<float>(s, kb, Akk, lda, linv, ldk, w.scratch);
     }
-    if (rc || m <= 0) {
-        gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0, 4.0 * kb * kb);
-        return rc;
-    }
+    // the inverse split from its row maxima (its elements have no bound from A)
+    if (!rc && m > 0) rc = split_f16s(s, kb, kb, linv, ldk, w.inv, ldk);
+    gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0, 4.0 * kb * kb);
+    return rc;
+}
+
+static int panel_solve(cudaStream_t s, int n, float *A, long lda, int k0, int kb, int nb, int np, const TcWs &w,
+                       int buf, int *d_err, int sms, bool bounds = true)
+{
+    const long ldk = ((long)nb + 63) / 64 * 64;
+    const int m = n - k0 - kb;
+    if (m <= 0) return GB300_OK;
+    const int slot = gb300_prof_begin(s, GB300_PROF_PANEL);
     float *P = A + (k0 + kb) + (long)k0 * lda;
-    rc = split_f16s(s, kb, kb, linv, ldk, w.inv, ldk);
-    if (!rc) rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk);
+    // the panel before its solve bounded by sqrt(d_r max d over the tile's
+    // columns), the solved panel by sqrt(d_r) (without the bounds -- the first
+    // panel, before the diagonal is saved -- both from their row maxima)
+    const float *d = bounds ? w.d : nullptr;
+    int rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk, d, k0 + kb, w.dtile + k0 / nb);
     if (!rc) rc = tc_update_f16s(s, m, kb, kb, w.pan[buf], ldk, w.inv, ldk, 3, 0, P, lda, d_err, 1, sms);
-    if (!rc) rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk);
-    // algorithmic work of the panel: POTRF kb^3/3 + TRSM m kb^2; bytes: the
-    // tile and the panel read and written once, the BF16 panel written
-    gb300_prof_end(s, slot, (double)kb * kb * kb / 3.0 + (double)m * kb * kb,
-                   8.0 * kb * kb + 8.0 * m * kb + 2.0 * m * ldk * np);
+    if (!rc) rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk, d, k0 + kb, nullptr);
+    // algorithmic work: TRSM m kb^2; bytes: the panel read and written, its split written twice
+    gb300_prof_end(s, slot, (double)m * kb * kb, 8.0 * m * kb + 4.0 * m * ldk * np);
     return rc;
 }
 
 // Tiled right-looking Cholesky of an FP32 matrix on the tensor cores
-// (split-BF16 products when nterms == 3) with a lookahead of one panel.
+// (split-precision products when nterms == 3) with a lookahead of one panel.
 // After step k's panel, its rank-kb update is applied first to the next
 // column block (its lower diagonal tile and the rectangle below), then step
 // k+1's panel -- which needs nothing else -- runs on a few SMs while the rest
@@ -441,7 +514,11 @@ static int panel_step(cudaStream_t s, int n, float *A, long lda, int k0, int kb,
 // other SMs, from a high-priority stream.  The two write disjoint parts of A
 // and read different panel buffers; the streams join before step k+1's
 // update.  The diagonal-tile factorisation, latency-bound on a few SMs, thus
-// hides behind the trailing update.
+// hides behind the trailing update.  (Measured and not kept: factoring only
+// the diagonal tile beside the first tiles of the trailing update and
+// running the panel's solve and the rest of the update on the whole GPU --
+// 75.9 ms per solve at n = 32768 against 70.7: the diagonal tile slows down
+// beside other kernels, and the early steps lose the overlap of the solve.)
 // `side(s)`, when given, is called once, from the loop, when the step whose
 // trailing triangle first has at most `side_rows` rows has been enqueued: the
 // caller starts work that only needs the GPU's idle resources there (the
@@ -459,12 +536,20 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
     const long ldk = ((long)nb + 63) / 64 * 64;
     TcWs w;
     tc_ws_layout(n, nb, work, &w);
-    const int np = nterms == 3 ? 3 : 2;  // split panel arrays an update reads: h, l, H (or H, h)
+    const int np = nterms == 3 ? 2 : 1;  // split panel arrays an update reads: h, l
     // a step has a trailing triangle beyond its next column block only when n > 2 nb
     LookaheadStream *la = n > 2 * nb ? lookahead_stream() : nullptr;
     int buf = 0;
-    int rc = panel_step(s, n, A, lda, 0, std::min(nb, n), nb, np, w, buf, linv_band, d_info, d_err, 0);
+    int rc = panel_diag(s, n, A, lda, 0, std::min(nb, n), nb, w, linv_band, d_info, d_err, 0);
+    if (!rc) rc = panel_solve(s, n, A, lda, 0, std::min(nb, n), nb, np, w, buf, d_err, 0, false);
     if (ready) cudaStreamWaitEvent(s, ready, 0);
+    // the diagonal of the matrix (rows past the first tile, which no step has
+    // touched yet) and its maxima per column tile: the later panels' row bounds
+    if (!rc && n > nb) {
+        const int ntiles = (n + nb - 1) / nb;
+        gb300_count_launch(), diag_bounds_kernel<<<ntiles, 256, 0, s>>>(n, A, lda, nb, w.d, w.dtile);
+        rc = gb300_last_launch_status();
+    }
     if (!rc && on_panel && n > nb) on_panel(s, 0, nb);
     for (int k0 = 0; k0 < n && !rc; k0 += nb) {
         const int kb = std::min(nb, n - k0);
@@ -500,7 +585,8 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
                                 num_sms() - la_sms);
             gb300_prof_end(la->s, slot, f2, b2);
             cudaEventRecord(la->join, la->s);
-            if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, la_sms);
+            if (!rc) rc = panel_diag(s, n, A, lda, k0 + kb, kb1, nb, w, linv_band, d_info, d_err, la_sms);
+            if (!rc) rc = panel_solve(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, d_err, la_sms);
             if (!rc && on_panel) on_panel(s, k0 + kb, kb1);
             cudaStreamWaitEvent(s, la->join, 0);  // joined before step k+1's update
         } else {
@@ -509,7 +595,8 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
                 rc = tc_update_f16s(s, m2, m2, kb, pan2, ldk, pan2, ldk, nterms, 1, C22, lda, d_err);
                 gb300_prof_end(s, slot, f2, b2);
             }
-            if (!rc) rc = panel_step(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, linv_band, d_info, d_err, 0);
+            if (!rc) rc = panel_diag(s, n, A, lda, k0 + kb, kb1, nb, w, linv_band, d_info, d_err, 0);
+            if (!rc) rc = panel_solve(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, d_err, 0);
             if (!rc && on_panel && m2 > 0) on_panel(s, k0 + kb, kb1);
         }
         buf = nbuf;

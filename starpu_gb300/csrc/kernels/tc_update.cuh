@@ -14,15 +14,16 @@
 // the FP32 panel into the product (the dropped A_lo B_lo^T term is ~2^-16
 // relative).
 //
-// Scaled FP16 operands (f16s = 1, the factorisation's panels): every row i of
-// a panel is scaled by a power of two 2^-e_i that brings its largest element
-// below 1, then split as x 2^-e_i = h + 2^-11 l with h = fp16(x 2^-e_i) and
-// l = fp16((x 2^-e_i - h) 2^11): about 22 significant bits (FP16 keeps 11,
-// and the split stays inside its normal range).  With H = 2^11 h (exact) the
-// three products H_A h_B^T + h_A l_B^T + l_A h_B^T accumulate 2^11 times the
-// scaled product in one accumulator; the epilogue multiplies by
-// 2^-11 2^e_i 2^e_j (rs_a[i] rs_b[j] gscale: powers of two, exact).  The
-// dropped l_A l_B^T term weighs 2^-22 of the product.
+// Scaled FP16 operands (f16s = 1, the factorisation's panels): row i of a
+// panel is multiplied by 2^-k_i, the power of two that brings a bound of its
+// elements just below 2^15 (FP16's largest binade), then split as
+// x = h + l with h = fp16(x), l = fp16(x - h): 11 + 11 significant bits, and l
+// stays a normal FP16 for every element above ~2^-18 of the bound.  The three
+// products h_A h_B^T + h_A l_B^T + l_A h_B^T (each exact in FP32) accumulate
+// the scaled product; the epilogue scales it by 2^(k_i + k_j) in one ldexp
+// (exact, and free of the overflow a product of two scale factors could meet
+// for matrices far from unit scale).  The dropped l_A l_B^T term weighs 2^-22
+// of the product.
 //
 // CTA = 6 warps, one CTA per SM (persistent, static round-robin over tiles):
 //   warp 0  TMA producer     (one elected lane)
@@ -63,10 +64,10 @@ struct TcUpdateArgs {
     int nterms;        // 1 or 3
     int lower;         // 1: only elements with row >= col (square trailing matrix)
     int store;         // 1: C = sum (C is not read), 0: C -= sum
-    int f16s;          // 1: scaled FP16 operands (rs_a, rs_b, gscale below); 0: BF16
-    const float *rs_a, *rs_b;  // f16s: row scales 2^e of A (m) and B (n)
-    float gscale;              // f16s: 2^-11
+    int f16s;          // 1: scaled FP16 operands (rk_a, rk_b below); 0: BF16
+    const int *rk_a, *rk_b;    // f16s: row scale exponents of A (m) and B (n)
     int tiles_m, tiles_n, num_tiles;
+    int tile_begin, tile_end;  // the launch covers tiles [tile_begin, tile_end) of the num_tiles
     int *err;
     unsigned long long wait_budget_ns;
 };
@@ -97,7 +98,7 @@ __device__ __forceinline__ void tcu_tile_coords(const TcUpdateArgs &a, int t, in
 __global__ void __launch_bounds__(TCU_THREADS, 1)
 tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_constant__ CUtensorMap tm_a_lo,
                  const __grid_constant__ CUtensorMap tm_b_hi, const __grid_constant__ CUtensorMap tm_b_lo,
-                 const __grid_constant__ CUtensorMap tm_a_hh, const TcUpdateArgs args)
+                 const TcUpdateArgs args)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte aligned tile area (required by the 128B swizzle atoms)
@@ -136,7 +137,6 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
             ptx::tma_prefetch_desc(&tm_a_lo);
             ptx::tma_prefetch_desc(&tm_b_lo);
         }
-        if (args.f16s) ptx::tma_prefetch_desc(&tm_a_hh);
     }
     if (warp == 1) {
         ptx::tmem_alloc(tmem_slot, TCU_TMEM_COLS);
@@ -157,7 +157,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
             uint32_t phase = 0;
             int issued = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < args.num_tiles && ok; t += gridDim.x) {
+            for (int t = args.tile_begin + blockIdx.x; t < args.tile_end && ok; t += gridDim.x) {
                 int tm, tn;
                 tcu_tile_coords(args, t, tm, tn);
                 const int m0 = tm * TCU_BM, n0 = tn * TCU_BN;
@@ -172,8 +172,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                     // their additions is 2^-8 smaller than on top of A_hi B_hi^T
                     const int term = args.nterms == 3 ? (kb / kblocks + 1) % 3 : 0;
                     const int kx = (kb % kblocks) * TCU_BK;
-                    // term 0: A_hi B_hi^T (scaled FP16: H_A h_B^T), 1: A_hi B_lo^T, 2: A_lo B_hi^T
-                    const CUtensorMap *ma = (term == 2) ? &tm_a_lo : (term == 0 && args.f16s) ? &tm_a_hh : &tm_a_hi;
+                    // term 0: A_hi B_hi^T, 1: A_hi B_lo^T, 2: A_lo B_hi^T
+                    const CUtensorMap *ma = (term == 2) ? &tm_a_lo : &tm_a_hi;
                     const CUtensorMap *mb = (term == 1) ? &tm_b_lo : &tm_b_hi;
                     ptx::mbar_arrive_expect_tx(&full[stage], TCU_A_BYTES + TCU_B_BYTES);
                     ptx::tma_load_2d(sA + stage * TCU_A_BYTES, ma, &full[stage], kx, m0);
@@ -213,7 +213,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
             int acc = 0;
             uint32_t acc_phase = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < args.num_tiles && ok; t += gridDim.x) {
+            for (int t = args.tile_begin + blockIdx.x; t < args.tile_end && ok; t += gridDim.x) {
                 if (!ptx::wait_parity(&acc_empty[acc], acc_phase ^ 1, abort_flag, args.wait_budget_ns)) {
                     ok = false;
                     break;
@@ -264,7 +264,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
         int acc = 0;
         uint32_t acc_phase = 0;
         bool ok = true;
-        for (int t = blockIdx.x; t < args.num_tiles; t += gridDim.x) {
+        for (int t = args.tile_begin + blockIdx.x; t < args.tile_end; t += gridDim.x) {
             int tm, tn;
             tcu_tile_coords(args, t, tm, tn);
             const int row = tm * TCU_BM + row_in_tile;
@@ -277,8 +277,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
             const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TCU_BN);
             float *crow = args.C + row;
             const bool row_ok = row < args.m;
-            // scaled FP16: the row's factor 2^-11 2^e_i (the columns' 2^e_j below)
-            const float rsc = (args.f16s && row_ok) ? args.gscale * args.rs_a[row] : 1.0f;
+            // scaled FP16: the row's scale exponent (the columns' below)
+            const int rka = (args.f16s && row_ok) ? args.rk_a[row] : 0;
 #pragma unroll 1
             for (int ch = 0; ch < TCU_BN / 32; ++ch) {
                 uint32_t r[32];
@@ -301,10 +301,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
 #pragma unroll
                         for (int j = 0; j < 32; ++j) {
                             const int col = c0 + j;
-                            const float cs = col < args.n ? args.rs_b[col] : 0.0f;
-                            // two exact power-of-two products, the first keeping the value
-                            // near its final size (no underflow for scales down to ~2^-60)
-                            r[j] = __float_as_uint((__uint_as_float(r[j]) * rsc) * cs);
+                            const int rkb = col < args.n ? args.rk_b[col] : 0;
+                            r[j] = __float_as_uint(ldexpf(__uint_as_float(r[j]), rka + rkb));
                         }
                     }
 #pragma unroll

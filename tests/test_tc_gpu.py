@@ -127,8 +127,11 @@ def test_spotrf_tc_gram_residual(gpu, oracle):
         L = np.tril(d.download((n, n), np.float32))
         assert info.download((1,), np.int32)[0] == 0
         res[nterms] = oracle.llt_residual(A, L)
-    assert res[1] < 1e-2
-    assert res[3] < 1e-5
+    # the factorisation's panels reach the tensor cores as row-scaled FP16
+    # splits (~22 bits; the BF16 split measured 3.9e-6 at n = 8192): three
+    # products land within a few times the FP32 accumulation error
+    assert res[1] < 1e-3
+    assert res[3] < 3e-6
 
 
 @pytest.mark.parametrize("n,nb", [(2000, 1000), (700, 333), (1088, 1024), (130, 64), (1024, 1024)])
