@@ -488,6 +488,20 @@ def run_ours(args):
         check(L.starpu_gb300_shift_diagonal(stream, n, A.ptr, n, a - cur_alpha))
         cur_alpha = a
 
+    # the schedule of the factorisation for this order and tile, tuned on this GPU and stored beside the
+    # perfmodels (StarPU calibrates its perfmodels the same way before timing); not timed
+    schedule = None
+    if not args.no_autotune:
+        ta = time.perf_counter()
+        rc = L.starpu_gb300_dense_autotune(n, nb, 2)
+        la, td, up, pr, st = C.c_int(), C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        if rc == 0 and L.starpu_gb300_dense_get_tuning(nb, C.byref(la), C.byref(td), C.byref(up), C.byref(pr),
+                                                        C.byref(st)):
+            schedule = {"lookahead_sms": la.value if la.value >= 0 else "per-step model",
+                        "t_diag_us": td.value, "update_tflops": up.value, "panel_rate": pr.value,
+                        "factor_ms": st.value, "tuning_s": time.perf_counter() - ta}
+        else:
+            schedule = {"autotune_rc": rc}
     lw = L.starpu_gb300_dsposv_workspace(n, nrhs, nb)
     W = DeviceBuffer(lw)
     info = IrInfo()
@@ -789,6 +803,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": bench_config(args, world), "factor_terms": args.nterms, "generation_s": gen_s,
+            "schedule": schedule,
             "backward_error": max(berrs), "backward_error_fp64_check": berr_fp64_check, "iterations": iters,
             "forward_error": accuracy["dsposv"]["forward_error"] if accuracy else None, "accuracy": accuracy,
             "vs_fp64_plain_same_n": (value / world / fp64_same["gflops"]) if fp64_same else None,
@@ -820,6 +835,7 @@ KERNEL_CASES_DOC = """Single-kernel cases for profiling (ncu) and quick timing, 
     python bench.py --case dsposv_host --n 8192 --nb 1024 --nrhs 16 --reps 2
     python bench.py --case factor_error --n 8192 --nb 1024 --kappa 1e4
     python bench.py --case update_error --m 2048 --k 1024
+    python bench.py --case tile_tc --m 8192 --k 1024 --reps 3
 
 Each case allocates its operands once, runs `--reps` launches of the same
 shape and prints the mean time per launch measured with CUDA events.
@@ -858,7 +874,7 @@ def run_case(argv):
     ap = argparse.ArgumentParser(prog="bench.py --case")
     ap.add_argument("case", choices=["tc_update", "residual", "potrs", "sweep", "spotrf_tc", "dpotrf", "dsposv",
                                      "tile_ops", "diag", "tile_sweep", "syresidual", "batched", "lu_tile",
-                                     "dsposv_host", "factor_error", "update_error"])
+                                     "dsposv_host", "factor_error", "update_error", "tile_tc"])
     ap.add_argument("--nsys", type=int, default=512)
     ap.add_argument("--kappa", type=float, default=1e4)
     ap.add_argument("--m", type=int, default=8192)
@@ -1123,6 +1139,20 @@ def run_case(argv):
             check(L.starpu_gb300_stream_sync(None))
             Lf = np.tril(d.download((n, n), np.float32).astype(np.float64))
             out[name] = float(np.linalg.norm(Lf @ Lf.T - A) / np.linalg.norm(A))
+    elif a.case == "tile_tc":
+        # the tensor-core tile update of the codelets on one m x m tile, K = k:
+        # FP32 operand split to row-scaled FP16, lower update C -= A A^T
+        m, k = a.m, a.k
+        rng = np.random.default_rng(2)
+        P = DeviceBuffer.from_array(np.asfortranarray(rng.standard_normal((m, k)).astype(np.float32)))
+        Cb = DeviceBuffer.from_array(np.zeros((m, m), np.float32, order="F"))
+        lw = L.starpu_gb300_tile_tc_workspace(max(m, k))
+        Wk = DeviceBuffer(lw)
+        err = DeviceBuffer.from_array(np.zeros(1, np.int32))
+        check(L.starpu_gb300_tile_tc_prepare())
+        ms = _timed(L, lambda: check(L.starpu_gb300_sgemm_nt_tile_tc(None, m, m, k, P.ptr, m, P.ptr, m, Cb.ptr, m, 1,
+                                                                      Wk.ptr, lw, err.ptr)), a.reps)
+        out.update(m=m, k=k, ms_including_split=ms, tflops=3.0 * k * m * (m + 1.0) / ms / 1e9)
     elif a.case == "update_error":
         # one BF16 split update C = -P P^T (m x K) against its FP64 product, rms relative error
         m, k = a.m, a.k
@@ -1166,6 +1196,7 @@ def main():
                     help="DRAM bytes per trailing-update launch (default: the ncu capture of an m = 8192 launch "
                          "scaled to the factorisation's launches)")
     ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the stored or default factorisation schedule")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-fp64-same-n", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -204,6 +204,23 @@ int starpu_gb300_tc_update(void *stream, int m, int n, int k, const void *a_hi, 
                            const void *b_hi, const void *b_lo, int ldb, int nterms, int lower, float *C, int ldc,
                            int *d_err);
 
+/* The FP32 tile update on the tensor cores, for the codelets of the tiled
+ * Cholesky: C[m x n] -= A B^T (A m x k, B n x k, FP32, column-major).  Each
+ * operand row is scaled by a power of two and split as h + l in FP16 (about
+ * 22 significant bits) in `work`; the three products h h + h l + l h
+ * accumulate in FP32 on the tensor cores.  lower = 1 (m == n) writes only
+ * row >= col: the SYRK form, and B == A (same pointer and ld) splits once.
+ * Replaces cublasSgemm(N, T, -1, +1) of examples/cholesky/cholesky_kernels.c:98
+ * and cublasSsyrk(L, N, -1, +1) of :177 for FP32 tiles.  `work`: device,
+ * >= starpu_gb300_tile_tc_workspace(max(m, n, k)) bytes.  d_err: device status
+ * word, set non-zero if an internal wait timed out.  _prepare sets the
+ * kernel's shared-memory limit on the current device (call it once before a
+ * stream capture that records these updates). */
+size_t starpu_gb300_tile_tc_workspace(int nmax);
+int starpu_gb300_tile_tc_prepare(void);
+int starpu_gb300_sgemm_nt_tile_tc(void *stream, int m, int n, int k, const float *A, int lda, const float *B,
+                                  int ldb, float *C, int ldc, int lower, void *work, size_t lwork, int *d_err);
+
 /* Bytes of BF16 panel workspace starpu_gb300_spotrf_tc needs. */
 size_t starpu_gb300_spotrf_tc_workspace(int n, int nb);
 

@@ -105,6 +105,24 @@ int starpu_gb300_batched_autotune(int systems_per_bucket, int reps);
 /* Current block size per bucket (6 buckets); returns the bucket count. */
 int starpu_gb300_batched_get_tuning(signed char *nb_per_bucket, int nbuckets);
 
+/* Autotunes the schedule of the mixed solve's tensor-core factorisation for
+ * tile nb (64..1024) at order n (>= 3 nb) on the current device: times the
+ * diagonal-tile kernel on a quarter of the SMs, the trailing update on the
+ * whole GPU and the panel solve on the quarter, then whole factorisations of
+ * an n x n matrix with the lookahead split of the per-step model on those
+ * times, and with a quarter, a third, half of the SMs and no lookahead; the
+ * fastest choice and the measured times are stored in the same table
+ * (gb300_chol_tuning.<host>, beside the perfmodels) and every later
+ * factorisation with tile nb uses them (GB300_LOOKAHEAD_SMS still overrides).
+ * Allocates its own buffers.  StarPU's counterpart is the calibration of the
+ * history perfmodels (src/core/perfmodel/perfmodel.c:663-713). */
+int starpu_gb300_dense_autotune(int n, int nb, int reps);
+/* The stored schedule for tile nb: lookahead SMs (-1: the per-step model),
+ * diagonal-tile time, update rate, panel-solve rate relative to it, and the
+ * tuning factorisation's time.  Returns 1 when a tuning exists, else 0. */
+int starpu_gb300_dense_get_tuning(int nb, int *lookahead_sms, double *t_diag_us, double *update_tflops,
+                                  double *panel_rate, double *step_ms);
+
 /* ---------------- serving: a request loop with continuous batching --------
  * A server owns `executors` worker threads, each with its own CUDA stream and
  * buffers for systems up to max_n x max_n with max_nrhs right-hand sides.

@@ -1,11 +1,14 @@
 // Batched SPD solve (many independent systems of uneven sizes in one
 // persistent launch) and its block-size autotuner.
 //
-// The tuning table -- the diagonal/panel block size NB per size bucket -- is
-// stored next to StarPU's history perfmodels, as
+// The tuning table is stored next to StarPU's history perfmodels, as
 //   <perfmodel dir>/codelets/45/gb300_chol_tuning.<hostname>
-// (the path starpu_perfmodel_get_model_path() gives for that symbol), one
-// "bucket max_n nb time_us" line per bucket.
+// (the path starpu_perfmodel_get_model_path() gives for that symbol):
+//   "bucket max_n nb time_us"   the batched solver's block size NB per size bucket;
+//   "dense nb lookahead_sms t_diag_us update_tflops panel_rate n step_ms"
+//                               the mixed solve's schedule for tile nb (written
+//                               by starpu_gb300_dense_autotune, capi_tc.cu).
+// Each autotuner rewrites its own lines and keeps the other's.
 #include <algorithm>
 #include <math.h>
 #include <mutex>
@@ -13,6 +16,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <sys/stat.h>
+#include <unistd.h>
 #include <vector>
 
 #include "gb300_internal.h"
@@ -24,6 +28,11 @@ namespace gb300 {
 
 static const int kBuckets = 6;                      // n <= 32, 64, 128, 256, 512, 1024
 static signed char g_nb_table[kBuckets] = {16, 32, 32, 64, 64, 64};
+static double g_nb_us[kBuckets] = {0, 0, 0, 0, 0, 0};
+static bool g_nb_tuned = false;
+static const int kDense = 8;
+static DenseTuning g_dense[kDense];
+static int g_ndense = 0;
 static bool g_table_loaded = false;
 static std::mutex g_table_mu;
 
@@ -49,11 +58,82 @@ static void load_table_locked()
         int b, maxn, nb;
         double us;
         if (line[0] == '#') continue;
+        DenseTuning d;
+        if (sscanf(line, "dense %d %d %lf %lf %lf %d %lf", &d.nb, &d.lookahead_sms, &d.t_diag_us, &d.update_tflops,
+                   &d.panel_rate, &d.n, &d.step_ms) == 7) {
+            if (d.nb > 0 && d.t_diag_us > 0 && d.update_tflops > 0 && d.panel_rate > 0 && g_ndense < kDense)
+                g_dense[g_ndense++] = d;
+            continue;
+        }
         if (sscanf(line, "%d %d %d %lf", &b, &maxn, &nb, &us) == 4 && b >= 0 && b < kBuckets &&
-            (nb == 16 || nb == 32 || nb == 64))
+            (nb == 16 || nb == 32 || nb == 64)) {
             g_nb_table[b] = (signed char)nb;
+            g_nb_us[b] = us;
+            g_nb_tuned = true;
+        }
     }
     fclose(f);
+}
+
+// the whole table (both autotuners' lines), written through a temporary file
+static int write_table_locked()
+{
+    char path[1200];
+    tuning_path(path, sizeof path);
+    // create the directory chain like the perfmodel writer does
+    for (char *p = path + 1; *p; ++p)
+        if (*p == '/') {
+            *p = 0;
+            mkdir(path, 0755);
+            *p = '/';
+        }
+    char tmp[1300];
+    snprintf(tmp, sizeof tmp, "%s.tmp", path);
+    FILE *f = fopen(tmp, "w");
+    if (!f) return GB300_EINVAL;
+    static const int maxn_of[kBuckets] = {32, 64, 128, 256, 512, 1024};
+    if (g_nb_tuned) {
+        fprintf(f, "# GB300 batched Cholesky tuning: diagonal/panel block size per size bucket\n");
+        fprintf(f, "# bucket max_n nb time_us\n");
+        for (int b = 0; b < kBuckets; ++b) fprintf(f, "%d %d %d %.3f\n", b, maxn_of[b], (int)g_nb_table[b], g_nb_us[b]);
+    }
+    if (g_ndense) {
+        fprintf(f, "# GB300 mixed-solve schedule per tile size (lookahead_sms -1: chosen per step by the model)\n");
+        fprintf(f, "# dense nb lookahead_sms t_diag_us update_tflops panel_rate n step_ms\n");
+        for (int i = 0; i < g_ndense; ++i)
+            fprintf(f, "dense %d %d %.3f %.3f %.4f %d %.4f\n", g_dense[i].nb, g_dense[i].lookahead_sms,
+                    g_dense[i].t_diag_us, g_dense[i].update_tflops, g_dense[i].panel_rate, g_dense[i].n,
+                    g_dense[i].step_ms);
+    }
+    const bool ok = fclose(f) == 0 && rename(tmp, path) == 0;
+    if (!ok) unlink(tmp);
+    return ok ? GB300_OK : GB300_EINVAL;
+}
+
+bool dense_tuning(int nb, DenseTuning *out)
+{
+    std::lock_guard<std::mutex> g(g_table_mu);
+    load_table_locked();
+    for (int i = 0; i < g_ndense; ++i)
+        if (g_dense[i].nb == nb) {
+            if (out) *out = g_dense[i];
+            return true;
+        }
+    return false;
+}
+
+int dense_tuning_store(const DenseTuning &d)
+{
+    std::lock_guard<std::mutex> g(g_table_mu);
+    load_table_locked();
+    int i = 0;
+    while (i < g_ndense && g_dense[i].nb != d.nb) ++i;
+    if (i == g_ndense) {
+        if (g_ndense == kDense) return GB300_ENOMEM;
+        ++g_ndense;
+    }
+    g_dense[i] = d;
+    return write_table_locked();
 }
 
 // Persistent grid of the batched kernel on the current device: the SMs times
@@ -308,25 +388,12 @@ int starpu_gb300_batched_autotune(int systems_per_bucket, int reps)
         cudaFree(X);
         cudaFree(work);
     }
-    char path[1200];
-    tuning_path(path, sizeof path);
-    // create the directory chain like the perfmodel writer does
-    for (char *p = path + 1; *p; ++p)
-        if (*p == '/') {
-            *p = 0;
-            mkdir(path, 0755);
-            *p = '/';
-        }
-    FILE *f = fopen(path, "w");
-    if (!f) return GB300_EINVAL;
-    fprintf(f, "# GB300 batched Cholesky tuning: diagonal/panel block size per size bucket\n");
-    fprintf(f, "# bucket max_n nb time_us (one batch of %d systems per bucket)\n", systems_per_bucket);
-    for (int b = 0; b < kBuckets; ++b) fprintf(f, "%d %d %d %.3f\n", b, maxn_of[b], (int)best_nb[b], best_us[b]);
-    fclose(f);
     std::lock_guard<std::mutex> g(g_table_mu);
+    load_table_locked();
     memcpy(g_nb_table, best_nb, kBuckets);
-    g_table_loaded = true;
-    return GB300_OK;
+    for (int b = 0; b < kBuckets; ++b) g_nb_us[b] = best_us[b];
+    g_nb_tuned = true;
+    return write_table_locked();
 }
 
 } // extern "C"

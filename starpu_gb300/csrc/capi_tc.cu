@@ -6,6 +6,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <atomic>
 #include <functional>
 #include <mutex>
 #include <stdio.h>
@@ -187,7 +188,7 @@ __global__ void split_f16s_kmajor_kernel(int m, int k, const float *__restrict__
     for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
         const int r = rb + rr, col = c0 + threadIdx.x;
         if (r < m && col < ldk) {
-            const float x = ldexpf(t[threadIdx.x][rr], sh[rr]);  // exact (no scale factor to overflow)
+            const float x = tcu_scale_pow2(t[threadIdx.x][rr], sh[rr]);  // exact
             const __half hh = __float2half_rn(x);
             const long o = (long)r * ldk + col;
             h[o] = hh;
@@ -420,27 +421,49 @@ static LookaheadStream *lookahead_stream()
 
 // SMs the panel of step k+1 keeps while step k's trailing update runs on the
 // others.  GB300_LOOKAHEAD_SMS fixes the count (0 runs the steps one after the
-// other); by default it is chosen per step to balance the two: the update's
-// 3 m2^2 kb flops on the remaining SMs, at the split-BF16 tensor rate measured
-// for this kernel (1.45 PFLOP/s on the whole GPU), against the panel's
-// latency-bound diagonal tile (about 0.75 ms) plus its 6 m2 kb^2 TRSM flops
-// and the panel splits, which together run at a fraction of that rate per SM
-// (GB300_PANEL_RATE, default 0.4: the per-step timeline of the n = 32768
-// solve gives 2.02 ms for a 27648-row panel on 38 SMs).
+// other).  Otherwise the autotuned schedule for the tile size
+// (starpu_gb300_dense_autotune, stored beside the perfmodels) gives either a
+// fixed count or the parameters of the per-step model; without one the model
+// runs on the defaults below.  The model balances the update's 3 m2^2 kb
+// flops on the remaining SMs, at the split-precision tensor rate of this
+// kernel (default 1.45 PFLOP/s on the whole GPU), against the panel's
+// latency-bound diagonal tile (default about 0.75 ms) plus its 6 m2 kb^2
+// TRSM flops and the panel splits, which together run at a fraction of that
+// rate per SM (default GB300_PANEL_RATE or 0.4: the per-step timeline of the
+// n = 32768 solve gave 2.02 ms for a 27648-row panel on 38 SMs).
+namespace {
+// set by the autotuner for its trials: a fixed count (>= 0), or -1 for the
+// model with the parameters below (rate <= 0: the defaults)
+std::atomic<int> g_la_trial{-2};
+double g_trial_rate = 0, g_trial_tdiag = 0, g_trial_panel = 0;
+} // namespace
+
 static int lookahead_sms(int m2, int kb)
 {
     static int fixed = -2;
-    static double panel_rate = 0.4;
+    static double panel_rate_env = 0.4;
     if (fixed == -2) {
         const char *e = getenv("GB300_LOOKAHEAD_SMS");
         fixed = e && *e ? std::max(0, atoi(e)) : -1;
         const char *r = getenv("GB300_PANEL_RATE");
-        if (r && *r && atof(r) > 0.0) panel_rate = atof(r);
+        if (r && *r && atof(r) > 0.0) panel_rate_env = atof(r);
     }
     const int S = num_sms();
     if (fixed >= 0) return fixed >= S ? 0 : fixed;
+    double rate = 1.45e15, t_diag = 0.75e-3, panel_rate = panel_rate_env;
+    const int trial = g_la_trial.load();
+    if (trial >= 0) return trial >= S ? 0 : trial;
+    if (trial == -1) {
+        if (g_trial_rate > 0) rate = g_trial_rate, t_diag = g_trial_tdiag, panel_rate = g_trial_panel;
+    } else {
+        DenseTuning t;
+        if (dense_tuning(kb, &t)) {
+            if (t.lookahead_sms >= 0) return t.lookahead_sms >= S ? 0 : t.lookahead_sms;
+            rate = t.update_tflops * 1e12, t_diag = t.t_diag_us * 1e-6, panel_rate = t.panel_rate;
+        }
+    }
     if (S < 32 || m2 <= 0) return 0;
-    const double R = 1.45e15 / S, t_diag = 0.75e-3;
+    const double R = rate / S;
     const double f_upd = 3.0 * m2 * (double)m2 * kb, f_trsm = 6.0 * m2 * (double)kb * kb / panel_rate;
     // below about a quarter of the GPU the diagonal-tile kernel itself slows down
     int best = S / 4;
@@ -724,6 +747,191 @@ int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int n
     if (d_info) cudaMemsetAsync(d_info, 0, sizeof(int), s);
     if (!n) return GB300_OK;
     return potrf_tc(s, n, A, lda, nb, nterms, work, d_info, d_err, nullptr, {}, 0, {}, nullptr);
+}
+
+// ---- tensor-core tile update for the codelets -----------------------------
+//
+// Workspace: the row-scaled FP16 splits of A (m rows) and B (n rows) for
+// m, n, k <= nmax: h and l (K-major, row stride round64(k)) and the row
+// exponents of each operand.
+static size_t tile_tc_operand_bytes(int rows, long ldk)
+{
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    return 2 * al((size_t)rows * ldk * 2) + al((size_t)rows * 4);
+}
+
+static F16Panel tile_tc_operand(void *base, int rows, long ldk)
+{
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    char *p = (char *)base;
+    const size_t half = al((size_t)rows * ldk * 2);
+    return {(__half *)p, (__half *)(p + half), (int *)(p + 2 * half)};
+}
+
+size_t starpu_gb300_tile_tc_workspace(int nmax)
+{
+    if (nmax <= 0) return 0;
+    const long ldk = ((long)nmax + 63) / 64 * 64;
+    return 2 * tile_tc_operand_bytes(nmax, ldk);
+}
+
+int starpu_gb300_tile_tc_prepare(void)
+{
+    return gb300_func_dyn_smem((const void *)tc_update_kernel, TCU_SMEM);
+}
+
+int starpu_gb300_sgemm_nt_tile_tc(void *stream, int m, int n, int k, const float *A, int lda, const float *B,
+                                  int ldb, float *C, int ldc, int lower, void *work, size_t lwork, int *d_err)
+{
+    if (m < 0 || n < 0 || k < 0 || lda < (m > 1 ? m : 1) || ldb < (n > 1 ? n : 1) || ldc < (m > 1 ? m : 1) ||
+        (lower && m != n) || !d_err || !work)
+        return GB300_EINVAL;
+    const int nmax = std::max(m, std::max(n, k));
+    if (lwork < starpu_gb300_tile_tc_workspace(nmax)) return GB300_EINVAL;
+    if (!m || !n || !k) return GB300_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long ldk = ((long)k + 63) / 64 * 64;
+    const F16Panel pa = tile_tc_operand(work, m, ldk);
+    int rc = split_f16s(s, m, k, A, lda, pa, ldk);
+    F16Panel pb = pa;
+    if (!rc && !(B == A && n == m && ldb == lda)) {
+        pb = tile_tc_operand((char *)work + tile_tc_operand_bytes(m, ldk), n, ldk);
+        rc = split_f16s(s, n, k, B, ldb, pb, ldk);
+    }
+    if (!rc) rc = tc_update_f16s(s, m, n, k, pa, ldk, pb, ldk, 3, lower ? 1 : 0, C, ldc, d_err);
+    return rc;
+}
+
+// A x A FP32 matrix 1/(1+i+j) + n delta_ij (the tuning input: SPD, and the
+// factorisation's time does not depend on the values)
+__global__ void fill_hilbert_f32_kernel(int n, float *A, long lda)
+{
+    const long total = (long)n * n;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        A[i + (long)j * lda] = 1.0f / (1.0f + i + j) + (i == j ? (float)n : 0.0f);
+    }
+}
+
+int starpu_gb300_dense_autotune(int n, int nb, int reps)
+{
+    if (nb < 64 || nb > DC_MAXN || n < 3 * nb) return GB300_EINVAL;
+    if (reps <= 0) reps = 2;
+    const int S = num_sms();
+    const int L = std::max(1, S / 4);
+    const long ldk = ((long)nb + 63) / 64 * 64;
+    const size_t lw = tc_ws_layout(n, nb, nullptr, nullptr);
+    float *A0 = nullptr, *A = nullptr;
+    void *work = nullptr;
+    int *flags = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = gb300_record_cuda_error(cudaMalloc(&A0, sizeof(float) * (size_t)n * n));
+    if (!rc) rc = gb300_record_cuda_error(cudaMalloc(&A, sizeof(float) * (size_t)n * n));
+    if (!rc) rc = gb300_record_cuda_error(cudaMalloc(&work, lw));
+    if (!rc) rc = gb300_record_cuda_error(cudaMalloc(&flags, 2 * sizeof(int)));
+    if (!rc) rc = gb300_record_cuda_error(cudaMemset(flags, 0, 2 * sizeof(int)));
+    if (!rc) rc = gb300_record_cuda_error(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    if (!rc) rc = gb300_record_cuda_error(cudaEventCreate(&e0));
+    if (!rc) rc = gb300_record_cuda_error(cudaEventCreate(&e1));
+    DenseTuning best;
+    best.nb = nb;
+    best.n = n;
+    auto timed = [&](const std::function<int()> &fn, double *ms_out) -> int {
+        double tot = 0;
+        for (int r = 0; r <= reps; ++r) {
+            int rc2 = gb300_record_cuda_error(cudaEventRecord(e0, s));
+            if (!rc2) rc2 = fn();
+            if (!rc2) rc2 = gb300_record_cuda_error(cudaEventRecord(e1, s));
+            if (!rc2) rc2 = gb300_record_cuda_error(cudaEventSynchronize(e1));
+            if (rc2) return rc2;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0) tot += ms;  // the first run is a warm-up
+        }
+        *ms_out = tot / reps;
+        return GB300_OK;
+    };
+    if (!rc) {
+        gb300_count_launch(), fill_hilbert_f32_kernel<<<1024, 256, 0, s>>>(n, A0, n);
+        rc = gb300_last_launch_status();
+    }
+    TcWs w;
+    tc_ws_layout(n, nb, work, &w);
+    if (!rc) rc = gb300_record_cuda_error(cudaMemsetAsync(work, 0, lw, s));
+    int *d_info = flags, *d_err = flags + 1;
+    // 1. the diagonal tile (factor + inverse) on a quarter of the SMs
+    double t_diag_ms = 0;
+    if (!rc)
+        rc = timed([&] {
+            cudaMemcpy2DAsync(A, sizeof(float) * n, A0, sizeof(float) * n, sizeof(float) * nb, nb,
+                              cudaMemcpyDeviceToDevice, s);
+            return diag_factor_inverse(s, nb, A, n, w.linv, ldk, w.scratch, w.bar, d_info, 0, d_err, true, L);
+        }, &t_diag_ms);
+    // 2. the trailing update (lower m x m, K = nb, 3 products) on the whole GPU
+    const int m = std::min(n - nb, 8192);
+    double t_upd_ms = 0, t_panel_ms = 0;
+    if (!rc)
+        rc = timed([&] { return tc_update_f16s(s, m, m, nb, w.pan[0], ldk, w.pan[0], ldk, 3, 1, A, n, d_err); },
+                   &t_upd_ms);
+    // 3. the panel solve (store form m x nb, K = nb) on the same quarter
+    if (!rc)
+        rc = timed([&] { return tc_update_f16s(s, m, nb, nb, w.pan[0], ldk, w.inv, ldk, 3, 0, A, n, d_err, 1, L); },
+                   &t_panel_ms);
+    if (!rc) {
+        best.t_diag_us = t_diag_ms * 1e3;
+        const double rate = 3.0 * nb * (double)m * (m + 1.0) / (t_upd_ms * 1e-3);
+        best.update_tflops = rate / 1e12;
+        best.panel_rate = (6.0 * m * (double)nb * nb / (t_panel_ms * 1e-3)) / (rate * L / S);
+    }
+    // 4. whole factorisations: the model on these parameters, and fixed splits
+    const int cands[5] = {-1, S / 4, S / 3, S / 2, 0};
+    best.step_ms = INFINITY;
+    for (int c = 0; c < 5 && !rc; ++c) {
+        g_trial_rate = best.update_tflops * 1e12;
+        g_trial_tdiag = best.t_diag_us * 1e-6;
+        g_trial_panel = best.panel_rate;
+        g_la_trial.store(cands[c]);
+        double ms = 0;
+        rc = timed([&] {
+            cudaMemcpyAsync(A, A0, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s);
+            return potrf_tc(s, n, A, n, nb, 3, work, d_info, d_err, nullptr, {}, 0, {}, nullptr);
+        }, &ms);
+        g_la_trial.store(-2);
+        if (!rc && ms < best.step_ms) {
+            best.step_ms = ms;
+            best.lookahead_sms = cands[c];
+        }
+    }
+    int hflags[2] = {0, 0};
+    if (!rc) rc = gb300_record_cuda_error(cudaMemcpy(hflags, flags, sizeof hflags, cudaMemcpyDeviceToHost));
+    if (!rc && (hflags[0] || hflags[1])) {
+        gb300_set_error("starpu_gb300_dense_autotune: the tuning factorisation failed");
+        rc = GB300_EINVAL;
+    }
+    if (s) cudaStreamSynchronize(s);
+    cudaFree(A0);
+    cudaFree(A);
+    cudaFree(work);
+    cudaFree(flags);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    if (rc) return rc;
+    return dense_tuning_store(best);
+}
+
+int starpu_gb300_dense_get_tuning(int nb, int *lookahead_sms, double *t_diag_us, double *update_tflops,
+                                  double *panel_rate, double *step_ms)
+{
+    DenseTuning t;
+    if (!dense_tuning(nb, &t)) return 0;
+    if (lookahead_sms) *lookahead_sms = t.lookahead_sms;
+    if (t_diag_us) *t_diag_us = t.t_diag_us;
+    if (update_tflops) *update_tflops = t.update_tflops;
+    if (panel_rate) *panel_rate = t.panel_rate;
+    if (step_ms) *step_ms = t.step_ms;
+    return 1;
 }
 
 } // extern "C"

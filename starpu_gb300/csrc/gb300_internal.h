@@ -30,6 +30,20 @@ void dsposv_prepared_targets(int n, int nrhs, int nb, void *work, float **W, uns
 int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
                   int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out);
 
+// The mixed solve's schedule for one tile size, from starpu_gb300_dense_autotune,
+// stored in the tuning table beside the perfmodels (capi_batched.cu).
+struct DenseTuning {
+    int nb = 0;
+    int lookahead_sms = -1;     // -1: chosen per step by the model below
+    double t_diag_us = 0;       // diagonal-tile factor + inverse on a quarter of the SMs
+    double update_tflops = 0;   // the split-precision trailing update on the whole GPU
+    double panel_rate = 0;      // the panel solve's tensor rate per SM, relative to the update's
+    int n = 0;                  // order the schedule was timed at
+    double step_ms = 0;         // its factorisation time
+};
+bool dense_tuning(int nb, DenseTuning *out);
+int dense_tuning_store(const DenseTuning &d);
+
 // Width of the register-blocked small triangular kernels and of the
 // unblocked diagonal POTRF leaf: 64 columns in FP32, 32 in FP64 (a 64-wide
 // FP64 row does not fit the register file without spilling).

@@ -72,6 +72,14 @@ struct TcUpdateArgs {
     unsigned long long wait_budget_ns;
 };
 
+// v 2^e, exact unless the result leaves FP32's normal range: one multiply by
+// the power of two when 2^e is a normal float, ldexp otherwise (matrices far
+// from unit scale).
+__device__ __forceinline__ float tcu_scale_pow2(float v, int e)
+{
+    return (e >= -126 && e <= 127) ? v * __int_as_float((e + 127) << 23) : ldexpf(v, e);
+}
+
 // Map a linear tile index to (tm, tn).  Lower: column tn holds tiles
 // tm = 2*tn .. tiles_m-1 (a 128-row tile crosses the diagonal of a 256-column
 // tile only from tm = 2*tn on).
@@ -301,8 +309,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
 #pragma unroll
                         for (int j = 0; j < 32; ++j) {
                             const int col = c0 + j;
-                            const int rkb = col < args.n ? args.rk_b[col] : 0;
-                            r[j] = __float_as_uint(ldexpf(__uint_as_float(r[j]), rka + rkb));
+                            const int e = rka + (col < args.n ? args.rk_b[col] : 0);
+                            r[j] = __float_as_uint(tcu_scale_pow2(__uint_as_float(r[j]), e));
                         }
                     }
 #pragma unroll

@@ -97,3 +97,58 @@ def test_batched_autotuner_writes_table_next_to_perfmodels(gpu, tmp_path):
     finally:
         del os.environ["STARPU_PERF_MODEL_DIR"]
         del os.environ["STARPU_HOSTNAME"]
+
+
+_DENSE_TUNE = r"""
+import ctypes as C, json, sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+import starpu_gb300
+from starpu_gb300 import DeviceBuffer
+from starpu_gb300.native import IrInfo, check
+L = starpu_gb300.load()
+check(L.starpu_gb300_dense_autotune(6144, 1024, 1), "dense autotune")
+la, td, up, pr, st = C.c_int(), C.c_double(), C.c_double(), C.c_double(), C.c_double()
+have = L.starpu_gb300_dense_get_tuning(1024, C.byref(la), C.byref(td), C.byref(up), C.byref(pr), C.byref(st))
+# a solve with the stored schedule
+n, nb, nrhs = 6144, 1024, 4
+A, W0 = DeviceBuffer(8 * n * n), DeviceBuffer(8 * n * n)
+check(L.starpu_gb300_gen_spd_gram(None, n, 3, 4.0 / (1e4 - 1), A.ptr, n, W0.ptr))
+B, X = DeviceBuffer(8 * n * nrhs), DeviceBuffer(8 * n * nrhs)
+check(L.starpu_gb300_gen_uniform_rhs(None, n, nrhs, 4, B.ptr, n))
+lw = L.starpu_gb300_dsposv_workspace(n, nrhs, nb)
+Wk = DeviceBuffer(lw)
+info = IrInfo()
+rc = L.starpu_gb300_dsposv(None, n, nrhs, A.ptr, n, B.ptr, n, X.ptr, n, nb, 3, 1e-12, 30, Wk.ptr, lw, C.byref(info))
+print(json.dumps({"have": have, "la": la.value, "t_diag_us": td.value, "tflops": up.value, "panel_rate": pr.value,
+                  "step_ms": st.value, "rc": rc, "berr": info.backward_error}))
+"""
+
+
+def test_dense_autotuner_stores_the_schedule_beside_the_perfmodels(gpu, tmp_path):
+    """starpu_gb300_dense_autotune times the diagonal tile, the update and the
+    panel solve, then whole factorisations under the model and fixed splits,
+    and stores the fastest in gb300_chol_tuning.<host> beside the perfmodels,
+    keeping the batched solver's lines; a solve afterwards uses it.  Run in a
+    child process so that the stored schedule does not reach other tests."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    d = tmp_path / "codelets" / "45"
+    d.mkdir(parents=True)
+    f = d / "gb300_chol_tuning.tunehost"
+    f.write_text("# an earlier batched tuning\n0 32 16 1.0\n1 64 32 1.0\n2 128 32 1.0\n3 256 64 1.0\n"
+                 "4 512 64 1.0\n5 1024 64 1.0\n")
+    env = dict(os.environ, STARPU_PERF_MODEL_DIR=str(tmp_path), STARPU_HOSTNAME="tunehost")
+    env.pop("GB300_LOOKAHEAD_SMS", None)
+    r = subprocess.run([sys.executable, "-c", _DENSE_TUNE, root], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["have"] == 1 and out["rc"] == 0 and out["berr"] <= 1e-12
+    assert out["t_diag_us"] > 0 and out["tflops"] > 10 and out["panel_rate"] > 0 and out["step_ms"] > 0
+    rows = [ln.split() for ln in f.read_text().splitlines() if ln and not ln.startswith("#")]
+    dense = [r for r in rows if r[0] == "dense"]
+    assert len(dense) == 1 and int(dense[0][1]) == 1024 and int(dense[0][2]) == out["la"]
+    assert len([r for r in rows if r[0] != "dense"]) == 6  # the batched lines are kept

@@ -194,3 +194,33 @@ def test_device_generator_matches_oracle(gpu, oracle):
     dB = DeviceBuffer(n * 3 * 8)
     check(gpu.starpu_gb300_gen_uniform_rhs(None, n, 3, 9, dB.ptr, n))
     np.testing.assert_array_equal(dB.download((n, 3), np.float64), oracle.uniform_rhs(n, 3, 9))
+
+
+@pytest.mark.parametrize("m,n,k,lower", [(512, 512, 512, 0), (700, 300, 1024, 0), (513, 513, 256, 1)])
+def test_tile_update_on_tensor_cores(gpu, m, n, k, lower):
+    """The codelets' FP32 tile update on the tensor cores (row-scaled FP16
+    splits): C -= A B^T within 1e-5 of the FP64 product relative to |A||B|^T,
+    the SYRK form writing only the lower triangle, B == A split once."""
+    rng = np.random.default_rng(m + n + k)
+    A = np.asfortranarray(rng.standard_normal((m, k)).astype(np.float32))
+    # rows of very different scales: the row scaling keeps each one's precision
+    A *= np.float32(2.0) ** rng.integers(-20, 20, m)[:, None].astype(np.float32)
+    B = A if lower else np.asfortranarray(rng.standard_normal((n, k)).astype(np.float32))
+    C0 = np.asfortranarray(rng.standard_normal((m, n)).astype(np.float32))
+    dA, dC = DeviceBuffer.from_array(A), DeviceBuffer.from_array(C0)
+    dB = dA if lower else DeviceBuffer.from_array(B)
+    lw = gpu.starpu_gb300_tile_tc_workspace(max(m, n, k))
+    W = DeviceBuffer(lw)
+    err = DeviceBuffer.from_array(np.zeros(1, np.int32))
+    check(gpu.starpu_gb300_tile_tc_prepare())
+    check(gpu.starpu_gb300_sgemm_nt_tile_tc(None, m, n, k, dA.ptr, m, dB.ptr, n, dC.ptr, m, lower, W.ptr, lw,
+                                            err.ptr))
+    C = dC.download((m, n), np.float32).astype(np.float64)
+    A64, B64 = A.astype(np.float64), B.astype(np.float64)
+    ref = C0.astype(np.float64) - A64 @ B64.T
+    scale = np.abs(A64) @ np.abs(B64).T + np.abs(C0)
+    keep = np.tril(np.ones((m, n), bool)) if lower else np.ones((m, n), bool)
+    assert np.max(np.abs(C - ref)[keep] / scale[keep]) <= 1e-5
+    if lower:
+        np.testing.assert_array_equal(C[~keep], C0.astype(np.float64)[~keep])
+    assert err.download((1,), np.int32)[0] == 0

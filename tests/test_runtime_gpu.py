@@ -51,3 +51,14 @@ def test_indefinite_input_reported_by_status_word(prec):
     # and the device is still usable: a normal run afterwards succeeds
     r2, _ = run_driver(["-size", "512", "-nblocks", "4", "-check", *prec], STARPU_NCPU=0)
     assert r2.returncode == 0, r2.stdout + r2.stderr
+
+
+@pytest.mark.parametrize("mode", ["graph", "per_task"])
+def test_tensor_core_tiles_through_the_runtime(mode):
+    """The codelets' FP32 GEMM/SYRK tiles on the tensor cores (forced down to
+    256-tiles): the driver's check holds and the factorisation is the same
+    DAG."""
+    env = {"graph": dict(STARPU_NCPU=0), "per_task": dict(STARPU_NCPU=0, STARPU_GB300_GRAPH=0)}[mode]
+    r, st = run_driver(["-size", "2048", "-nblocks", "8", "-check"], STARPU_GB300_CHOL_TC_MIN=256, **env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert re.search(r"^\d+\t\d+\t[\d.]+$", r.stdout, re.M)
