@@ -107,8 +107,15 @@ int split_bf16(cudaStream_t s, int m, int k, const float *P, long ldp, void *hi,
 // not SPD may break the bound; its factorisation then fails on a pivot.
 struct F16Panel {
     __half *h, *l;
-    int *rk;
+    int *rk;    // row exponents k_i (the split divides by 2^k_i)
+    float *rs;  // 2^k_i as floats, for the epilogue; both arrays hold 64 entries past the rows
 };
+
+// bytes of one row-scale array (rows + 64 entries of padding: the epilogue
+// loads the scales of 32 columns at a time past the last row)
+static size_t scale_bytes(size_t rows) { return ((rows + 64) * 4 + 255) & ~(size_t)255; }
+
+__device__ __forceinline__ float pow2f(int k) { return ldexpf(1.0f, k < -149 ? -149 : k); }
 
 // k with bound 2^-k < 2^15
 __device__ __forceinline__ int f16_row_exp(float bound)
@@ -121,7 +128,8 @@ __device__ __forceinline__ int f16_row_exp(float bound)
 // rk[i] from the actual row maxima (the inverse of a diagonal tile, whose
 // elements have no bound from the matrix): 32 rows per CTA, the k loop split
 // over 8 thread rows.
-__global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P, long ldp, int *__restrict__ rk)
+__global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P, long ldp, int *__restrict__ rk,
+                                       float *__restrict__ rs)
 {
     __shared__ float red[8][33];
     const int r = blockIdx.x * 32 + threadIdx.x;
@@ -133,6 +141,7 @@ __global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P
     if (threadIdx.y == 0 && r < m) {
         for (int y = 1; y < 8; ++y) mx = fmaxf(mx, red[y][threadIdx.x]);
         rk[r] = f16_row_exp(mx);
+        rs[r] = pow2f(rk[r]);
     }
 }
 
@@ -160,6 +169,7 @@ __global__ void diag_bounds_kernel(int n, const float *__restrict__ A, long lda,
 // the split; rk given (from_bounds = 0) or computed from d / f (from_bounds = 1:
 // rows r0.. of the matrix, d indexed by matrix row, *f or 1 when f is NULL)
 __global__ void split_f16s_kmajor_kernel(int m, int k, const float *__restrict__ P, long ldp, int *__restrict__ rk,
+                                         float *__restrict__ rs,
                                          int from_bounds, const float *__restrict__ d, int r0,
                                          const float *__restrict__ f, __half *__restrict__ h, __half *__restrict__ l,
                                          long ldk)
@@ -174,7 +184,10 @@ __global__ void split_f16s_kmajor_kernel(int m, int k, const float *__restrict__
             // sqrt(d_r) sqrt(f): no underflow or overflow of the product for
             // matrices scaled far from 1
             e = f16_row_exp(sqrtf(fmaxf(d[r0 + rb + tid], 0.0f)) * (f ? sqrtf(*f) : 1.0f));
-            if (blockIdx.y == 0) rk[rb + tid] = e;
+            if (blockIdx.y == 0) {
+                rk[rb + tid] = e;
+                rs[rb + tid] = pow2f(e);
+            }
         } else {
             e = rk[rb + tid];
         }
@@ -188,7 +201,9 @@ __global__ void split_f16s_kmajor_kernel(int m, int k, const float *__restrict__
     for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
         const int r = rb + rr, col = c0 + threadIdx.x;
         if (r < m && col < ldk) {
-            const float x = tcu_scale_pow2(t[threadIdx.x][rr], sh[rr]);  // exact
+            const int sx = sh[rr];  // exact: a power-of-two scaling (ldexp only outside the normal range)
+            const float x = (sx >= -126 && sx <= 127) ? t[threadIdx.x][rr] * __int_as_float((sx + 127) << 23)
+                                                      : ldexpf(t[threadIdx.x][rr], sx);
             const __half hh = __float2half_rn(x);
             const long o = (long)r * ldk + col;
             h[o] = hh;
@@ -202,9 +217,10 @@ static int split_f16s(cudaStream_t s, int m, int k, const float *P, long ldp, co
                       const float *d = nullptr, int r0 = 0, const float *f = nullptr)
 {
     if (m <= 0 || k <= 0) return GB300_OK;
-    if (!d) gb300_count_launch(), panel_row_scale_kernel<<<(m + 31) / 32, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rk);
+    if (!d)
+        gb300_count_launch(), panel_row_scale_kernel<<<(m + 31) / 32, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rk, o.rs);
     dim3 g((m + 31) / 32, (unsigned)((ldk + 31) / 32));
-    gb300_count_launch(), split_f16s_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rk, d ? 1 : 0, d, r0, f,
+    gb300_count_launch(), split_f16s_kmajor_kernel<<<g, dim3(32, 8), 0, s>>>(m, k, P, ldp, o.rk, o.rs, d ? 1 : 0, d, r0, f,
                                                                            o.h, o.l, ldk);
     return gb300_last_launch_status();
 }
@@ -212,14 +228,14 @@ static int split_f16s(cudaStream_t s, int m, int k, const float *P, long ldp, co
 // rows [r, ...) of a split panel
 static F16Panel rows_of(const F16Panel &p, long r, long ldk)
 {
-    return {p.h + r * ldk, p.l + r * ldk, p.rk + r};
+    return {p.h + r * ldk, p.l + r * ldk, p.rk + r, p.rs + r};
 }
 
 // One operand of the update: BF16 hi / lo, or the scaled FP16 split
 // (hi = h, lo = l, rk = the row scale exponents).
 struct TcOperand {
     const void *hi, *lo;
-    const int *rk;
+    const float *rs;
 };
 
 // max_grid > 0 caps the persistent grid (CTAs, one per SM): the trailing
@@ -233,7 +249,7 @@ static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A,
 {
     if (m <= 0 || n <= 0 || K <= 0) return GB300_OK;
     if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!A.lo || !B.lo)) || (lower && m != n) || !d_err ||
-        (f16s && (!A.rk || !B.rk)))
+        (f16s && (!A.rs || !B.rs)))
         return GB300_EINVAL;
     CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
     int rc;
@@ -248,8 +264,9 @@ static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A,
     }
     TcUpdateArgs a;
     a.f16s = f16s ? 1 : 0;
-    a.rk_a = f16s ? A.rk : nullptr;
-    a.rk_b = f16s ? B.rk : nullptr;
+    a.rs_a = f16s ? A.rs : nullptr;
+    a.rs_b = f16s ? B.rs : nullptr;
+    a.rs_b_vec = f16s && ((uintptr_t)B.rs & 15) == 0;
     a.C = C;
     a.ldc = ldc;
     a.m = m;
@@ -293,7 +310,7 @@ static int tc_update_f16s(cudaStream_t s, int m, int n, int K, const F16Panel &A
                           long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
                           int max_grid = 0, int t0 = 0, int t1 = -1)
 {
-    return tc_update_op(s, m, n, K, {A.h, A.l, A.rk}, lda, {B.h, B.l, B.rk}, ldb, nterms, lower, C, ldc,
+    return tc_update_op(s, m, n, K, {A.h, A.l, A.rs}, lda, {B.h, B.l, B.rs}, ldb, nterms, lower, C, ldc,
                         d_err, store, max_grid, true, t0, t1);
 }
 
@@ -316,20 +333,20 @@ static size_t tc_ws_layout(int n, int nb, void *base, TcWs *w)
 {
     const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t panel = al((size_t)n * ldk * 2), rsn = al((size_t)n * 4);
-    const size_t inv = ldk * ldk, invh = al(inv * 2), rsk = al(ldk * 4);
+    const size_t panel = al((size_t)n * ldk * 2), rsn = scale_bytes(n);
+    const size_t inv = ldk * ldk, invh = al(inv * 2), rsk = scale_bytes(ldk);
     const size_t ntiles = nb > 0 ? ((size_t)n + nb - 1) / nb : 1;
-    const size_t off_inv = 2 * (2 * panel + rsn);
-    const size_t off_d = off_inv + 2 * invh + rsk;
+    const size_t off_inv = 2 * (2 * panel + 2 * rsn);
+    const size_t off_d = off_inv + 2 * invh + 2 * rsk;
     const size_t off_linv = off_d + rsn + al(ntiles * 4);
     if (w && base) {
         char *b = (char *)base;
         for (int i = 0; i < 2; ++i) {
-            char *p = b + i * (2 * panel + rsn);
-            w->pan[i] = {(__half *)p, (__half *)(p + panel), (int *)(p + 2 * panel)};
+            char *p = b + i * (2 * panel + 2 * rsn);
+            w->pan[i] = {(__half *)p, (__half *)(p + panel), (int *)(p + 2 * panel), (float *)(p + 2 * panel + rsn)};
         }
         char *q = b + off_inv;
-        w->inv = {(__half *)q, (__half *)(q + invh), (int *)(q + 2 * invh)};
+        w->inv = {(__half *)q, (__half *)(q + invh), (int *)(q + 2 * invh), (float *)(q + 2 * invh + rsk)};
         w->d = (float *)(b + off_d);
         w->dtile = (float *)(b + off_d + rsn);
         w->linv = (float *)(b + off_linv);
@@ -757,7 +774,7 @@ int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int n
 static size_t tile_tc_operand_bytes(int rows, long ldk)
 {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    return 2 * al((size_t)rows * ldk * 2) + al((size_t)rows * 4);
+    return 2 * al((size_t)rows * ldk * 2) + 2 * scale_bytes(rows);
 }
 
 static F16Panel tile_tc_operand(void *base, int rows, long ldk)
@@ -765,7 +782,7 @@ static F16Panel tile_tc_operand(void *base, int rows, long ldk)
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     char *p = (char *)base;
     const size_t half = al((size_t)rows * ldk * 2);
-    return {(__half *)p, (__half *)(p + half), (int *)(p + 2 * half)};
+    return {(__half *)p, (__half *)(p + half), (int *)(p + 2 * half), (float *)(p + 2 * half + scale_bytes(rows))};
 }
 
 size_t starpu_gb300_tile_tc_workspace(int nmax)

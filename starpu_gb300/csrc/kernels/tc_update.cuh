@@ -20,10 +20,11 @@
 // x = h + l with h = fp16(x), l = fp16(x - h): 11 + 11 significant bits, and l
 // stays a normal FP16 for every element above ~2^-18 of the bound.  The three
 // products h_A h_B^T + h_A l_B^T + l_A h_B^T (each exact in FP32) accumulate
-// the scaled product; the epilogue scales it by 2^(k_i + k_j) in one ldexp
-// (exact, and free of the overflow a product of two scale factors could meet
-// for matrices far from unit scale).  The dropped l_A l_B^T term weighs 2^-22
-// of the product.
+// the scaled product; the epilogue multiplies the row's 2^k_i by the column's
+// 2^k_j (a power of two: exact) and applies it inside the FMA that updates C.
+// The column scales are
+// read 4 at a time when rs_b is 16-byte aligned (it is padded past its rows).  The
+// dropped l_A l_B^T term weighs 2^-22 of the product.
 //
 // CTA = 6 warps, one CTA per SM (persistent, static round-robin over tiles):
 //   warp 0  TMA producer     (one elected lane)
@@ -64,21 +65,14 @@ struct TcUpdateArgs {
     int nterms;        // 1 or 3
     int lower;         // 1: only elements with row >= col (square trailing matrix)
     int store;         // 1: C = sum (C is not read), 0: C -= sum
-    int f16s;          // 1: scaled FP16 operands (rk_a, rk_b below); 0: BF16
-    const int *rk_a, *rk_b;    // f16s: row scale exponents of A (m) and B (n)
+    int f16s;          // 1: scaled FP16 operands (rs_a, rs_b below); 0: BF16
+    const float *rs_a, *rs_b;  // f16s: row scales (powers of two) of A (m) and B (n, padded)
+    int rs_b_vec;              // rs_b is 16-byte aligned: the column scales load 4 at a time
     int tiles_m, tiles_n, num_tiles;
     int tile_begin, tile_end;  // the launch covers tiles [tile_begin, tile_end) of the num_tiles
     int *err;
     unsigned long long wait_budget_ns;
 };
-
-// v 2^e, exact unless the result leaves FP32's normal range: one multiply by
-// the power of two when 2^e is a normal float, ldexp otherwise (matrices far
-// from unit scale).
-__device__ __forceinline__ float tcu_scale_pow2(float v, int e)
-{
-    return (e >= -126 && e <= 127) ? v * __int_as_float((e + 127) << 23) : ldexpf(v, e);
-}
 
 // Map a linear tile index to (tm, tn).  Lower: column tn holds tiles
 // tm = 2*tn .. tiles_m-1 (a 128-row tile crosses the diagonal of a 256-column
@@ -285,8 +279,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
             const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TCU_BN);
             float *crow = args.C + row;
             const bool row_ok = row < args.m;
-            // scaled FP16: the row's scale exponent (the columns' below)
-            const int rka = (args.f16s && row_ok) ? args.rk_a[row] : 0;
+            // scaled FP16: the row's scale (the columns' below)
+            const float rsc = (args.f16s && row_ok) ? args.rs_a[row] : 1.0f;
 #pragma unroll 1
             for (int ch = 0; ch < TCU_BN / 32; ++ch) {
                 uint32_t r[32];
@@ -305,21 +299,33 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                         const bool w = col < args.n && (!args.lower || row >= col);
                         cv[j] = (w && !args.store) ? crow[(long)col * args.ldc] : 0.0f;
                     }
-                    if (args.f16s) {
+                    float cs[32];
+                    if (args.f16s && !args.rs_b_vec) {
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const int col = c0 + j;
-                            const int e = rka + (col < args.n ? args.rk_b[col] : 0);
-                            r[j] = __float_as_uint(tcu_scale_pow2(__uint_as_float(r[j]), e));
+                        for (int j = 0; j < 32; ++j) cs[j] = args.rs_b[c0 + j];
+                    } else if (args.f16s) {
+                        const float4 *c4 = reinterpret_cast<const float4 *>(args.rs_b + c0);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const float4 v = c4[q];
+                            cs[4 * q] = v.x;
+                            cs[4 * q + 1] = v.y;
+                            cs[4 * q + 2] = v.z;
+                            cs[4 * q + 3] = v.w;
                         }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) cs[j] = 1.0f;
                     }
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const int col = c0 + j;
                         const bool w = col < args.n && (!args.lower || row >= col);
-                        if (w)
-                            crow[(long)col * args.ldc] =
-                                args.store ? __uint_as_float(r[j]) : cv[j] - __uint_as_float(r[j]);
+                        // 2^(k_i + k_j): a product of two powers of two, exact (subnormal
+                        // for matrices far below unit scale), never overflowing where C does not
+                        const float sc = rsc * cs[j];
+                        const float a = __uint_as_float(r[j]);
+                        if (w) crow[(long)col * args.ldc] = args.store ? a * sc : fmaf(-a, sc, cv[j]);
                     }
                 }
             }
