@@ -34,7 +34,7 @@ METRIC = "SPD solve GFLOP/s @1e-12 backward err, mixed vs FP64; solves/s + p99 l
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one tc_update_kernel launch,
-# m = 8192, k = 1024, 3 split-BF16 products (ncu, GB300)
+# m = 8192, k = 1024, 3 scaled-FP16 split products (ncu, GB300)
 TC_TRAFFIC_M8192 = 249.5e6
 
 def solve_flops(n: int, nrhs: int) -> float:
@@ -602,7 +602,7 @@ def run_ours(args):
                 "sm_share": sm_share.value,
                 "frac_of_sm_share": (tc["tflops"] / (peak_tc * sm_share.value)) if tc["tflops"] else None,
                 "traffic": traffic, "traffic_source": traffic_src,
-                "kernel": "tc_update_kernel (split-BF16 tcgen05 trailing update)",
+                "kernel": "tc_update_kernel (row-scaled FP16 split, tcgen05 trailing update)",
                 "peak_source": f"{peaks['source']} bf16 sustained (kernel timed inside a long step)",
                 "algorithmic": "flops = nterms * kb * 2 * (cells updated) per launch: per step the next column block "
                                "(kb1 lower tile + m2 x kb1 rectangle) and the m2 x m2 lower triangle beyond it; "
@@ -611,18 +611,24 @@ def run_ours(args):
     # ---- kappa sweep (same Gram matrix, shifted diagonal)
     sweep = []
     if not args.no_sweep:
-        for kap in (1e2, 1e4, 1e6):
+        # the default refinement policy at each kappa; at 1e6 also classic
+        # corrections alone, the rung the policy switches away from
+        for kap, modes in ((1e2, (2,)), (1e4, (2,)), (1e6, (2, 0))):
             set_kappa(kap)
-            for nt in (args.nterms,):
+            for mode in modes:
+                prev_mode = L.starpu_gb300_dsposv_set_refinement(mode)
                 t0e, t1e = L.starpu_gb300_event_create(), L.starpu_gb300_event_create()
                 check(L.starpu_gb300_event_record(t0e, stream))
-                rc = step(nt)
+                rc = step(args.nterms)
                 check(L.starpu_gb300_event_record(t1e, stream))
                 tms = L.starpu_gb300_event_elapsed_ms(t0e, t1e)
-                sweep.append({"kappa": kap, "nterms": nt, "status": rc, "iterations": info.iterations,
+                L.starpu_gb300_dsposv_set_refinement(prev_mode)
+                sweep.append({"kappa": kap, "nterms": args.nterms, "status": rc, "iterations": info.iterations,
+                              "refinement": ("classic", "pcg", "auto")[mode],
+                              "method_at_end": ("classic", "pcg")[info.method], "fp64_fallback": info.fallback,
                               "factor_terms": info.factor_terms, "backward_error": info.backward_error,
                               "gflops": flops / (tms * 1e-3) / 1e9, "ms": tms,
-                              "_X": Xd.download((n, nrhs), np.float64) if want_oracle else None})
+                              "_X": Xd.download((n, nrhs), np.float64) if want_oracle and mode == 2 else None})
         set_kappa(args.kappa)
 
     # ---- plain FP64 GPU solve (the baseline of the ">= 3x" target)

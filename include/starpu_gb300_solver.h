@@ -36,27 +36,48 @@ int starpu_gb300_memcpy_d2d(void *stream, void *dst, const void *src, size_t byt
 /* Outcome of one starpu_gb300_dsposv call. */
 typedef struct starpu_gb300_ir_info {
     int status;            /* 0 converged; GB300_EDOM factor failed; GB300_ETIMEDOUT not converged */
-    int iterations;        /* refinement corrections applied */
-    int factor_terms;      /* BF16 products per trailing-update term (1 or 3) */
-    int potrf_info;        /* LAPACK-style info of the low-precision factorisation */
+    int iterations;        /* refinement corrections applied (each: one solve with the factor) */
+    int factor_terms;      /* products per trailing-update term (1: BF16; 3: split operands) */
+    int potrf_info;        /* LAPACK-style info of the last factorisation (mixed, or FP64 after a fallback) */
     double backward_error; /* max over RHS of ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) */
     double anorm;          /* ||A||_inf */
+    int method;            /* refinement at the end: 0 classic corrections, 1 preconditioned conjugate gradients */
+    int fallback;          /* LAPACK dsposv ITER < 0: 0 none; 1 the mixed factorisation failed (ITER -3);
+                              2 its refinement did not converge (ITER -31); then the FP64 factorisation on the
+                              GPU solved the system and status/backward_error describe that solve */
 } starpu_gb300_ir_info;
+
+/* Refinement policy of starpu_gb300_dsposv (process-wide; returns the
+ * previous value, a negative argument only queries):
+ *   mode 0 classic corrections only, 1 preconditioned conjugate gradients
+ *   from the first correction, 2 (default; STARPU_GB300_REFINE=ir|pcg sets
+ *   0|1) classic corrections, switching to conjugate gradients when one
+ *   leaves more than 5 % of the backward error;
+ *   on 1 (default; STARPU_GB300_FP64_FALLBACK=0 sets 0) LAPACK's FP64
+ *   fallback after a failed factorisation or a refinement that stalls. */
+int starpu_gb300_dsposv_set_refinement(int mode);
+int starpu_gb300_dsposv_set_fp64_fallback(int on);
 
 /* Bytes of device workspace starpu_gb300_dsposv needs (tile nb, 0 = 1024). */
 size_t starpu_gb300_dsposv_workspace(int n, int nrhs, int nb);
 
 /* Solve A X = B (A SPD, FP64; only the lower triangle of A is read, LAPACK
  * dsposv with uplo = 'L') with an FP32-storage tiled Cholesky whose panel
- * TRSM and trailing updates run on the tensor cores (split-BF16, nterms = 3,
- * or plain BF16, nterms = 1), then iterative refinement: r = b - A x with
- * ~2^-47 relative accuracy (double-float on the FP32 pipe), correction solved
- * with the low-precision factor, x += d in FP64, until every column's
- * normwise backward error <= tol or max_iter corrections were applied
- * (LAPACK dsposv semantics).  X is output
+ * TRSM and trailing updates run on the tensor cores (row-scaled FP16 split
+ * operands, nterms = 3, or plain BF16, nterms = 1), then iterative
+ * refinement: r = b - A x to ~2^-55 of ||A|| ||x|| (exact digit products on
+ * the tensor cores, FP64 sums), correction solved with the low-precision
+ * factor, x += d in FP64, until every column's normwise backward error <= tol
+ * or max_iter corrections were applied.  When a correction contracts the
+ * error slowly (kappa(A) near 1e6 and above) the refinement continues as
+ * preconditioned conjugate gradients with the same factor.  As LAPACK
+ * dsposv, a failed low-precision factorisation or a refinement that does
+ * not converge falls back to the FP64 factorisation and solve on the GPU
+ * (info->fallback; STARPU_GB300_FP64_FALLBACK=0 disables it).  X is output
  * only.  Synchronises the stream once per refinement step to read the error.
- * Returns 0, GB300_EDOM (low-precision factor not positive definite) or
- * GB300_ETIMEDOUT (no convergence); *info (may be NULL) gets the details. */
+ * Returns 0, GB300_EDOM (not positive definite) or GB300_ETIMEDOUT (no
+ * convergence, or a bounded wait ran out); *info (may be NULL) gets the
+ * details. */
 int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
                         int ldx, int nb, int nterms, double tol, int max_iter, void *work, size_t lwork,
                         starpu_gb300_ir_info *info);

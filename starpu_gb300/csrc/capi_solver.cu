@@ -11,7 +11,10 @@
 // until every right-hand side meets `tol` or `max_iter` corrections ran.
 // FP64 is used only for A, the residual and the solution accumulation.
 #include <algorithm>
+#include <atomic>
 #include <functional>
+#include <vector>
+#include <stdlib.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -200,13 +203,14 @@ __global__ void copy_f64_kernel(int n, const double *__restrict__ B, long ldb, d
 }
 
 // R = B + sum_z P_z, the K-split partials of -A X, added in a fixed order
+// (B null: R = -A X, the product the conjugate-gradient steps need)
 __global__ void residual_reduce_kernel(int n, int nrhs, int nk, const double *__restrict__ B, long ldb,
                                        const double *__restrict__ P, double *__restrict__ R, long ldr)
 {
     const long j = blockIdx.y;
     const long stride = (long)n * nrhs;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double v = B[i + j * ldb];
+        double v = B ? B[i + j * ldb] : 0.0;
         for (int z = 0; z < nk; ++z) v += P[z * stride + i + j * (long)n];
         R[i + j * ldr] = v;
     }
@@ -344,6 +348,126 @@ __global__ void backward_error_kernel(int n, const double *__restrict__ R, long 
     }
 }
 
+// Sum of v over the CTA in a fixed order (warp trees, then the warps in
+// order): deterministic, the same value in every thread.  red: 32 doubles.
+__device__ __forceinline__ double block_sum_fixed(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    return s;
+}
+
+__device__ __forceinline__ double block_max(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+    return m;
+}
+
+// Flexible preconditioned conjugate gradients, the refinement used once a
+// classic correction has contracted the error slowly (ill-conditioned A).
+// One CTA per right-hand side j not yet done.  After the preconditioner
+// solve Y = L^-T L^-1 fp32(r 2^-e) with the mixed factor:
+//   z = fp64(Y) 2^e,  rz = r.z,  beta = (rz - r.z_prev) / rho   (0 on a restart:
+//   Polak-Ribiere, which tolerates the FP32 preconditioner not being exactly
+//   the same linear map every time),  p = z + beta p,  z_prev = z,  rho = rz.
+__global__ void __launch_bounds__(512) pcg_direction_kernel(int n, const float *__restrict__ Y, long ldy,
+                                                            const int *__restrict__ exps, const double *__restrict__ R,
+                                                            long ldr, double *__restrict__ Zp, double *__restrict__ P,
+                                                            double *__restrict__ rho, const int *__restrict__ done,
+                                                            int restart)
+{
+    const long j = blockIdx.x;
+    if (done[j]) return;
+    __shared__ double red[32];
+    const int e = exps[j];
+    const float *y = Y + j * ldy;
+    const double *r = R + j * ldr;
+    double *zp = Zp + j * (long)n, *p = P + j * (long)n;
+    double rz = 0.0, rzp = 0.0;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double z = scalbn((double)y[i], e);
+        rz += r[i] * z;
+        if (!restart) rzp += r[i] * zp[i];
+    }
+    rz = block_sum_fixed(rz, red);
+    rzp = block_sum_fixed(rzp, red);
+    const double old = rho[j];
+    double beta = restart ? 0.0 : (rz - rzp) / old;
+    if (!(old > 0.0) || !isfinite(beta)) beta = 0.0;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double z = scalbn((double)y[i], e);
+        p[i] = restart ? z : z + beta * p[i];
+        zp[i] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) rho[j] = rz;
+}
+
+// The step along p (Qn = -A p from the residual kernel with no right-hand
+// side): alpha = rho / (p^T A p), x += alpha p, r -= alpha A p (the
+// recurrence residual), then the backward error of that residual as
+// backward_error_kernel computes it.  A direction with p^T A p <= 0 (the
+// preconditioned operator lost definiteness in rounding) is not taken and
+// *breakdown is set: the host restarts from the true residual.
+__global__ void __launch_bounds__(512) pcg_step_kernel(int n, const double *__restrict__ P, const double *__restrict__ Qn,
+                                                       const double *__restrict__ rho, double *__restrict__ X, long ldx,
+                                                       double *__restrict__ R, long ldr, const double *__restrict__ B,
+                                                       long ldb, const unsigned long long *anorm_bits, double tol,
+                                                       double *berr, int *done, int *rexp, int *breakdown)
+{
+    const long j = blockIdx.x;
+    if (done[j]) return;
+    __shared__ double red[32];
+    const double *p = P + j * (long)n, *q = Qn + j * (long)n;
+    double *x = X + j * ldx, *r = R + j * ldr;
+    const double *b = B + j * ldb;
+    double pap = 0.0;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) pap -= p[i] * q[i];
+    pap = block_sum_fixed(pap, red);
+    double alpha = rho[j] / pap;
+    if (!(pap > 0.0) || !isfinite(alpha)) {
+        alpha = 0.0;
+        if (threadIdx.x == 0) *breakdown = 1;
+    }
+    double rm = 0.0, xm = 0.0, bm = 0.0;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double xi = x[i] + alpha * p[i], ri = r[i] + alpha * q[i];
+        x[i] = xi;
+        r[i] = ri;
+        rm = fmax(rm, fabs(ri));
+        xm = fmax(xm, fabs(xi));
+        bm = fmax(bm, fabs(b[i]));
+    }
+    rm = block_max(rm, red);
+    xm = block_max(xm, red);
+    bm = block_max(bm, red);
+    if (threadIdx.x == 0) {
+        const double an = __longlong_as_double((long long)*anorm_bits);
+        const double den = an * xm + bm;
+        const double e = den > 0 ? rm / den : (rm > 0 ? INFINITY : 0.0);
+        berr[j] = e;
+        done[j] = (e <= tol) ? 1 : 0;
+        rexp[j] = column_exp(rm);
+    }
+}
+
+// F (n x n, ld n) = the lower triangle of A, zeros above: the FP64 copy the
+// fallback factorisation works on (the strict upper part of A is never read)
+__global__ void copy_lower_f64_kernel(int n, const double *__restrict__ A, long lda, double *__restrict__ F)
+{
+    const long j = blockIdx.x;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) F[i + j * n] = i >= j ? A[i + j * lda] : 0.0;
+}
+
 struct SolverWs {
     float *W;              // n x n FP32 working factor (ld = n)
     void *panel;           // split-BF16 panels
@@ -351,8 +475,7 @@ struct SolverWs {
     float *Y;              // n x nrhs FP32 right-hand side / correction
     void *sweep;           // inverted 64 x 64 diagonal blocks + flags of the 64-row POTRS sweeps
     float *band;           // inverses of the nb x nb diagonal tiles (tile T at band + T * ldk * ldk), or null
-    float *Z;              // n x 16 scratch of the tile-row sweeps
-    int *cnt;              // 2 * ntiles + 1 counters of the tile-row sweeps
+    void *tsw;             // scratch of the tile-row sweeps (tsw_scratch_bytes)
     double *partials;      // K-split partials of the residual
     float2 *xs;            // double-float split of X (n x 16 per group of 16 columns)
     int *sx;               // per-column scale exponents of X
@@ -361,6 +484,9 @@ struct SolverWs {
     float *rowsum;         // n/64 x n row sums of the slicing pass, for ||A||_inf
     double *berr;          // nrhs
     int *done;             // nrhs
+    double *P, *Qn, *Zp;   // n x nrhs each: direction, -A p and the previous z of the conjugate-gradient steps
+    double *rho;           // nrhs: r.z of the conjugate-gradient steps
+    int *brk;              // breakdown word of the conjugate-gradient steps
     int *rexp;             // nrhs: power-of-two scales of the FP32 right-hand sides
     unsigned long long *anorm_bits;
     int *info, *err;
@@ -375,40 +501,62 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 static bool tile_sweep_ok(int nb) { return nb > 0 && nb % TSW_SLAB == 0 && nb <= GB300_DIAG_TILE_MAX; }
 
 // L y = b then L^T x = y with the inverted nb x nb diagonal tiles in `band`
-// (ld ldk, tile T at band + T * ldk * ldk): one launch per sweep and group
-// of 16 right-hand sides.
+// (ld ldk, tile T at band + T * ldk * ldk): one persistent launch per sweep
+// and group of 16 right-hand sides.  scratch: tsw_scratch_bytes(n, nb).
 static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L, long ldl, const float *band, long ldk,
-                        float *Y, long ldy, float *Z, int *cnt, int *err, int upper = 0)
+                        float *Y, long ldy, void *scratch, int *err, int upper = 0)
 {
     if (n <= 0 || nrhs <= 0) return;
     TileSweepArgs a;
     a.n = n;
     a.nb = nb;
     a.ntiles = (n + nb - 1) / nb;
-    a.nslabs = (a.ntiles - 1) * (nb / TSW_SLAB) + (n - (a.ntiles - 1) * nb + TSW_SLAB - 1) / TSW_SLAB;
+    a.spt = nb / TSW_SLAB;
+    a.total = (unsigned)((size_t)a.spt * a.ntiles * (a.ntiles + 1) / 2);
+    size_t zp_off = 0, cnt_off = 0;
+    tsw_scratch_bytes(n, nb, &zp_off, &cnt_off);
     a.L = L;
     a.ldl = ldl;
     a.Dinv = band;
     a.ldd = ldk;
     a.dstride = ldk * ldk;
     a.ldb = ldy;
-    a.Z = Z;
+    a.Z = (float *)scratch;
+    a.Zp = (float *)((char *)scratch + zp_off);
+    int *cnt = (int *)((char *)scratch + cnt_off);
     a.zcount = cnt;
     a.ycount = cnt + a.ntiles;
-    a.ticket = (unsigned *)(cnt + 2 * a.ntiles);
+    a.pcount = cnt + 2 * a.ntiles;
+    a.ticket = (unsigned *)(cnt + 3 * a.ntiles);
     a.err = err;
     a.upper = upper;
     a.budget_ns = gb300_wait_budget_ns();
+    // persistent CTAs: as many as fit on the device, and at least one per slab
+    // of a tile row (the diagonal tasks of a tile row wait for one another)
+    static thread_local int per_sm[3] = {0, 0, 0};
+    if (!per_sm[0]) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], tile_sweep_kernel<false, false>, TSW_T, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], tile_sweep_kernel<true, false>, TSW_T, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[2], tile_sweep_kernel<true, true>, TSW_T, 0);
+        for (int &x : per_sm) x = std::max(x, 1);
+    }
+    const int sms = gb300_device_sms();
+    auto grid = [&](int which) {
+        const long g = std::min<long>((long)a.total, (long)per_sm[which] * sms);
+        return (unsigned)std::max<long>(g, a.spt);
+    };
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
-    a.vec = al(L) && al(band) && al(Y) && al(Z) && ldl % 4 == 0 && ldk % 4 == 0 && ldy % 4 == 0 && n % 4 == 0;
+    a.vec = al(L) && al(band) && al(Y) && al(a.Z) && ldl % 4 == 0 && ldk % 4 == 0 && ldy % 4 == 0 && n % 4 == 0;
+    const size_t cbytes = (3 * (size_t)a.ntiles + 1) * sizeof(int);
     for (int c0 = 0; c0 < nrhs; c0 += 16) {
         a.nrhs = std::min(16, nrhs - c0);
         a.B = Y + (long)c0 * ldy;
         a.vec = a.vec && al(a.B);
-        cudaMemsetAsync(cnt, 0, (2 * a.ntiles + 1) * sizeof(int), s);
-        gb300_count_launch(), tile_sweep_kernel<false><<<a.nslabs, TSW_T, 0, s>>>(a);
-        cudaMemsetAsync(cnt, 0, (2 * a.ntiles + 1) * sizeof(int), s);
-        gb300_count_launch(), tile_sweep_kernel<true><<<a.nslabs, TSW_T, 0, s>>>(a);
+        cudaMemsetAsync(cnt, 0, cbytes, s);
+        gb300_count_launch(), tile_sweep_kernel<false, false><<<grid(0), TSW_T, 0, s>>>(a);
+        cudaMemsetAsync(cnt, 0, cbytes, s);
+        if (upper) gb300_count_launch(), tile_sweep_kernel<true, true><<<grid(2), TSW_T, 0, s>>>(a);
+        else gb300_count_launch(), tile_sweep_kernel<true, false><<<grid(1), TSW_T, 0, s>>>(a);
     }
 }
 
@@ -430,8 +578,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const bool tiles = tile_sweep_ok(nb);
     const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64, ntiles = nb > 0 ? ((size_t)n + nb - 1) / nb : 0;
     const size_t oB = tiles ? take(ntiles * ldk * ldk * sizeof(float)) : 0;
-    const size_t oZ = tiles ? take((size_t)n * 16 * sizeof(float)) : 0;
-    const size_t oC = tiles ? take((2 * ntiles + 1) * sizeof(int)) : 0;
+    const size_t oZ = tiles ? take(tsw_scratch_bytes(n, nb)) : 0;
     const size_t oA = take(residual_tc_a_bytes(n));
     const size_t oN = take((size_t)((n + 63) / 64) * n * sizeof(float));
     const size_t oS = take(4 * sizeof(unsigned long long));
@@ -444,6 +591,8 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t oI = take((size_t)nrhs * sizeof(int));
     const size_t oJ = take((size_t)nrhs * sizeof(int));
     const size_t oK = take(residual_tc_xs_bytes(n, nrhs));
+    const size_t oG = take(3 * (size_t)n * nrhs * sizeof(double));
+    const size_t oH = take((size_t)nrhs * sizeof(double) + 16);
     if (ws && base) {
         char *b = (char *)base;
         ws->W = (float *)(b + oW);
@@ -453,8 +602,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->Y = (float *)(b + oY);
         ws->sweep = b + oT;
         ws->band = tiles ? (float *)(b + oB) : nullptr;
-        ws->Z = tiles ? (float *)(b + oZ) : nullptr;
-        ws->cnt = tiles ? (int *)(b + oC) : nullptr;
+        ws->tsw = tiles ? (void *)(b + oZ) : nullptr;
         ws->rtc_a = b + oA;
         ws->rowsum = (float *)(b + oN);
         ws->partials = (double *)(b + oQ);
@@ -463,6 +611,11 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->rexp = (int *)(b + oJ);
         ws->rtc_xs = b + oK;
         ws->berr = (double *)(b + oE);
+        ws->P = (double *)(b + oG);
+        ws->Qn = ws->P + (size_t)n * nrhs;
+        ws->Zp = ws->Qn + (size_t)n * nrhs;
+        ws->rho = (double *)(b + oH);
+        ws->brk = (int *)(ws->rho + nrhs);
         ws->done = (int *)(b + oD);
         ws->anorm_bits = (unsigned long long *)(b + oS);
         ws->info = (int *)(b + oS + 8);
@@ -478,7 +631,7 @@ static void correction_solve(cudaStream_t s, int n, int nrhs, int nb, const Solv
 {
     const long ldk = ((long)nb + 63) / 64 * 64;
     // the factor phase mirrors L^T into W's strictly upper part (outside the diagonal tiles)
-    if (ws.band) tile_sweeps(s, n, nrhs, nb, ws.W, n, ws.band, ldk, ws.Y, n, ws.Z, ws.cnt, ws.err, 1);
+    if (ws.band) tile_sweeps(s, n, nrhs, nb, ws.W, n, ws.band, ldk, ws.Y, n, ws.tsw, ws.err, 1);
     else potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
 }
 
@@ -642,16 +795,48 @@ int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int
     return GB300_OK;
 }
 
+// How the refinement proceeds (STARPU_GB300_REFINE, or
+// starpu_gb300_dsposv_set_refinement): 0 classic corrections only ("ir"),
+// 1 conjugate gradients from the first correction on ("pcg"), 2 (default)
+// classic corrections until one contracts the backward error by less than
+// PCG_SWITCH, then conjugate gradients.
+static std::atomic<int> g_refine{-1};
+static int refine_mode()
+{
+    int m = g_refine.load(std::memory_order_relaxed);
+    if (m >= 0) return m;
+    const char *e = getenv("STARPU_GB300_REFINE");
+    m = (e && !strcmp(e, "ir")) ? 0 : (e && !strcmp(e, "pcg")) ? 1 : 2;
+    int expect = -1;
+    g_refine.compare_exchange_strong(expect, m);
+    return g_refine.load(std::memory_order_relaxed);
+}
+// A classic correction that leaves more than this fraction of the backward
+// error marks an ill-conditioned system (kappa times the factor's error near
+// 1e-1): from there conjugate gradients with the same factor as
+// preconditioner contract the error faster per correction.
+static constexpr double PCG_SWITCH = 0.05;
+// corrections without halving the best backward error seen: stalled
+static constexpr int STALL_STEPS = 6;
+
 // Refine phase: x = L^-T L^-1 b in FP32, then FP64 refinement with the factor
-// left in the workspace by dsposv_factor (for the same A).
+// left in the workspace by dsposv_factor (for the same A): classic
+// corrections x += L^-T L^-1 r, switching to flexible preconditioned
+// conjugate gradients (preconditioner L L^T, FP64 vectors, the recurrence
+// residual checked against a true residual before it is accepted) when the
+// corrections contract slowly.  *stalled (optional): set when the refinement
+// stopped without converging (max_iter corrections, or no progress) -- the
+// case in which LAPACK dsposv falls back to the FP64 factorisation.
 int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
-                  int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out)
+                  int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out, bool *stalled)
 {
     SolverWs ws;
     layout(n, nrhs, nb, work, &ws);
+    if (stalled) *stalled = false;
     const unsigned gx = (unsigned)std::min<long>(((long)n + 255) / 256, 1024);
     cudaMemsetAsync(ws.done, 0, nrhs * sizeof(int), s);
     cudaMemsetAsync(ws.err, 0, sizeof(int), s);
+    cudaMemsetAsync(ws.brk, 0, sizeof(int), s);
     gb300_count_launch(), colmax_exp_kernel<<<nrhs, 256, 0, s>>>(n, B, ldb, ws.rexp);
     gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, B, ldb, ws.Y, n, ws.rexp);
     int slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
@@ -662,39 +847,89 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
     double *hberr = (double *)malloc(sizeof(double) * (size_t)nrhs);
     int status = GB300_ETIMEDOUT;
     int it = 0, rc = 0;
-    double worst = INFINITY;
-    for (;; ++it) {
-        slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
-        if ((rc = residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx, ws.rtc_a,
-                                 ws.rtc_xs, ws.anorm_bits, ws.err)))
-            break;
-        gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
-        gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb, ws.anorm_bits, tol, ws.berr, ws.done,
-                                                                     ws.rexp);
-        if ((rc = gb300_record_cuda_error(
-                 cudaMemcpyAsync(hberr, ws.berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s))))
-            break;
-        int herr = 0;  // a wait that ran out in a sweep or a residual invalidates the iteration
-        if ((rc = gb300_record_cuda_error(cudaMemcpyAsync(&herr, ws.err, sizeof herr, cudaMemcpyDeviceToHost, s))))
-            break;
-        if ((rc = gb300_record_cuda_error(cudaStreamSynchronize(s)))) break;
-        if (herr) {
-            status = GB300_ETIMEDOUT;
-            break;
-        }
+    const int mode = refine_mode();
+    bool pcg = false, restart = true, true_residual = true;
+    double worst = INFINITY, prev = INFINITY, best = INFINITY;
+    int since_best = 0;
+    // read the backward errors (and the wait-timeout word) of the step just queued
+    auto read_berr = [&](int *herr, int *hbreak) -> int {
+        int r = gb300_record_cuda_error(cudaMemcpyAsync(hberr, ws.berr, sizeof(double) * nrhs,
+                                                        cudaMemcpyDeviceToHost, s));
+        if (!r) r = gb300_record_cuda_error(cudaMemcpyAsync(herr, ws.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if (!r) r = gb300_record_cuda_error(cudaMemcpyAsync(hbreak, ws.brk, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if (!r) r = gb300_record_cuda_error(cudaStreamSynchronize(s));
         worst = 0;
         for (int j = 0; j < nrhs; ++j) worst = fmax(worst, hberr[j]);
-        if (worst <= tol) {
-            status = GB300_OK;
+        return r;
+    };
+    for (;;) {
+        int herr = 0, hbreak = 0;
+        if (true_residual) {
+            // r = b - A x, its backward error; every column's done flag from it
+            slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
+            if ((rc = residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx,
+                                     ws.rtc_a, ws.rtc_xs, ws.anorm_bits, ws.err)))
+                break;
+            gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
+            gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb,
+                                                                             ws.anorm_bits, tol, ws.berr, ws.done,
+                                                                             ws.rexp);
+            if ((rc = read_berr(&herr, &hbreak))) break;
+            if (herr) {  // a wait that ran out in a sweep or a residual invalidates the iteration
+                status = GB300_ETIMEDOUT;
+                break;
+            }
+            if (worst <= tol) {
+                status = GB300_OK;
+                break;
+            }
+            if (pcg) restart = true;  // the recurrence residual had drifted: start again from the true one
+            else if (mode == 1 || (mode == 2 && it >= 1 && worst > PCG_SWITCH * prev)) pcg = true;
+        }
+        if (worst < 0.5 * best) {
+            best = worst;
+            since_best = 0;
+        } else if (++since_best >= STALL_STEPS) {
+            if (stalled) *stalled = true;
             break;
         }
-        if (it >= max_iter) break;
+        if (it >= max_iter) {
+            if (stalled) *stalled = true;
+            break;
+        }
+        prev = worst;
+        // the preconditioner / correction solve on the scaled residual
         gb300_count_launch(), to_f32_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.R, n, ws.Y, n, ws.rexp);
         slot = gb300_prof_begin(s, GB300_PROF_SOLVE);
         correction_solve(s, n, nrhs, nb, ws);
         gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 4.0 * n * (double)n);
-        gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 1, ws.done,
-                                                                               ws.rexp);
+        ++it;
+        if (!pcg) {
+            gb300_count_launch(), accumulate_kernel<<<dim3(gx, nrhs), 256, 0, s>>>(n, nrhs, ws.Y, n, X, ldx, 1,
+                                                                                   ws.done, ws.rexp);
+            true_residual = true;
+            continue;
+        }
+        // conjugate-gradient step: direction, -A p, step and the recurrence residual's backward error
+        gb300_count_launch(), pcg_direction_kernel<<<nrhs, 512, 0, s>>>(n, ws.Y, n, ws.rexp, ws.R, n, ws.Zp, ws.P,
+                                                                        ws.rho, ws.done, restart ? 1 : 0);
+        restart = false;
+        slot = gb300_prof_begin(s, GB300_PROF_RESIDUAL);
+        if ((rc = residual_mixed(s, n, nrhs, A, lda, ws.P, n, nullptr, 0, ws.Qn, n, ws.partials, ws.xs, ws.sx,
+                                 ws.rtc_a, ws.rtc_xs, ws.anorm_bits, ws.err)))
+            break;
+        gb300_prof_end(s, slot, 2.0 * n * (double)n * nrhs, 8.0 * n * (double)n + 32.0 * n * nrhs);
+        gb300_count_launch(), pcg_step_kernel<<<nrhs, 512, 0, s>>>(n, ws.P, ws.Qn, ws.rho, X, ldx, ws.R, n, B, ldb,
+                                                                   ws.anorm_bits, tol, ws.berr, ws.done, ws.rexp,
+                                                                   ws.brk);
+        if ((rc = read_berr(&herr, &hbreak))) break;
+        if (herr) {
+            status = GB300_ETIMEDOUT;
+            break;
+        }
+        // accepted only after a true residual agrees; a breakdown restarts from one
+        true_residual = worst <= tol || hbreak;
+        if (hbreak) cudaMemsetAsync(ws.brk, 0, sizeof(int), s);
     }
     free(hberr);
     if (rc) return rc;
@@ -702,6 +937,7 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
         out->iterations = it;
         out->backward_error = worst;
         out->status = status;
+        out->method = pcg ? 1 : 0;
         unsigned long long ab = 0;
         cudaMemcpyAsync(&ab, ws.anorm_bits, sizeof ab, cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
@@ -712,11 +948,117 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
     return status;
 }
 
+// LAPACK dsposv's fallback (ITER < 0): the FP64 tiled Cholesky of A on the GPU
+// and its two triangular solves, when the mixed factorisation failed or its
+// refinement did not converge.  The FP64 factor takes the place of the
+// residual's digit slices in the workspace (16 n ldk bytes >= 8 n^2), which
+// are cut again from A afterwards for the backward error; the FP32 factor in
+// the workspace is not valid after a fallback.
+int dsposv_fp64(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                int ldx, int nb, double tol, void *work, starpu_gb300_ir_info *out)
+{
+    SolverWs ws;
+    layout(n, nrhs, nb, work, &ws);
+    double *F = (double *)ws.rtc_a;
+    gb300_count_launch(), copy_lower_f64_kernel<<<n, 256, 0, s>>>(n, A, lda, F);
+    int rc = gb300_record_cuda_error(cudaMemcpy2DAsync(X, sizeof(double) * ldx, B, sizeof(double) * ldb,
+                                                       sizeof(double) * n, nrhs, cudaMemcpyDeviceToDevice, s));
+    if (!rc) rc = starpu_gb300_dpotrf(s, n, F, n, nb, ws.info);
+    int hinfo = 0;
+    if (!rc) rc = gb300_record_cuda_error(cudaMemcpyAsync(&hinfo, ws.info, sizeof hinfo, cudaMemcpyDeviceToHost, s));
+    if (!rc) rc = gb300_record_cuda_error(cudaStreamSynchronize(s));
+    if (rc) return rc;
+    if (out) out->potrf_info = hinfo;
+    if (hinfo) {
+        if (out) out->status = GB300_EDOM;
+        return GB300_EDOM;
+    }
+    if ((rc = starpu_gb300_dpotrs(s, n, nrhs, F, n, X, ldx))) return rc;
+    // the factor is no longer needed: A is cut into its digit slices again
+    // (max |A_ij| and ||A||_inf from the lower triangle on the way) and
+    // r = b - A x is formed as the refinement forms it
+    cudaMemsetAsync(ws.anorm_bits, 0, 4 * sizeof(unsigned long long), s);
+    gb300_count_launch(), convert_lower_max_kernel<<<n, 256, 0, s>>>(n, A, lda, nullptr, 0, ws.anorm_bits + 2);
+    if ((rc = residual_tc_slice_a(s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum))) return rc;
+    gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, (n + 63) / 64, ws.rowsum,
+                                                                                  ws.anorm_bits + 2, ws.anorm_bits);
+    if ((rc = residual_mixed(s, n, nrhs, A, lda, X, ldx, B, ldb, ws.R, n, ws.partials, ws.xs, ws.sx, ws.rtc_a,
+                             ws.rtc_xs, ws.anorm_bits, ws.err)))
+        return rc;
+    gb300_count_launch(), backward_error_kernel<<<nrhs, 256, 0, s>>>(n, ws.R, n, X, ldx, B, ldb, ws.anorm_bits, tol,
+                                                                     ws.berr, ws.done, nullptr);
+    std::vector<double> hb((size_t)nrhs);
+    unsigned long long ab = 0;
+    rc = gb300_record_cuda_error(cudaMemcpyAsync(hb.data(), ws.berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+    if (!rc) rc = gb300_record_cuda_error(cudaMemcpyAsync(&ab, ws.anorm_bits, sizeof ab, cudaMemcpyDeviceToHost, s));
+    if (!rc) rc = gb300_record_cuda_error(cudaStreamSynchronize(s));
+    if (rc) return rc;
+    double worst = 0;
+    for (double v : hb) worst = fmax(worst, v);
+    const int status = worst <= tol ? GB300_OK : GB300_ETIMEDOUT;
+    if (out) {
+        out->backward_error = worst;
+        memcpy(&out->anorm, &ab, sizeof ab);
+        out->status = status;
+    }
+    return status;
+}
+
+// The ladder of one mixed solve: the factor and its refinement, then LAPACK's
+// FP64 fallback when the factor failed (GB300_EDOM: fallback 1, ITER = -3) or
+// the refinement stalled (fallback 2, ITER = -31).  STARPU_GB300_FP64_FALLBACK=0
+// turns the fallback off (the mixed outcome is returned as it is).
+static std::atomic<int> g_fallback{-1};
+static bool fp64_fallback_enabled()
+{
+    int f = g_fallback.load(std::memory_order_relaxed);
+    if (f < 0) {
+        const char *e = getenv("STARPU_GB300_FP64_FALLBACK");
+        int expect = -1;
+        g_fallback.compare_exchange_strong(expect, (e && !strcmp(e, "0")) ? 0 : 1);
+        f = g_fallback.load(std::memory_order_relaxed);
+    }
+    return f != 0;
+}
+
+int dsposv_ladder(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                  int ldx, int nb, int nterms, double tol, int max_iter, void *work, starpu_gb300_ir_info *out,
+                  bool prepared)
+{
+    int rc = dsposv_factor(s, n, nrhs, A, lda, nb, nterms, work, out, prepared);
+    int reason = 0;
+    if (rc == GB300_EDOM) reason = 1;
+    else if (rc) return rc;
+    if (!reason) {
+        bool stalled = false;
+        rc = dsposv_refine(s, n, nrhs, A, lda, B, ldb, X, ldx, nb, tol, max_iter, work, out, &stalled);
+        if (rc != GB300_ETIMEDOUT || !stalled) return rc;
+        reason = 2;
+    }
+    if (!fp64_fallback_enabled()) return rc;
+    if (out) out->fallback = reason;
+    return dsposv_fp64(s, n, nrhs, A, lda, B, ldb, X, ldx, nb, tol, work, out);
+}
+
 } // namespace gb300
 
 using namespace gb300;
 
 extern "C" {
+
+int starpu_gb300_dsposv_set_refinement(int mode)
+{
+    const int prev = refine_mode();
+    if (mode >= 0 && mode <= 2) g_refine.store(mode);
+    return prev;
+}
+
+int starpu_gb300_dsposv_set_fp64_fallback(int on)
+{
+    const int prev = fp64_fallback_enabled() ? 1 : 0;
+    if (on >= 0) g_fallback.store(on ? 1 : 0);
+    return prev;
+}
 
 size_t starpu_gb300_dsposv_workspace(int n, int nrhs, int nb)
 {
@@ -736,10 +1078,8 @@ int starpu_gb300_dsposv(void *stream, int n, int nrhs, const double *A, int lda,
     if (nb <= 0) nb = 1024;
     if (!work || lwork < starpu_gb300_dsposv_workspace(n, nrhs, nb)) return GB300_EINVAL;
     if (!n || !nrhs) return GB300_OK;
-    cudaStream_t s = (cudaStream_t)stream;
-    int rc = gb300::dsposv_factor(s, n, nrhs, A, lda, nb, nterms, work, out);
-    if (rc) return rc;
-    return gb300::dsposv_refine(s, n, nrhs, A, lda, B, ldb, X, ldx, nb, tol, max_iter, work, out);
+    return gb300::dsposv_ladder((cudaStream_t)stream, n, nrhs, A, lda, B, ldb, X, ldx, nb, nterms, tol, max_iter,
+                                work, out, false);
 }
 
 // ---- persistent solver context: device buffers sized once, host-buffer calls
@@ -927,9 +1267,8 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
         // the factor phase's first pass was fused into the gather
         if (info) memset(info, 0, sizeof *info);
         if ((h->nterms != 1 && h->nterms != 3) || max_iter < 0 || !(tol >= 0)) return GB300_EINVAL;
-        status = dsposv_factor(s, n, nrhs, h->A, n, nb_eff, h->nterms, h->work, info, true);
-        if (status == GB300_OK)
-            status = dsposv_refine(s, n, nrhs, h->A, n, h->B, n, h->X, n, nb_eff, tol, max_iter, h->work, info);
+        status = dsposv_ladder(s, n, nrhs, h->A, n, h->B, n, h->X, n, nb_eff, h->nterms, tol, max_iter, h->work,
+                               info, true);
     } else {
         status = starpu_gb300_dsposv(s, n, nrhs, h->A, n, h->B, n, h->X, n, h->nb, h->nterms, tol, max_iter, h->work,
                                      h->lwork, info);
@@ -949,8 +1288,7 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
 size_t starpu_gb300_spotrs_inv_tiles_workspace(int n, int nb)
 {
     if (n < 0 || !tile_sweep_ok(nb)) return 0;
-    const size_t ntiles = ((size_t)n + nb - 1) / nb;
-    return align256((size_t)n * 16 * sizeof(float)) + align256((2 * ntiles + 1) * sizeof(int));
+    return tsw_scratch_bytes(n, nb);
 }
 
 int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const float *L, int ldl, const float *Dinv,
@@ -960,9 +1298,7 @@ int starpu_gb300_spotrs_inv_tiles(void *stream, int n, int nrhs, int nb, const f
         (n && (!L || !Dinv || !B || !work || !d_err || lwork < starpu_gb300_spotrs_inv_tiles_workspace(n, nb))))
         return GB300_EINVAL;
     if (!n || !nrhs) return GB300_OK;
-    float *Z = (float *)work;
-    int *cnt = (int *)((char *)work + align256((size_t)n * 16 * sizeof(float)));
-    tile_sweeps((cudaStream_t)stream, n, nrhs, nb, L, ldl, Dinv, ldd, B, ldb, Z, cnt, d_err);
+    tile_sweeps((cudaStream_t)stream, n, nrhs, nb, L, ldl, Dinv, ldd, B, ldb, work, d_err);
     return gb300_last_launch_status();
 }
 

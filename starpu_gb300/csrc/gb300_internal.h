@@ -27,8 +27,17 @@ int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int
 // the workspace regions the host path's fused gather writes: W (n x n FP32)
 // and the word that receives max |A_ij| (zeroed with its three neighbours)
 void dsposv_prepared_targets(int n, int nrhs, int nb, void *work, float **W, unsigned long long **amax_block);
+// stalled (optional): set when the refinement stopped without converging
 int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
-                  int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out);
+                  int ldx, int nb, double tol, int max_iter, void *work, starpu_gb300_ir_info *out,
+                  bool *stalled = nullptr);
+// LAPACK dsposv's fallback: FP64 factorisation and solve of A on the GPU
+int dsposv_fp64(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                int ldx, int nb, double tol, void *work, starpu_gb300_ir_info *out);
+// factor + refinement, then the FP64 fallback when either fails
+int dsposv_ladder(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
+                  int ldx, int nb, int nterms, double tol, int max_iter, void *work, starpu_gb300_ir_info *out,
+                  bool prepared);
 
 // The mixed solve's schedule for one tile size, from starpu_gb300_dense_autotune,
 // stored in the tuning table beside the perfmodels (capi_batched.cu).

@@ -321,11 +321,16 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                     for (int j = 0; j < 32; ++j) {
                         const int col = c0 + j;
                         const bool w = col < args.n && (!args.lower || row >= col);
-                        // 2^(k_i + k_j): a product of two powers of two, exact (subnormal
-                        // for matrices far below unit scale), never overflowing where C does not
+                        // 2^(k_i + k_j) as one exact factor: it cannot overflow where C does
+                        // not (a panel scale of 2^105 times an inverse's 2^-75 is fine, while
+                        // the accumulator times 2^105 alone is not).  Below FP32's normal
+                        // range (both scales tiny, matrices ~1e-30) the two are applied one
+                        // after the other instead, the accumulator keeping the product normal.
                         const float sc = rsc * cs[j];
+                        const bool tiny = sc < 1.17549435e-38f;
                         const float a = __uint_as_float(r[j]);
-                        if (w) crow[(long)col * args.ldc] = args.store ? a * sc : fmaf(-a, sc, cv[j]);
+                        const float f1 = tiny ? a * rsc : a, f2 = tiny ? cs[j] : sc;
+                        if (w) crow[(long)col * args.ldc] = args.store ? f1 * f2 : fmaf(-f1, f2, cv[j]);
                     }
                 }
             }

@@ -4,26 +4,31 @@
 // diagonal tiles the factorisation leaves behind.  The chain of dependent
 // steps is n / nb long (32 at n = 32768, nb = 1024) instead of n / 64.
 //
-// One CTA per 32-row slab; a CTA takes a ticket when it starts and solves the
-// slab of that rank in solve order.  Forward, slab of tile row T:
-//   z = b_slab - sum_{j<T} L_slab,j y_j   (each y_j as soon as tile row j is
-//                                          complete: ycount[j] slabs stored)
-//   z is published (Z rows, zcount[T]); once the whole tile row's z is there,
-//   y_slab = (L_TT^-1)_slab,0..slab z_T    (the lower-triangular inverse)
-//   y is stored in place of b and counted in ycount[T].
-// Backward, slab of tile row T (tile rows in reverse order):
-//   z = y_slab - sum_{j>T} (L_j,slab)^T x_j,   x_slab = ((L_TT^-1)^T)_slab z_T.
-// A CTA only waits on slabs with earlier tickets or on the other slabs of its
-// own tile row, whose tickets are consecutive: every CTA it waits for either
-// runs or starts once earlier tile rows finish, so the sweep cannot deadlock
-// however CTAs are scheduled.  Every wait is bounded by a %globaltimer budget;
-// on timeout the CTA records an error and carries on, so the launch ends.
+// Persistent CTAs take tasks by ticket, in solve order.  Tile row u of the
+// solve order (u = T forward, T = ntiles - 1 - u backward) has, for each of
+// its 32-row slabs s:
+//   u products   P_{u,v,s} = L_{slab, tile v} y_v for the earlier tile rows v
+//                (backward: (L_{v, slab})^T x_v), each waiting only for tile
+//                row v to be solved, written to its own partial block;
+//   one diagonal task: z_s = b_s - sum_v P_{u,v,s} (v in order: deterministic),
+//                published (Z rows, zcount[u]); once the tile row's z is
+//                complete, y_s = (L_TT^-1)_{slab, 0..slab end} z_T (backward
+//                the transposed inverse), stored in place of b (ycount[u]).
+// Tickets run over the products of tile row u (v ascending, slabs inner),
+// then its diagonal tasks, then tile row u + 1.  The products of a tile row
+// therefore spread over all CTAs instead of running one after the other in
+// the slab's own CTA, and only the product with the newest tile row and the
+// diagonal task are on the chain.  A CTA waits only on tasks with smaller
+// tickets (already held by running CTAs) or, in a diagonal task, on the other
+// diagonal tasks of its tile row, which publish before they wait; with at
+// least as many CTAs as slabs per tile row the sweep cannot deadlock however
+// CTAs are scheduled.  Every wait is bounded by a %globaltimer budget; on
+// timeout the CTA records an error and stops waiting, so the launch ends.
 //
 // The products are register-blocked: the K range of every chunk (128 columns)
 // is split over the 8 warps, each lane keeps 4 rows x 4 right-hand sides, and
 // the next two chunks are fetched into registers while the current one is
-// used; the operands of a slab's next tile row are prefetched into L2 while it
-// waits for that row.
+// used; a task's operand is prefetched into L2 before it waits.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -38,16 +43,18 @@ constexpr int TSW_T = 256;
 
 struct TileSweepArgs {
     int n, nrhs, nb;
-    int ntiles, nslabs;
+    int ntiles, spt;  // tile rows; slabs per tile row (nb / 32)
+    unsigned total;   // tasks: spt * ntiles * (ntiles + 1) / 2
     const float *L;
     long ldl;
     const float *Dinv;  // tile T's inverse at Dinv + T * dstride, leading dimension ldd
     long ldd, dstride;
     float *B;  // right-hand sides in, solution out (n x nrhs, ld ldb)
     long ldb;
-    float *Z;  // n x 16 scratch, ld n
+    float *Z;   // n x 16 scratch, ld n
+    float *Zp;  // partial products: pair (u, v < u) at Zp + (u (u - 1) / 2 + v) * nb * 16, slab-major 32 x 16
     unsigned *ticket;
-    int *zcount, *ycount;  // per tile row, zero at launch
+    int *zcount, *ycount, *pcount;  // per tile row of the solve order, zero at launch
     int *err;
     unsigned long long budget_ns;
     int vec;  // L, Dinv, B, Z and their leading dimensions allow 16-byte loads
@@ -56,6 +63,19 @@ struct TileSweepArgs {
     // of L^T are read column by column like the forward sweep's operands
     int upper;
 };
+
+// Bytes of scratch a sweep pair needs: Z (n x 16), the partial products of
+// every pair of tile rows, and the 3 ntiles + 1 counters.
+inline size_t tsw_scratch_bytes(int n, int nb, size_t *zp_off = nullptr, size_t *cnt_off = nullptr)
+{
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t nt = ((size_t)n + nb - 1) / nb;
+    const size_t z = al((size_t)n * 16 * sizeof(float));
+    const size_t zp = al(nt * (nt > 0 ? nt - 1 : 0) / 2 * (size_t)nb * 16 * sizeof(float));
+    if (zp_off) *zp_off = z;
+    if (cnt_off) *cnt_off = z + zp;
+    return z + zp + al((3 * nt + 1) * sizeof(int));
+}
 
 __device__ __forceinline__ int tsw_ld_acquire(const int *p)
 {
@@ -299,77 +319,120 @@ __device__ __forceinline__ void tsw_reduce(const float acc[4][4], float *red, fl
     __syncthreads();
 }
 
-template <bool TRANS>
-__global__ void __launch_bounds__(TSW_T) tile_sweep_kernel(TileSweepArgs a)
+// One product task: P_{u,v,s} = L_{slab, tile v} y_v (backward the transposed
+// block), written to its partial block and counted in pcount[u].
+template <bool TRANS, bool UPPER>
+__device__ __forceinline__ void tsw_product_task(const TileSweepArgs &a, int u, int v, int s, float *Ms, float *Vs,
+                                                 float *zs, int *skip)
 {
-    __shared__ __align__(16) float Ms[TSW_KC * TSW_MP];
-    __shared__ __align__(16) float Vs[TSW_KC * TSW_VP];
-    __shared__ float zs[TSW_SLAB * 16];
-    __shared__ unsigned s_ticket;
-    __shared__ int s_skip;
-    float *red = Ms;  // 8 x 512 floats after the products
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        s_ticket = atomicAdd(a.ticket, 1u);
-        s_skip = 0;
-    }
-    __syncthreads();
-    const int t = (int)s_ticket;
-    if (t >= a.nslabs) return;
-    const int spt = a.nb / TSW_SLAB;
-    const int q = TRANS ? a.nslabs - 1 - t : t;
-    const int T = q / spt, s = q % spt;
+    const int T = TRANS ? a.ntiles - 1 - u : u, j = TRANS ? a.ntiles - 1 - v : v;
     const int t0 = T * a.nb, kbT = min(a.nb, a.n - t0);
-    const int nsT = (kbT + TSW_SLAB - 1) / TSW_SLAB;
     const int r0 = t0 + s * TSW_SLAB, rows = min(TSW_SLAB, kbT - s * TSW_SLAB);
-    const bool vec = a.vec != 0;
-
-    // the slab's rows (forward) or columns (backward) of the diagonal tile's inverse, needed last
-    const float *D = a.Dinv + (long)T * a.dstride;
-    if (!TRANS) tsw_prefetch_l2<false>(D + s * TSW_SLAB, a.ldd, rows, s * TSW_SLAB + rows);
-    else tsw_prefetch_l2<true>(D + s * TSW_SLAB + (long)(s * TSW_SLAB) * a.ldd, a.ldd, rows, kbT - s * TSW_SLAB);
-
-    // contributions of the other tile rows: acc = sum (L_slab,j y_j) or sum (L_j,slab^T x_j)
-    float acc[4][4] = {};
-    const int jbeg = TRANS ? a.ntiles - 1 : 0, jend = TRANS ? T : T, jstep = TRANS ? -1 : 1;
-    for (int j = jbeg; j != jend; j += jstep) {
-        const int j0 = j * a.nb, kbj = min(a.nb, a.n - j0);
-        const bool direct = !TRANS || a.upper;  // operand read as rows of 32 per column
-        if (direct) tsw_prefetch_l2<false>(a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, kbj);
+    const int j0 = j * a.nb, kbj = min(a.nb, a.n - j0);
+    if (rows > 0) {
+        constexpr bool direct = !TRANS || UPPER;  // operand read as rows of 32 per column
+        if constexpr (direct) tsw_prefetch_l2<false>(a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, kbj);
         else tsw_prefetch_l2<true>(a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, kbj);
-        tsw_wait(a, &a.ycount[j], (kbj + TSW_SLAB - 1) / TSW_SLAB, &s_skip);
-        if (direct) tsw_product<false>(acc, a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
-        else tsw_product<true>(acc, a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs, vec, Ms, Vs);
+        tsw_wait(a, &a.ycount[v], a.spt, skip);
+        float acc[4][4] = {};
+        if constexpr (direct)
+            tsw_product<false>(acc, a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs,
+                               a.vec != 0, Ms, Vs);
+        else
+            tsw_product<true>(acc, a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs,
+                              a.vec != 0, Ms, Vs);
+        tsw_reduce(acc, Ms, zs);
+        float *P = a.Zp + ((long)u * (u - 1) / 2 + v) * (long)a.nb * 16 + (long)s * TSW_SLAB * 16;
+        for (int e = threadIdx.x; e < TSW_SLAB * 16; e += TSW_T) P[e] = zs[e];
+        __threadfence();
     }
-    tsw_reduce(acc, red, zs);
-    // z = b_slab - sum: publish
-    for (int e = tid; e < TSW_SLAB * 16; e += TSW_T) {
-        const int r = e >> 4, c = e & 15;
-        if (r < rows && c < a.nrhs) a.Z[(long)(r0 + r) + (long)c * a.n] = __ldcg(&a.B[(long)(r0 + r) + (long)c * a.ldb]) - zs[e];
-    }
-    __threadfence();
     __syncthreads();
-    if (tid == 0) atomicAdd(&a.zcount[T], 1);
-    tsw_wait(a, &a.zcount[T], nsT, &s_skip);
+    if (threadIdx.x == 0) atomicAdd(&a.pcount[u], 1);
+}
+
+// The diagonal task of slab s of tile row u: z = b - sum of the partials,
+// published; then y = (slab rows of the inverse) z_T once z_T is complete.
+template <bool TRANS>
+__device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int s, float *Ms, float *Vs, float *zs,
+                                              int *skip)
+{
+    const int T = TRANS ? a.ntiles - 1 - u : u;
+    const int t0 = T * a.nb, kbT = min(a.nb, a.n - t0);
+    const int r0 = t0 + s * TSW_SLAB, rows = min(TSW_SLAB, kbT - s * TSW_SLAB);
+    const float *D = a.Dinv + (long)T * a.dstride;
+    if (rows > 0) {
+        // the slab's rows (forward) or columns (backward) of the diagonal tile's inverse, needed last
+        if (!TRANS) tsw_prefetch_l2<false>(D + s * TSW_SLAB, a.ldd, rows, s * TSW_SLAB + rows);
+        else tsw_prefetch_l2<true>(D + s * TSW_SLAB + (long)(s * TSW_SLAB) * a.ldd, a.ldd, rows, kbT - s * TSW_SLAB);
+        tsw_wait(a, &a.pcount[u], u * a.spt, skip);
+        const float *P = a.Zp + (long)u * (u - 1) / 2 * (long)a.nb * 16 + (long)s * TSW_SLAB * 16;
+        for (int e = threadIdx.x; e < TSW_SLAB * 16; e += TSW_T) {
+            const int r = e >> 4, c = e & 15;
+            if (r < rows && c < a.nrhs) {
+                float sum = 0.0f;
+                for (int v = 0; v < u; ++v) sum += __ldcg(P + (long)v * a.nb * 16 + e);
+                a.Z[(long)(r0 + r) + (long)c * a.n] = __ldcg(&a.B[(long)(r0 + r) + (long)c * a.ldb]) - sum;
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(&a.zcount[u], 1);
+    if (rows <= 0) {
+        if (threadIdx.x == 0) atomicAdd(&a.ycount[u], 1);
+        return;
+    }
+    tsw_wait(a, &a.zcount[u], a.spt, skip);
 
     // diagonal tile: forward y_slab = Dinv(slab rows, 0 .. slab end) z_T;
     // backward x_slab = Dinv(slab start .. kbT, slab columns)^T z_T
     float acc2[4][4] = {};
     if (!TRANS) {
-        tsw_product<false>(acc2, D + s * TSW_SLAB, a.ldd, rows, a.Z + t0, a.n, s * TSW_SLAB + rows, a.nrhs, vec, Ms, Vs);
+        tsw_product<false>(acc2, D + s * TSW_SLAB, a.ldd, rows, a.Z + t0, a.n, s * TSW_SLAB + rows, a.nrhs,
+                           a.vec != 0, Ms, Vs);
     } else {
         const int k0 = s * TSW_SLAB;
-        tsw_product<true>(acc2, D + k0 + (long)k0 * a.ldd, a.ldd, rows, a.Z + t0 + k0, a.n, kbT - k0, a.nrhs, vec, Ms,
-                          Vs);
+        tsw_product<true>(acc2, D + k0 + (long)k0 * a.ldd, a.ldd, rows, a.Z + t0 + k0, a.n, kbT - k0, a.nrhs,
+                          a.vec != 0, Ms, Vs);
     }
-    tsw_reduce(acc2, red, zs);
-    for (int e = tid; e < TSW_SLAB * 16; e += TSW_T) {
+    tsw_reduce(acc2, Ms, zs);
+    for (int e = threadIdx.x; e < TSW_SLAB * 16; e += TSW_T) {
         const int r = e >> 4, c = e & 15;
         if (r < rows && c < a.nrhs) a.B[(long)(r0 + r) + (long)c * a.ldb] = zs[e];
     }
     __threadfence();
     __syncthreads();
-    if (tid == 0) atomicAdd(&a.ycount[T], 1);
+    if (threadIdx.x == 0) atomicAdd(&a.ycount[u], 1);
+}
+
+// UPPER (backward only): the strictly upper part of L's storage holds L^T
+// outside the diagonal tiles (args.upper), read like the forward operand
+template <bool TRANS, bool UPPER>
+__global__ void __launch_bounds__(TSW_T, 2) tile_sweep_kernel(TileSweepArgs a)
+{
+    __shared__ __align__(16) float Ms[TSW_KC * TSW_MP];  // also the 8 x 512 reduction buffer
+    __shared__ __align__(16) float Vs[TSW_KC * TSW_VP];
+    __shared__ float zs[TSW_SLAB * 16];
+    __shared__ unsigned s_ticket;
+    __shared__ int s_skip;
+    if (threadIdx.x == 0) s_skip = 0;
+    for (;;) {
+        __syncthreads();  // the previous task is done with s_ticket and the buffers
+        if (threadIdx.x == 0) s_ticket = atomicAdd(a.ticket, 1u);
+        __syncthreads();
+        const unsigned t = s_ticket;
+        if (t >= a.total) return;
+        // tile row u of the solve order: its tickets start at spt * u (u + 1) / 2
+        const unsigned q = t / (unsigned)a.spt;
+        int u = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+        while (u > 0 && (unsigned)u * (u + 1) / 2 > q) --u;
+        while ((unsigned)(u + 1) * (u + 2) / 2 <= q) ++u;
+        const unsigned r = t - (unsigned)a.spt * ((unsigned)u * (u + 1) / 2);
+        if (r < (unsigned)(u * a.spt))
+            tsw_product_task<TRANS, UPPER>(a, u, (int)(r / a.spt), (int)(r % a.spt), Ms, Vs, zs, &s_skip);
+        else
+            tsw_diag_task<TRANS>(a, u, (int)(r - u * a.spt), Ms, Vs, zs, &s_skip);
+    }
 }
 
 } // namespace gb300

@@ -115,7 +115,7 @@ def check(rc: int, what: str = "") -> None:
 class IrInfo(C.Structure):
     """ctypes mirror of starpu_gb300_ir_info (include/starpu_gb300_solver.h)."""
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("factor_terms", C.c_int), ("potrf_info", C.c_int),
-                ("backward_error", C.c_double), ("anorm", C.c_double)]
+                ("backward_error", C.c_double), ("anorm", C.c_double), ("method", C.c_int), ("fallback", C.c_int)]
 
 
 class Request(C.Structure):

@@ -105,15 +105,94 @@ def test_dsposv_reads_only_the_lower_triangle(gpu, oracle, n, nb):
     np.testing.assert_array_equal(X2, X)
 
 
-def test_dsposv_ill_conditioned_reports_status(gpu, oracle):
+def test_dsposv_ill_conditioned_converges(gpu, oracle):
     n, nb, nrhs = 768, 256, 2
     A = oracle.spd_gram(n, 33, oracle.alpha_for_kappa(1e6))
     B = oracle.uniform_rhs(n, nrhs, 34)
     rc, info, X = solve(gpu, A, B, nb, 3, max_iter=40)
-    assert rc in (0, GB300_ETIMEDOUT, GB300_EDOM)
-    if rc == 0:
-        be, _ = oracle.backward_error(A, X, B)
+    assert rc == 0, (rc, info.iterations, info.backward_error, info.fallback)
+    be, _ = oracle.backward_error(A, X, B)
+    assert be <= 1e-12
+
+
+@pytest.fixture
+def refinement(gpu):
+    """Sets the refinement mode for the test body and restores it."""
+    prev = gpu.starpu_gb300_dsposv_set_refinement(-1)
+    yield lambda m: gpu.starpu_gb300_dsposv_set_refinement(m)
+    gpu.starpu_gb300_dsposv_set_refinement(prev)
+
+
+def test_conjugate_gradients_rung_at_kappa_1e6(gpu, oracle, refinement):
+    """kappa = 1e6: classic refinement contracts the error by ~0.3 per
+    correction with the mixed factor; the automatic policy switches to
+    preconditioned conjugate gradients after the first slow correction and
+    needs fewer corrections, to the same backward error, and the solution
+    agrees with the FP64 oracle's within kappa * 1e-12 (forward error)."""
+    n, nb, nrhs = 4096, 1024, 4
+    A = oracle.spd_gram(n, 35, oracle.alpha_for_kappa(1e6))
+    B = oracle.uniform_rhs(n, nrhs, 36)
+    refinement(0)
+    rc0, info0, X0 = solve(gpu, A, B, nb, 3, max_iter=60)
+    refinement(2)
+    rc, info, X = solve(gpu, A, B, nb, 3, max_iter=60)
+    assert rc0 == 0 and rc == 0, (rc0, rc)
+    assert info0.method == 0 and info.method == 1 and info.fallback == 0
+    assert info.iterations < info0.iterations, (info.iterations, info0.iterations)
+    for Xk in (X0, X):
+        be, _ = oracle.backward_error(A, Xk, B)
         assert be <= 1e-12
+    Xo = oracle.cpu_solve(A, B, nb, 8)
+    fe = np.max(np.abs(X - Xo)) / np.max(np.abs(Xo))
+    assert fe <= 1e6 * 1e-12 * 10, fe
+
+
+def test_pcg_only_matches_classic_on_easy_systems(gpu, oracle, refinement):
+    """Conjugate gradients from the first correction also converge on a
+    well-conditioned system (kappa = 1e2), to the same backward error."""
+    n, nb, nrhs = 1024, 256, 3
+    A = oracle.spd_gram(n, 37, oracle.alpha_for_kappa(1e2))
+    B = oracle.uniform_rhs(n, nrhs, 38)
+    refinement(1)
+    rc, info, X = solve(gpu, A, B, nb, 3)
+    assert rc == 0 and info.method == 1
+    be, _ = oracle.backward_error(A, X, B)
+    assert be <= 1e-12
+
+
+@pytest.fixture
+def fallback(gpu):
+    prev = gpu.starpu_gb300_dsposv_set_fp64_fallback(-1)
+    yield lambda on: gpu.starpu_gb300_dsposv_set_fp64_fallback(on)
+    gpu.starpu_gb300_dsposv_set_fp64_fallback(prev)
+
+
+def _fp32_singular(n, seed):
+    """SPD in FP64 (eigenvalues 1e-9 and 1 + (n - 1)(1 - 1e-9): kappa ~ n 1e9)
+    but singular once rounded to FP32: every off-diagonal entry is 1 - 1e-9,
+    which FP32 rounds to 1."""
+    rng = np.random.default_rng(seed)
+    A = np.full((n, n), 1.0 - 1e-9)
+    np.fill_diagonal(A, 1.0)
+    return np.asfortranarray(A), np.asfortranarray(rng.uniform(-1, 1, (n, 2)))
+
+
+def test_fp64_fallback_when_the_mixed_factor_fails(gpu, oracle, fallback):
+    """LAPACK dsposv semantics: the FP32-storage factorisation breaks down
+    (or its refinement cannot converge) on a matrix that is SPD only in FP64;
+    the FP64 factorisation on the GPU then solves it to FP64 accuracy.  With
+    the fallback off the mixed outcome is returned as it is."""
+    n, nb = 512, 256
+    A, B = _fp32_singular(n, 39)
+    assert np.linalg.eigvalsh(A).min() > 0
+    fallback(1)
+    rc, info, X = solve(gpu, A, B, nb, 3)
+    assert rc == 0 and info.status == 0 and info.fallback in (1, 2), (rc, info.fallback, info.potrf_info)
+    be, _ = oracle.backward_error(A, X, B)
+    assert be <= 1e-12 and abs(be - info.backward_error) <= 1e-13 + 0.05 * be, (be, info.backward_error)
+    fallback(0)
+    rc0, info0, _ = solve(gpu, A, B, nb, 3)
+    assert rc0 in (GB300_EDOM, GB300_ETIMEDOUT) and info0.fallback == 0
 
 
 def test_dsposv_not_spd(gpu):
@@ -122,7 +201,8 @@ def test_dsposv_not_spd(gpu):
     A[100, 100] = -2.0
     B = np.ones((n, 1))
     rc, info, X = solve(gpu, A, B, 128, 3)
-    assert rc == GB300_EDOM and info.potrf_info == 101
+    # the mixed factor fails, and so does the FP64 fallback, at the same pivot
+    assert rc == GB300_EDOM and info.potrf_info == 101 and info.fallback == 1
 
 
 def test_solver_context_host_buffers_match_device_call(gpu, oracle):
