@@ -475,6 +475,7 @@ struct SolverWs {
     float *Y;              // n x nrhs FP32 right-hand side / correction
     void *sweep;           // inverted 64 x 64 diagonal blocks + flags of the 64-row POTRS sweeps
     float *band;           // inverses of the nb x nb diagonal tiles (tile T at band + T * ldk * ldk), or null
+    float *band_t;         // the same tiles transposed (the backward sweep's operand)
     void *tsw;             // scratch of the tile-row sweeps (tsw_scratch_bytes)
     double *partials;      // K-split partials of the residual
     float2 *xs;            // double-float split of X (n x 16 per group of 16 columns)
@@ -501,10 +502,11 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 static bool tile_sweep_ok(int nb) { return nb > 0 && nb % TSW_SLAB == 0 && nb <= GB300_DIAG_TILE_MAX; }
 
 // L y = b then L^T x = y with the inverted nb x nb diagonal tiles in `band`
-// (ld ldk, tile T at band + T * ldk * ldk): one persistent launch per sweep
-// and group of 16 right-hand sides.  scratch: tsw_scratch_bytes(n, nb).
+// (ld ldk, tile T at band + T * ldk * ldk; band_t, optional: the same tiles
+// transposed): one persistent launch per sweep and group of 16 right-hand
+// sides.  scratch: tsw_scratch_bytes(n, nb).
 static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L, long ldl, const float *band, long ldk,
-                        float *Y, long ldy, void *scratch, int *err, int upper = 0)
+                        float *Y, long ldy, void *scratch, int *err, int upper = 0, const float *band_t = nullptr)
 {
     if (n <= 0 || nrhs <= 0) return;
     TileSweepArgs a;
@@ -513,15 +515,17 @@ static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L,
     a.ntiles = (n + nb - 1) / nb;
     a.spt = nb / TSW_SLAB;
     a.total = (unsigned)((size_t)a.spt * a.ntiles * (a.ntiles + 1) / 2);
-    size_t zp_off = 0, cnt_off = 0;
-    tsw_scratch_bytes(n, nb, &zp_off, &cnt_off);
+    size_t yt_off = 0, zp_off = 0, cnt_off = 0;
+    tsw_scratch_bytes(n, nb, &yt_off, &zp_off, &cnt_off);
     a.L = L;
     a.ldl = ldl;
     a.Dinv = band;
+    a.DinvT = band_t;
     a.ldd = ldk;
     a.dstride = ldk * ldk;
     a.ldb = ldy;
-    a.Z = (float *)scratch;
+    a.Zt = (float *)scratch;
+    a.Yt = (float *)((char *)scratch + yt_off);
     a.Zp = (float *)((char *)scratch + zp_off);
     int *cnt = (int *)((char *)scratch + cnt_off);
     a.zcount = cnt;
@@ -533,31 +537,50 @@ static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L,
     a.budget_ns = gb300_wait_budget_ns();
     // persistent CTAs: as many as fit on the device, and at least one per slab
     // of a tile row (the diagonal tasks of a tile row wait for one another)
-    static thread_local int per_sm[3] = {0, 0, 0};
-    if (!per_sm[0]) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], tile_sweep_kernel<false, false>, TSW_T, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], tile_sweep_kernel<true, false>, TSW_T, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[2], tile_sweep_kernel<true, true>, TSW_T, 0);
-        for (int &x : per_sm) x = std::max(x, 1);
+    const void *fns[3] = {(const void *)tile_sweep_kernel<false, false>, (const void *)tile_sweep_kernel<true, false>,
+                          (const void *)tile_sweep_kernel<true, true>};
+    static thread_local int per_sm[16][3];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int *per = per_sm[dev & 15];
+    if (!per[0]) {
+        for (int i = 0; i < 3; ++i) {
+            if (gb300_func_dyn_smem(fns[i], TSW_DSMEM)) return;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[i], fns[i], TSW_T, TSW_DSMEM);
+            per[i] = std::max(per[i], 1);
+        }
     }
     const int sms = gb300_device_sms();
     auto grid = [&](int which) {
-        const long g = std::min<long>((long)a.total, (long)per_sm[which] * sms);
+        const long g = std::min<long>((long)a.total, (long)per[which] * sms);
         return (unsigned)std::max<long>(g, a.spt);
     };
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
-    a.vec = al(L) && al(band) && al(Y) && al(a.Z) && ldl % 4 == 0 && ldk % 4 == 0 && ldy % 4 == 0 && n % 4 == 0;
+    const bool vec = al(L) && al(band) && (!band_t || al(band_t)) && ldl % 4 == 0 && ldk % 4 == 0;
     const size_t cbytes = (3 * (size_t)a.ntiles + 1) * sizeof(int);
     for (int c0 = 0; c0 < nrhs; c0 += 16) {
         a.nrhs = std::min(16, nrhs - c0);
         a.B = Y + (long)c0 * ldy;
-        a.vec = a.vec && al(a.B);
+        a.vec = vec;
         cudaMemsetAsync(cnt, 0, cbytes, s);
-        gb300_count_launch(), tile_sweep_kernel<false, false><<<grid(0), TSW_T, 0, s>>>(a);
+        gb300_count_launch(), tile_sweep_kernel<false, false><<<grid(0), TSW_T, TSW_DSMEM, s>>>(a);
         cudaMemsetAsync(cnt, 0, cbytes, s);
-        if (upper) gb300_count_launch(), tile_sweep_kernel<true, true><<<grid(2), TSW_T, 0, s>>>(a);
-        else gb300_count_launch(), tile_sweep_kernel<true, false><<<grid(1), TSW_T, 0, s>>>(a);
+        if (upper) gb300_count_launch(), tile_sweep_kernel<true, true><<<grid(2), TSW_T, TSW_DSMEM, s>>>(a);
+        else gb300_count_launch(), tile_sweep_kernel<true, false><<<grid(1), TSW_T, TSW_DSMEM, s>>>(a);
     }
+}
+
+// band_t = the nb x nb tiles of band transposed (ld ldk each, ntiles tiles),
+// for the backward sweep's direct reads; 32 x 32 blocks through shared memory
+__global__ void transpose_tiles_kernel(int ldk, const float *__restrict__ band, float *__restrict__ band_t)
+{
+    __shared__ float t[32][33];
+    const long base = (long)blockIdx.z * ldk * ldk;
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) t[y][threadIdx.x] = band[base + r0 + threadIdx.x + (long)(c0 + y) * ldk];
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y)
+        band_t[base + c0 + threadIdx.x + (long)(r0 + y) * ldk] = t[threadIdx.x][y];
 }
 
 static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
@@ -577,7 +600,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
     const size_t oT = take(potrs_sweep_workspace<float>(n));
     const bool tiles = tile_sweep_ok(nb);
     const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64, ntiles = nb > 0 ? ((size_t)n + nb - 1) / nb : 0;
-    const size_t oB = tiles ? take(ntiles * ldk * ldk * sizeof(float)) : 0;
+    const size_t oB = tiles ? take(2 * ntiles * ldk * ldk * sizeof(float)) : 0;
     const size_t oZ = tiles ? take(tsw_scratch_bytes(n, nb)) : 0;
     const size_t oA = take(residual_tc_a_bytes(n));
     const size_t oN = take((size_t)((n + 63) / 64) * n * sizeof(float));
@@ -602,6 +625,7 @@ static size_t layout(int n, int nrhs, int nb, void *base, SolverWs *ws)
         ws->Y = (float *)(b + oY);
         ws->sweep = b + oT;
         ws->band = tiles ? (float *)(b + oB) : nullptr;
+        ws->band_t = tiles ? ws->band + ntiles * ldk * ldk : nullptr;
         ws->tsw = tiles ? (void *)(b + oZ) : nullptr;
         ws->rtc_a = b + oA;
         ws->rowsum = (float *)(b + oN);
@@ -631,7 +655,7 @@ static void correction_solve(cudaStream_t s, int n, int nrhs, int nb, const Solv
 {
     const long ldk = ((long)nb + 63) / 64 * 64;
     // the factor phase mirrors L^T into W's strictly upper part (outside the diagonal tiles)
-    if (ws.band) tile_sweeps(s, n, nrhs, nb, ws.W, n, ws.band, ldk, ws.Y, n, ws.tsw, ws.err, 1);
+    if (ws.band) tile_sweeps(s, n, nrhs, nb, ws.W, n, ws.band, ldk, ws.Y, n, ws.tsw, ws.err, 1, ws.band_t);
     else potrs_sweep<float>(s, n, nrhs, ws.W, n, ws.sweep, ws.Y, n, ws.err);
 }
 
@@ -754,6 +778,12 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
     cudaStreamWaitEvent(s, ss->join, 0);  // joined before anything reads the factor, the slices or the norm
     if (rc) return rc;
     if (!ws.band) potrs_sweep_prepare<float>(s, n, ws.W, n, ws.sweep);
+    else {
+        const long ldk = ((long)nb + 63) / 64 * 64;
+        const unsigned nt = (unsigned)((n + nb - 1) / nb), bt = (unsigned)(ldk / 32);
+        gb300_count_launch(), transpose_tiles_kernel<<<dim3(bt, bt, nt), dim3(32, 8), 0, s>>>((int)ldk, ws.band,
+                                                                                            ws.band_t);
+    }
     return gb300_last_launch_status();
 }
 

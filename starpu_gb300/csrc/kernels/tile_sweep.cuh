@@ -25,10 +25,15 @@
 // CTAs are scheduled.  Every wait is bounded by a %globaltimer budget; on
 // timeout the CTA records an error and stops waiting, so the launch ends.
 //
-// The products are register-blocked: the K range of every chunk (128 columns)
-// is split over the 8 warps, each lane keeps 4 rows x 4 right-hand sides, and
-// the next two chunks are fetched into registers while the current one is
-// used; a task's operand is prefetched into L2 before it waits.
+// The products M (32 x K) V (K x 16) read their operand M as 32-row columns
+// (L, the mirrored L^T in the upper part, the diagonal-tile inverses and their
+// transposes) and V from row-major copies of y / z (16 floats per row) that
+// the diagonal tasks keep beside the column-major result.  Both are staged by
+// cp.async in a 6-deep ring of 64-column stages (~70 KB in flight per CTA),
+// and each lane keeps 4 rows x 16 right-hand sides (one 16-byte operand load
+// and four broadcast loads of V per 64 FMAs; the 8 warps split the K range).
+// Operands that are only available transposed (the public entry point's L^T
+// and inverses) take a register-staged path with the same partial layout.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -40,6 +45,14 @@ constexpr int TSW_KC = 128;    // K chunk
 constexpr int TSW_MP = 36;     // pitch of one K index of the operand chunk (32 rows + 4)
 constexpr int TSW_VP = 20;     // pitch of one K index of the right-hand-side chunk (16 + 4)
 constexpr int TSW_T = 256;
+constexpr int TSW_KS = 64;   // K per cp.async stage
+constexpr int TSW_NS = 6;    // stages in the ring
+constexpr int TSW_STAGE = TSW_KS * (TSW_MP + TSW_VP);  // floats per stage
+// dynamic shared memory of the kernel: the ring (the register-staged path and
+// the reductions reuse it)
+constexpr int TSW_DSMEM = TSW_NS * TSW_STAGE * 4;
+static_assert(TSW_NS * TSW_STAGE >= TSW_KC * (TSW_MP + TSW_VP), "register-staged buffers fit the ring");
+static_assert(TSW_NS * TSW_STAGE >= 8 * 512, "reduction buffer fits the ring");
 
 struct TileSweepArgs {
     int n, nrhs, nb;
@@ -51,8 +64,10 @@ struct TileSweepArgs {
     long ldd, dstride;
     float *B;  // right-hand sides in, solution out (n x nrhs, ld ldb)
     long ldb;
-    float *Z;   // n x 16 scratch, ld n
+    float *Zt;  // z of the tile rows, row-major n x 16
+    float *Yt;  // solved rows (y forward, x backward), row-major n x 16: the products' right-hand operand
     float *Zp;  // partial products: pair (u, v < u) at Zp + (u (u - 1) / 2 + v) * nb * 16, slab-major 32 x 16
+    const float *DinvT;  // optional: tile T's inverse transposed at DinvT + T * dstride (ld ldd)
     unsigned *ticket;
     int *zcount, *ycount, *pcount;  // per tile row of the solve order, zero at launch
     int *err;
@@ -64,17 +79,30 @@ struct TileSweepArgs {
     int upper;
 };
 
-// Bytes of scratch a sweep pair needs: Z (n x 16), the partial products of
-// every pair of tile rows, and the 3 ntiles + 1 counters.
-inline size_t tsw_scratch_bytes(int n, int nb, size_t *zp_off = nullptr, size_t *cnt_off = nullptr)
+// Bytes of scratch a sweep pair needs: Zt and Yt (n x 16 each), the partial
+// products of every pair of tile rows, and the 3 ntiles + 1 counters.
+inline size_t tsw_scratch_bytes(int n, int nb, size_t *yt_off = nullptr, size_t *zp_off = nullptr,
+                                size_t *cnt_off = nullptr)
 {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t nt = ((size_t)n + nb - 1) / nb;
     const size_t z = al((size_t)n * 16 * sizeof(float));
     const size_t zp = al(nt * (nt > 0 ? nt - 1 : 0) / 2 * (size_t)nb * 16 * sizeof(float));
-    if (zp_off) *zp_off = z;
-    if (cnt_off) *cnt_off = z + zp;
-    return z + zp + al((3 * nt + 1) * sizeof(int));
+    if (yt_off) *yt_off = z;
+    if (zp_off) *zp_off = 2 * z;
+    if (cnt_off) *cnt_off = 2 * z + zp;
+    return 2 * z + zp + al((3 * nt + 1) * sizeof(int));
+}
+
+__device__ __forceinline__ void tsw_cp16(float *smem, const float *gmem, int src_bytes)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void tsw_cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void tsw_cp_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 __device__ __forceinline__ int tsw_ld_acquire(const int *p)
@@ -132,7 +160,7 @@ __device__ __forceinline__ void tsw_prefetch_l2(const float *M, long ldm, int ro
 // right-hand sides V (kc x 16, element (p, c)).
 //   TR = false: M(r, p) = M[r + p * ldm]  (rows of L or of the inverse)
 //   TR = true : M(r, p) = M[p + r * ldm]  (columns: the transposed operand)
-//   V(p, c) = V[p + c * ldv]
+//   V(p, c) = V[16 p + c]                 (row-major, 16-byte aligned rows)
 struct TswStage {
     float4 m[4];
     float4 v[2];
@@ -143,8 +171,8 @@ struct TswStage {
 //   M, TR = false: float4 = 4 consecutive rows r of column p (coalesced rows);
 //   M, TR = true : lane = row r, a thread's 4 float4 = 16 consecutive p (two
 //                  whole 32-byte sectors of column r);
-//   V: lane = (c = lane % 16, half-warp h), float4 f = 16 u + 2 w + h of
-//      column c (V is small and stays in L2).
+//   V: float4 = right-hand sides 4 q .. 4 q + 3 of row p (V is small and
+//      stays in L2).
 template <bool TR>
 __device__ __forceinline__ void tsw_map_m(int u, int &r, int &p)
 {
@@ -158,16 +186,16 @@ __device__ __forceinline__ void tsw_map_m(int u, int &r, int &p)
         p = ((tid >> 5) * 4 + u) * 4;
     }
 }
-__device__ __forceinline__ void tsw_map_v(int u, int &p, int &c)
+__device__ __forceinline__ void tsw_map_v(int u, int &p, int &q)
 {
-    const int tid = threadIdx.x;
-    c = tid & 15;
-    p = (16 * u + (tid >> 4)) * 4;
+    const int e = threadIdx.x + TSW_T * u;
+    p = e >> 2;
+    q = e & 3;
 }
 
 template <bool TR>
-__device__ __forceinline__ void tsw_fetch(TswStage &st, const float *M, long ldm, int rows, const float *V, long ldv,
-                                          int kc, int nrhs, bool vec)
+__device__ __forceinline__ void tsw_fetch(TswStage &st, const float *M, long ldm, int rows, const float *V, int kc,
+                                          bool vec)
 {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -201,20 +229,10 @@ __device__ __forceinline__ void tsw_fetch(TswStage &st, const float *M, long ldm
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-        int p, c;
-        tsw_map_v(u, p, c);
-        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (c < nrhs) {
-            const float *src = V + p + (long)c * ldv;
-            if (vec && p + 3 < kc) x = __ldcg(reinterpret_cast<const float4 *>(src));
-            else {
-                if (p < kc) x.x = __ldcg(src);
-                if (p + 1 < kc) x.y = __ldcg(src + 1);
-                if (p + 2 < kc) x.z = __ldcg(src + 2);
-                if (p + 3 < kc) x.w = __ldcg(src + 3);
-            }
-        }
-        st.v[u] = x;
+        int p, q;
+        tsw_map_v(u, p, q);
+        st.v[u] = p < kc ? __ldcg(reinterpret_cast<const float4 *>(V + (long)p * 16 + 4 * q))
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
@@ -236,12 +254,9 @@ __device__ __forceinline__ void tsw_put(const TswStage &st, float *Ms, float *Vs
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-        int p, c;
-        tsw_map_v(u, p, c);
-        Vs[p * TSW_VP + c] = st.v[u].x;
-        Vs[(p + 1) * TSW_VP + c] = st.v[u].y;
-        Vs[(p + 2) * TSW_VP + c] = st.v[u].z;
-        Vs[(p + 3) * TSW_VP + c] = st.v[u].w;
+        int p, q;
+        tsw_map_v(u, p, q);
+        *reinterpret_cast<float4 *>(Vs + p * TSW_VP + 4 * q) = st.v[u];
     }
 }
 
@@ -271,14 +286,14 @@ __device__ __forceinline__ void tsw_chunk_mma(float acc[4][4], const float *Ms, 
 // multiplied from shared memory (the loop is unrolled by two so that both
 // register sets stay statically indexed).
 template <bool TR>
-__device__ __forceinline__ void tsw_product(float acc[4][4], const float *M, long ldm, int rows, const float *V,
-                                            long ldv, int K, int nrhs, bool vec, float *Ms, float *Vs)
+__device__ __forceinline__ void tsw_product(float acc[4][4], const float *M, long ldm, int rows, const float *V, int K,
+                                            bool vec, float *Ms, float *Vs)
 {
     if (K <= 0) return;
     auto fetch = [&](TswStage &st, int c) {
         const int p0 = c * TSW_KC;
         const float *Mc = TR ? M + p0 : M + (long)p0 * ldm;
-        tsw_fetch<TR>(st, Mc, ldm, rows, V + p0, ldv, min(TSW_KC, K - p0), nrhs, vec);
+        tsw_fetch<TR>(st, Mc, ldm, rows, V + (long)p0 * 16, min(TSW_KC, K - p0), vec);
     };
     const int nch = (K + TSW_KC - 1) / TSW_KC;
     TswStage s0, s1;
@@ -319,10 +334,126 @@ __device__ __forceinline__ void tsw_reduce(const float acc[4][4], float *red, fl
     __syncthreads();
 }
 
+// acc += M(32 x K) V(K x 16) for an operand read as 32-row columns
+// (M(r, p) = M[r + p * ldm], 16-byte aligned columns) and a row-major V, in a
+// TSW_NS-deep cp.async ring of TSW_KS-column stages; elements past `rows` and
+// K are zero-filled.  Warp w takes columns 8 w .. 8 w + 7 of every stage;
+// lane (rr = lane % 8, kk = lane / 8) keeps rows 4 rr .. 4 rr + 3 of all 16
+// right-hand sides for the columns congruent to kk mod 4.
+__device__ __forceinline__ void tsw_product_direct(float acc[4][16], const float *M, long ldm, int rows,
+                                                   const float *V, int K, float *ring)
+{
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, rr = lane & 7, kk = lane >> 3;
+    const int nst = (K + TSW_KS - 1) / TSW_KS;
+    auto issue = [&](int st) {
+        float *Ms = ring + (st % TSW_NS) * TSW_STAGE, *Vs = Ms + TSW_KS * TSW_MP;
+        const int p0 = st * TSW_KS, kc = min(TSW_KS, K - p0);
+#pragma unroll
+        for (int u = 0; u < TSW_KS * 8 / TSW_T; ++u) {
+            const int e = tid + TSW_T * u, p = e >> 3, q = e & 7;
+            const int valid = p < kc ? max(0, min(4, rows - 4 * q)) : 0;
+            tsw_cp16(Ms + p * TSW_MP + 4 * q, valid ? M + 4 * q + (long)(p0 + p) * ldm : M, 4 * valid);
+        }
+        if (tid < TSW_KS * 4) {
+            const int p = tid >> 2, q = tid & 3;
+            tsw_cp16(Vs + p * TSW_VP + 4 * q, p < kc ? V + (long)(p0 + p) * 16 + 4 * q : V, p < kc ? 16 : 0);
+        }
+    };
+#pragma unroll 1
+    for (int st = 0; st < TSW_NS - 1; ++st) {
+        if (st < nst) issue(st);
+        tsw_cp_commit();
+    }
+#pragma unroll 1
+    for (int st = 0; st < nst; ++st) {
+        tsw_cp_wait<TSW_NS - 2>();
+        __syncthreads();  // stage st is in; every warp is done with the buffer reloaded next
+        if (st + TSW_NS - 1 < nst) issue(st + TSW_NS - 1);
+        tsw_cp_commit();
+        const float *Ms = ring + (st % TSW_NS) * TSW_STAGE, *Vs = Ms + TSW_KS * TSW_MP;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int p = 8 * warp + 4 * h + kk;
+            const float4 m = *reinterpret_cast<const float4 *>(Ms + p * TSW_MP + 4 * rr);
+            const float mv[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 x = *reinterpret_cast<const float4 *>(Vs + p * TSW_VP + 4 * q);
+                const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[i][4 * q + c] = fmaf(mv[i], xv[c], acc[i][4 * q + c]);
+            }
+        }
+    }
+    tsw_cp_wait<0>();
+    __syncthreads();  // the ring is free for the reduction
+}
+
+// Sum tsw_product_direct's partials (the four column classes of a warp by
+// shuffles, then the 8 warps in order) into out (32 x 16, row-major).
+__device__ __forceinline__ void tsw_reduce16(float acc[4][16], float *red, float *out)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane & 7, kk = lane >> 3;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            acc[i][c] += __shfl_xor_sync(0xffffffffu, acc[i][c], 8);
+            acc[i][c] += __shfl_xor_sync(0xffffffffu, acc[i][c], 16);
+        }
+    if (kk == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                *reinterpret_cast<float4 *>(red + warp * 512 + (4 * rr + i) * 16 + 4 * q) =
+                    make_float4(acc[i][4 * q], acc[i][4 * q + 1], acc[i][4 * q + 2], acc[i][4 * q + 3]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 512; e += TSW_T) {
+        float s = 0.0f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += red[w * 512 + e];
+        out[e] = s;
+    }
+    __syncthreads();
+}
+
+// out (32 x 16) = M(32 x K) V(K x 16).  Each form is its own function so that
+// its registers are allocated alone (the cp.async path holds 64 accumulators).
+__device__ __noinline__ void tsw_gemv_direct(const float *M, long ldm, int rows, const float *V, int K, float *ring,
+                                             float *out)
+{
+    float acc[4][16] = {};
+    if (K > 0) tsw_product_direct(acc, M, ldm, rows, V, K, ring);
+    tsw_reduce16(acc, ring, out);
+}
+
+template <bool TR>
+__device__ __noinline__ void tsw_gemv_staged(const float *M, long ldm, int rows, const float *V, int K, bool vec,
+                                             float *ring, float *out)
+{
+    float acc[4][4] = {};
+    tsw_product<TR>(acc, M, ldm, rows, V, K, vec, ring, ring + TSW_KC * TSW_MP);
+    tsw_reduce(acc, ring, out);
+}
+
+// the cp.async path for a direct operand with aligned columns, else the
+// register-staged one (TR: M transposed)
+template <bool TR>
+__device__ __forceinline__ void tsw_gemv(const float *M, long ldm, int rows, const float *V, int K, bool vec,
+                                         float *ring, float *out)
+{
+    if (!TR && vec) tsw_gemv_direct(M, ldm, rows, V, K, ring, out);
+    else tsw_gemv_staged<TR>(M, ldm, rows, V, K, vec, ring, out);
+}
+
 // One product task: P_{u,v,s} = L_{slab, tile v} y_v (backward the transposed
 // block), written to its partial block and counted in pcount[u].
 template <bool TRANS, bool UPPER>
-__device__ __forceinline__ void tsw_product_task(const TileSweepArgs &a, int u, int v, int s, float *Ms, float *Vs,
+__device__ __forceinline__ void tsw_product_task(const TileSweepArgs &a, int u, int v, int s, float *ring,
                                                  float *zs, int *skip)
 {
     const int T = TRANS ? a.ntiles - 1 - u : u, j = TRANS ? a.ntiles - 1 - v : v;
@@ -334,14 +465,12 @@ __device__ __forceinline__ void tsw_product_task(const TileSweepArgs &a, int u, 
         if constexpr (direct) tsw_prefetch_l2<false>(a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, kbj);
         else tsw_prefetch_l2<true>(a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, kbj);
         tsw_wait(a, &a.ycount[v], a.spt, skip);
-        float acc[4][4] = {};
         if constexpr (direct)
-            tsw_product<false>(acc, a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs,
-                               a.vec != 0, Ms, Vs);
+            tsw_gemv<false>(a.L + r0 + (long)j0 * a.ldl, a.ldl, rows, a.Yt + (long)j0 * 16, kbj, a.vec != 0, ring,
+                            zs);
         else
-            tsw_product<true>(acc, a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, a.B + j0, a.ldb, kbj, a.nrhs,
-                              a.vec != 0, Ms, Vs);
-        tsw_reduce(acc, Ms, zs);
+            tsw_gemv<true>(a.L + j0 + (long)r0 * a.ldl, a.ldl, rows, a.Yt + (long)j0 * 16, kbj, a.vec != 0, ring,
+                           zs);
         float *P = a.Zp + ((long)u * (u - 1) / 2 + v) * (long)a.nb * 16 + (long)s * TSW_SLAB * 16;
         for (int e = threadIdx.x; e < TSW_SLAB * 16; e += TSW_T) P[e] = zs[e];
         __threadfence();
@@ -353,7 +482,7 @@ __device__ __forceinline__ void tsw_product_task(const TileSweepArgs &a, int u, 
 // The diagonal task of slab s of tile row u: z = b - sum of the partials,
 // published; then y = (slab rows of the inverse) z_T once z_T is complete.
 template <bool TRANS>
-__device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int s, float *Ms, float *Vs, float *zs,
+__device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int s, float *ring, float *zs,
                                               int *skip)
 {
     const int T = TRANS ? a.ntiles - 1 - u : u;
@@ -362,8 +491,10 @@ __device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int
     const float *D = a.Dinv + (long)T * a.dstride;
     if (rows > 0) {
         // the slab's rows (forward) or columns (backward) of the diagonal tile's inverse, needed last
-        if (!TRANS) tsw_prefetch_l2<false>(D + s * TSW_SLAB, a.ldd, rows, s * TSW_SLAB + rows);
-        else tsw_prefetch_l2<true>(D + s * TSW_SLAB + (long)(s * TSW_SLAB) * a.ldd, a.ldd, rows, kbT - s * TSW_SLAB);
+        const int k0 = s * TSW_SLAB;
+        if (!TRANS) tsw_prefetch_l2<false>(D + k0, a.ldd, rows, k0 + rows);
+        else if (a.DinvT) tsw_prefetch_l2<false>(a.DinvT + (long)T * a.dstride + k0 + (long)k0 * a.ldd, a.ldd, rows, kbT - k0);
+        else tsw_prefetch_l2<true>(D + k0 + (long)k0 * a.ldd, a.ldd, rows, kbT - k0);
         tsw_wait(a, &a.pcount[u], u * a.spt, skip);
         const float *P = a.Zp + (long)u * (u - 1) / 2 * (long)a.nb * 16 + (long)s * TSW_SLAB * 16;
         for (int e = threadIdx.x; e < TSW_SLAB * 16; e += TSW_T) {
@@ -371,7 +502,7 @@ __device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int
             if (r < rows && c < a.nrhs) {
                 float sum = 0.0f;
                 for (int v = 0; v < u; ++v) sum += __ldcg(P + (long)v * a.nb * 16 + e);
-                a.Z[(long)(r0 + r) + (long)c * a.n] = __ldcg(&a.B[(long)(r0 + r) + (long)c * a.ldb]) - sum;
+                a.Zt[(long)(r0 + r) * 16 + c] = __ldcg(&a.B[(long)(r0 + r) + (long)c * a.ldb]) - sum;
             }
         }
         __threadfence();
@@ -385,20 +516,23 @@ __device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int
     tsw_wait(a, &a.zcount[u], a.spt, skip);
 
     // diagonal tile: forward y_slab = Dinv(slab rows, 0 .. slab end) z_T;
-    // backward x_slab = Dinv(slab start .. kbT, slab columns)^T z_T
-    float acc2[4][4] = {};
-    if (!TRANS) {
-        tsw_product<false>(acc2, D + s * TSW_SLAB, a.ldd, rows, a.Z + t0, a.n, s * TSW_SLAB + rows, a.nrhs,
-                           a.vec != 0, Ms, Vs);
-    } else {
-        const int k0 = s * TSW_SLAB;
-        tsw_product<true>(acc2, D + k0 + (long)k0 * a.ldd, a.ldd, rows, a.Z + t0 + k0, a.n, kbT - k0, a.nrhs,
-                          a.vec != 0, Ms, Vs);
-    }
-    tsw_reduce(acc2, Ms, zs);
+    // backward x_slab = Dinv(slab start .. kbT, slab columns)^T z_T (read
+    // from the transposed tiles when they are kept)
+    const int k0 = s * TSW_SLAB;
+    if (!TRANS)
+        tsw_gemv<false>(D + k0, a.ldd, rows, a.Zt + (long)t0 * 16, k0 + rows, a.vec != 0, ring, zs);
+    else if (a.DinvT)
+        tsw_gemv<false>(a.DinvT + (long)T * a.dstride + k0 + (long)k0 * a.ldd, a.ldd, rows,
+                        a.Zt + (long)(t0 + k0) * 16, kbT - k0, a.vec != 0, ring, zs);
+    else
+        tsw_gemv<true>(D + k0 + (long)k0 * a.ldd, a.ldd, rows, a.Zt + (long)(t0 + k0) * 16, kbT - k0, a.vec != 0,
+                       ring, zs);
     for (int e = threadIdx.x; e < TSW_SLAB * 16; e += TSW_T) {
         const int r = e >> 4, c = e & 15;
-        if (r < rows && c < a.nrhs) a.B[(long)(r0 + r) + (long)c * a.ldb] = zs[e];
+        if (r < rows && c < a.nrhs) {
+            a.B[(long)(r0 + r) + (long)c * a.ldb] = zs[e];
+            a.Yt[(long)(r0 + r) * 16 + c] = zs[e];
+        }
     }
     __threadfence();
     __syncthreads();
@@ -410,9 +544,9 @@ __device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int
 template <bool TRANS, bool UPPER>
 __global__ void __launch_bounds__(TSW_T, 2) tile_sweep_kernel(TileSweepArgs a)
 {
-    __shared__ __align__(16) float Ms[TSW_KC * TSW_MP];  // also the 8 x 512 reduction buffer
-    __shared__ __align__(16) float Vs[TSW_KC * TSW_VP];
-    __shared__ float zs[TSW_SLAB * 16];
+    extern __shared__ float4 tsw_dsmem[];
+    float *ring = reinterpret_cast<float *>(tsw_dsmem);  // TSW_DSMEM bytes
+    __shared__ __align__(16) float zs[TSW_SLAB * 16];
     __shared__ unsigned s_ticket;
     __shared__ int s_skip;
     if (threadIdx.x == 0) s_skip = 0;
@@ -429,9 +563,9 @@ __global__ void __launch_bounds__(TSW_T, 2) tile_sweep_kernel(TileSweepArgs a)
         while ((unsigned)(u + 1) * (u + 2) / 2 <= q) ++u;
         const unsigned r = t - (unsigned)a.spt * ((unsigned)u * (u + 1) / 2);
         if (r < (unsigned)(u * a.spt))
-            tsw_product_task<TRANS, UPPER>(a, u, (int)(r / a.spt), (int)(r % a.spt), Ms, Vs, zs, &s_skip);
+            tsw_product_task<TRANS, UPPER>(a, u, (int)(r / a.spt), (int)(r % a.spt), ring, zs, &s_skip);
         else
-            tsw_diag_task<TRANS>(a, u, (int)(r - u * a.spt), Ms, Vs, zs, &s_skip);
+            tsw_diag_task<TRANS>(a, u, (int)(r - u * a.spt), ring, zs, &s_skip);
     }
 }
 
