@@ -460,6 +460,36 @@ __global__ void __launch_bounds__(512) pcg_step_kernel(int n, const double *__re
     }
 }
 
+// max_i L_ii^2 / min_i L_ii^2 of the FP32 factor (one CTA): the ratio of the
+// largest to the smallest Cholesky pivot, a lower bound of kappa_2(A) (every
+// pivot lies between the extreme eigenvalues).
+__global__ void pivot_ratio_kernel(int n, const float *__restrict__ W, long ldw, double *ratio)
+{
+    __shared__ double rmx[32], rmn[32];
+    double mx = 0.0, mn = INFINITY;
+    for (long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double d = (double)W[i + i * ldw];
+        mx = fmax(mx, d * d);
+        mn = fmin(mn, d * d);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        rmx[threadIdx.x >> 5] = mx;
+        rmn[threadIdx.x >> 5] = mn;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            mx = fmax(mx, rmx[w]);
+            mn = fmin(mn, rmn[w]);
+        }
+        *ratio = mn > 0.0 ? mx / mn : INFINITY;
+    }
+}
+
 // F (n x n, ld n) = the lower triangle of A, zeros above: the FP64 copy the
 // fallback factorisation works on (the strict upper part of A is never read)
 __global__ void copy_lower_f64_kernel(int n, const double *__restrict__ A, long lda, double *__restrict__ F)
@@ -846,6 +876,10 @@ static int refine_mode()
 // 1e-1): from there conjugate gradients with the same factor as
 // preconditioner contract the error faster per correction.
 static constexpr double PCG_SWITCH = 0.05;
+// A pivot ratio above this (kappa at least that large; on the Gram test
+// matrices the ratio is ~0.6 sqrt(kappa)) starts with conjugate gradients:
+// the classic correction it would replace is known to contract slowly.
+static constexpr double PCG_PIVOT_RATIO = 300.0;
 // corrections without halving the best backward error seen: stalled
 static constexpr int STALL_STEPS = 6;
 
@@ -879,6 +913,11 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
     int it = 0, rc = 0;
     const int mode = refine_mode();
     bool pcg = false, restart = true, true_residual = true;
+    double hratio = 0.0;
+    if (mode == 2) {  // the factor's pivot ratio, read with the first backward error
+        gb300_count_launch(), pivot_ratio_kernel<<<1, 1024, 0, s>>>(n, ws.W, n, ws.rho);
+        cudaMemcpyAsync(&hratio, ws.rho, sizeof(double), cudaMemcpyDeviceToHost, s);
+    }
     double worst = INFINITY, prev = INFINITY, best = INFINITY;
     int since_best = 0;
     // read the backward errors (and the wait-timeout word) of the step just queued
@@ -914,7 +953,9 @@ int dsposv_refine(cudaStream_t s, int n, int nrhs, const double *A, int lda, con
                 break;
             }
             if (pcg) restart = true;  // the recurrence residual had drifted: start again from the true one
-            else if (mode == 1 || (mode == 2 && it >= 1 && worst > PCG_SWITCH * prev)) pcg = true;
+            else if (mode == 1 || (mode == 2 && it >= 1 && worst > PCG_SWITCH * prev) ||
+                     (mode == 2 && it == 0 && hratio > PCG_PIVOT_RATIO))
+                pcg = true;
         }
         if (worst < 0.5 * best) {
             best = worst;

@@ -29,11 +29,16 @@
 // (L, the mirrored L^T in the upper part, the diagonal-tile inverses and their
 // transposes) and V from row-major copies of y / z (16 floats per row) that
 // the diagonal tasks keep beside the column-major result.  Both are staged by
-// cp.async in a 6-deep ring of 64-column stages (~70 KB in flight per CTA),
-// and each lane keeps 4 rows x 16 right-hand sides (one 16-byte operand load
-// and four broadcast loads of V per 64 FMAs; the 8 warps split the K range).
-// Operands that are only available transposed (the public entry point's L^T
-// and inverses) take a register-staged path with the same partial layout.
+// cp.async in a 6-deep ring of 64-column stages (~80 KB in flight per CTA),
+// and multiplied on the tensor cores with warp-level m16n8k8 TF32 MMAs, three
+// per tile on the split x = hi + lo of both operands (about 21 significant
+// bits, the FP32 solve's own accuracy); each warp takes 8 of a stage's 64
+// columns and the 8 warps' 32 x 16 blocks are summed in a fixed order.  (A
+// 32-row slab and 16 right-hand sides are below the smallest tcgen05 tile, and
+// the chain of the sweep wants the accumulator in registers: the warp-level
+// MMA is the instruction that fits.)  Operands that are only available
+// transposed (the public entry point's L^T and inverses) take a
+// register-staged FP32 FMA path with the same partial layout.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -47,7 +52,10 @@ constexpr int TSW_VP = 20;     // pitch of one K index of the right-hand-side ch
 constexpr int TSW_T = 256;
 constexpr int TSW_KS = 64;   // K per cp.async stage
 constexpr int TSW_NS = 6;    // stages in the ring
-constexpr int TSW_STAGE = TSW_KS * (TSW_MP + TSW_VP);  // floats per stage
+// pitches of the ring's operand and right-hand-side rows, chosen so that the
+// tensor-core fragment loads (8 rows x 4 columns per warp) hit 32 banks
+constexpr int TSW_DMP = 40, TSW_DVP = 24;
+constexpr int TSW_STAGE = TSW_KS * (TSW_DMP + TSW_DVP);  // floats per stage
 // dynamic shared memory of the kernel: the ring (the register-staged path and
 // the reductions reuse it)
 constexpr int TSW_DSMEM = TSW_NS * TSW_STAGE * 4;
@@ -334,29 +342,49 @@ __device__ __forceinline__ void tsw_reduce(const float acc[4][4], float *red, fl
     __syncthreads();
 }
 
+// TF32 split of x: hi = tf32(x) (round to nearest), lo = tf32(x - hi).
+__device__ __forceinline__ void tsw_split_tf32(float x, uint32_t &hi, uint32_t &lo)
+{
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    const float r = x - __uint_as_float(hi);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+
+// d += a b for one 16 x 8 x 8 TF32 tile (warp-wide, FP32 accumulation)
+__device__ __forceinline__ void tsw_mma_tf32(float d[4], const uint32_t a[4], const uint32_t b[2])
+{
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                 "{%8, %9}, {%0, %1, %2, %3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 // acc += M(32 x K) V(K x 16) for an operand read as 32-row columns
 // (M(r, p) = M[r + p * ldm], 16-byte aligned columns) and a row-major V, in a
 // TSW_NS-deep cp.async ring of TSW_KS-column stages; elements past `rows` and
-// K are zero-filled.  Warp w takes columns 8 w .. 8 w + 7 of every stage;
-// lane (rr = lane % 8, kk = lane / 8) keeps rows 4 rr .. 4 rr + 3 of all 16
-// right-hand sides for the columns congruent to kk mod 4.
-__device__ __forceinline__ void tsw_product_direct(float acc[4][16], const float *M, long ldm, int rows,
+// K are zero-filled.  The products run on the tensor cores as three TF32
+// products per tile, hi hi + hi lo + lo hi with x = hi + lo split in
+// registers (about 21 significant bits: the FP32 correction solve's own
+// accuracy), accumulated in FP32.  Warp w takes columns 8 w .. 8 w + 7 of
+// every stage and keeps the whole 32 x 16 block: acc[mt][nt][4] holds the
+// m16n8 accumulator fragment of rows 16 mt .., right-hand sides 8 nt ...
+__device__ __forceinline__ void tsw_product_direct(float acc[2][2][4], const float *M, long ldm, int rows,
                                                    const float *V, int K, float *ring)
 {
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, rr = lane & 7, kk = lane >> 3;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
     const int nst = (K + TSW_KS - 1) / TSW_KS;
     auto issue = [&](int st) {
-        float *Ms = ring + (st % TSW_NS) * TSW_STAGE, *Vs = Ms + TSW_KS * TSW_MP;
+        float *Ms = ring + (st % TSW_NS) * TSW_STAGE, *Vs = Ms + TSW_KS * TSW_DMP;
         const int p0 = st * TSW_KS, kc = min(TSW_KS, K - p0);
 #pragma unroll
         for (int u = 0; u < TSW_KS * 8 / TSW_T; ++u) {
             const int e = tid + TSW_T * u, p = e >> 3, q = e & 7;
             const int valid = p < kc ? max(0, min(4, rows - 4 * q)) : 0;
-            tsw_cp16(Ms + p * TSW_MP + 4 * q, valid ? M + 4 * q + (long)(p0 + p) * ldm : M, 4 * valid);
+            tsw_cp16(Ms + p * TSW_DMP + 4 * q, valid ? M + 4 * q + (long)(p0 + p) * ldm : M, 4 * valid);
         }
         if (tid < TSW_KS * 4) {
             const int p = tid >> 2, q = tid & 3;
-            tsw_cp16(Vs + p * TSW_VP + 4 * q, p < kc ? V + (long)(p0 + p) * 16 + 4 * q : V, p < kc ? 16 : 0);
+            tsw_cp16(Vs + p * TSW_DVP + 4 * q, p < kc ? V + (long)(p0 + p) * 16 + 4 * q : V, p < kc ? 16 : 0);
         }
     };
 #pragma unroll 1
@@ -370,20 +398,28 @@ __device__ __forceinline__ void tsw_product_direct(float acc[4][16], const float
         __syncthreads();  // stage st is in; every warp is done with the buffer reloaded next
         if (st + TSW_NS - 1 < nst) issue(st + TSW_NS - 1);
         tsw_cp_commit();
-        const float *Ms = ring + (st % TSW_NS) * TSW_STAGE, *Vs = Ms + TSW_KS * TSW_MP;
+        const float *Ms = ring + (st % TSW_NS) * TSW_STAGE + 8 * warp * TSW_DMP;
+        const float *Vs = ring + (st % TSW_NS) * TSW_STAGE + TSW_KS * TSW_DMP + 8 * warp * TSW_DVP;
+        // B fragments (k = t, t + 4; right-hand side g of each 8-column half)
+        uint32_t bh[2][2], bl[2][2];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int p = 8 * warp + 4 * h + kk;
-            const float4 m = *reinterpret_cast<const float4 *>(Ms + p * TSW_MP + 4 * rr);
-            const float mv[4] = {m.x, m.y, m.z, m.w};
+        for (int nt = 0; nt < 2; ++nt) {
+            tsw_split_tf32(Vs[t * TSW_DVP + 8 * nt + g], bh[nt][0], bl[nt][0]);
+            tsw_split_tf32(Vs[(t + 4) * TSW_DVP + 8 * nt + g], bh[nt][1], bl[nt][1]);
+        }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float4 x = *reinterpret_cast<const float4 *>(Vs + p * TSW_VP + 4 * q);
-                const float xv[4] = {x.x, x.y, x.z, x.w};
+        for (int mt = 0; mt < 2; ++mt) {
+            // A fragment: rows g, g + 8 of the m-tile, k = t, t + 4
+            uint32_t ah[4], al[4];
+            tsw_split_tf32(Ms[t * TSW_DMP + 16 * mt + g], ah[0], al[0]);
+            tsw_split_tf32(Ms[t * TSW_DMP + 16 * mt + g + 8], ah[1], al[1]);
+            tsw_split_tf32(Ms[(t + 4) * TSW_DMP + 16 * mt + g], ah[2], al[2]);
+            tsw_split_tf32(Ms[(t + 4) * TSW_DMP + 16 * mt + g + 8], ah[3], al[3]);
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) acc[i][4 * q + c] = fmaf(mv[i], xv[c], acc[i][4 * q + c]);
+            for (int nt = 0; nt < 2; ++nt) {
+                tsw_mma_tf32(acc[mt][nt], al, bh[nt]);  // the small terms first
+                tsw_mma_tf32(acc[mt][nt], ah, bl[nt]);
+                tsw_mma_tf32(acc[mt][nt], ah, bh[nt]);
             }
         }
     }
@@ -391,26 +427,20 @@ __device__ __forceinline__ void tsw_product_direct(float acc[4][16], const float
     __syncthreads();  // the ring is free for the reduction
 }
 
-// Sum tsw_product_direct's partials (the four column classes of a warp by
-// shuffles, then the 8 warps in order) into out (32 x 16, row-major).
-__device__ __forceinline__ void tsw_reduce16(float acc[4][16], float *red, float *out)
+// Sum tsw_product_direct's per-warp blocks (the 8 warps in order) into out
+// (32 x 16, row-major).  Fragment element (mt, nt, i) of lane (g, t) is
+// row 16 mt + g + 8 (i / 2), right-hand side 8 nt + 2 t + i % 2.
+__device__ __forceinline__ void tsw_reduce_frag(const float acc[2][2][4], float *red, float *out)
 {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane & 7, kk = lane >> 3;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            acc[i][c] += __shfl_xor_sync(0xffffffffu, acc[i][c], 8);
-            acc[i][c] += __shfl_xor_sync(0xffffffffu, acc[i][c], 16);
-        }
-    if (kk == 0) {
+        for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                *reinterpret_cast<float4 *>(red + warp * 512 + (4 * rr + i) * 16 + 4 * q) =
-                    make_float4(acc[i][4 * q], acc[i][4 * q + 1], acc[i][4 * q + 2], acc[i][4 * q + 3]);
-    }
+            for (int h = 0; h < 2; ++h)
+                *reinterpret_cast<float2 *>(red + warp * 512 + (16 * mt + g + 8 * h) * 16 + 8 * nt + 2 * t) =
+                    make_float2(acc[mt][nt][2 * h], acc[mt][nt][2 * h + 1]);
     __syncthreads();
     for (int e = threadIdx.x; e < 512; e += TSW_T) {
         float s = 0.0f;
@@ -426,9 +456,9 @@ __device__ __forceinline__ void tsw_reduce16(float acc[4][16], float *red, float
 __device__ __noinline__ void tsw_gemv_direct(const float *M, long ldm, int rows, const float *V, int K, float *ring,
                                              float *out)
 {
-    float acc[4][16] = {};
+    float acc[2][2][4] = {};
     if (K > 0) tsw_product_direct(acc, M, ldm, rows, V, K, ring);
-    tsw_reduce16(acc, ring, out);
+    tsw_reduce_frag(acc, ring, out);
 }
 
 template <bool TR>
