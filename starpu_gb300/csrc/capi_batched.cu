@@ -36,7 +36,7 @@ static int g_ndense = 0;
 static bool g_table_loaded = false;
 static std::mutex g_table_mu;
 
-static size_t smem_bytes() { return (size_t)(64 * 65 + 2 * 64 * BAT_TILE) * sizeof(float); }
+static size_t smem_bytes() { return (size_t)(64 * 65 + 2 * 64 * BAT_TP) * sizeof(float); }
 
 // the existing table file, else where a new one is written
 static void tuning_path(char *path, size_t len)
@@ -231,6 +231,7 @@ static int run_batched(cudaStream_t s, int nsys, const int *n, const double *A, 
     a.a_off = ws.a_off;
     a.b_off = ws.b_off;
     a.order = ws.order;
+    a.smem_bytes = smem_bytes();
     a.A = A;
     a.B = B;
     a.X = X;

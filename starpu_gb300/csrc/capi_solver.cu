@@ -575,7 +575,11 @@ static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L,
     int *per = per_sm[dev & 15];
     if (!per[0]) {
         for (int i = 0; i < 3; ++i) {
-            if (gb300_func_dyn_smem(fns[i], TSW_DSMEM)) return;
+            if (gb300_func_dyn_smem(fns[i], TSW_DSMEM)) {
+                // the kernels cannot run on this device: report it in the error word
+                if (err) cudaMemsetAsync(err, 1, 1, s);
+                return;
+            }
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[i], fns[i], TSW_T, TSW_DSMEM);
             per[i] = std::max(per[i], 1);
         }

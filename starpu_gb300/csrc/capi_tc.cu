@@ -245,7 +245,7 @@ struct TcOperand {
 // tcu_tile_coords gives them (lower: column by column from the diagonal).
 static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A, long lda, const TcOperand &B,
                         long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store, int max_grid,
-                        bool f16s, int t0 = 0, int t1 = -1)
+                        bool f16s, int t0 = 0, int t1 = -1, bool b_lower = false)
 {
     if (m <= 0 || n <= 0 || K <= 0) return GB300_OK;
     if ((nterms != 1 && nterms != 3) || (nterms == 3 && (!A.lo || !B.lo)) || (lower && m != n) || !d_err ||
@@ -275,6 +275,7 @@ static int tc_update_op(cudaStream_t s, int m, int n, int K, const TcOperand &A,
     a.nterms = nterms;
     a.lower = lower;
     a.store = store;
+    a.b_lower = b_lower ? 1 : 0;
     a.tiles_m = (m + TCU_BM - 1) / TCU_BM;
     a.tiles_n = (n + TCU_BN - 1) / TCU_BN;
     if (lower) {
@@ -308,10 +309,10 @@ int tc_update(cudaStream_t s, int m, int n, int K, const void *a_hi, const void 
 // scaled FP16 panels (the factorisation)
 static int tc_update_f16s(cudaStream_t s, int m, int n, int K, const F16Panel &A, long lda, const F16Panel &B,
                           long ldb, int nterms, int lower, float *C, long ldc, int *d_err, int store = 0,
-                          int max_grid = 0, int t0 = 0, int t1 = -1)
+                          int max_grid = 0, int t0 = 0, int t1 = -1, bool b_lower = false)
 {
     return tc_update_op(s, m, n, K, {A.h, A.l, A.rs}, lda, {B.h, B.l, B.rs}, ldb, nterms, lower, C, ldc,
-                        d_err, store, max_grid, true, t0, t1);
+                        d_err, store, max_grid, true, t0, t1, b_lower);
 }
 
 
@@ -538,7 +539,8 @@ static int panel_solve(cudaStream_t s, int n, float *A, long lda, int k0, int kb
     // panel, before the diagonal is saved -- both from their row maxima)
     const float *d = bounds ? w.d : nullptr;
     int rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk, d, k0 + kb, w.dtile + k0 / nb);
-    if (!rc) rc = tc_update_f16s(s, m, kb, kb, w.pan[buf], ldk, w.inv, ldk, 3, 0, P, lda, d_err, 1, sms);
+    // the inverse is lower triangular: a tile of columns n0 .. n0 + 255 needs k <= n0 + 255 only
+    if (!rc) rc = tc_update_f16s(s, m, kb, kb, w.pan[buf], ldk, w.inv, ldk, 3, 0, P, lda, d_err, 1, sms, 0, -1, true);
     if (!rc) rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk, d, k0 + kb, nullptr);
     // algorithmic work: TRSM m kb^2; bytes: the panel read and written, its split written twice
     gb300_prof_end(s, slot, (double)m * kb * kb, 8.0 * m * kb + 4.0 * m * ldk * np);

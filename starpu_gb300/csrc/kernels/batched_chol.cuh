@@ -13,11 +13,19 @@
 //   right-looking blocked Cholesky with block NB (the tuned parameter):
 //     POTRF of the NB x NB diagonal block in shared memory
 //     TRSM of the panel rows, one row per thread, registers
-//     lower-triangular trailing update in 64 x 64 tiles staged in shared memory
-//   x = fp64(L^-T L^-1 fp32(b)); repeat r = b - A x (FP64), berr, x += corr.
+//     lower-triangular trailing update in 64 x 64 tiles staged in shared memory,
+//       on the tensor cores (warp-level TF32 MMAs on split operands)
+//   x = fp64(L^-T L^-1 fp32(b)); repeat r = b - A x, berr, x += corr.
+//   The residual runs in double-float arithmetic on the FP32 pipe (A split
+//   per element, X split once per residual into shared memory, FP64 flush
+//   every 128 terms; ~2^-47 relative per block), GB300 issuing FP64 FMAs at
+//   ~1/60 of its FP32 rate; with more right-hand sides than the shared
+//   memory holds it runs in FP64.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "df_arith.cuh"
 
 namespace gb300 {
 
@@ -25,6 +33,7 @@ constexpr int BAT_THREADS = 256;
 constexpr int BAT_MAXN = 1024;
 constexpr int BAT_MAXRHS = 8;
 constexpr int BAT_TILE = 64;
+constexpr int BAT_TP = 72;  // pitch of a staged panel slice row (64 + 8): conflict-free MMA fragment loads
 
 struct BatchedArgs {
     int nsys;
@@ -45,6 +54,7 @@ struct BatchedArgs {
     double *berr;                 // [nsys] final max backward error
     unsigned *ticket;
     const signed char *nb_of_bucket;  // block size per size bucket (log2 of ceil(n/32))
+    size_t smem_bytes;                // dynamic shared memory of the launch
 };
 
 __device__ __forceinline__ int bucket_of(int n)
@@ -55,13 +65,30 @@ __device__ __forceinline__ int bucket_of(int n)
     return b > 5 ? 5 : b;  // 32, 64, 128, 256, 512, 1024
 }
 
+// TF32 split of x: hi = tf32(x) (round to nearest), lo = tf32(x - hi)
+__device__ __forceinline__ void bat_split_tf32(float x, uint32_t &hi, uint32_t &lo)
+{
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    const float r = x - __uint_as_float(hi);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+
+// d += a b for one 16 x 8 x 8 TF32 tile (warp-wide, FP32 accumulation)
+__device__ __forceinline__ void bat_mma_tf32(float d[4], const uint32_t a[4], const uint32_t b[2])
+{
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                 "{%8, %9}, {%0, %1, %2, %3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 // ----------------------------------------------------------------- factor
 template <int NB>
 __device__ int bat_factor(float *W, int n, float *smem)
 {
     float(*D)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(smem);   // diagonal block
-    float *As = smem + NB * (NB + 1);                                  // [NB][64] panel slice (k-major)
-    float *Bs = As + NB * BAT_TILE;                                    // [NB][64]
+    float *As = smem + NB * (NB + 1);                                  // [NB][BAT_TP] panel slice (k-major)
+    float *Bs = As + NB * BAT_TP;                                      // [NB][BAT_TP]
     __shared__ int s_info;
     const int tid = threadIdx.x;
     if (tid == 0) s_info = 0;
@@ -117,49 +144,61 @@ __device__ int bat_factor(float *W, int n, float *smem)
                 if (c < kb) W[i + (long)(k0 + c) * n] = x[c];
         }
         __syncthreads();
-        // ---- trailing update of the lower triangle, 64 x 64 tiles
+        // ---- trailing update of the lower triangle, 64 x 64 tiles, on the
+        // tensor cores: warp-level m16n8k8 TF32 MMAs, three per tile on the
+        // split x = hi + lo of both operands (about 21 significant bits, the
+        // FP32 factor's working accuracy; the refinement recovers FP64).
+        // Warp w owns rows 16 (w % 4) .. + 15 and columns 32 (w / 4) .. + 31
+        // of the tile (four n8 fragments); K = the block width, padded to 8
+        // with zeros.
         const int nt = (m + BAT_TILE - 1) / BAT_TILE;
-        const int tr = tid % 16, tcn = tid / 16;  // 16 x 16 threads, 4 x 4 outputs each
+        const int kp = (kb + 7) & ~7;
+        const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
+        const int wr = 16 * (warp & 3), wc = 32 * (warp >> 2);
         for (int tj = 0; tj < nt; ++tj) {
             // stage the panel rows of tile column tj once per column
-            for (int idx = tid; idx < NB * BAT_TILE; idx += BAT_THREADS) {
+            for (int idx = tid; idx < kp * BAT_TILE; idx += BAT_THREADS) {
                 const int rr = idx % BAT_TILE, p = idx / BAT_TILE;
                 const int row = r0 + tj * BAT_TILE + rr;
-                Bs[p * BAT_TILE + rr] = (p < kb && row < n) ? W[row + (long)(k0 + p) * n] : 0.0f;
+                Bs[p * BAT_TP + rr] = (p < kb && row < n) ? W[row + (long)(k0 + p) * n] : 0.0f;
             }
             for (int ti2 = tj; ti2 < nt; ++ti2) {
-                for (int idx = tid; idx < NB * BAT_TILE; idx += BAT_THREADS) {
+                for (int idx = tid; idx < kp * BAT_TILE; idx += BAT_THREADS) {
                     const int rr = idx % BAT_TILE, p = idx / BAT_TILE;
                     const int row = r0 + ti2 * BAT_TILE + rr;
-                    As[p * BAT_TILE + rr] = (p < kb && row < n) ? W[row + (long)(k0 + p) * n] : 0.0f;
+                    As[p * BAT_TP + rr] = (p < kb && row < n) ? W[row + (long)(k0 + p) * n] : 0.0f;
                 }
                 __syncthreads();
                 float acc[4][4];
 #pragma unroll
-                for (int a = 0; a < 4; ++a)
+                for (int j = 0; j < 4; ++j)
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
-                for (int p = 0; p < kb; ++p) {
-                    float av[4], bv[4];
+                    for (int q = 0; q < 4; ++q) acc[j][q] = 0.0f;
+                for (int p = 0; p < kp; p += 8) {
+                    uint32_t ah[4], al[4];
+                    bat_split_tf32(As[(p + t4) * BAT_TP + wr + g], ah[0], al[0]);
+                    bat_split_tf32(As[(p + t4) * BAT_TP + wr + g + 8], ah[1], al[1]);
+                    bat_split_tf32(As[(p + t4 + 4) * BAT_TP + wr + g], ah[2], al[2]);
+                    bat_split_tf32(As[(p + t4 + 4) * BAT_TP + wr + g + 8], ah[3], al[3]);
 #pragma unroll
-                    for (int a = 0; a < 4; ++a) av[a] = As[p * BAT_TILE + tr + 16 * a];
-#pragma unroll
-                    for (int b = 0; b < 4; ++b) bv[b] = Bs[p * BAT_TILE + tcn + 16 * b];
-#pragma unroll
-                    for (int a = 0; a < 4; ++a)
-#pragma unroll
-                        for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
-                }
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const int col = r0 + tj * BAT_TILE + tcn + 16 * b;
-                    if (col >= n) continue;
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) {
-                        const int row = r0 + ti2 * BAT_TILE + tr + 16 * a;
-                        if (row < n && row >= col) W[row + (long)col * n] -= acc[a][b];
+                    for (int j = 0; j < 4; ++j) {
+                        uint32_t bh[2], bl[2];
+                        bat_split_tf32(Bs[(p + t4) * BAT_TP + wc + 8 * j + g], bh[0], bl[0]);
+                        bat_split_tf32(Bs[(p + t4 + 4) * BAT_TP + wc + 8 * j + g], bh[1], bl[1]);
+                        bat_mma_tf32(acc[j], al, bh);  // the small terms first
+                        bat_mma_tf32(acc[j], ah, bl);
+                        bat_mma_tf32(acc[j], ah, bh);
                     }
                 }
+                // fragment element q of n-tile j: row wr + g + 8 (q / 2), column wc + 8 j + 2 t4 + q % 2
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int col = r0 + tj * BAT_TILE + wc + 8 * j + 2 * t4 + (q & 1);
+                        const int row = r0 + ti2 * BAT_TILE + wr + g + 8 * (q >> 1);
+                        if (col < n && row < n && row >= col) W[row + (long)col * n] -= acc[j][q];
+                    }
                 __syncthreads();
             }
         }
@@ -180,37 +219,165 @@ __device__ void bat_mirror_upper(float *W, int n)
     __syncthreads();
 }
 
-// Y (n x nrhs, ld n) <- L^-T L^-1 Y.  Column-oriented substitution: at step j
-// the owner of row j finishes y_j, then every thread updates its rows with
-// column j of L (forward) or of L^T (backward, read from the mirrored upper
-// triangle); both reads are contiguous along the rows the threads own.
+// Y (n x nrhs, ld n) <- L^-T L^-1 Y, in blocks of 32 columns.  Per block,
+// warp 0 solves the 32 x 32 diagonal block (lane = row, the solved entry
+// broadcast by shuffles), then every thread updates its rows outside the
+// block with the block's 32 columns of L (forward) or of L^T (backward, read
+// from the mirrored upper triangle); both reads are contiguous along the rows
+// the threads own.  Each row sees its updates in the same column order as a
+// column-by-column substitution, with two barriers per 32 columns.
 __device__ void bat_potrs(const float *W, int n, float *Y, int nrhs)
 {
-    const int tid = threadIdx.x;
-    for (int j = 0; j < n; ++j) {
-        const float *Lj = W + (long)j * n;  // L[:, j]
-        if (j % BAT_THREADS == tid) {
-            const float d = Lj[j];
-            for (int c = 0; c < nrhs; ++c) Y[j + (long)c * n] /= d;
+    const int tid = threadIdx.x, lane = tid & 31;
+    // forward: L y = b
+    for (int j0 = 0; j0 < n; j0 += 32) {
+        const int jb = min(32, n - j0);
+        if (tid < 32) {
+            float y[BAT_MAXRHS];
+#pragma unroll
+            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = (c < nrhs && lane < jb) ? Y[j0 + lane + (long)c * n] : 0.0f;
+            for (int j = 0; j < jb; ++j) {
+                const float l = lane < jb ? W[j0 + lane + (long)(j0 + j) * n] : 0.0f;  // L[j0 + lane, j0 + j]
+                if (lane == j) {
+#pragma unroll
+                    for (int c = 0; c < BAT_MAXRHS; ++c) y[c] /= l;
+                }
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c) {
+                    const float yj = __shfl_sync(0xffffffffu, y[c], j);
+                    if (lane > j) y[c] = fmaf(-l, yj, y[c]);
+                }
+            }
+            if (lane < jb) {
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c)
+                    if (c < nrhs) Y[j0 + lane + (long)c * n] = y[c];
+            }
         }
         __syncthreads();
-        for (int i = j + 1 + ((tid - (j + 1) % BAT_THREADS + BAT_THREADS) % BAT_THREADS); i < n; i += BAT_THREADS) {
-            const float l = Lj[i];
-            for (int c = 0; c < nrhs; ++c) Y[i + (long)c * n] = fmaf(-l, Y[j + (long)c * n], Y[i + (long)c * n]);
+        for (int i = j0 + jb + tid; i < n; i += BAT_THREADS) {
+            float y[BAT_MAXRHS];
+#pragma unroll
+            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = c < nrhs ? Y[i + (long)c * n] : 0.0f;
+            for (int j = 0; j < jb; ++j) {
+                const float l = W[i + (long)(j0 + j) * n];
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c)
+                    if (c < nrhs) y[c] = fmaf(-l, Y[j0 + j + (long)c * n], y[c]);
+            }
+#pragma unroll
+            for (int c = 0; c < BAT_MAXRHS; ++c)
+                if (c < nrhs) Y[i + (long)c * n] = y[c];
         }
+        __syncthreads();
+    }
+    // backward: L^T x = y, U = L^T read from the mirrored upper triangle
+    // (U[i, j] = W[i + j n] for i < j)
+    for (int j1 = n; j1 > 0; j1 -= 32) {
+        const int j0 = max(0, j1 - 32), jb = j1 - j0;
+        if (tid < 32) {
+            float y[BAT_MAXRHS];
+#pragma unroll
+            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = (c < nrhs && lane < jb) ? Y[j0 + lane + (long)c * n] : 0.0f;
+            for (int j = jb - 1; j >= 0; --j) {
+                const float u = lane < jb ? W[j0 + lane + (long)(j0 + j) * n] : 0.0f;  // U[j0 + lane, j0 + j]
+                if (lane == j) {
+#pragma unroll
+                    for (int c = 0; c < BAT_MAXRHS; ++c) y[c] /= u;
+                }
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c) {
+                    const float yj = __shfl_sync(0xffffffffu, y[c], j);
+                    if (lane < j) y[c] = fmaf(-u, yj, y[c]);
+                }
+            }
+            if (lane < jb) {
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c)
+                    if (c < nrhs) Y[j0 + lane + (long)c * n] = y[c];
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < j0; i += BAT_THREADS) {
+            float y[BAT_MAXRHS];
+#pragma unroll
+            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = c < nrhs ? Y[i + (long)c * n] : 0.0f;
+            for (int j = jb - 1; j >= 0; --j) {
+                const float u = W[i + (long)(j0 + j) * n];
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c)
+                    if (c < nrhs) y[c] = fmaf(-u, Y[j0 + j + (long)c * n], y[c]);
+            }
+#pragma unroll
+            for (int c = 0; c < BAT_MAXRHS; ++c)
+                if (c < nrhs) Y[i + (long)c * n] = y[c];
+        }
+        __syncthreads();
+    }
+}
+
+// R = B - A X (n x nrhs) in double-float arithmetic on the FP32 pipe: A
+// scaled by 2^-ea (ea = exponent of ||A||_inf, an upper bound of |a_ij|) and
+// split per element by bit operations, each column of X scaled by 2^-ex_c
+// and split once into shared memory (Xs[k nrhs + c]); per row (one thread)
+// and right-hand side an error-free running sum, flushed to FP64 every 128
+// terms, in a fixed order (deterministic).
+__device__ void bat_residual_df(const double *A, int n, const double *X, const double *B, double *R, int nrhs,
+                                double anorm, float *smem)
+{
+    __shared__ int s_ex[BAT_MAXRHS];
+    __shared__ double s_xm[BAT_THREADS / 32];
+    const int tid = threadIdx.x;
+    float2 *Xs = reinterpret_cast<float2 *>(smem);
+    for (int c = 0; c < nrhs; ++c) {
+        double m = 0.0;
+        for (int k = tid; k < n; k += BAT_THREADS) m = fmax(m, fabs(X[k + (long)c * n]));
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((tid & 31) == 0) s_xm[tid >> 5] = m;
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < BAT_THREADS / 32; ++w) m = fmax(m, s_xm[w]);
+            s_ex[c] = df_scale_exp(m);
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < n * nrhs; e += BAT_THREADS) {
+        const int k = e / nrhs, c = e - k * nrhs;
+        Xs[e] = df_split_scaled(X[k + (long)c * n], s_ex[c]);
     }
     __syncthreads();
-    for (int j = n - 1; j >= 0; --j) {
-        const float *Uj = W + (long)j * n;  // U[:, j] = L[j, :] in rows 0..j
-        if (j % BAT_THREADS == tid) {
-            const float d = Uj[j];
-            for (int c = 0; c < nrhs; ++c) Y[j + (long)c * n] /= d;
+    const int ea = df_scale_exp(anorm);
+    for (int i = tid; i < n; i += BAT_THREADS) {
+        double acc[BAT_MAXRHS];
+        float sh[BAT_MAXRHS], sl[BAT_MAXRHS];
+#pragma unroll
+        for (int c = 0; c < BAT_MAXRHS; ++c) {
+            acc[c] = c < nrhs ? B[i + (long)c * n] : 0.0;
+            sh[c] = 0.0f;
+            sl[c] = 0.0f;
         }
-        __syncthreads();
-        for (int i = tid; i < j; i += BAT_THREADS) {
-            const float u = Uj[i];
-            for (int c = 0; c < nrhs; ++c) Y[i + (long)c * n] = fmaf(-u, Y[j + (long)c * n], Y[i + (long)c * n]);
+        for (int j0 = 0; j0 < n; j0 += 128) {
+            const int j1 = min(n, j0 + 128);
+            for (int j = j0; j < j1; ++j) {
+                const float2 av = df_split_scaled(A[i + (long)j * n], ea);
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c)
+                    if (c < nrhs) {
+                        const float2 xv = Xs[j * nrhs + c];
+                        df_mac(sh[c], sl[c], av.x, av.y, xv.x, xv.y);
+                    }
+            }
+#pragma unroll
+            for (int c = 0; c < BAT_MAXRHS; ++c)
+                if (c < nrhs) {
+                    acc[c] -= ldexp((double)sh[c] + (double)sl[c], ea + s_ex[c]);
+                    sh[c] = 0.0f;
+                    sl[c] = 0.0f;
+                }
         }
+#pragma unroll
+        for (int c = 0; c < BAT_MAXRHS; ++c)
+            if (c < nrhs) R[i + (long)c * n] = acc[c];
     }
     __syncthreads();
 }
@@ -281,7 +448,12 @@ __global__ void __launch_bounds__(BAT_THREADS, 2) batched_dposv_kernel(BatchedAr
         __syncthreads();
         int it = 0;
         double worst = INFINITY;
+        // the double-float residual's X split fits the shared memory
+        const bool df = (size_t)n * nrhs * sizeof(float2) <= a.smem_bytes;
         for (;; ++it) {
+            if (df) {
+                bat_residual_df(A, n, X, B, R, nrhs, s_anorm, bat_smem);
+            } else
             // R = B - A X, columns of A streamed, one row per thread (coalesced)
             for (int i = tid; i < n; i += BAT_THREADS) {
                 double acc[BAT_MAXRHS];

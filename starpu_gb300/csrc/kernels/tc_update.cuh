@@ -70,9 +70,18 @@ struct TcUpdateArgs {
     int rs_b_vec;              // rs_b is 16-byte aligned: the column scales load 4 at a time
     int tiles_m, tiles_n, num_tiles;
     int tile_begin, tile_end;  // the launch covers tiles [tile_begin, tile_end) of the num_tiles
+    // 1: B is lower triangular in (row, k) (B(c, k) = 0 for k > c, the panel TRSM's
+    // inverse), so a tile of columns n0 .. n0 + 255 stops at k = n0 + 255
+    int b_lower;
     int *err;
     unsigned long long wait_budget_ns;
 };
+
+// K blocks a tile of columns n0 .. needs (all of them unless B is lower triangular)
+__device__ __forceinline__ int tcu_tile_kblocks(const TcUpdateArgs &a, int kblocks, int n0)
+{
+    return a.b_lower ? min(kblocks, (n0 + TCU_BN + TCU_BK - 1) / TCU_BK) : kblocks;
+}
 
 // Map a linear tile index to (tm, tn).  Lower: column tn holds tiles
 // tm = 2*tn .. tiles_m-1 (a 128-row tile crosses the diagonal of a 256-column
@@ -150,7 +159,6 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
     const uint32_t tmem_base = *tmem_slot;
 
     const int kblocks = (args.K + TCU_BK - 1) / TCU_BK;
-    const int total_kb = kblocks * args.nterms;
 
     if (warp == 0) {
         // ------------------------------------------------------ TMA producer
@@ -163,6 +171,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                 int tm, tn;
                 tcu_tile_coords(args, t, tm, tn);
                 const int m0 = tm * TCU_BM, n0 = tn * TCU_BN;
+                const int kbt = tcu_tile_kblocks(args, kblocks, n0), total_kb = kbt * args.nterms;
                 for (int kb = 0; kb < total_kb; ++kb) {
                     if (!ptx::wait_parity(&empty[stage], phase ^ 1, abort_flag, args.wait_budget_ns)) {
                         ok = false;
@@ -172,8 +181,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                     // cross products accumulate, the accumulator holds only their
                     // sum (about 2^-8 of the result), so the rounding of each of
                     // their additions is 2^-8 smaller than on top of A_hi B_hi^T
-                    const int term = args.nterms == 3 ? (kb / kblocks + 1) % 3 : 0;
-                    const int kx = (kb % kblocks) * TCU_BK;
+                    const int term = args.nterms == 3 ? (kb / kbt + 1) % 3 : 0;
+                    const int kx = (kb % kbt) * TCU_BK;
                     // term 0: A_hi B_hi^T, 1: A_hi B_lo^T, 2: A_lo B_hi^T
                     const CUtensorMap *ma = (term == 2) ? &tm_a_lo : &tm_a_hi;
                     const CUtensorMap *mb = (term == 1) ? &tm_b_lo : &tm_b_hi;
@@ -222,6 +231,9 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_const
                 }
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem_base + (uint32_t)(acc * TCU_BN);
+                int tm, tn;
+                tcu_tile_coords(args, t, tm, tn);
+                const int total_kb = tcu_tile_kblocks(args, kblocks, tn * TCU_BN) * args.nterms;
                 for (int kb = 0; kb < total_kb; ++kb) {
                     if (!ptx::wait_parity(&full[stage], phase, abort_flag, args.wait_budget_ns)) {
                         ok = false;
