@@ -1107,11 +1107,16 @@ def run_case(argv):
         W = DeviceBuffer(8 * n * n)
         check(L.starpu_gb300_gen_spd_gram(None, n, 3, 4.0 / (a.kappa - 1.0), A.ptr, n, W.ptr))
         del W
-        # pinned host A: the context's gather kernel reads it over the host link
+        # pinned host A: the context's gather kernel reads it over the host link.
+        # Written by the CPU, as a host program produces it (pinned pages last
+        # written by a device-to-host copy read back at a fraction of the link rate)
         hA = L.starpu_gb300_host_malloc_pinned(8 * n * n)
-        assert hA, L.starpu_gb300_last_error()
-        check(L.starpu_gb300_memcpy_d2h(None, hA, A.ptr, 8 * n * n))
+        tmp = L.starpu_gb300_host_malloc_pinned(8 * n * n)
+        assert hA and tmp, L.starpu_gb300_last_error()
+        check(L.starpu_gb300_memcpy_d2h(None, tmp, A.ptr, 8 * n * n))
         check(L.starpu_gb300_stream_sync(None))
+        C.memmove(hA, tmp, 8 * n * n)
+        L.starpu_gb300_host_free_pinned(tmp)
         hB = np.asfortranarray(np.random.default_rng(4).uniform(-1, 1, (n, nrhs)))
         hX = np.zeros((n, nrhs), order="F")
         ctx = L.starpu_gb300_solver_create(n, nrhs, nb, a.nterms)

@@ -29,9 +29,6 @@
 
 namespace gb300 {
 
-int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err,
-             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows,
-             const std::function<void(cudaStream_t, int, int)> &on_panel, cudaEvent_t ready);
 
 // W(c, r) = W(r, c) for the rows r in [r0, n) below the column block
 // [c0, c0 + w): the strictly upper part of W then holds L^T outside the
@@ -753,8 +750,10 @@ static int slice_rows(int n)
 // prepared: W and max |A_ij| were written while A was gathered from the host
 // (gather_convert_kernel), the first pass is skipped
 static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double *A, int lda, const SolverWs &ws,
-                        bool prepared)
+                        bool prepared, const TcArrival *arr = nullptr)
 {
+    // columns arriving over time: the passes over all of A wait for the last superblock
+    cudaEvent_t all_in = arr && arr->nsb > 0 ? arr->ready[arr->nsb - 1] : nullptr;
     // anorm_bits[0] = ||A||_inf, [1] = info + err, [2] = max |A_ij|
     // the first column block is converted first; the rest converts beside the
     // first panel, which reads nothing else, and the factorisation waits for
@@ -784,6 +783,7 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
     auto slice = [&](cudaStream_t from) {
         cudaEventRecord(ss->fork, from);
         cudaStreamWaitEvent(ss->s, ss->fork, 0);
+        if (all_in) cudaStreamWaitEvent(ss->s, all_in, 0);
         side_rc = residual_tc_slice_a(ss->s, n, A, lda, ws.anorm_bits + 2, ws.rtc_a, ws.rowsum);
         gb300_count_launch(), norm_from_rowsums_kernel<<<(n + 255) / 256, 256, 0, ss->s>>>(
             n, (n + 63) / 64, ws.rowsum, ws.anorm_bits + 2, ws.anorm_bits);
@@ -801,7 +801,8 @@ static int factor_phase(cudaStream_t s, int n, int nb, int nterms, const double 
         mirrored = true;
     };
     int rc = potrf_tc(fs->s, n, ws.W, n, nb, nterms, ws.panel, ws.info, ws.err, ws.band, slice, slice_rows(n),
-                      mirror, converted);
+                      mirror, converted, arr);
+    if (all_in) cudaStreamWaitEvent(s, all_in, 0);
     if (!rc) rc = side_rc;
     if (mirrored) {
         cudaEventRecord(ms->join, ms->s);
@@ -835,11 +836,11 @@ void dsposv_prepared_targets(int n, int nrhs, int nb, void *work, float **W, uns
 }
 
 int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
-                  starpu_gb300_ir_info *out, bool prepared)
+                  starpu_gb300_ir_info *out, bool prepared, const TcArrival *arr)
 {
     SolverWs ws;
     layout(n, nrhs, nb, work, &ws);
-    int rc = factor_phase(s, n, nb, nterms, A, lda, ws, prepared);
+    int rc = factor_phase(s, n, nb, nterms, A, lda, ws, prepared, arr);
     int hinfo[2] = {0, 0};
     if (!rc) rc = gb300_record_cuda_error(cudaMemcpyAsync(hinfo, ws.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     if (!rc) rc = gb300_record_cuda_error(cudaStreamSynchronize(s));
@@ -1098,9 +1099,9 @@ static bool fp64_fallback_enabled()
 
 int dsposv_ladder(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
                   int ldx, int nb, int nterms, double tol, int max_iter, void *work, starpu_gb300_ir_info *out,
-                  bool prepared)
+                  bool prepared, const TcArrival *arr)
 {
-    int rc = dsposv_factor(s, n, nrhs, A, lda, nb, nterms, work, out, prepared);
+    int rc = dsposv_factor(s, n, nrhs, A, lda, nb, nterms, work, out, prepared, arr);
     int reason = 0;
     if (rc == GB300_EDOM) reason = 1;
     else if (rc) return rc;
@@ -1165,12 +1166,20 @@ struct starpu_gb300_solver {
     double *A, *B, *X;
     void *work;
     size_t lwork;
+    // the pinned-input path's overlap of the host link with the factorisation:
+    // a copy stream, one event per superblock, every step's split panel, the diagonal
+    cudaStream_t copy = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> ready;
+    void *panels = nullptr;
+    float *diag = nullptr;
+    bool overlap_failed = false;
 };
 
 starpu_gb300_solver *starpu_gb300_solver_create(int n_max, int nrhs_max, int nb, int nterms)
 {
     if (n_max <= 0 || nrhs_max <= 0 || (nterms != 1 && nterms != 3)) return nullptr;
-    starpu_gb300_solver *h = (starpu_gb300_solver *)calloc(1, sizeof *h);
+    starpu_gb300_solver *h = new starpu_gb300_solver();
     h->n_max = n_max;
     h->nrhs_max = nrhs_max;
     h->nb = nb > 0 ? nb : 1024;
@@ -1192,12 +1201,18 @@ int starpu_gb300_solver_destroy(starpu_gb300_solver *h)
 {
     if (!h) return GB300_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->copy) cudaStreamSynchronize(h->copy);
     cudaFree(h->A);
     cudaFree(h->B);
     cudaFree(h->X);
     cudaFree(h->work);
+    cudaFree(h->panels);
+    cudaFree(h->diag);
+    for (cudaEvent_t e : h->ready) cudaEventDestroy(e);
+    if (h->fork) cudaEventDestroy(h->fork);
+    if (h->copy) cudaStreamDestroy(h->copy);
     if (h->stream) cudaStreamDestroy(h->stream);
-    free(h);
+    delete h;
     return GB300_OK;
 }
 
@@ -1215,9 +1230,9 @@ static constexpr int HOST_PANEL = 512;
 // flight per thread.
 __global__ void __launch_bounds__(256) gather_convert_kernel(int n, const double *__restrict__ H, long ldh,
                                                              double *__restrict__ D, long ldd, float *__restrict__ W,
-                                                             long ldw, unsigned long long *amax_bits)
+                                                             long ldw, unsigned long long *amax_bits, int j0 = 0)
 {
-    const long j = blockIdx.x;
+    const long j = j0 + (long)blockIdx.x;
     const double *src = H + j * ldh;
     double *dst = D + j * ldd;
     float *w = W + j * ldw;
@@ -1266,6 +1281,14 @@ __global__ void __launch_bounds__(256) gather_convert_kernel(int n, const double
     }
 }
 
+// d[i] = fp32(A_ii) from the mapped host matrix (the factorisation's row
+// bounds need the whole diagonal before the columns have arrived)
+__global__ void gather_diag_kernel(int n, const double *__restrict__ H, long ldh, float *__restrict__ d)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = (float)H[i + i * ldh];
+}
+
 // Device address of a pinned (page-locked, mapped) host buffer, or NULL when
 // `p` is not one -- ordinary pageable memory takes the copy path.
 static const double *device_view_of_pinned(const double *p)
@@ -1291,6 +1314,38 @@ static const double *device_view_of_pinned_matrix(const double *A, int n, int ld
     return d1 == d0 + last ? d0 : nullptr;
 }
 
+// The overlapped gather needs a copy stream, one event per superblock, a
+// store for every step's split panel and the diagonal, allocated once for
+// n_max; it applies to the tensor-core path with a lookahead (n > 2 nb) and
+// tile sizes the diagonal-tile kernel handles.  STARPU_GB300_HOST_OVERLAP=0
+// turns it off (the whole matrix is gathered before the factorisation).
+static bool overlap_ready(starpu_gb300_solver *h, int n, int nb)
+{
+    static const bool off = [] {
+        const char *e = getenv("STARPU_GB300_HOST_OVERLAP");
+        return e && !strcmp(e, "0");
+    }();
+    if (off || h->overlap_failed || n <= 2 * nb || nb > GB300_DIAG_TILE_MAX || h->nterms != 3) return false;
+    if (!h->copy) {
+        const int nsb_max = (h->n_max + 2 * nb - 1) / (2 * nb);
+        bool ok = cudaStreamCreateWithFlags(&h->copy, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming) == cudaSuccess &&
+                  cudaMalloc(&h->panels, tc_arrival_store_bytes(h->n_max, nb)) == cudaSuccess &&
+                  cudaMalloc((void **)&h->diag, sizeof(float) * (size_t)h->n_max) == cudaSuccess;
+        for (int q = 0; ok && q < nsb_max; ++q) {
+            cudaEvent_t e = nullptr;
+            ok = cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+            if (ok) h->ready.push_back(e);
+        }
+        if (!ok) {  // no room: gather the whole matrix first, as before
+            cudaGetLastError();
+            h->overlap_failed = true;
+            return false;
+        }
+    }
+    return true;
+}
+
 int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, const double *A, int lda,
                                     const double *B, int ldb, double *X, int ldx, double tol, int max_iter,
                                     starpu_gb300_ir_info *info)
@@ -1307,6 +1362,8 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
     double abytes = 0.0;
     const double *mapped = device_view_of_pinned_matrix(A, n, lda);
     const int nb_eff = h->nb > 0 ? h->nb : 1024;
+    TcArrival arr;
+    std::vector<int> starts;
     if (mapped) {
         // pinned host memory the GPU can read: one kernel pulls exactly the
         // lower triangle over the host link (pitched copies of column
@@ -1316,7 +1373,29 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
         unsigned long long *amax = nullptr;
         dsposv_prepared_targets(n, nrhs, nb_eff, h->work, &W, &amax);
         cudaMemsetAsync(amax, 0, 4 * sizeof(unsigned long long), s);
-        gb300_count_launch(), gather_convert_kernel<<<n, 256, 0, s>>>(n, mapped, lda, h->A, n, W, n, amax + 2);
+        if (overlap_ready(h, n, nb_eff)) {
+            // superblocks of two column blocks on the copy stream, each
+            // announced by an event: the factorisation starts on the first
+            // columns while the rest is still crossing the host link
+            const int sbw = 2 * nb_eff, nsb = (n + sbw - 1) / sbw;
+            starts.resize(nsb + 1);
+            for (int q = 0; q <= nsb; ++q) starts[q] = std::min(n, q * sbw);
+            cudaEventRecord(h->fork, s);
+            cudaStreamWaitEvent(h->copy, h->fork, 0);
+            gb300_count_launch(), gather_diag_kernel<<<(n + 255) / 256, 256, 0, h->copy>>>(n, mapped, lda, h->diag);
+            for (int q = 0; q < nsb; ++q) {
+                gb300_count_launch(), gather_convert_kernel<<<starts[q + 1] - starts[q], 256, 0, h->copy>>>(
+                    n, mapped, lda, h->A, n, W, n, amax + 2, starts[q]);
+                cudaEventRecord(h->ready[q], h->copy);
+            }
+            arr.nsb = nsb;
+            arr.start = starts.data();
+            arr.ready = h->ready.data();
+            arr.diag = h->diag;
+            arr.panel_store = h->panels;
+        } else {
+            gb300_count_launch(), gather_convert_kernel<<<n, 256, 0, s>>>(n, mapped, lda, h->A, n, W, n, amax + 2);
+        }
         if ((rc = gb300_last_launch_status())) return rc;
         abytes = 8.0 * n * (n + 1.0) / 2.0;
     } else {
@@ -1343,7 +1422,7 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
         if (info) memset(info, 0, sizeof *info);
         if ((h->nterms != 1 && h->nterms != 3) || max_iter < 0 || !(tol >= 0)) return GB300_EINVAL;
         status = dsposv_ladder(s, n, nrhs, h->A, n, h->B, n, h->X, n, nb_eff, h->nterms, tol, max_iter, h->work,
-                               info, true);
+                               info, true, arr.nsb ? &arr : nullptr);
     } else {
         status = starpu_gb300_dsposv(s, n, nrhs, h->A, n, h->B, n, h->X, n, h->nb, h->nterms, tol, max_iter, h->work,
                                      h->lwork, info);

@@ -145,15 +145,16 @@ __global__ void panel_row_scale_kernel(int m, int k, const float *__restrict__ P
     }
 }
 
-// d[r] = A_rr, and dtile[t] = max of d over the nb rows of column tile t
+// d[r] = A_rr (from A's diagonal, or from dsrc when given), and dtile[t] =
+// max of d over the nb rows of column tile t
 __global__ void diag_bounds_kernel(int n, const float *__restrict__ A, long lda, int nb, float *__restrict__ d,
-                                   float *__restrict__ dtile)
+                                   float *__restrict__ dtile, const float *__restrict__ dsrc)
 {
     __shared__ float red[256];
     const int t = blockIdx.x;
     float mx = 0.0f;
     for (int r = t * nb + threadIdx.x; r < min(n, (t + 1) * nb); r += blockDim.x) {
-        const float v = A[r + (long)r * lda];
+        const float v = dsrc ? dsrc[r] : A[r + (long)r * lda];
         d[r] = v;
         mx = fmaxf(mx, fabsf(v));
     }
@@ -527,7 +528,7 @@ static int panel_diag(cudaStream_t s, int n, float *A, long lda, int k0, int kb,
 }
 
 static int panel_solve(cudaStream_t s, int n, float *A, long lda, int k0, int kb, int nb, int np, const TcWs &w,
-                       int buf, int *d_err, int sms, bool bounds = true)
+                       const F16Panel &pan, int *d_err, int sms, bool bounds = true)
 {
     const long ldk = ((long)nb + 63) / 64 * 64;
     const int m = n - k0 - kb;
@@ -538,10 +539,10 @@ static int panel_solve(cudaStream_t s, int n, float *A, long lda, int k0, int kb
     // columns), the solved panel by sqrt(d_r) (without the bounds -- the first
     // panel, before the diagonal is saved -- both from their row maxima)
     const float *d = bounds ? w.d : nullptr;
-    int rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk, d, k0 + kb, w.dtile + k0 / nb);
+    int rc = split_f16s(s, m, kb, P, lda, pan, ldk, d, k0 + kb, w.dtile + k0 / nb);
     // the inverse is lower triangular: a tile of columns n0 .. n0 + 255 needs k <= n0 + 255 only
-    if (!rc) rc = tc_update_f16s(s, m, kb, kb, w.pan[buf], ldk, w.inv, ldk, 3, 0, P, lda, d_err, 1, sms, 0, -1, true);
-    if (!rc) rc = split_f16s(s, m, kb, P, lda, w.pan[buf], ldk, d, k0 + kb, nullptr);
+    if (!rc) rc = tc_update_f16s(s, m, kb, kb, pan, ldk, w.inv, ldk, 3, 0, P, lda, d_err, 1, sms, 0, -1, true);
+    if (!rc) rc = split_f16s(s, m, kb, P, lda, pan, ldk, d, k0 + kb, nullptr);
     // algorithmic work: TRSM m kb^2; bytes: the panel read and written, its split written twice
     gb300_prof_end(s, slot, (double)m * kb * kb, 8.0 * m * kb + 4.0 * m * ldk * np);
     return rc;
@@ -570,9 +571,33 @@ static int panel_solve(cudaStream_t s, int n, float *A, long lda, int k0, int kb
 // enqueued: that block of the factor is final from then on.  `ready`, when
 // given, is an event the first update waits for: the first panel reads only
 // the first column block, the rest of A may still be being written.
+// One split panel per step for TcArrival::panel_store: h and l (n x ldk) and
+// the row scales, step after step.
+static size_t arrival_panel_bytes(int n, int nb)
+{
+    const size_t ldk = ((size_t)(nb > 0 ? nb : 1) + 63) / 64 * 64;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    return 2 * al((size_t)n * ldk * 2) + 2 * scale_bytes(n);
+}
+
+size_t tc_arrival_store_bytes(int n, int nb)
+{
+    if (n <= 0 || nb <= 0) return 0;
+    return ((size_t)n + nb - 1) / nb * arrival_panel_bytes(n, nb);
+}
+
+static F16Panel arrival_panel(void *store, int n, int nb, int step)
+{
+    const size_t ldk = ((size_t)nb + 63) / 64 * 64;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t panel = al((size_t)n * ldk * 2), rsn = scale_bytes(n);
+    char *p = (char *)store + (size_t)step * arrival_panel_bytes(n, nb);
+    return {(__half *)p, (__half *)(p + panel), (int *)(p + 2 * panel), (float *)(p + 2 * panel + rsn)};
+}
+
 int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *work, int *d_info, int *d_err,
              float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows,
-             const std::function<void(cudaStream_t, int, int)> &on_panel, cudaEvent_t ready)
+             const std::function<void(cudaStream_t, int, int)> &on_panel, cudaEvent_t ready, const TcArrival *arr)
 {
     bool side_done = !side;
     const long ldk = ((long)nb + 63) / 64 * 64;
@@ -581,23 +606,61 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
     const int np = nterms == 3 ? 2 : 1;  // split panel arrays an update reads: h, l
     // a step has a trailing triangle beyond its next column block only when n > 2 nb
     LookaheadStream *la = n > 2 * nb ? lookahead_stream() : nullptr;
-    int buf = 0;
-    int rc = panel_diag(s, n, A, lda, 0, std::min(nb, n), nb, w, linv_band, d_info, d_err, 0);
-    if (!rc) rc = panel_solve(s, n, A, lda, 0, std::min(nb, n), nb, np, w, buf, d_err, 0, false);
+    // the split panel of step k: two buffers in turn, or one per step when
+    // the columns arrive over time (the late columns replay every step)
+    auto panel_of = [&](int step) -> F16Panel {
+        return arr ? arrival_panel(arr->panel_store, n, nb, step) : w.pan[step & 1];
+    };
+    // arriving columns: superblocks [0, included) are in the update region,
+    // which ends at column avail
+    int included = 0;
+    long avail = n;
+    int rc = 0;
+    auto include_below = [&](long col_limit, cudaStream_t st, int steps_done, int max_grid) {
+        while (!rc && included < arr->nsb && arr->start[included] < col_limit) {
+            const int c0 = arr->start[included], c1 = arr->start[included + 1];
+            cudaStreamWaitEvent(st, arr->ready[included], 0);
+            // the updates of steps 0 .. steps_done - 1 on the new columns (rows >= c0),
+            // in step order: the lower square of the superblock and the rectangle below
+            for (int i = 0; i < steps_done && !rc; ++i) {
+                const F16Panel pi = panel_of(i);
+                const long r0 = (long)(i + 1) * nb;  // the panel's first row
+                const int kbi = std::min(nb, n - i * nb);
+                const int slot = gb300_prof_begin(st, GB300_PROF_TC_UPDATE);
+                rc = tc_update_f16s(st, c1 - c0, c1 - c0, kbi, rows_of(pi, c0 - r0, ldk), ldk, rows_of(pi, c0 - r0, ldk),
+                                    ldk, nterms, 1, A + c0 + (long)c0 * lda, lda, d_err, 0, max_grid);
+                if (!rc && n > c1)
+                    rc = tc_update_f16s(st, n - c1, c1 - c0, kbi, rows_of(pi, c1 - r0, ldk), ldk,
+                                        rows_of(pi, c0 - r0, ldk), ldk, nterms, 0, A + c1 + (long)c0 * lda, lda, d_err,
+                                        0, max_grid);
+                const double w1 = (double)(c1 - c0);
+                gb300_prof_end(st, slot, (double)nterms * kbi * (w1 * (w1 + 1.0) + 2.0 * (n - c1) * w1),
+                               8.0 * (w1 * (w1 + 1.0) / 2.0 + (double)(n - c1) * w1) + 2.0 * (n - c0) * ldk * np);
+            }
+            ++included;
+        }
+        avail = included < arr->nsb ? arr->start[included] : n;
+    };
+    const int D = arr ? std::max(0, arr->lookahead_blocks) : 0;
+    if (arr) include_below(std::min<long>(n, (long)(2 + D) * nb), s, 0, 0);
+    if (!rc) rc = panel_diag(s, n, A, lda, 0, std::min(nb, n), nb, w, linv_band, d_info, d_err, 0);
+    if (!rc) rc = panel_solve(s, n, A, lda, 0, std::min(nb, n), nb, np, w, panel_of(0), d_err, 0, false);
     if (ready) cudaStreamWaitEvent(s, ready, 0);
     // the diagonal of the matrix (rows past the first tile, which no step has
     // touched yet) and its maxima per column tile: the later panels' row bounds
     if (!rc && n > nb) {
         const int ntiles = (n + nb - 1) / nb;
-        gb300_count_launch(), diag_bounds_kernel<<<ntiles, 256, 0, s>>>(n, A, lda, nb, w.d, w.dtile);
+        gb300_count_launch(), diag_bounds_kernel<<<ntiles, 256, 0, s>>>(n, A, lda, nb, w.d, w.dtile,
+                                                                        arr ? arr->diag : nullptr);
         rc = gb300_last_launch_status();
     }
     if (!rc && on_panel && n > nb) on_panel(s, 0, nb);
-    for (int k0 = 0; k0 < n && !rc; k0 += nb) {
+    int step = 0;
+    for (int k0 = 0; k0 < n && !rc; k0 += nb, ++step) {
         const int kb = std::min(nb, n - k0);
         const int m = n - k0 - kb;
         if (m <= 0) break;
-        const F16Panel &pan = w.pan[buf];
+        const F16Panel pan = panel_of(step);
         const int kb1 = std::min(nb, m);  // width of the next column block
         const int m2 = m - kb1;           // rows and columns beyond it
         float *C11 = A + (k0 + kb) + (long)(k0 + kb) * lda;
@@ -611,37 +674,43 @@ int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void
         gb300_prof_end(s, slot, (double)nterms * kb * ((double)kb1 * (kb1 + 1.0) + 2.0 * m2 * kb1),
                        8.0 * ((double)kb1 * (kb1 + 1.0) / 2.0 + (double)m2 * kb1) + 2.0 * m * ldk * np);
         if (rc) break;
-        const int nbuf = buf ^ 1;
         float *C22 = C11 + kb1 + (long)kb1 * lda;
         const F16Panel pan2 = rows_of(pan, kb1, ldk);
-        // algorithmic work of the trailing triangle, as for one lower update
-        const double f2 = (double)nterms * kb * (double)m2 * (m2 + 1.0);
-        const double b2 = 8.0 * m2 * (m2 + 1.0) / 2.0 + 2.0 * m2 * ldk * np;
+        const F16Panel next = panel_of(step + 1);
+        // the trailing update of this step: the lower triangle of the columns
+        // [k0 + kb + kb1, avail) and, when columns are still to arrive, the
+        // rectangle below it (avail = n: the whole trailing triangle)
+        auto trailing = [&](cudaStream_t st, int max_grid) {
+            if (arr) include_below(std::min<long>(n, (long)(step + 3 + D) * nb), st, step, max_grid);
+            const int ms = (int)(avail - (k0 + kb + kb1));  // columns of the region
+            if (rc || ms <= 0) return;
+            const double f2 = (double)nterms * kb * ((double)ms * (ms + 1.0) + 2.0 * (m2 - ms) * ms);
+            const double b2 = 8.0 * ((double)ms * (ms + 1.0) / 2.0 + (double)(m2 - ms) * ms) + 2.0 * m2 * ldk * np;
+            const int slot2 = gb300_prof_begin(st, GB300_PROF_TC_UPDATE);
+            if (max_grid > 0) gb300_prof_set_share(slot2, (double)max_grid / num_sms());
+            rc = tc_update_f16s(st, ms, ms, kb, pan2, ldk, pan2, ldk, nterms, 1, C22, lda, d_err, 0, max_grid);
+            if (!rc && m2 > ms)
+                rc = tc_update_f16s(st, m2 - ms, ms, kb, rows_of(pan2, ms, ldk), ldk, pan2, ldk, nterms, 0, C22 + ms,
+                                    lda, d_err, 0, max_grid);
+            gb300_prof_end(st, slot2, f2, b2);
+        };
         const int la_sms = lookahead_sms(m2, kb);
         if (m2 > 0 && la && la_sms > 0) {
             cudaEventRecord(la->fork, s);
             cudaStreamWaitEvent(la->s, la->fork, 0);
-            slot = gb300_prof_begin(la->s, GB300_PROF_TC_UPDATE);
-            gb300_prof_set_share(slot, (double)(num_sms() - la_sms) / num_sms());
-            rc = tc_update_f16s(la->s, m2, m2, kb, pan2, ldk, pan2, ldk, nterms, 1, C22, lda, d_err, 0,
-                                num_sms() - la_sms);
-            gb300_prof_end(la->s, slot, f2, b2);
+            trailing(la->s, num_sms() - la_sms);
             cudaEventRecord(la->join, la->s);
             if (!rc) rc = panel_diag(s, n, A, lda, k0 + kb, kb1, nb, w, linv_band, d_info, d_err, la_sms);
-            if (!rc) rc = panel_solve(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, d_err, la_sms);
+            if (!rc) rc = panel_solve(s, n, A, lda, k0 + kb, kb1, nb, np, w, next, d_err, la_sms);
             if (!rc && on_panel) on_panel(s, k0 + kb, kb1);
             cudaStreamWaitEvent(s, la->join, 0);  // joined before step k+1's update
         } else {
-            if (m2 > 0) {
-                slot = gb300_prof_begin(s, GB300_PROF_TC_UPDATE);
-                rc = tc_update_f16s(s, m2, m2, kb, pan2, ldk, pan2, ldk, nterms, 1, C22, lda, d_err);
-                gb300_prof_end(s, slot, f2, b2);
-            }
+            if (m2 > 0) trailing(s, 0);
+            else if (arr) include_below(n, s, step, 0);
             if (!rc) rc = panel_diag(s, n, A, lda, k0 + kb, kb1, nb, w, linv_band, d_info, d_err, 0);
-            if (!rc) rc = panel_solve(s, n, A, lda, k0 + kb, kb1, nb, np, w, nbuf, d_err, 0);
+            if (!rc) rc = panel_solve(s, n, A, lda, k0 + kb, kb1, nb, np, w, next, d_err, 0);
             if (!rc && on_panel && m2 > 0) on_panel(s, k0 + kb, kb1);
         }
-        buf = nbuf;
         if (!side_done && m2 <= side_rows) {
             side(s);
             side_done = true;

@@ -2,6 +2,7 @@
 // layer (not part of the public C-ABI).
 #pragma once
 #include <cuda_runtime.h>
+#include <functional>
 #include "starpu_gb300_kernels.h"
 #include "starpu_gb300_solver.h"
 
@@ -20,10 +21,32 @@ int residual_tc(cudaStream_t s, int n, int nrhs, const void *a_slices, const dou
                 const unsigned long long *anorm_bits, int kchunk, void *xs, double *partials, int *d_err);
 
 
+// Columns of the matrix arriving while the tensor-core factorisation runs
+// (the host-buffer solve gathers A over the host link superblock by
+// superblock): superblock s holds columns [start[s], start[s + 1]) of W (rows
+// >= start[s]) once ready[s] has completed; diag is the diagonal of A (n
+// floats), complete before the factorisation starts; panel_store holds every
+// step's split panel (tc_arrival_store_bytes), which the updates of columns
+// that arrive late replay in step order.  The result is bit-identical to
+// the factorisation of the whole matrix.
+struct TcArrival {
+    int nsb = 0;
+    const int *start = nullptr;
+    const cudaEvent_t *ready = nullptr;
+    const float *diag = nullptr;
+    void *panel_store = nullptr;
+    int lookahead_blocks = 2;  // superblocks are taken in this many column blocks ahead of need
+};
+size_t tc_arrival_store_bytes(int n, int nb);
+int potrf_tc(cudaStream_t s, int n, float *A, long lda, int nb, int nterms, void *panel, int *d_info, int *d_err,
+             float *linv_band, const std::function<void(cudaStream_t)> &side, int side_rows,
+             const std::function<void(cudaStream_t, int, int)> &on_panel, cudaEvent_t ready,
+             const TcArrival *arr = nullptr);
+
 // the two phases of starpu_gb300_dsposv (capi_solver.cu)
 // prepared: W (FP32 lower A) and max |A_ij| are already in the workspace
 int dsposv_factor(cudaStream_t s, int n, int nrhs, const double *A, int lda, int nb, int nterms, void *work,
-                  starpu_gb300_ir_info *out, bool prepared = false);
+                  starpu_gb300_ir_info *out, bool prepared = false, const TcArrival *arr = nullptr);
 // the workspace regions the host path's fused gather writes: W (n x n FP32)
 // and the word that receives max |A_ij| (zeroed with its three neighbours)
 void dsposv_prepared_targets(int n, int nrhs, int nb, void *work, float **W, unsigned long long **amax_block);
@@ -37,7 +60,7 @@ int dsposv_fp64(cudaStream_t s, int n, int nrhs, const double *A, int lda, const
 // factor + refinement, then the FP64 fallback when either fails
 int dsposv_ladder(cudaStream_t s, int n, int nrhs, const double *A, int lda, const double *B, int ldb, double *X,
                   int ldx, int nb, int nterms, double tol, int max_iter, void *work, starpu_gb300_ir_info *out,
-                  bool prepared);
+                  bool prepared, const TcArrival *arr = nullptr);
 
 // The mixed solve's schedule for one tile size, from starpu_gb300_dense_autotune,
 // stored in the tuning table beside the perfmodels (capi_batched.cu).

@@ -157,18 +157,30 @@ __device__ int bat_factor(float *W, int n, float *smem)
         const int wr = 16 * (warp & 3), wc = 32 * (warp >> 2);
         for (int tj = 0; tj < nt; ++tj) {
             // stage the panel rows of tile column tj once per column
+#pragma unroll 4
             for (int idx = tid; idx < kp * BAT_TILE; idx += BAT_THREADS) {
                 const int rr = idx % BAT_TILE, p = idx / BAT_TILE;
                 const int row = r0 + tj * BAT_TILE + rr;
                 Bs[p * BAT_TP + rr] = (p < kb && row < n) ? W[row + (long)(k0 + p) * n] : 0.0f;
             }
             for (int ti2 = tj; ti2 < nt; ++ti2) {
+#pragma unroll 4
                 for (int idx = tid; idx < kp * BAT_TILE; idx += BAT_THREADS) {
                     const int rr = idx % BAT_TILE, p = idx / BAT_TILE;
                     const int row = r0 + ti2 * BAT_TILE + rr;
                     As[p * BAT_TP + rr] = (p < kb && row < n) ? W[row + (long)(k0 + p) * n] : 0.0f;
                 }
                 __syncthreads();
+                // this thread's 16 elements of the tile, loaded before the products
+                float cv[4][4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int col = r0 + tj * BAT_TILE + wc + 8 * j + 2 * t4 + (q & 1);
+                        const int row = r0 + ti2 * BAT_TILE + wr + g + 8 * (q >> 1);
+                        cv[j][q] = (col < n && row < n && row >= col) ? W[row + (long)col * n] : 0.0f;
+                    }
                 float acc[4][4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
@@ -197,7 +209,7 @@ __device__ int bat_factor(float *W, int n, float *smem)
                     for (int q = 0; q < 4; ++q) {
                         const int col = r0 + tj * BAT_TILE + wc + 8 * j + 2 * t4 + (q & 1);
                         const int row = r0 + ti2 * BAT_TILE + wr + g + 8 * (q >> 1);
-                        if (col < n && row < n && row >= col) W[row + (long)col * n] -= acc[j][q];
+                        if (col < n && row < n && row >= col) W[row + (long)col * n] = cv[j][q] - acc[j][q];
                     }
                 __syncthreads();
             }
@@ -210,109 +222,104 @@ __device__ int bat_factor(float *W, int n, float *smem)
 // --------------------------------------------------------------- solves
 // Mirror the factor into the upper triangle of W (W[j, i] = L[i, j]) so that
 // both sweeps below read contiguous columns.
-__device__ void bat_mirror_upper(float *W, int n)
+__device__ void bat_mirror_upper(float *W, int n, float *smem)
 {
-    for (long idx = threadIdx.x; idx < (long)n * n; idx += BAT_THREADS) {
-        const int i = (int)(idx % n), j = (int)(idx / n);  // write (i, j) with i < j from (j, i)
-        if (i < j) W[i + (long)j * n] = W[j + (long)i * n];
+    // 32 x 32 tiles below the diagonal, transposed through shared memory so
+    // that both the reads (down the columns of L) and the writes (down the
+    // columns of the upper part) are coalesced; 8 warps, one tile row each
+    float(*T)[33] = reinterpret_cast<float(*)[33]>(smem) + (threadIdx.x >> 5) * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nt = (n + 31) / 32;
+    for (int t = warp; t < nt * (nt + 1) / 2; t += BAT_THREADS / 32) {
+        int ti = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+        while (ti * (ti + 1) / 2 > t) --ti;
+        while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+        const int tj = t - ti * (ti + 1) / 2;  // tile (ti, tj), tj <= ti
+        const int r0 = 32 * ti, c0 = 32 * tj;
+        for (int c = 0; c < 32; ++c)
+            T[c][lane] = (r0 + lane < n && c0 + c < n) ? W[r0 + lane + (long)(c0 + c) * n] : 0.0f;
+        __syncwarp();
+        // W(c0 + lane, r0 + r) = L(r0 + r, c0 + lane) for c0 + lane < r0 + r
+        for (int r = 0; r < 32; ++r)
+            if (r0 + r < n && c0 + lane < n && c0 + lane < r0 + r) W[c0 + lane + (long)(r0 + r) * n] = T[lane][r];
+        __syncwarp();
     }
     __syncthreads();
 }
 
 // Y (n x nrhs, ld n) <- L^-T L^-1 Y, in blocks of 32 columns.  Per block,
-// warp 0 solves the 32 x 32 diagonal block (lane = row, the solved entry
-// broadcast by shuffles), then every thread updates its rows outside the
-// block with the block's 32 columns of L (forward) or of L^T (backward, read
-// from the mirrored upper triangle); both reads are contiguous along the rows
-// the threads own.  Each row sees its updates in the same column order as a
-// column-by-column substitution, with two barriers per 32 columns.
-__device__ void bat_potrs(const float *W, int n, float *Y, int nrhs)
+// the 32 x 32 diagonal block is staged in shared memory (coalesced) and warp
+// 0 solves it (lane = row, the solved entry broadcast by shuffles) into
+// shared memory; then every thread updates its rows outside the block with
+// the block's 32 columns of L (forward) or of L^T (backward, read from the
+// mirrored upper triangle), all 32 loads of a row in flight at once.  Each
+// row sees its updates in the same column order as a column-by-column
+// substitution.
+__device__ void bat_potrs(const float *W, int n, float *Y, int nrhs, float *smem)
 {
     const int tid = threadIdx.x, lane = tid & 31;
-    // forward: L y = b
-    for (int j0 = 0; j0 < n; j0 += 32) {
-        const int jb = min(32, n - j0);
-        if (tid < 32) {
-            float y[BAT_MAXRHS];
-#pragma unroll
-            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = (c < nrhs && lane < jb) ? Y[j0 + lane + (long)c * n] : 0.0f;
-            for (int j = 0; j < jb; ++j) {
-                const float l = lane < jb ? W[j0 + lane + (long)(j0 + j) * n] : 0.0f;  // L[j0 + lane, j0 + j]
-                if (lane == j) {
-#pragma unroll
-                    for (int c = 0; c < BAT_MAXRHS; ++c) y[c] /= l;
-                }
-#pragma unroll
-                for (int c = 0; c < BAT_MAXRHS; ++c) {
-                    const float yj = __shfl_sync(0xffffffffu, y[c], j);
-                    if (lane > j) y[c] = fmaf(-l, yj, y[c]);
-                }
+    float(*D)[33] = reinterpret_cast<float(*)[33]>(smem);  // D[c][r] = block (r, c)
+    float *ys = smem + 32 * 33;                             // ys[j * BAT_MAXRHS + c]: the solved block
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool fwd = pass == 0;
+        const int nblk = (n + 31) / 32;
+        for (int bb = 0; bb < nblk; ++bb) {
+            const int j0 = fwd ? 32 * bb : 32 * (nblk - 1 - bb), jb = min(32, n - j0);
+            // stage the diagonal block (forward: L, backward: the mirrored U = L^T)
+            for (int e = tid; e < 32 * 32; e += BAT_THREADS) {
+                const int r = e & 31, c = e >> 5;
+                D[c][r] = (r < jb && c < jb) ? W[j0 + r + (long)(j0 + c) * n] : 0.0f;
             }
-            if (lane < jb) {
+            __syncthreads();
+            if (tid < 32) {
+                float y[BAT_MAXRHS];
 #pragma unroll
                 for (int c = 0; c < BAT_MAXRHS; ++c)
-                    if (c < nrhs) Y[j0 + lane + (long)c * n] = y[c];
-            }
-        }
-        __syncthreads();
-        for (int i = j0 + jb + tid; i < n; i += BAT_THREADS) {
-            float y[BAT_MAXRHS];
+                    y[c] = (c < nrhs && lane < jb) ? Y[j0 + lane + (long)c * n] : 0.0f;
+                for (int q = 0; q < jb; ++q) {
+                    const int j = fwd ? q : jb - 1 - q;
+                    const float l = D[j][lane];  // (lane, j) of the block
+                    if (lane == j) {
 #pragma unroll
-            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = c < nrhs ? Y[i + (long)c * n] : 0.0f;
-            for (int j = 0; j < jb; ++j) {
-                const float l = W[i + (long)(j0 + j) * n];
+                        for (int c = 0; c < BAT_MAXRHS; ++c) y[c] /= l;
+                    }
 #pragma unroll
-                for (int c = 0; c < BAT_MAXRHS; ++c)
-                    if (c < nrhs) y[c] = fmaf(-l, Y[j0 + j + (long)c * n], y[c]);
-            }
-#pragma unroll
-            for (int c = 0; c < BAT_MAXRHS; ++c)
-                if (c < nrhs) Y[i + (long)c * n] = y[c];
-        }
-        __syncthreads();
-    }
-    // backward: L^T x = y, U = L^T read from the mirrored upper triangle
-    // (U[i, j] = W[i + j n] for i < j)
-    for (int j1 = n; j1 > 0; j1 -= 32) {
-        const int j0 = max(0, j1 - 32), jb = j1 - j0;
-        if (tid < 32) {
-            float y[BAT_MAXRHS];
-#pragma unroll
-            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = (c < nrhs && lane < jb) ? Y[j0 + lane + (long)c * n] : 0.0f;
-            for (int j = jb - 1; j >= 0; --j) {
-                const float u = lane < jb ? W[j0 + lane + (long)(j0 + j) * n] : 0.0f;  // U[j0 + lane, j0 + j]
-                if (lane == j) {
-#pragma unroll
-                    for (int c = 0; c < BAT_MAXRHS; ++c) y[c] /= u;
+                    for (int c = 0; c < BAT_MAXRHS; ++c) {
+                        const float yj = __shfl_sync(0xffffffffu, y[c], j);
+                        if (fwd ? lane > j : lane < j) y[c] = fmaf(-l, yj, y[c]);
+                    }
                 }
+                if (lane < jb) {
 #pragma unroll
-                for (int c = 0; c < BAT_MAXRHS; ++c) {
-                    const float yj = __shfl_sync(0xffffffffu, y[c], j);
-                    if (lane < j) y[c] = fmaf(-u, yj, y[c]);
+                    for (int c = 0; c < BAT_MAXRHS; ++c) {
+                        ys[lane * BAT_MAXRHS + c] = y[c];
+                        if (c < nrhs) Y[j0 + lane + (long)c * n] = y[c];
+                    }
                 }
             }
-            if (lane < jb) {
+            __syncthreads();
+            // rows outside the block: below it (forward) or above it (backward)
+            const int i_lo = fwd ? j0 + jb : 0, i_hi = fwd ? n : j0;
+            for (int i = i_lo + tid; i < i_hi; i += BAT_THREADS) {
+                float l[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) l[q] = q < jb ? W[i + (long)(j0 + q) * n] : 0.0f;
+                float y[BAT_MAXRHS];
+#pragma unroll
+                for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = c < nrhs ? Y[i + (long)c * n] : 0.0f;
+#pragma unroll
+                for (int q = 0; q < 32; ++q) {
+                    const int j = fwd ? q : 31 - q;
+                    if (j < jb) {
+#pragma unroll
+                        for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = fmaf(-l[j], ys[j * BAT_MAXRHS + c], y[c]);
+                    }
+                }
 #pragma unroll
                 for (int c = 0; c < BAT_MAXRHS; ++c)
-                    if (c < nrhs) Y[j0 + lane + (long)c * n] = y[c];
+                    if (c < nrhs) Y[i + (long)c * n] = y[c];
             }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int i = tid; i < j0; i += BAT_THREADS) {
-            float y[BAT_MAXRHS];
-#pragma unroll
-            for (int c = 0; c < BAT_MAXRHS; ++c) y[c] = c < nrhs ? Y[i + (long)c * n] : 0.0f;
-            for (int j = jb - 1; j >= 0; --j) {
-                const float u = W[i + (long)(j0 + j) * n];
-#pragma unroll
-                for (int c = 0; c < BAT_MAXRHS; ++c)
-                    if (c < nrhs) y[c] = fmaf(-u, Y[j0 + j + (long)c * n], y[c]);
-            }
-#pragma unroll
-            for (int c = 0; c < BAT_MAXRHS; ++c)
-                if (c < nrhs) Y[i + (long)c * n] = y[c];
-        }
-        __syncthreads();
     }
 }
 
@@ -358,14 +365,22 @@ __device__ void bat_residual_df(const double *A, int n, const double *X, const d
         }
         for (int j0 = 0; j0 < n; j0 += 128) {
             const int j1 = min(n, j0 + 128);
-            for (int j = j0; j < j1; ++j) {
-                const float2 av = df_split_scaled(A[i + (long)j * n], ea);
+            for (int j = j0; j < j1; j += 8) {
+                // eight loads of the row in flight before their products
+                double av8[8];
 #pragma unroll
-                for (int c = 0; c < BAT_MAXRHS; ++c)
-                    if (c < nrhs) {
-                        const float2 xv = Xs[j * nrhs + c];
-                        df_mac(sh[c], sl[c], av.x, av.y, xv.x, xv.y);
-                    }
+                for (int u = 0; u < 8; ++u) av8[u] = j + u < j1 ? A[i + (long)(j + u) * n] : 0.0;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    if (j + u >= j1) break;
+                    const float2 av = df_split_scaled(av8[u], ea);
+#pragma unroll
+                    for (int c = 0; c < BAT_MAXRHS; ++c)
+                        if (c < nrhs) {
+                            const float2 xv = Xs[(j + u) * nrhs + c];
+                            df_mac(sh[c], sl[c], av.x, av.y, xv.x, xv.y);
+                        }
+                }
             }
 #pragma unroll
             for (int c = 0; c < BAT_MAXRHS; ++c)
@@ -410,10 +425,15 @@ __global__ void __launch_bounds__(BAT_THREADS, 2) batched_dposv_kernel(BatchedAr
         double rowmax = 0.0;
         for (int i = tid; i < n; i += BAT_THREADS) {
             double s = 0.0;
-            for (int j = 0; j < n; ++j) {
-                const double v = A[i + (long)j * n];
-                s += fabs(v);
-                if (i >= j) W[i + (long)j * n] = (float)v;
+            for (int j = 0; j < n; j += 8) {
+                double v8[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v8[u] = j + u < n ? A[i + (long)(j + u) * n] : 0.0;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    s += fabs(v8[u]);
+                    if (j + u < n && i >= j + u) W[i + (long)(j + u) * n] = (float)v8[u];
+                }
             }
             rowmax = fmax(rowmax, s);
         }
@@ -439,11 +459,11 @@ __global__ void __launch_bounds__(BAT_THREADS, 2) batched_dposv_kernel(BatchedAr
             __syncthreads();
             continue;
         }
-        bat_mirror_upper(W, n);
+        bat_mirror_upper(W, n, bat_smem);
         // initial solve
         for (int idx = tid; idx < n * nrhs; idx += BAT_THREADS) Y[idx] = (float)B[idx];
         __syncthreads();
-        bat_potrs(W, n, Y, nrhs);
+        bat_potrs(W, n, Y, nrhs, bat_smem);
         for (int idx = tid; idx < n * nrhs; idx += BAT_THREADS) X[idx] = (double)Y[idx];
         __syncthreads();
         int it = 0;
@@ -510,7 +530,7 @@ __global__ void __launch_bounds__(BAT_THREADS, 2) batched_dposv_kernel(BatchedAr
             __syncthreads();
             for (int idx = tid; idx < n * nrhs; idx += BAT_THREADS) Y[idx] = (float)R[idx];
             __syncthreads();
-            bat_potrs(W, n, Y, nrhs);
+            bat_potrs(W, n, Y, nrhs, bat_smem);
             for (int idx = tid; idx < n * nrhs; idx += BAT_THREADS) X[idx] += (double)Y[idx];
             __syncthreads();
         }
