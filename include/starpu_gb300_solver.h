@@ -92,6 +92,13 @@ typedef struct starpu_gb300_solver starpu_gb300_solver;
 starpu_gb300_solver *starpu_gb300_solver_create(int n_max, int nrhs_max, int nb, int nterms);
 int starpu_gb300_solver_destroy(starpu_gb300_solver *solver);
 void *starpu_gb300_solver_stream(starpu_gb300_solver *solver);
+/* Pinned-input path of _dsposv_host: 1 gathers A superblock by superblock
+ * while the factorisation starts on the first columns (bit-identical
+ * result, more device memory: every step's split panel is kept), 0 gathers
+ * the whole matrix first; -1 (the default) follows
+ * STARPU_GB300_HOST_OVERLAP=1 (otherwise off).  Returns the previous
+ * setting. */
+int starpu_gb300_solver_host_overlap(starpu_gb300_solver *solver, int on);
 int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *solver, int n, int nrhs, const double *A, int lda,
                                     const double *B, int ldb, double *X, int ldx, double tol, int max_iter,
                                     starpu_gb300_ir_info *info);

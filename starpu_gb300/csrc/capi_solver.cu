@@ -1174,6 +1174,7 @@ struct starpu_gb300_solver {
     void *panels = nullptr;
     float *diag = nullptr;
     bool overlap_failed = false;
+    int overlap = -1;  // -1: STARPU_GB300_HOST_OVERLAP decides
 };
 
 starpu_gb300_solver *starpu_gb300_solver_create(int n_max, int nrhs_max, int nb, int nterms)
@@ -1218,6 +1219,14 @@ int starpu_gb300_solver_destroy(starpu_gb300_solver *h)
 
 void *starpu_gb300_solver_stream(starpu_gb300_solver *h) { return h ? (void *)h->stream : nullptr; }
 
+int starpu_gb300_solver_host_overlap(starpu_gb300_solver *h, int on)
+{
+    if (!h) return GB300_EINVAL;
+    const int prev = h->overlap;
+    if (on >= 0) h->overlap = on ? 1 : 0;
+    return prev;
+}
+
 // column panel width of the host-to-device copy of A's lower triangle
 static constexpr int HOST_PANEL = 512;
 
@@ -1228,11 +1237,10 @@ static constexpr int HOST_PANEL = 512;
 // convert_lower_max_kernel computes -- so the host path reads A over the link
 // once and the factor phase skips its own conversion.  16-byte loads, four in
 // flight per thread.
-__global__ void __launch_bounds__(256) gather_convert_kernel(int n, const double *__restrict__ H, long ldh,
-                                                             double *__restrict__ D, long ldd, float *__restrict__ W,
-                                                             long ldw, unsigned long long *amax_bits, int j0 = 0)
+__device__ __forceinline__ void gather_convert_column(int n, const double *__restrict__ H, long ldh,
+                                                      double *__restrict__ D, long ldd, float *__restrict__ W,
+                                                      long ldw, unsigned long long *amax_bits, long j)
 {
-    const long j = j0 + (long)blockIdx.x;
     const double *src = H + j * ldh;
     double *dst = D + j * ldd;
     float *w = W + j * ldw;
@@ -1281,6 +1289,19 @@ __global__ void __launch_bounds__(256) gather_convert_kernel(int n, const double
     }
 }
 
+__global__ void __launch_bounds__(256) gather_convert_kernel(int n, const double *__restrict__ H, long ldh,
+                                                             double *__restrict__ D, long ldd, float *__restrict__ W,
+                                                             long ldw, unsigned long long *amax_bits, int j0 = 0,
+                                                             int j1 = -1)
+{
+    // one column per CTA (j1 < 0), or columns j0 + blockIdx.x, + gridDim.x, ... below j1
+    const int jend = j1 < 0 ? j0 + (int)gridDim.x : j1;
+    for (long j = j0 + (long)blockIdx.x; j < jend; j += gridDim.x) {
+        gather_convert_column(n, H, ldh, D, ldd, W, ldw, amax_bits, j);
+        __syncthreads();  // the column's reduction buffer is free
+    }
+}
+
 // d[i] = fp32(A_ii) from the mapped host matrix (the factorisation's row
 // bounds need the whole diagonal before the columns have arrived)
 __global__ void gather_diag_kernel(int n, const double *__restrict__ H, long ldh, float *__restrict__ d)
@@ -1314,18 +1335,24 @@ static const double *device_view_of_pinned_matrix(const double *A, int n, int ld
     return d1 == d0 + last ? d0 : nullptr;
 }
 
-// The overlapped gather needs a copy stream, one event per superblock, a
-// store for every step's split panel and the diagonal, allocated once for
-// n_max; it applies to the tensor-core path with a lookahead (n > 2 nb) and
-// tile sizes the diagonal-tile kernel handles.  STARPU_GB300_HOST_OVERLAP=0
-// turns it off (the whole matrix is gathered before the factorisation).
+// The overlapped gather (STARPU_GB300_HOST_OVERLAP=1; off by default) needs
+// a copy stream, one event per superblock, a store for every step's split
+// panel and the diagonal, allocated once for n_max; it applies to the
+// tensor-core path with a lookahead (n > 2 nb) and tile sizes the
+// diagonal-tile kernel handles.  Measured at n = 32768 it is slower than
+// gathering first (104-111 ms against 91 ms per host-buffer solve): the early
+// steps, their updates cut to the columns that have arrived, lose the overlap
+// of the diagonal tile with a large update, and the replays of the late
+// columns crowd the lookahead stream.
+static constexpr int GATHER_CTAS = 48;
 static bool overlap_ready(starpu_gb300_solver *h, int n, int nb)
 {
-    static const bool off = [] {
+    static const bool env_on = [] {
         const char *e = getenv("STARPU_GB300_HOST_OVERLAP");
-        return e && !strcmp(e, "0");
+        return e && !strcmp(e, "1");
     }();
-    if (off || h->overlap_failed || n <= 2 * nb || nb > GB300_DIAG_TILE_MAX || h->nterms != 3) return false;
+    const bool on = h->overlap >= 0 ? h->overlap != 0 : env_on;
+    if (!on || h->overlap_failed || n <= 2 * nb || nb > GB300_DIAG_TILE_MAX || h->nterms != 3) return false;
     if (!h->copy) {
         const int nsb_max = (h->n_max + 2 * nb - 1) / (2 * nb);
         bool ok = cudaStreamCreateWithFlags(&h->copy, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1384,8 +1411,11 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
             cudaStreamWaitEvent(h->copy, h->fork, 0);
             gb300_count_launch(), gather_diag_kernel<<<(n + 255) / 256, 256, 0, h->copy>>>(n, mapped, lda, h->diag);
             for (int q = 0; q < nsb; ++q) {
-                gb300_count_launch(), gather_convert_kernel<<<starts[q + 1] - starts[q], 256, 0, h->copy>>>(
-                    n, mapped, lda, h->A, n, W, n, amax + 2, starts[q]);
+                // a few CTAs, each with its columns' loads in flight: they reach the
+                // link rate and fit beside the factorisation's kernels on their SMs
+                gb300_count_launch(), gather_convert_kernel<<<std::min(GATHER_CTAS, starts[q + 1] - starts[q]), 256, 0,
+                                                              h->copy>>>(n, mapped, lda, h->A, n, W, n, amax + 2,
+                                                                         starts[q], starts[q + 1]);
                 cudaEventRecord(h->ready[q], h->copy);
             }
             arr.nsb = nsb;

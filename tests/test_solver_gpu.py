@@ -225,13 +225,17 @@ def test_solver_context_host_buffers_match_device_call(gpu, oracle):
         gpu.starpu_gb300_solver_destroy(h)
 
 
-@pytest.mark.parametrize("n", [900, 777])
-def test_solver_context_pinned_host_buffers(gpu, oracle, n):
+@pytest.mark.parametrize("overlap", [0, 1])
+@pytest.mark.parametrize("n,nb", [(900, 256), (777, 256), (2600, 128)])
+def test_solver_context_pinned_host_buffers(gpu, oracle, n, nb, overlap):
     """Pinned host input: the context reads A's lower triangle with a gather
     kernel instead of copies, writing the factor phase's FP32 copy and max
-    |A_ij| on the way (odd n: columns start off 16-byte boundaries); the
-    solution is bit-identical to the device call."""
-    nrhs, nb = 4, 256
+    |A_ij| on the way (odd n: columns start off 16-byte boundaries).  With
+    the overlap on, the gather runs superblock by superblock beside the
+    factorisation, whose updates of the late columns replay the stored
+    panels in step order.  Either way the solution is bit-identical to the
+    device call."""
+    nrhs = 4
     A = np.asfortranarray(oracle.spd_gram(n, 47, 0.5))
     B = np.asfortranarray(oracle.uniform_rhs(n, nrhs, 48))
     hA = gpu.starpu_gb300_host_malloc_pinned(8 * n * n)
@@ -239,6 +243,7 @@ def test_solver_context_pinned_host_buffers(gpu, oracle, n):
     hX = gpu.starpu_gb300_host_malloc_pinned(8 * n * nrhs)
     h = gpu.starpu_gb300_solver_create(n, nrhs, nb, 3)
     assert hA and hB and hX and h
+    gpu.starpu_gb300_solver_host_overlap(h, overlap)
     try:
         C.memmove(hA, A.ctypes.data, 8 * n * n)
         C.memmove(hB, B.ctypes.data, 8 * n * nrhs)
