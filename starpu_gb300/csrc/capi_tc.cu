@@ -367,11 +367,14 @@ static_assert(DC_MAXN == GB300_DIAG_TILE_MAX, "one limit for the diagonal-tile k
 static int diag_factor_inverse(cudaStream_t s, int n, float *A, long lda, float *Linv, long ldi, float *T,
                                unsigned *bar, int *info, int info_base, int *err, bool invert, int max_sms = 0)
 {
-    static int occ = -1;
-    if (occ < 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, diag_coop_kernel, DC_T, 0) != cudaSuccess) {
-        cudaGetLastError();
-        occ = 1;
-    }
+    static const int occ = [] {
+        int o = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, diag_coop_kernel, DC_T, 0) != cudaSuccess) {
+            cudaGetLastError();
+            o = 1;
+        }
+        return o;
+    }();
     // widest phase: block rows + inverse combines (A), tile updates +
     // inverse products (B), the last row's products
     const int nblk = (n + DC_B - 1) / DC_B;
@@ -459,14 +462,15 @@ double g_trial_rate = 0, g_trial_tdiag = 0, g_trial_panel = 0;
 
 static int lookahead_sms(int m2, int kb)
 {
-    static int fixed = -2;
-    static double panel_rate_env = 0.4;
-    if (fixed == -2) {
+    // read once (function-local statics initialise thread-safely)
+    static const int fixed = [] {
         const char *e = getenv("GB300_LOOKAHEAD_SMS");
-        fixed = e && *e ? std::max(0, atoi(e)) : -1;
+        return e && *e ? std::max(0, atoi(e)) : -1;
+    }();
+    static const double panel_rate_env = [] {
         const char *r = getenv("GB300_PANEL_RATE");
-        if (r && *r && atof(r) > 0.0) panel_rate_env = atof(r);
-    }
+        return (r && *r && atof(r) > 0.0) ? atof(r) : 0.4;
+    }();
     const int S = num_sms();
     if (fixed >= 0) return fixed >= S ? 0 : fixed;
     double rate = 1.45e15, t_diag = 0.75e-3, panel_rate = panel_rate_env;
