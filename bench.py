@@ -7,7 +7,8 @@ mixed precision vs plain FP64, on one GB300 per process.
 Workload (one "step" = one full solve through the C-ABI, inputs resident in HBM):
   mixed-precision SPD solve, N=32768, tile 1024, A = B B^T / N + alpha I
   (B iid N(0,1), alpha set for kappa = 1e4), 16 right-hand sides U[-1,1];
-  split-BF16 tcgen05 factorisation + FP64 iterative refinement to 1e-12.
+  tcgen05 factorisation on row-scaled FP16 split operands + FP64 iterative
+  refinement to 1e-12.
   flops = N^3/3 + 2 N^2 nrhs (FP64-equivalent, LAPACK dsposv convention).
 Beside it, in the same run: the plain FP64 GPU solve (dposv) of the same
 system and of the FP64 config N=16384 / tile 512 / 64 RHS, a kappa sweep
@@ -282,7 +283,7 @@ def bench_config(args, world, n=None, nb=None):
     """The workload both arms name: the mixed-precision solve's configuration."""
     n, nb = n or args.n, nb or args.nb
     return {"workload": f"SPD solve, N={n}, tile {nb}, A=B*B^T/N+alpha*I (kappa={args.kappa:g}), {args.nrhs} RHS "
-                        f"U[-1,1], to backward error <= 1e-12 (GPU: split-BF16 tcgen05 factor + FP64 iterative "
+                        f"U[-1,1], to backward error <= 1e-12 (GPU: scaled-FP16 split tcgen05 factor + FP64 iterative "
                         f"refinement)",
             "n": n, "nb": nb, "nrhs": args.nrhs, "kappa": args.kappa,
             "l2": "inputs larger than L2 (A is 8 GiB FP64 at N=32768; L2 129 MB)",

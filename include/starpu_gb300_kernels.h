@@ -221,14 +221,14 @@ int starpu_gb300_tile_tc_prepare(void);
 int starpu_gb300_sgemm_nt_tile_tc(void *stream, int m, int n, int k, const float *A, int lda, const float *B,
                                   int ldb, float *C, int ldc, int lower, void *work, size_t lwork, int *d_err);
 
-/* Bytes of BF16 panel workspace starpu_gb300_spotrf_tc needs. */
+/* Bytes of split-panel workspace starpu_gb300_spotrf_tc needs. */
 size_t starpu_gb300_spotrf_tc_workspace(int n, int nb);
 
 /* Tiled Cholesky of an FP32 matrix (tile nb): FP32 POTRF of the diagonal
- * tile (CUDA cores), its explicit inverse, the panel TRSM as one split-BF16
+ * tile (CUDA cores), its explicit inverse, the panel TRSM as one split
  * tensor-core product P * L_kk^-T, and the trailing update on the tensor
- * cores with the panel split to BF16 (nterms 1 or 3, as in
- * starpu_gb300_tc_update). */
+ * cores with the panel split per row to FP16 h + l scaled by a power of two
+ * (nterms 3, ~22 bits; nterms 1: plain BF16 operands). */
 int starpu_gb300_spotrf_tc(void *stream, int n, float *A, int lda, int nb, int nterms, void *work, size_t lwork,
                            int *d_info, int *d_err);
 

@@ -4,7 +4,7 @@
 // examples/cholesky/cholesky_kernels.c:53-55).
 //
 //   W = fp32(A)                       (lower triangle, fused with ||A||_inf)
-//   W = L L^T                         tensor-core tiled Cholesky (split-BF16)
+//   W = L L^T                         tensor-core tiled Cholesky (scaled-FP16 split)
 //   x = fp64(L^-T L^-1 fp32(b))
 //   repeat: r = b - A x   (FP64)      backward error ||r||/(||A|| ||x|| + ||b||)
 //           x += fp64(L^-T L^-1 fp32(r))
@@ -497,7 +497,7 @@ __global__ void copy_lower_f64_kernel(int n, const double *__restrict__ A, long 
 
 struct SolverWs {
     float *W;              // n x n FP32 working factor (ld = n)
-    void *panel;           // split-BF16 panels
+    void *panel;           // split panels of the tensor-core factorisation
     double *R;             // n x nrhs FP64 residual
     float *Y;              // n x nrhs FP32 right-hand side / correction
     void *sweep;           // inverted 64 x 64 diagonal blocks + flags of the 64-row POTRS sweeps

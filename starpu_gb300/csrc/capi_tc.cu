@@ -1,5 +1,5 @@
 // Host side of the tensor-core trailing update: TMA descriptor encoding, the
-// FP32 -> split-BF16 (K-major) panel converter, and the C-ABI entry points
+// FP32 -> split (K-major; BF16, or FP16 with row scales) panel converters, and the C-ABI entry points
 // that use them (the bare update, and the tiled factorisation whose trailing
 // updates run on the tensor cores).
 #include <cuda.h>
