@@ -185,6 +185,12 @@ unsigned long long starpu_gb300_set_wait_budget_ns(unsigned long long ns);
  * Needs no GPU; returns 0 on success, else the number of the failing step. */
 int starpu_gb300_selftest_attr_book(void);
 
+/* Host-only self-check of the tile sweeps' task order (starpu_gb300_spotrs_inv_tiles
+ * and the mixed solve's correction solves) for ntiles tile rows of spt slabs:
+ * every ticket maps to one task and every dependency has a smaller ticket.
+ * Needs no GPU; returns 0 on success. */
+int starpu_gb300_selftest_sweep_tickets(int ntiles, int spt);
+
 /* ---------------- tensor-core trailing update (tcgen05, sm_103a) ---------- */
 
 /* P (m x k FP32, column-major, ldp) -> hi = bf16(P), lo = bf16(P - hi), both

@@ -1469,6 +1469,39 @@ int starpu_gb300_solver_dsposv_host(starpu_gb300_solver *h, int n, int nrhs, con
     return status;
 }
 
+// Host check of the tile sweeps' ticket order for ntiles tile rows of spt
+// slabs: every ticket decodes to one task, each task appears once, and every
+// task a ticket waits for has a smaller ticket -- a product of tile row u with
+// earlier row v waits for all spt diagonal tasks of v, a diagonal task of row
+// u for all u spt products of u.  With at least spt CTAs taking tickets in
+// order, that makes the sweeps deadlock-free.  0 on success.
+int starpu_gb300_selftest_sweep_tickets(int ntiles, int spt)
+{
+    if (ntiles <= 0 || spt <= 0) return -1;
+    const unsigned total = (unsigned)((size_t)spt * ntiles * (ntiles + 1) / 2);
+    std::vector<int> diag_done(ntiles, 0), prod_done(ntiles, 0);
+    std::vector<char> seen((size_t)ntiles * (ntiles + 1) * spt, 0);
+    for (unsigned t = 0; t < total; ++t) {
+        int u;
+        unsigned r;
+        tsw_decode(t, spt, u, r);
+        if (u < 0 || u >= ntiles || r >= (unsigned)((u + 1) * spt)) return 1;
+        char &mark = seen[((size_t)u * (ntiles + 1) + r / spt) * spt + r % spt];
+        if (mark) return 2;
+        mark = 1;
+        if (r < (unsigned)(u * spt)) {
+            if (diag_done[r / spt] != spt) return 3;
+            ++prod_done[u];
+        } else {
+            if (prod_done[u] != u * spt) return 4;
+            ++diag_done[u];
+        }
+    }
+    for (int u = 0; u < ntiles; ++u)
+        if (diag_done[u] != spt || prod_done[u] != u * spt) return 5;
+    return 0;
+}
+
 size_t starpu_gb300_spotrs_inv_tiles_workspace(int n, int nb)
 {
     if (n < 0 || !tile_sweep_ok(nb)) return 0;

@@ -571,6 +571,19 @@ __device__ __forceinline__ void tsw_diag_task(const TileSweepArgs &a, int u, int
 
 // UPPER (backward only): the strictly upper part of L's storage holds L^T
 // outside the diagonal tiles (args.upper), read like the forward operand
+// Task of ticket t: tile row u of the solve order (its tickets start at
+// spt u (u + 1) / 2: u spt products, then spt diagonal tasks) and the rank r
+// within the row (r < u spt: product with earlier tile row r / spt, slab
+// r % spt; else diagonal task of slab r - u spt).
+__host__ __device__ __forceinline__ void tsw_decode(unsigned t, int spt, int &u, unsigned &r)
+{
+    const unsigned q = t / (unsigned)spt;
+    u = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+    while (u > 0 && (unsigned)u * (u + 1) / 2 > q) --u;
+    while ((unsigned)(u + 1) * (u + 2) / 2 <= q) ++u;
+    r = t - (unsigned)spt * ((unsigned)u * (u + 1) / 2);
+}
+
 template <bool TRANS, bool UPPER>
 __global__ void __launch_bounds__(TSW_T, 2) tile_sweep_kernel(TileSweepArgs a)
 {
@@ -586,12 +599,9 @@ __global__ void __launch_bounds__(TSW_T, 2) tile_sweep_kernel(TileSweepArgs a)
         __syncthreads();
         const unsigned t = s_ticket;
         if (t >= a.total) return;
-        // tile row u of the solve order: its tickets start at spt * u (u + 1) / 2
-        const unsigned q = t / (unsigned)a.spt;
-        int u = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
-        while (u > 0 && (unsigned)u * (u + 1) / 2 > q) --u;
-        while ((unsigned)(u + 1) * (u + 2) / 2 <= q) ++u;
-        const unsigned r = t - (unsigned)a.spt * ((unsigned)u * (u + 1) / 2);
+        int u;
+        unsigned r;
+        tsw_decode(t, a.spt, u, r);
         if (r < (unsigned)(u * a.spt))
             tsw_product_task<TRANS, UPPER>(a, u, (int)(r / a.spt), (int)(r % a.spt), ring, zs, &s_skip);
         else

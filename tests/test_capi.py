@@ -101,6 +101,14 @@ def test_kernel_attributes_are_set_once_per_device(libs):
     assert main.starpu_gb300_selftest_attr_book() == 0
 
 
+@pytest.mark.parametrize("ntiles,spt", [(1, 1), (2, 32), (32, 32), (17, 3), (512, 1), (64, 32)])
+def test_sweep_ticket_order(libs, ntiles, spt):
+    """The tile sweeps' persistent CTAs take tasks by ticket; each ticket
+    decodes to one task and every task it waits for has a smaller ticket."""
+    main, _ = libs
+    assert main.starpu_gb300_selftest_sweep_tickets(ntiles, spt) == 0
+
+
 def test_wait_budget_knob_without_a_gpu(libs):
     main, _ = libs
     default = main.starpu_gb300_set_wait_budget_ns(0)
