@@ -468,6 +468,9 @@ struct starpu_perfmodel {
 };
 
 double starpu_task_expected_length(struct starpu_task *task, struct starpu_perfmodel_arch *arch, unsigned nimpl);
+double starpu_task_worker_expected_length(struct starpu_task *task, unsigned workerid, unsigned sched_ctx_id,
+                                          unsigned nimpl);
+double starpu_worker_get_relative_speedup(struct starpu_perfmodel_arch *perf_arch);
 double starpu_task_expected_data_transfer_time(unsigned memory_node, struct starpu_task *task);
 uint32_t starpu_task_footprint(struct starpu_perfmodel *model, struct starpu_task *task,
                                struct starpu_perfmodel_arch *arch, unsigned nimpl);

@@ -18,7 +18,12 @@ Followed:
   * src/core/perfmodel/perfmodel_history.c:1546-1560 (architecture names);
   * tools/starpu_perfmodel_plot.c:330-470 (the averages file);
   * src/core/perfmodel/perfmodel_history.c:1915-1990 (recording a measurement
-    into a history entry: HistoryRecord).
+    into a history entry: HistoryRecord);
+  * src/core/perfmodel/perfmodel_history.c:1993-2023 and 66-67 (the log-log
+    least-squares sums of a regression model: RegressionSums),
+    src/core/perfmodel/regression.c:25-300 (the non-linear fit y = a x^b + c:
+    nl_power_fit), perfmodel_history.c:1575-1680 (their predictions) and
+    src/core/perfmodel/perfmodel.c:133-196 (cost-function models).
 """
 from __future__ import annotations
 
@@ -288,3 +293,148 @@ class HistoryRecord:
         n = self.nsample
         self.mean = self.sum / n
         self.deviation = math.sqrt(abs(self.sum2 - self.sum * self.sum / n) / n)
+
+
+class RegressionSums:
+    """The per-architecture regression of a (non-)linear regression model,
+    perfmodel_history.c:1993-2023: every recorded call, whatever its batch
+    size and whether or not its history entry kept it, adds ln(size) and
+    ln(time) to the least-squares sums and widens [minx, maxx]; once
+    VALID_REGRESSION holds (minx < 9 maxx / 10 in integer arithmetic, and
+    at least STARPU_CALIBRATE_MINIMUM samples: 66-67) the fit time = alpha
+    size^beta is recomputed."""
+
+    def __init__(self, calibrate_minimum: int = 10):
+        self.calibrate_minimum = calibrate_minimum
+        self.sumlnx = self.sumlnx2 = self.sumlny = self.sumlnxlny = 0.0
+        self.alpha = self.beta = 0.0
+        self.nsample = self.minx = self.maxx = 0
+        self.valid = False
+
+    def record(self, size: int, measured: float) -> None:
+        lx, ly = math.log(float(size)), math.log(measured)
+        self.sumlnx += lx
+        self.sumlnx2 += lx * lx
+        self.sumlny += ly
+        self.sumlnxlny += lx * ly
+        if self.minx == 0 or size < self.minx:
+            self.minx = size
+        if self.maxx == 0 or size > self.maxx:
+            self.maxx = size
+        self.nsample += 1
+        if self.minx < (9 * self.maxx) // 10 and self.nsample >= self.calibrate_minimum:
+            n = float(self.nsample)
+            self.beta = (n * self.sumlnxlny - self.sumlnx * self.sumlny) / (n * self.sumlnx2 - self.sumlnx * self.sumlnx)
+            self.alpha = math.exp((self.sumlny - self.beta * self.sumlnx) / n)
+            self.valid = True
+
+    def predict(self, size: int) -> float:
+        """perfmodel_history.c:1600-1601: only inside [0.9 minx, 1.1 maxx]."""
+        if self.valid and self.minx * 0.9 <= size <= self.maxx * 1.1:
+            return self.alpha * math.pow(float(size), self.beta)
+        return math.nan
+
+
+def _nl_level(t):
+    # regression.c:25-35
+    if t <= 0.0:
+        return 0.0
+    if t >= 1.0:
+        return 1.0
+    if t < 0.5:
+        return -2 * t * t + 4 * t - 1
+    return 2 * t * t
+
+
+# IEEE double arithmetic where Python would raise (C gives inf / NaN there);
+# exp, log and sqrt are the C library's, as in the compiled reference
+def _div(a, b):
+    if b != 0 or a != a or b != b:
+        return a / b if b != 0 else math.nan
+    return math.nan if a == 0 else math.copysign(math.inf, a) * math.copysign(1.0, b)
+
+
+def _sqrt(x):
+    return math.nan if x < 0 else math.sqrt(x)
+
+
+def _log(x):
+    return -math.inf if x == 0 else (math.nan if x < 0 else math.log(x))
+
+
+def _exp(x):
+    try:
+        return math.exp(x)
+    except OverflowError:
+        return math.inf
+
+
+def _nl_moments(c, x, y, pop):
+    # regression.c:37-144: the weighted sums over the points whose weight
+    # pop * level((y - c) / c - 1) is positive, in point order
+    sxy = sx = sx2 = sy = sy2 = nn = 0.0
+    for xi, yi, pi in zip(x, y, pop):
+        w = pi * _nl_level(_div(yi - c, c) - 1.0)
+        if w <= 0:  # a NaN weight is not skipped
+            continue
+        X, Y = _log(float(xi)), _log(yi - c)
+        sxy += X * Y * w
+        sx += X * w
+        sx2 += X * X * w
+        sy += Y * w
+        sy2 += Y * Y * w
+        nn += w
+    return sxy, sx, sx2, sy, sy2, nn
+
+
+def nl_power_fit(points):
+    """regression.c:218-300 on `points` = [(size, mean, nsample), ...] in
+    list order (entries without samples are skipped): (a, b, c) of
+    time = a size^b + c, or None when no point holds samples.  IEEE double
+    arithmetic throughout (a fit whose weights all vanish gives NaN, as in C)."""
+    pts = [p for p in points if p[2]]
+    if not pts:
+        return None
+    x = [p[0] for p in pts]
+    y = [float(p[1]) for p in pts]
+    pop = [p[2] for p in pts]
+    cmin, cmax = 0.0, sorted(y)[len(y) // 3]
+    err = 100000.0
+    for _ in range(1000):
+        c1 = cmin + 0.33 * (cmax - cmin)
+        c2 = cmin + 0.67 * (cmax - cmin)
+        r = []
+        for c in (c1, c2):
+            sxy, sx, sx2, sy, sy2, nn = _nl_moments(c, x, y, pop)
+            r.append(_div(nn * sxy - sx * sy, _sqrt((nn * sx2 - sx * sx) * (nn * sy2 - sy * sy))))
+        e1, e2 = abs(1.0 - r[0]), abs(1.0 - r[1])
+        if e1 < e2:
+            cmax = c2
+        else:
+            cmin = c1
+        best = e1 if e1 < e2 else e2
+        if abs(err - best) < 1.0e-10:
+            break
+        err = best
+    c = (cmin + cmax) / 2
+    sxy, sx, sx2, sy, sy2, nn = _nl_moments(c, x, y, pop)
+    b = _div(nn * sxy - sx * sy, nn * sx2 - sx * sx)
+    a = _exp(_div(sy - b * sx, nn))
+    return a, b, c
+
+
+def nl_predict(a, b, c, minx, maxx, size, entry_mean=math.nan):
+    """perfmodel_history.c:1643-1663: the fit inside [0.9 minx, 1.1 maxx],
+    else the calibrated mean of the task's history entry."""
+    if minx * 0.9 <= size <= maxx * 1.1:
+        return a * math.pow(float(size), b) + c
+    return entry_mean
+
+
+def relative_speedup(devices) -> float:
+    """perfmodel.c:133-144 over [(archtype, ncores), ...]: CPU cores count
+    0.5 each, CUDA devices 13.33 (the drivers' single-precision factors)."""
+    import numpy as np
+    coef = {"cpu": float(np.float32(0.5)), "cuda": float(np.float32(13.33))}
+    return sum(coef[t] * n for t, n in devices)
+

@@ -141,7 +141,6 @@ void rt_flush_and_wait(void);
 /* rt_sched.c */
 void rt_sched_push(struct rt_job *j);
 struct rt_job *rt_sched_pop(struct rt_worker *w);
-double rt_expected_length(struct starpu_task *t, struct starpu_perfmodel_arch *arch);
 void rt_perfmodel_feedback(struct starpu_task *t, struct starpu_perfmodel_arch *arch, double us);
 void rt_perfmodel_init(void);
 void rt_perfmodel_save_all(void);

@@ -34,7 +34,20 @@
  * STARPU_HISTORY_MAX_ERROR percent (default 50) away from the current mean
  * counts as an error and is dropped; when errors reach the sample count the
  * entry is reset.  A history model predicts once an entry holds
- * STARPU_CALIBRATE_MINIMUM (default 10) samples.
+ * STARPU_CALIBRATE_MINIMUM (default 10) samples.  Regression-based models
+ * (linear and non-linear) keep the same entries and, per call, the log-log
+ * least-squares sums of time = alpha size^beta (perfmodel_history.c:1993-2023);
+ * a non-linear model fits time = a size^b + c over its entries when it is
+ * saved (regression.c) and predicts from the fit its file holds.
+ *
+ * Prediction (perfmodel.c:199-258): per-arch and per-worker models call the
+ * codelet's cost function, a common model divides its cost by the
+ * architecture's relative speed (CPU core 0.5, CUDA device 13.33), history
+ * models take the entry's mean, regression models evaluate their fit inside
+ * [0.9 minx, 1.1 maxx] of the sizes measured (a non-linear model falls back
+ * to the entry's mean outside it).  Multiple-regression models (an offline
+ * fit over codelet parameters) read, print and save their coefficients but
+ * predict nothing here.
  *
  * Malformed files are reported and the load fails with 1, where the
  * reference asserts.
@@ -375,10 +388,11 @@ static pthread_mutex_t model_mu = PTHREAD_MUTEX_INITIALIZER;
 static struct starpu_perfmodel *models[MAX_MODELS];
 static int nmodels;
 
+/* a fresh per-arch regression: all zero, as perfmodel.c's calloc leaves it
+ * (a file written before the fit is valid holds alpha = beta = 0) */
 static void reg_init(struct pm_regression *r)
 {
     memset(r, 0, sizeof *r);
-    r->alpha = r->beta = r->a = r->b = r->c = NAN;
 }
 
 static struct pm_per_arch *per_arch(struct starpu_perfmodel_history_state *s, int comb, int impl)
@@ -597,8 +611,10 @@ static void parse_entry(struct pm_reader *r, struct pm_per_arch *pa)
     pa->list = e;
 }
 
-/* parse a whole file into m->state (created if needed); 0 on success */
-static int parse_file(const char *path, struct starpu_perfmodel *m)
+/* parse a whole file into m->state (created if needed); 0 on success.
+ * Without keep_entries the entries are read and dropped, as a runtime load
+ * of a linear- or multiple-regression model does (perfmodel.c:177-183). */
+static int parse_file(const char *path, struct starpu_perfmodel *m, int keep_entries)
 {
     struct pm_reader r;
     if (reader_open(&r, path) != 0) return 1;
@@ -644,7 +660,7 @@ static int parse_file(const char *path, struct starpu_perfmodel *m)
             end_line(&r);
             parse_regression(&r, pa ? &pa->reg : &dummy);
             free(dummy.coeff);
-            for (long e = 0; e < nentries && !r.bad; ++e) parse_entry(&r, pa);
+            for (long e = 0; e < nentries && !r.bad; ++e) parse_entry(&r, keep_entries ? pa : NULL);
             if (pa && m->type == STARPU_PERFMODEL_INVALID) {
                 if (pa->reg.ncoeff) m->type = STARPU_MULTIPLE_REGRESSION_BASED;
                 else if (!isnan(pa->reg.a) && !isnan(pa->reg.b) && !isnan(pa->reg.c))
@@ -658,6 +674,126 @@ static int parse_file(const char *path, struct starpu_perfmodel *m)
     reader_close(&r);
     if (bad) fprintf(stderr, "[starpu_gb300] incorrect performance model file %s\n", path);
     return bad ? 1 : 0;
+}
+
+/* ------------------------------------------------------ regression models */
+
+/* One measurement into the log-log least-squares sums of time = alpha
+ * size^beta, and the fit once valid_regression() holds
+ * (perfmodel_history.c:1993-2023): one sample per call, whatever the batch
+ * size, outliers of the history entry included. */
+static void regression_add(struct pm_regression *g, size_t size, double us)
+{
+    const double lx = log((double)size), ly = log(us);
+    g->sumlnx += lx;
+    g->sumlnx2 += lx * lx;
+    g->sumlny += ly;
+    g->sumlnxlny += lx * ly;
+    if (g->minx == 0 || size < g->minx) g->minx = size;
+    if (g->maxx == 0 || size > g->maxx) g->maxx = size;
+    g->nsample++;
+    if (valid_regression(g)) {
+        const unsigned n = g->nsample;
+        g->beta = (n * g->sumlnxlny - g->sumlnx * g->sumlny) / (n * g->sumlnx2 - g->sumlnx * g->sumlnx);
+        g->alpha = exp((g->sumlny - g->beta * g->sumlnx) / n);
+        g->valid = 1;
+    }
+}
+
+/* Weight of an entry (its sample count `pop`, mean `y`) in the fit of
+ * log(y - c) against log(size) (regression.c:25-45): entries whose time
+ * does not exceed 2c are left out and those above 3c count fully, through
+ * the reference's piecewise ramp of the relative distance (y - c) / c. */
+static double nl_weight(unsigned pop, double c, double y)
+{
+    const double t = (y - c) / c - 1.0;
+    double w;
+    if (t <= 0.) w = 0.;
+    else if (t >= 1.) w = 1.;
+    else if (t < 0.5) w = -2 * t * t + 4 * t - 1;
+    else w = 2 * t * t;
+    return pop * w;
+}
+
+/* Weighted moments of X = log(size), Y = log(y - c) over the entries. */
+struct nl_moments {
+    double sxy, sx, sx2, sy, sy2, n;
+};
+
+static struct nl_moments nl_moments(double c, unsigned n, const size_t *x, const double *y, const unsigned *pop)
+{
+    struct nl_moments m = {0, 0, 0, 0, 0, 0};
+    for (unsigned i = 0; i < n; ++i) {
+        const double w = nl_weight(pop[i], c, y[i]);
+        if (w <= 0) continue;
+        const double X = log((double)x[i]), Y = log(y[i] - c);
+        m.sxy += X * Y * w;
+        m.sx += X * w;
+        m.sx2 += X * X * w;
+        m.sy += Y * w;
+        m.sy2 += Y * Y * w;
+        m.n += w;
+    }
+    return m;
+}
+
+static int cmp_double(const void *pa, const void *pb)
+{
+    const double a = *(const double *)pa, b = *(const double *)pb;
+    return a < b ? -1 : a > b;
+}
+
+/* Fit time = a size^b + c over the entries that hold samples, in list order
+ * (regression.c:218-300, after Augonnet's thesis, appendix B): c is searched
+ * in [0, the n/3-th smallest mean] by repeatedly dropping the outer third on
+ * the side of the worse correlation coefficient of the weighted log-log fit,
+ * until that coefficient's distance to 1 changes by less than 1e-10 (at most
+ * 1000 steps); b and a then come from the weighted least squares at the
+ * middle of the last interval.  -1 when no entry holds samples. */
+static int nl_fit(const struct pm_entry *list, double *pa, double *pb, double *pc)
+{
+    unsigned n = 0;
+    for (const struct pm_entry *e = list; e; e = e->next) n += e->nsample != 0;
+    if (!n) return -1;
+    size_t *x = malloc(n * sizeof *x);
+    double *y = malloc(n * sizeof *y), *sorted = malloc(n * sizeof *sorted);
+    unsigned *pop = malloc(n * sizeof *pop);
+    unsigned i = 0;
+    for (const struct pm_entry *e = list; e; e = e->next)
+        if (e->nsample) {
+            x[i] = e->size;
+            y[i] = e->mean;
+            pop[i] = e->nsample;
+            ++i;
+        }
+    memcpy(sorted, y, n * sizeof *y);
+    qsort(sorted, n, sizeof *sorted, cmp_double);
+    double lo = 0.0, hi = sorted[n / 3], err = 100000.0;
+    for (int it = 0; it < 1000; ++it) {
+        const double c1 = lo + 0.33 * (hi - lo), c2 = lo + 0.67 * (hi - lo);
+        double r[2];
+        for (int k = 0; k < 2; ++k) {
+            const struct nl_moments m = nl_moments(k ? c2 : c1, n, x, y, pop);
+            r[k] = (m.n * m.sxy - m.sx * m.sy) / sqrt((m.n * m.sx2 - m.sx * m.sx) * (m.n * m.sy2 - m.sy * m.sy));
+        }
+        const double e1 = fabs(1.0 - r[0]), e2 = fabs(1.0 - r[1]);
+        if (e1 < e2) hi = c2;
+        else lo = c1;
+        const double best = e1 < e2 ? e1 : e2;
+        if (fabs(err - best) < 1.0e-10) break;
+        err = best;
+    }
+    const double c = (lo + hi) / 2;
+    const struct nl_moments m = nl_moments(c, n, x, y, pop);
+    const double b = (m.n * m.sxy - m.sx * m.sy) / (m.n * m.sx2 - m.sx * m.sx);
+    *pa = exp((m.sy - b * m.sx) / m.n);
+    *pb = b;
+    *pc = c;
+    free(x);
+    free(y);
+    free(sorted);
+    free(pop);
+    return 0;
 }
 
 /* ------------------------------------------------------------ file writer */
@@ -701,13 +837,18 @@ static void write_file(FILE *f, struct starpu_perfmodel *m)
             fprintf(f, "\t");
             write_double(f, "%-15e", lin ? g->beta : NAN);
             fprintf(f, "\t%u\t%-15lu\t%-15lu\n", g->nsample, g->minx, g->maxx);
-            const int nl = m->type == STARPU_NL_REGRESSION_BASED;
+            /* a non-linear model's fit is made from its entries as it is
+             * written (perfmodel_history.c:410-425) */
+            double a = NAN, b = NAN, c = NAN;
+            if (m->type == STARPU_NL_REGRESSION_BASED && nl_fit(pa->list, &a, &b, &c) != 0)
+                fprintf(stderr, "[starpu_gb300] could not compute a non-linear regression for model %s\n",
+                        m->symbol ? m->symbol : "?");
             fprintf(f, "# a\t\tb\t\tc\n");
-            write_double(f, "%-15e", nl ? g->a : NAN);
+            write_double(f, "%-15e", a);
             fprintf(f, "\t");
-            write_double(f, "%-15e", nl ? g->b : NAN);
+            write_double(f, "%-15e", b);
             fprintf(f, "\t");
-            write_double(f, "%-15e", nl ? g->c : NAN);
+            write_double(f, "%-15e", c);
             fprintf(f, "\n");
             if (g->ncoeff) {
                 fprintf(f, "# n\tintercept\t\n%u", g->ncoeff);
@@ -761,7 +902,8 @@ static void ensure_model(struct starpu_perfmodel *m)
         if (m->symbol) {
             char path[PM_DIRLEN + 512];
             starpu_perfmodel_get_model_path(m->symbol, path, sizeof path);
-            if (path[0] && parse_file(path, m) != 0) {
+            const int keep = m->type != STARPU_REGRESSION_BASED && m->type != STARPU_MULTIPLE_REGRESSION_BASED;
+            if (path[0] && parse_file(path, m, keep) != 0) {
                 /* a damaged file is ignored: the model calibrates again */
                 free_state(m->state);
                 m->state = calloc(1, sizeof *m->state);
@@ -803,25 +945,90 @@ static struct pm_entry *find_entry(struct pm_per_arch *pa, uint32_t fp)
     return NULL;
 }
 
-double rt_expected_length(struct starpu_task *t, struct starpu_perfmodel_arch *arch)
+/* Relative speed of an architecture: the sum over its devices of the
+ * driver's speed factor times the device's cores (perfmodel.c:133-144; the
+ * factors of drivers/cpu/driver_cpu.c:84-88 and drivers/cuda/driver_cuda_init.c:26-30). */
+double starpu_worker_get_relative_speedup(struct starpu_perfmodel_arch *perf_arch)
 {
-    struct starpu_perfmodel *m = t->cl ? t->cl->model : NULL;
-    if (!m || m->type != STARPU_HISTORY_BASED || !arch) return NAN;
+    double speedup = 0;
+    for (int d = 0; d < perf_arch->ndevices; ++d) {
+        const double coef = perf_arch->devices[d].type == STARPU_CUDA_WORKER ? 13.33f
+                            : perf_arch->devices[d].type == STARPU_CPU_WORKER ? 0.5f
+                                                                              : 1.0f;
+        speedup += coef * perf_arch->devices[d].ncores;
+    }
+    return speedup;
+}
+
+/* The calibrated mean of the task's entry, NAN below STARPU_CALIBRATE_MINIMUM
+ * samples; called with model_mu held. */
+static double entry_mean(struct pm_per_arch *pa, struct starpu_task *t)
+{
+    struct pm_entry *e = find_entry(pa, task_footprint(t));
+    return (e && e->nsample >= (unsigned)calibrate_minimum) ? e->mean : NAN;
+}
+
+/* Expected duration (us) of task t on architecture arch for one model type
+ * (perfmodel.c:199-244, perfmodel_history.c:1575-1680, 1740-1826); NAN when
+ * the model cannot tell yet. */
+static double model_expected(struct starpu_perfmodel *m, struct starpu_task *t, struct starpu_perfmodel_arch *arch,
+                             unsigned nimpl)
+{
+    switch (m->type) {
+    case STARPU_PER_ARCH:
+        STARPU_ASSERT_MSG(m->arch_cost_function, "STARPU_PER_ARCH needs arch_cost_function to be defined");
+        return m->arch_cost_function(t, arch, nimpl);
+    case STARPU_COMMON: {
+        STARPU_ASSERT_MSG(m->cost_function, "STARPU_COMMON requires common cost_function to be defined");
+        const double alpha = starpu_worker_get_relative_speedup(arch);
+        STARPU_ASSERT(alpha != 0.);
+        return m->cost_function(t, nimpl) / alpha;
+    }
+    case STARPU_HISTORY_BASED:
+    case STARPU_REGRESSION_BASED:
+    case STARPU_NL_REGRESSION_BASED:
+        break;
+    default:
+        return NAN;
+    }
+    if (nimpl >= PM_MAXIMPL) return NAN;
     ensure_model(m);
     const int comb = comb_of(arch);
-    const uint32_t fp = task_footprint(t);
+    const size_t size = task_size(t, nimpl);
     pthread_mutex_lock(&model_mu);
-    struct pm_entry *e = find_entry(per_arch_if_any(m->state, comb, 0), fp);
-    double v = (e && e->nsample >= (unsigned)calibrate_minimum) ? e->mean : NAN;
+    struct pm_per_arch *pa = per_arch_if_any(m->state, comb, (int)nimpl);
+    double v = NAN;
+    if (pa) {
+        const struct pm_regression *g = &pa->reg;
+        const int in_range = size >= g->minx * 0.9 && size <= g->maxx * 1.1;
+        if (m->type == STARPU_HISTORY_BASED) v = entry_mean(pa, t);
+        else if (m->type == STARPU_REGRESSION_BASED) v = g->valid && in_range ? g->alpha * pow((double)size, g->beta) : NAN;
+        else v = g->nl_valid && in_range ? g->a * pow((double)size, g->b) + g->c : entry_mean(pa, t);
+    }
     pthread_mutex_unlock(&model_mu);
     return v;
 }
 
 double starpu_task_expected_length(struct starpu_task *task, struct starpu_perfmodel_arch *arch, unsigned nimpl)
 {
-    (void)nimpl;
-    if (!arch || arch->ndevices < 1) return NAN;
-    return rt_expected_length(task, arch);
+    struct starpu_perfmodel *m = task->cl ? task->cl->model : NULL;
+    if (!m || !arch || arch->ndevices < 1) return NAN;
+    return model_expected(m, task, arch, nimpl);
+}
+
+/* A per-worker model calls the codelet's worker cost function; the others
+ * predict for the worker's architecture (perfmodel.c:246-258). */
+double starpu_task_worker_expected_length(struct starpu_task *task, unsigned workerid, unsigned sched_ctx_id,
+                                          unsigned nimpl)
+{
+    struct starpu_perfmodel *m = task->cl ? task->cl->model : NULL;
+    if (!m) return NAN;
+    if (m->type == STARPU_PER_WORKER) {
+        STARPU_ASSERT_MSG(m->worker_cost_function, "STARPU_PER_WORKER needs worker_cost_function to be defined");
+        return m->worker_cost_function(task, workerid, nimpl);
+    }
+    struct starpu_perfmodel_arch *arch = starpu_worker_get_perf_archtype((int)workerid, sched_ctx_id);
+    return arch ? model_expected(m, task, arch, nimpl) : NAN;
 }
 
 uint32_t starpu_task_footprint(struct starpu_perfmodel *model, struct starpu_task *task,
@@ -833,38 +1040,11 @@ uint32_t starpu_task_footprint(struct starpu_perfmodel *model, struct starpu_tas
     return task_footprint(task);
 }
 
-static void record(struct starpu_perfmodel *m, struct starpu_task *t, struct starpu_perfmodel_arch *arch,
-                   unsigned nimpl, double us, unsigned number)
+/* A further measurement of an existing entry (perfmodel_history.c:1941-1989);
+ * called with model_mu held. */
+static void update_entry(struct pm_entry *e, struct starpu_task *t, double us, unsigned number,
+                         struct starpu_perfmodel *m)
 {
-    ensure_model(m);
-    if (nimpl >= PM_MAXIMPL) return;
-    const int comb = comb_of(arch);
-    const uint32_t fp = task_footprint(t);
-    const size_t size = task_size(t, nimpl);
-    pthread_mutex_lock(&model_mu);
-    struct pm_per_arch *pa = per_arch(m->state, comb, (int)nimpl);
-    struct pm_entry *e = find_entry(pa, fp);
-    if (!e) {
-        /* a new footprint (perfmodel_history.c:1915-1940): a history-based
-         * model does not keep a single first measurement, which is very often
-         * bogus (cold caches, lazy initialisation), and starts counting from
-         * the second; other models, and batches of several, keep it */
-        e = calloc(1, sizeof *e);
-        e->footprint = fp;
-        e->size = size;
-        e->flops = t->flops;
-        if (number != 1 || m->type != STARPU_HISTORY_BASED) {
-            e->sum = us * number;
-            e->sum2 = us * us * number;
-            e->nsample = number;
-            e->mean = us;
-        }
-        e->next = pa->list;
-        pa->list = e;
-        m->state->dirty = 1;
-        pthread_mutex_unlock(&model_mu);
-        return;
-    }
     const double ratio = e->mean > 0 ? us / e->mean : 1.0;
     if (e->nsample && (100 * ratio > 100 + history_max_error || 100 / ratio > 100 + history_max_error)) {
         e->nerror += number;
@@ -888,6 +1068,47 @@ static void record(struct starpu_perfmodel *m, struct starpu_task *t, struct sta
         if (e->flops == 0.) e->flops = t->flops;
         else if (fabs(e->flops - t->flops) / e->flops > 0.00001) e->flops = NAN;
     }
+}
+
+/* the model types that keep measurements (perfmodel_history.c:1898) */
+static int records_history(const struct starpu_perfmodel *m)
+{
+    return m->type == STARPU_HISTORY_BASED || m->type == STARPU_REGRESSION_BASED ||
+           m->type == STARPU_NL_REGRESSION_BASED;
+}
+
+static void record(struct starpu_perfmodel *m, struct starpu_task *t, struct starpu_perfmodel_arch *arch,
+                   unsigned nimpl, double us, unsigned number)
+{
+    ensure_model(m);
+    if (nimpl >= PM_MAXIMPL || !records_history(m)) return;
+    const int comb = comb_of(arch);
+    const uint32_t fp = task_footprint(t);
+    const size_t size = task_size(t, nimpl);
+    pthread_mutex_lock(&model_mu);
+    struct pm_per_arch *pa = per_arch(m->state, comb, (int)nimpl);
+    struct pm_entry *e = find_entry(pa, fp);
+    if (!e) {
+        /* a new footprint (perfmodel_history.c:1915-1940): a history-based
+         * model does not keep a single first measurement, which is very often
+         * bogus (cold caches, lazy initialisation), and starts counting from
+         * the second; other models, and batches of several, keep it */
+        e = calloc(1, sizeof *e);
+        e->footprint = fp;
+        e->size = size;
+        e->flops = t->flops;
+        if (number != 1 || m->type != STARPU_HISTORY_BASED) {
+            e->sum = us * number;
+            e->sum2 = us * us * number;
+            e->nsample = number;
+            e->mean = us;
+        }
+        e->next = pa->list;
+        pa->list = e;
+    } else {
+        update_entry(e, t, us, number, m);
+    }
+    if (m->type == STARPU_REGRESSION_BASED || m->type == STARPU_NL_REGRESSION_BASED) regression_add(&pa->reg, size, us);
     m->state->dirty = 1;
     pthread_mutex_unlock(&model_mu);
 }
@@ -895,7 +1116,7 @@ static void record(struct starpu_perfmodel *m, struct starpu_task *t, struct sta
 void rt_perfmodel_feedback(struct starpu_task *t, struct starpu_perfmodel_arch *arch, double us)
 {
     struct starpu_perfmodel *m = t->cl->model;
-    if (!m || m->type != STARPU_HISTORY_BASED || !arch) return;
+    if (!m || !records_history(m) || !arch) return;
     record(m, t, arch, 0, us, 1);
 }
 
@@ -982,7 +1203,7 @@ int starpu_perfmodel_deinit(struct starpu_perfmodel *model) { return starpu_perf
 int starpu_perfmodel_load_file(const char *filename, struct starpu_perfmodel *model)
 {
     if (!model->state) model->state = calloc(1, sizeof *model->state);
-    int rc = parse_file(filename, model);
+    int rc = parse_file(filename, model, 1);
     if (rc) {
         starpu_perfmodel_unload_model(model);
         return 1;

@@ -4,12 +4,13 @@
  * Push (src/sched_policies/deque_modeling_policy_data_aware.c:604 semantics):
  * for every worker able to run the task, fitness = the worker's expected
  * availability + the expected transfer time of the data not valid on its
- * memory node + the expected length from the history model; the task goes to
+ * memory node + the expected length from the codelet's performance model
+ * (history, regression or cost function, for the worker); the task goes to
  * the worker with the smallest fitness (uncalibrated archs predict 0, so they
  * get tasks and calibrate).  Each worker pops its queue by priority, then
  * submission order.
  *
- * The history models the expected lengths come from are in rt_perfmodel.c.
+ * The performance models the expected lengths come from are in rt_perfmodel.c.
  */
 #include <math.h>
 #include <sys/stat.h>
@@ -84,7 +85,7 @@ void rt_sched_push(struct rt_job *j)
     for (int i = 0; i < rt.nworkers; ++i) {
         struct rt_worker *w = &rt.workers[i];
         if (!rt_can_execute(w, t)) continue;
-        double len = rt_expected_length(t, &w->arch);
+        double len = starpu_task_worker_expected_length(t, (unsigned)i, 0, 0);
         if (isnan(len)) len = 0;
         double avail = w->expected_end > now ? w->expected_end : now;
         double fit = avail + transfer_time(t, w) + len;
