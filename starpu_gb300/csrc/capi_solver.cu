@@ -571,15 +571,17 @@ static void tile_sweeps(cudaStream_t s, int n, int nrhs, int nb, const float *L,
     cudaGetDevice(&dev);
     int *per = per_sm[dev & 15];
     if (!per[0]) {
+        // the table is filled only once all three kernels are set up
+        int occ[3];
         for (int i = 0; i < 3; ++i) {
-            if (gb300_func_dyn_smem(fns[i], TSW_DSMEM)) {
+            if (gb300_func_dyn_smem(fns[i], TSW_DSMEM) ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[i], fns[i], TSW_T, TSW_DSMEM) != cudaSuccess) {
                 // the kernels cannot run on this device: report it in the error word
                 if (err) cudaMemsetAsync(err, 1, 1, s);
                 return;
             }
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[i], fns[i], TSW_T, TSW_DSMEM);
-            per[i] = std::max(per[i], 1);
         }
+        for (int i = 2; i >= 0; --i) per[i] = std::max(occ[i], 1);
     }
     const int sms = gb300_device_sms();
     auto grid = [&](int which) {

@@ -455,9 +455,11 @@ static LookaheadStream *lookahead_stream()
 // n = 32768 solve gave 2.02 ms for a 27648-row panel on 38 SMs).
 namespace {
 // set by the autotuner for its trials: a fixed count (>= 0), or -1 for the
-// model with the parameters below (rate <= 0: the defaults)
-std::atomic<int> g_la_trial{-2};
-double g_trial_rate = 0, g_trial_tdiag = 0, g_trial_panel = 0;
+// model with the parameters below (rate <= 0: the defaults).  Per host
+// thread: the trials' factorisations run on the autotuning thread, and a
+// factorisation another thread runs meanwhile keeps its own schedule.
+thread_local int g_la_trial = -2;
+thread_local double g_trial_rate = 0, g_trial_tdiag = 0, g_trial_panel = 0;
 } // namespace
 
 static int lookahead_sms(int m2, int kb)
@@ -474,7 +476,7 @@ static int lookahead_sms(int m2, int kb)
     const int S = num_sms();
     if (fixed >= 0) return fixed >= S ? 0 : fixed;
     double rate = 1.45e15, t_diag = 0.75e-3, panel_rate = panel_rate_env;
-    const int trial = g_la_trial.load();
+    const int trial = g_la_trial;
     if (trial >= 0) return trial >= S ? 0 : trial;
     if (trial == -1) {
         if (g_trial_rate > 0) rate = g_trial_rate, t_diag = g_trial_tdiag, panel_rate = g_trial_panel;
@@ -983,13 +985,13 @@ int starpu_gb300_dense_autotune(int n, int nb, int reps)
         g_trial_rate = best.update_tflops * 1e12;
         g_trial_tdiag = best.t_diag_us * 1e-6;
         g_trial_panel = best.panel_rate;
-        g_la_trial.store(cands[c]);
+        g_la_trial = cands[c];
         double ms = 0;
         rc = timed([&] {
             cudaMemcpyAsync(A, A0, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s);
             return potrf_tc(s, n, A, n, nb, 3, work, d_info, d_err, nullptr, {}, 0, {}, nullptr);
         }, &ms);
-        g_la_trial.store(-2);
+        g_la_trial = -2;
         if (!rc && ms < best.step_ms) {
             best.step_ms = ms;
             best.lookahead_sms = cands[c];
