@@ -122,16 +122,20 @@ def dist_setup():
 
 
 class Dist:
-    """Barrier + max-over-ranks through torch.distributed (plumbing only)."""
+    """Barrier + max-over-ranks through torch.distributed (plumbing only):
+    NCCL on the rank's GPU, gloo on host tensors where no GPU is visible.
+    The replicas exchange nothing else."""
 
     def __init__(self, world: int, local: int):
         self.world = world
-        self.pg = None
         if world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(local)
-            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+            self.device = "cpu"
+            if torch.cuda.is_available():
+                torch.cuda.set_device(local)
+                self.device = f"cuda:{local}"
+            dist.init_process_group("nccl" if self.device != "cpu" else "gloo")
             self.dist, self.torch = dist, torch
 
     def barrier(self):
@@ -141,7 +145,7 @@ class Dist:
     def max(self, v: float) -> float:
         if self.world == 1:
             return v
-        t = self.torch.tensor([v], dtype=self.torch.float64, device="cuda")
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=self.device)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
         return float(t.item())
 
