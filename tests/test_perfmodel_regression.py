@@ -47,6 +47,8 @@ def run(tmp_path_factory):
     r = subprocess.run([str(exe)], env=env, capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.rstrip().endswith("ALL OK"), r.stdout + r.stderr
     out = dict(l.split(" ", 1) for l in r.stdout.splitlines() if " " in l)
+    out["_env"] = env
+    out["_display"] = B.example_path("starpu_perfmodel_display")
     return out
 
 
@@ -101,6 +103,32 @@ def test_nonlinear_regression_fit_at_save(run):
     size = 4 * 64 * 64
     assert float(run["NL_RELOAD"]) == PO.nl_predict(pa.a, pa.b, pa.c, pa.minx, pa.maxx, size)
     assert math.isnan(float(run["NL_OUT"]))
+
+
+@pytest.mark.parametrize("symbol,path_key", [("gb300_test_perfmodel_lreg", "LIN_PATH"),
+                                             ("gb300_test_perfmodel_nlreg", "NL_PATH")])
+@pytest.mark.parametrize("args,kw", [([], {}), (["-p", "alpha"], {"parameter": "alpha"}),
+                                     (["-p", "beta"], {"parameter": "beta"}), (["-p", "a"], {"parameter": "a"}),
+                                     (["-p", "c"], {"parameter": "c"})])
+def test_display_tools_print_the_regression_models(run, symbol, path_key, args, kw):
+    """The GB300 display tool, and StarPU's own tool compiled unchanged against
+    this runtime where the reference tree is present, print the runtime's
+    regression models as the oracle reads them."""
+    with open(run[path_key]) as f:
+        text = f.read()
+    reg = PO.Registry()
+    m = PO.parse(text, reg)
+    want = PO.print_all(m, reg, **kw)
+    t = subprocess.run([run["_display"], "-s", symbol, *args], env=run["_env"], capture_output=True, text=True,
+                       timeout=60)
+    assert t.returncode == 0, t.stderr
+    assert t.stdout == want
+    if os.path.isfile(os.path.join(REF, "tools", "starpu_perfmodel_display.c")):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}", "ref-tools"], check=True)
+        ref = os.path.join(ROOT, "oracle", "_ref", "starpu_perfmodel_display_ref")
+        r = subprocess.run([ref, "-s", symbol, *args], env=run["_env"], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0, r.stderr
+        assert r.stdout == want
 
 
 def test_cost_function_models(run):
