@@ -7,6 +7,8 @@
   `ref-driver`): with the reference's CPU codelets it must pass the
   reference's -check (config 1: N=2048, 8x8 tiles); with the GB300 codelet
   library and no GPU it must report "skipped" (exit 77) like the reference.
+  Likewise cholesky_tag.c, cholesky_tile_tag.c, cholesky_grain_tag.c and
+  cholesky_compil.c on the reference's CPU codelets.
 """
 import os
 import re
@@ -105,6 +107,63 @@ def test_unchanged_tag_driver_entry_task_submitted_last():
         m = re.search(r"Error\[(\d+), (\d+)\] --> ([\d.]+)", r.stderr)
         outs.append(m.groups() if m else None)
     assert outs[0] is not None and outs[0] == outs[1], outs
+
+
+@pytest.mark.parametrize("args", [["-size", "2048", "-nblocks", "8", "-check"],
+                                  ["-size", "960", "-nblocks", "6", "-check", "-no-prio"]])
+def test_unchanged_compil_driver_on_cpu_workers(args):
+    """cholesky_compil.c: the tile DAG written as an externally generated loop
+    nest (cholesky_compiled.c), submitted with starpu_task_insert; it must
+    pass the reference's own -check."""
+    exe = _ref_driver("_ref/cholesky_compil_cpu")
+    for ncpu in (1, 4):
+        r = subprocess.run([exe, *args], env=_env(STARPU_NCUDA=0, STARPU_NCPU=ncpu), capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "comparing results" in r.stderr and "Error[" not in r.stderr
+        assert re.search(rf"^{args[1]}\t\d+\t[\d.]+", r.stdout, re.M), r.stdout
+
+
+@pytest.mark.parametrize("nbigblocks", [8, 4, 2])
+def test_unchanged_grain_tag_driver_refines_the_trailing_matrix(nbigblocks):
+    """cholesky_grain_tag.c: a tag DAG over 8 x 8 tiles for the first
+    `nbigblocks` steps; the trailing matrix is then unpartitioned,
+    unregistered, registered again in place (a sub-matrix of the same host
+    array, ld = N) and factored with twice as many tiles per dimension.
+    Its GEMM task has cholesky_tag.h's operand order (A_nk, A_mk), so the
+    reference's 1e-4 check stops at its first element over the threshold by a
+    hair, as for cholesky_tag.c; a wrong partition or a lost write-back would
+    miss by orders of magnitude.  The run must otherwise complete, and its
+    result must not depend on the worker count."""
+    exe = _ref_driver("_ref/cholesky_grain_tag_cpu")
+    outs = []
+    for ncpu in (1, 4):
+        r = subprocess.run([exe, "-size", "1024", "-nblocks", "8", "-nbigblocks", str(nbigblocks), "-check"],
+                           env=_env(STARPU_NCUDA=0, STARPU_NCPU=ncpu), capture_output=True, text=True, timeout=300)
+        assert "comparing results" in r.stderr, r.stdout + r.stderr
+        m = re.search(r"Error\[(\d+), (\d+)\] --> ([\d.]+) != ([\d.]+) \(err ([\d.]+)\)", r.stderr)
+        if m:
+            assert float(m.group(5)) < 2e-4, m.group(0)
+        else:
+            assert r.returncode == 0, r.stdout + r.stderr
+        outs.append(m.groups() if m else None)
+    assert outs[0] == outs[1], outs
+
+
+@pytest.mark.parametrize("size", [1024, 2048])
+def test_unchanged_grain_tag_driver_exact_check_through_the_refinement(size):
+    """With 2 x 2 tiles and one coarse step every update is a SYRK (no GEMM
+    between different tiles), so the operand order above never enters: the
+    reference's own check must pass everywhere, including the trailing half
+    that was unregistered, registered again as a sub-matrix and factored as
+    2 x 2 finer tiles."""
+    exe = _ref_driver("_ref/cholesky_grain_tag_cpu")
+    for ncpu in (1, 4):
+        r = subprocess.run([exe, "-size", str(size), "-nblocks", "2", "-nbigblocks", "1", "-check"],
+                           env=_env(STARPU_NCUDA=0, STARPU_NCPU=ncpu), capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "comparing results" in r.stderr and "Error[" not in r.stderr
+        assert re.search(rf"^{size}\t\d+\t[\d.]+", r.stdout, re.M), r.stdout
 
 
 def test_unchanged_reference_driver_links_gb300_codelets():
