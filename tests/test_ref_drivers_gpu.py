@@ -1,5 +1,6 @@
 """The reference's own drivers, unchanged, on the GPU: examples/cholesky's
-cholesky_implicit.c, cholesky_tag.c and cholesky_tile_tag.c, and
+cholesky_implicit.c, cholesky_tag.c, cholesky_tile_tag.c, cholesky_grain_tag.c
+and cholesky_compil.c, and
 examples/lu's lu_example.c with xlu_implicit*.c, compiled against include/
 and linked with this runtime and the GB300 codelet libraries
 (libstarpu_gb300_chol.so in place of cholesky_kernels.c,
@@ -83,6 +84,28 @@ def test_unchanged_cholesky_tag_on_gpu(drivers, mode):
         assert float(m.group(1)) < 1e-3, r.stderr[-2000:]
     else:
         assert r.returncode == 0 and re.search(r"^1024\t\d+\t[\d.]+", r.stdout, re.M), r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_unchanged_cholesky_compil_on_gpu(drivers, mode):
+    """cholesky_compil.c: the tile DAG as an externally generated loop nest."""
+    r = _run(os.path.join(drivers, "cholesky_compil_gb300"), ["-size", "2048", "-nblocks", "8", "-check"], mode)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "comparing results" in r.stderr and "Error[" not in r.stderr
+    assert re.search(r"^2048\t\d+\t[\d.]+", r.stdout, re.M), r.stdout
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_unchanged_cholesky_grain_tag_on_gpu(drivers, mode):
+    """cholesky_grain_tag.c with 2 x 2 tiles and one coarse step: the
+    trailing half is gathered back, unregistered, registered again in place
+    and factored as 2 x 2 finer tiles; with no GEMM between different tiles
+    the reference's check must pass everywhere."""
+    r = _run(os.path.join(drivers, "cholesky_grain_tag_gb300"),
+             ["-size", "2048", "-nblocks", "2", "-nbigblocks", "1", "-check"], mode)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "comparing results" in r.stderr and "Error[" not in r.stderr
+    assert re.search(r"^2048\t\d+\t[\d.]+", r.stdout, re.M), r.stdout
 
 
 @pytest.mark.parametrize("mode", list(MODES))
