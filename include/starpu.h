@@ -551,11 +551,17 @@ int starpu_sched_set_max_priority(int max_prio);
 #define STARPU_MIN_PRIO (starpu_sched_get_min_priority())
 #define STARPU_MAX_PRIO (starpu_sched_get_max_priority())
 
+/* contexts 1 .. STARPU_NMAX_SCHED_CTXS - 1 (0 is the initial context, every
+ * worker); STARPU_NMAX_SCHED_CTXS also means "no context" */
+#define STARPU_NMAX_SCHED_CTXS 10
 unsigned starpu_sched_ctx_create(int *workerids_ctx, int nworkers_ctx, const char *sched_ctx_name, ...);
 void starpu_sched_ctx_delete(unsigned sched_ctx_id);
 void starpu_sched_ctx_set_inheritor(unsigned sched_ctx_id, unsigned inheritor);
+unsigned starpu_sched_ctx_get_inheritor(unsigned sched_ctx_id);
 void starpu_sched_ctx_set_context(unsigned *sched_ctx_id);
 unsigned starpu_sched_ctx_get_context(void);
+unsigned starpu_sched_ctx_get_nworkers(unsigned sched_ctx_id);
+unsigned starpu_sched_ctx_contains_worker(int workerid, unsigned sched_ctx_id);
 void starpu_reset_scheduler(void);
 
 /* ============================================================= init / conf */

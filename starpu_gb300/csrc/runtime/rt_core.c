@@ -11,6 +11,7 @@
  */
 #define _GNU_SOURCE
 #include <stdarg.h>
+#include <string.h>
 #include <sched.h>
 #include <time.h>
 #include <unistd.h>
@@ -176,6 +177,7 @@ void starpu_shutdown(void)
     rt.npending = rt.cappending = 0;
     rt_cuda_shutdown();
     rt.nworkers = rt.ncpu = rt.ncuda = 0;
+    rt_ctx_reset();
 }
 
 void starpu_pause(void)
@@ -259,15 +261,57 @@ int starpu_sched_set_max_priority(int p)
     return 0;
 }
 
-static __thread unsigned tls_ctx = 0;
-static unsigned next_ctx = 1;
+/* ------------------------------------------------ scheduling contexts
+ *
+ * A context is a set of workers (src/core/sched_ctx.c): a task runs only on
+ * the workers of its context -- the STARPU_SCHED_CTX it was given, else the
+ * submitting thread's current context (starpu_sched_ctx_set_context), else
+ * the initial context 0, which holds every worker (task.c:973-977,
+ * sched_ctx.c:1689-1696).  Deleting a context hands its workers to its
+ * inheritor, waits for the context's submitted tasks, then frees its id
+ * (sched_ctx.c:1004-1079).  Every context uses the runtime's one policy
+ * (dmda); a policy requested for a context is accepted and not used. */
+struct rt_ctx {
+    int used;
+    unsigned inheritor; /* STARPU_NMAX_SCHED_CTXS: none */
+    long nsubmitted;    /* submitted and not terminated */
+    char member[STARPU_NMAXWORKERS];
+};
+static struct rt_ctx ctxs[STARPU_NMAX_SCHED_CTXS]; /* [0] is the initial context */
+static __thread unsigned tls_ctx = STARPU_NMAX_SCHED_CTXS;
 
-/* One scheduler (dmda) over every worker: a context is a label whose policy
- * arguments are parsed and accepted so that context-aware drivers run. */
+/* the context a task belongs to: an id that names no live context is the
+ * initial one */
+static unsigned ctx_live(unsigned id)
+{
+    return id > 0 && id < STARPU_NMAX_SCHED_CTXS && ctxs[id].used ? id : 0;
+}
+
+void rt_ctx_reset(void) { memset(ctxs, 0, sizeof ctxs); }
+
+unsigned rt_ctx_resolve(struct starpu_task *t)
+{
+    unsigned id = t->sched_ctx;
+    if (id == STARPU_NMAX_SCHED_CTXS) id = tls_ctx == STARPU_NMAX_SCHED_CTXS ? 0 : tls_ctx;
+    return ctx_live(id);
+}
+
+/* called with the runtime lock held */
+int rt_ctx_has_worker(unsigned id, int worker)
+{
+    id = ctx_live(id);
+    return id == 0 || (worker >= 0 && worker < STARPU_NMAXWORKERS && ctxs[id].member[worker]);
+}
+
+/* called with the runtime lock held */
+void rt_ctx_count(unsigned id, int delta)
+{
+    id = ctx_live(id);
+    if (id) ctxs[id].nsubmitted += delta;
+}
+
 unsigned starpu_sched_ctx_create(int *workerids_ctx, int nworkers_ctx, const char *name, ...)
 {
-    (void)workerids_ctx;
-    (void)nworkers_ctx;
     (void)name;
     va_list ap;
     va_start(ap, name);
@@ -279,12 +323,74 @@ unsigned starpu_sched_ctx_create(int *workerids_ctx, int nworkers_ctx, const cha
         else STARPU_ABORT_MSG("unknown starpu_sched_ctx_create argument %d", key);
     }
     va_end(ap);
-    return __sync_fetch_and_add(&next_ctx, 1);
+    rt_lock();
+    unsigned id = 1;
+    while (id < STARPU_NMAX_SCHED_CTXS && ctxs[id].used) ++id;
+    STARPU_ASSERT_MSG(id < STARPU_NMAX_SCHED_CTXS, "too many scheduling contexts (%d)", STARPU_NMAX_SCHED_CTXS);
+    struct rt_ctx *c = &ctxs[id];
+    memset(c, 0, sizeof *c);
+    c->used = 1;
+    c->inheritor = STARPU_NMAX_SCHED_CTXS;
+    /* -1 workers: all of them; no list: workers 0 .. n-1 (sched_ctx.c:367-385) */
+    const int n = nworkers_ctx == -1 ? rt.nworkers : nworkers_ctx;
+    STARPU_ASSERT_MSG(n >= 0 && n <= rt.nworkers, "%d workers asked for a context, %d exist", n, rt.nworkers);
+    for (int k = 0; k < n; ++k) {
+        const int w = workerids_ctx && nworkers_ctx != -1 ? workerids_ctx[k] : k;
+        STARPU_ASSERT_MSG(w >= 0 && w < rt.nworkers, "no worker %d", w);
+        c->member[w] = 1;
+    }
+    rt_unlock();
+    return id;
 }
 
-void starpu_sched_ctx_delete(unsigned id) { (void)id; }
-void starpu_sched_ctx_set_inheritor(unsigned id, unsigned inheritor) { (void)id; (void)inheritor; }
-void starpu_sched_ctx_set_context(unsigned *id) { tls_ctx = id ? *id : 0; }
+void starpu_sched_ctx_set_inheritor(unsigned id, unsigned inheritor)
+{
+    STARPU_ASSERT_MSG(id < STARPU_NMAX_SCHED_CTXS, "no scheduling context %u", id);
+    rt_lock();
+    ctxs[id].inheritor = inheritor;
+    rt_unlock();
+}
+
+unsigned starpu_sched_ctx_get_inheritor(unsigned id)
+{
+    return id < STARPU_NMAX_SCHED_CTXS ? ctxs[id].inheritor : STARPU_NMAX_SCHED_CTXS;
+}
+
+void starpu_sched_ctx_delete(unsigned id)
+{
+    if (id == 0 || id >= STARPU_NMAX_SCHED_CTXS || !ctxs[id].used) return;
+    rt_lock();
+    struct rt_ctx *c = &ctxs[id];
+    const unsigned inh = c->inheritor;
+    for (unsigned k = 1; k < STARPU_NMAX_SCHED_CTXS; ++k)
+        if (ctxs[k].used && ctxs[k].inheritor == id) ctxs[k].inheritor = inh;
+    /* the workers move to a live inheritor (the initial context has them all) */
+    if (inh > 0 && inh < STARPU_NMAX_SCHED_CTXS && ctxs[inh].used)
+        for (int w = 0; w < rt.nworkers; ++w)
+            if (c->member[w]) ctxs[inh].member[w] = 1;
+    rt_unlock();
+    rt_flush_and_wait();
+    rt_lock();
+    while (c->nsubmitted > 0) pthread_cond_wait(&rt.all_done, &rt.lock);
+    c->used = 0;
+    rt_unlock();
+}
+
+unsigned starpu_sched_ctx_get_nworkers(unsigned id)
+{
+    id = ctx_live(id);
+    if (id == 0) return (unsigned)rt.nworkers;
+    unsigned n = 0;
+    for (int w = 0; w < rt.nworkers; ++w) n += ctxs[id].member[w] != 0;
+    return n;
+}
+
+unsigned starpu_sched_ctx_contains_worker(int workerid, unsigned id)
+{
+    return workerid >= 0 && workerid < rt.nworkers && rt_ctx_has_worker(id, workerid);
+}
+
+void starpu_sched_ctx_set_context(unsigned *id) { tls_ctx = id ? *id : STARPU_NMAX_SCHED_CTXS; }
 unsigned starpu_sched_ctx_get_context(void) { return tls_ctx; }
 
 void starpu_reset_scheduler(void)

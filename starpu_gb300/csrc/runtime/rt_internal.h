@@ -138,6 +138,13 @@ void rt_job_terminate(struct rt_job *j, double measured_us);
 int rt_can_execute(struct rt_worker *w, struct starpu_task *t);
 void rt_flush_and_wait(void);
 
+/* rt_core.c: scheduling contexts (rt_ctx_has_worker / rt_ctx_count with the
+ * runtime lock held) */
+unsigned rt_ctx_resolve(struct starpu_task *t);
+int rt_ctx_has_worker(unsigned ctx, int worker);
+void rt_ctx_count(unsigned ctx, int delta);
+void rt_ctx_reset(void);
+
 /* rt_sched.c */
 void rt_sched_push(struct rt_job *j);
 struct rt_job *rt_sched_pop(struct rt_worker *w);

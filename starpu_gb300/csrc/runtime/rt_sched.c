@@ -84,7 +84,7 @@ void rt_sched_push(struct rt_job *j)
     double best_fit = INFINITY, best_len = 0;
     for (int i = 0; i < rt.nworkers; ++i) {
         struct rt_worker *w = &rt.workers[i];
-        if (!rt_can_execute(w, t)) continue;
+        if (!rt_can_execute(w, t) || !rt_ctx_has_worker(t->sched_ctx, i)) continue;
         double len = starpu_task_worker_expected_length(t, (unsigned)i, 0, 0);
         if (isnan(len)) len = 0;
         double avail = w->expected_end > now ? w->expected_end : now;

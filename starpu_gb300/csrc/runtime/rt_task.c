@@ -19,6 +19,7 @@ void starpu_task_init(struct starpu_task *t)
     t->priority = STARPU_DEFAULT_PRIO;
     t->status = STARPU_TASK_INIT;
     t->magic = 42;
+    t->sched_ctx = STARPU_NMAX_SCHED_CTXS; /* the submitting thread's context */
 }
 
 struct starpu_task *starpu_task_create(void)
@@ -222,8 +223,16 @@ int starpu_task_submit(struct starpu_task *t)
         STARPU_ASSERT_MSG(nb <= STARPU_NMAXBUFS, "too many buffers (%d)", nb);
         for (int i = 0; i < nb; ++i)
             if (!t->modes[i]) t->modes[i] = t->cl->modes[i];
+    }
+    t->sched_ctx = rt_ctx_resolve(t);
+    if (t->cl) {
+        /* a worker of the task's context must be able to run it
+         * (workers.c _starpu_worker_exists) */
         int ok = 0;
-        for (int w = 0; w < rt.nworkers && !ok; ++w) ok = rt_can_execute(&rt.workers[w], t);
+        rt_lock();
+        for (int w = 0; w < rt.nworkers && !ok; ++w)
+            ok = rt_can_execute(&rt.workers[w], t) && rt_ctx_has_worker(t->sched_ctx, w);
+        rt_unlock();
         if (!ok) return -ENODEV;
     }
     struct rt_job *j = calloc(1, sizeof *j);
@@ -237,6 +246,7 @@ int starpu_task_submit(struct starpu_task *t)
     rt_lock();
     j->seq = rt.seq++;
     rt.nsubmitted++;
+    rt_ctx_count(t->sched_ctx, +1);
     j->ndeps = 1; /* held until submission completes */
     if (t->sequential_consistency) {
         for (int i = 0; i < t->nbuffers; ++i) {
@@ -336,6 +346,7 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
     free(j->prev);
     free(j);
     rt.nsubmitted--;
+    rt_ctx_count(t->sched_ctx, -1);
     pthread_cond_broadcast(&rt.all_done);
     rt_unlock();
     if (destroy) starpu_task_destroy(t);

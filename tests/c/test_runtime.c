@@ -59,6 +59,17 @@ static void noop_cuda(void *descr[], void *arg) { (void)descr; (void)arg; }
 static struct starpu_codelet cl_cuda_only = {.cuda_funcs = {noop_cuda}, .nbuffers = 0};
 static struct starpu_codelet cl_noop = {.cpu_funcs = {noop}, .nbuffers = 0};
 
+/* records the worker that ran task k */
+static int ran_on[64];
+static void where_k(void *descr[], void *arg)
+{
+    (void)descr;
+    int k;
+    starpu_codelet_unpack_args(arg, &k, NULL);
+    ran_on[k] = starpu_worker_get_id();
+}
+static struct starpu_codelet cl_where = {.cpu_funcs = {where_k}, .nbuffers = 0};
+
 static int cb_count = 0;
 static void cb(void *arg) { __sync_fetch_and_add(&cb_count, *(int *)arg); }
 
@@ -190,6 +201,51 @@ int main(void)
         struct starpu_perfmodel loaded;
         CHECK(starpu_perfmodel_load_symbol("gb300_test_tile_inc", &loaded) == 0, "perfmodel_reload");
         starpu_perfmodel_unload_model(&loaded);
+    }
+    /* scheduling contexts (src/core/sched_ctx.c): a context's tasks run on
+     * its workers only; a context without a capable worker refuses tasks;
+     * a deleted context hands its workers to its inheritor */
+    {
+        const int nw = (int)starpu_worker_get_count();
+        const int half = nw >= 2 ? nw / 2 : 1;
+        int wa[STARPU_NMAXWORKERS], wb[STARPU_NMAXWORKERS], na = 0, nb = 0;
+        for (int w = 0; w < nw; ++w) {
+            if (w < half) wa[na++] = w;
+            if (w >= half || nw == 1) wb[nb++] = w;
+        }
+        unsigned ca = starpu_sched_ctx_create(wa, na, "ctx_a", STARPU_SCHED_CTX_POLICY_NAME, "dmda", 0);
+        unsigned cb2 = starpu_sched_ctx_create(wb, nb, "ctx_b", 0);
+        CHECK(ca != 0 && cb2 != 0 && ca != cb2, "ctx_create");
+        CHECK(starpu_sched_ctx_get_context() == STARPU_NMAX_SCHED_CTXS, "ctx_none_current");
+        CHECK(starpu_sched_ctx_get_nworkers(ca) == (unsigned)na && starpu_sched_ctx_get_nworkers(cb2) == (unsigned)nb,
+              "ctx_nworkers");
+        for (int k = 0; k < 64; ++k) ran_on[k] = -1;
+        /* 32 tasks named to a context by STARPU_SCHED_CTX, 32 through the current one */
+        int submitted = 1;
+        for (int k = 0; k < 32; ++k)
+            submitted &= starpu_task_insert(&cl_where, STARPU_VALUE, &k, sizeof k, STARPU_SCHED_CTX,
+                                            (k & 1) ? ca : cb2, 0) == 0;
+        starpu_sched_ctx_set_context(&ca);
+        for (int k = 32; k < 64; ++k) submitted &= starpu_task_insert(&cl_where, STARPU_VALUE, &k, sizeof k, 0) == 0;
+        CHECK(starpu_sched_ctx_get_context() == ca, "ctx_current");
+        starpu_sched_ctx_set_context(NULL);
+        starpu_task_wait_for_all();
+        int placed = submitted;
+        for (int k = 0; k < 64; ++k) {
+            const unsigned c = k < 32 ? ((k & 1) ? ca : cb2) : ca;
+            placed &= ran_on[k] >= 0 && starpu_sched_ctx_contains_worker(ran_on[k], c);
+        }
+        CHECK(placed, "ctx_tasks_on_their_workers");
+        unsigned empty = starpu_sched_ctx_create(NULL, 0, "ctx_empty", 0);
+        CHECK(starpu_task_insert(&cl_noop, STARPU_SCHED_CTX, empty, 0) == -ENODEV, "ctx_enodev_without_workers");
+        starpu_sched_ctx_set_inheritor(ca, cb2);
+        starpu_sched_ctx_delete(ca);
+        CHECK(starpu_sched_ctx_get_nworkers(cb2) == (unsigned)nw, "ctx_delete_hands_workers_to_inheritor");
+        starpu_sched_ctx_delete(cb2);
+        starpu_sched_ctx_delete(empty);
+        /* a task named to a deleted context runs in the initial one */
+        CHECK(starpu_task_insert(&cl_noop, STARPU_SCHED_CTX, ca, 0) == 0, "ctx_deleted_falls_back_to_initial");
+        starpu_task_wait_for_all();
     }
     starpu_shutdown();
     printf("%s\n", failures ? "FAILED" : "ALL OK");

@@ -166,6 +166,35 @@ def test_unchanged_grain_tag_driver_exact_check_through_the_refinement(size):
         assert re.search(rf"^{size}\t\d+\t[\d.]+", r.stdout, re.M), r.stdout
 
 
+@pytest.mark.parametrize("mode,nbench", [("-with_ctxs", 2), ("-with_noctxs", 2), ("-chole1", 1), ("-chole2", 1)])
+def test_unchanged_driver_scheduling_contexts(mode, nbench):
+    """cholesky_implicit.c's context modes (examples/sched_ctx_utils): two
+    factorisations in two threads, each in its own context of two CPU
+    workers (-with_ctxs; the first to finish hands its workers to the other,
+    its inheritor), both in the initial context (-with_noctxs), or one of
+    them alone (-chole1, -chole2).  Every factorisation must run (positive
+    GFlop/s on the summary line)."""
+    exe = _ref_driver("_ref/cholesky_implicit_cpu")
+    sizes = ["-size1", "1024", "-nblocks1", "8", "-size2", "1024", "-nblocks2", "8"]
+    r = subprocess.run([exe, mode, "-cpu1", "2", "-cpu2", "2", *sizes], env=_env(STARPU_NCUDA=0, STARPU_NCPU=4),
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    nums = [float(x) for x in r.stdout.strip().splitlines()[-1].split()]
+    assert len(nums) == nbench + nbench + 1 and all(g > 0 for g in nums[:nbench]), r.stdout
+
+
+def test_unchanged_driver_empty_contexts_submit_nothing():
+    """Without -cpu1/-cpu2 the driver's two contexts hold no worker: every
+    submission is refused with -ENODEV (workers.c _starpu_worker_exists), the
+    driver skips the factorisations and reports 0 GFlop/s for both."""
+    exe = _ref_driver("_ref/cholesky_implicit_cpu")
+    r = subprocess.run([exe, "-with_ctxs", "-size1", "512", "-nblocks1", "4", "-size2", "512", "-nblocks2", "4"],
+                       env=_env(STARPU_NCUDA=0, STARPU_NCPU=4), capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    nums = [float(x) for x in r.stdout.strip().splitlines()[-1].split()]
+    assert nums[:2] == [0.0, 0.0], r.stdout
+
+
 def test_unchanged_reference_driver_links_gb300_codelets():
     exe = _ref_driver("_ref/cholesky_implicit_gb300")
     r = subprocess.run([exe, "-size", "256", "-nblocks", "2"], env=_env(STARPU_NCUDA=0, STARPU_NCPU=2),
