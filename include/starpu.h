@@ -341,8 +341,9 @@ struct starpu_task {
     void (*callback_func)(void *);
     void *callback_arg;
     unsigned callback_arg_free;
-    void (*prologue_callback_func)(void *);
+    void (*prologue_callback_func)(void *); /* run when the task becomes ready, before scheduling */
     void *prologue_callback_arg;
+    unsigned prologue_callback_arg_free;
     unsigned use_tag;
     starpu_tag_t tag_id;
     unsigned sequential_consistency;
@@ -363,6 +364,8 @@ struct starpu_task {
     unsigned long magic;
     void *sched_data;
     unsigned color;        /* display colour of the task in traces */
+    unsigned failed;       /* set by starpu_task_ft_failed */
+    int nb_termination_call_required; /* starpu_task_end_dep_add calls not yet released */
     void *starpu_private;  /* runtime job */
 };
 
@@ -380,6 +383,22 @@ int starpu_task_wait_for_n_submitted(unsigned n);
 int starpu_task_nsubmitted(void);
 int starpu_task_nready(void);
 struct starpu_task *starpu_task_get_current(void);
+/* submission without data or tag dependencies (the caller already holds the data) */
+int starpu_task_submit_nodeps(struct starpu_task *task);
+/* termination of `task` waits for nb_deps more starpu_task_end_dep_release calls */
+void starpu_task_end_dep_add(struct starpu_task *task, int nb_deps);
+void starpu_task_end_dep_release(struct starpu_task *task);
+
+/* fault tolerance (src/core/task.c): a task given starpu_task_ft_prologue as
+ * prologue becomes a meta task that holds its data and runs nothing; a copy
+ * of it does the work, and its callback (check_ft) either releases the meta
+ * task (starpu_task_ft_success) or submits another copy when the work
+ * reported starpu_task_ft_failed.  Only STARPU_R and STARPU_W accesses. */
+void starpu_task_ft_prologue(void *check_ft);
+struct starpu_task *starpu_task_ft_create_retry(const struct starpu_task *meta_task,
+                                                const struct starpu_task *template_task, void (*check_ft)(void *));
+void starpu_task_ft_failed(struct starpu_task *task);
+void starpu_task_ft_success(struct starpu_task *meta_task);
 void starpu_codelet_init(struct starpu_codelet *cl);
 void starpu_iteration_push(unsigned long iteration);
 void starpu_iteration_pop(void);
@@ -409,6 +428,9 @@ void starpu_iteration_pop(void);
 #define STARPU_TASK_SYNCHRONOUS (31 << STARPU_MODE_SHIFT)
 #define STARPU_SEQUENTIAL_CONSISTENCY (35 << STARPU_MODE_SHIFT)
 #define STARPU_TASK_NO_SUBMITORDER (37 << STARPU_MODE_SHIFT)
+#define STARPU_PROLOGUE_CALLBACK (15 << STARPU_MODE_SHIFT)
+#define STARPU_PROLOGUE_CALLBACK_ARG (16 << STARPU_MODE_SHIFT)
+#define STARPU_PROLOGUE_CALLBACK_ARG_NFREE (40 << STARPU_MODE_SHIFT)
 
 struct starpu_data_descr {
     starpu_data_handle_t handle;
@@ -578,9 +600,22 @@ struct starpu_conf {
     int single_combined_worker;
     int disable_asynchronous_copy;
     int precedence_over_environment_variables;
+    int nsycl, nmax_fpga, nmpi_sc, ntcpip_sc; /* accepted; this runtime has no such workers */
 };
 
 int starpu_conf_init(struct starpu_conf *conf);
+int starpu_conf_noworker(struct starpu_conf *conf);
+
+/* integer environment variables (starpu_helper.h): -1 when unset; a value
+ * that is not a non-negative integer aborts */
+int starpu_get_env_number(const char *str);
+static inline int starpu_get_env_number_default(const char *str, int defval)
+{
+    const int n = starpu_get_env_number(str);
+    return n == -1 ? defval : n;
+}
+#define starpu_getenv_number(s) starpu_get_env_number(s)
+#define starpu_getenv_number_default(s, d) starpu_get_env_number_default(s, d)
 int starpu_init(struct starpu_conf *conf);
 int starpu_initialize(struct starpu_conf *user_conf, int *argc, char ***argv);
 int starpu_is_initialized(void);

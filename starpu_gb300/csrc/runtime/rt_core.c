@@ -69,6 +69,24 @@ int starpu_conf_init(struct starpu_conf *conf)
     return 0;
 }
 
+int starpu_get_env_number(const char *str)
+{
+    const char *v = getenv(str);
+    if (!v) return -1;
+    char *end;
+    const long n = strtol(v, &end, 10);
+    if (*end || n < 0) starpu_gb300_abort_msg(__FILE__, __LINE__, __func__,
+                                              "The %s environment variable must contain a non-negative integer", str);
+    return (int)n;
+}
+
+int starpu_conf_noworker(struct starpu_conf *conf)
+{
+    conf->ncpus = conf->ncuda = conf->nhip = conf->nopencl = 0;
+    conf->nsycl = conf->nmax_fpga = conf->nmpi_sc = conf->ntcpip_sc = 0;
+    return 0;
+}
+
 int starpu_init(struct starpu_conf *conf) { return starpu_initialize(conf, NULL, NULL); }
 
 int starpu_initialize(struct starpu_conf *user_conf, int *argc, char ***argv)

@@ -77,6 +77,8 @@ struct rt_job {
     starpu_tag_t tag;
     int has_tag;
     int tag_waits;              /* tags awaited whose task is not submitted yet */
+    int prologue_done;
+    struct rt_job *defer_next;  /* queue of ready jobs whose prologue / NOWHERE step runs unlocked */
 };
 
 struct rt_worker {
@@ -111,6 +113,9 @@ struct rt_state {
     /* graph mode: jobs submitted since the last flush, in submission order */
     struct rt_job **pending;
     int npending, cappending;
+    /* ready jobs with a prologue callback to run or no worker to run on
+     * (STARPU_NOWHERE): handled by rt_drain outside the lock */
+    struct rt_job *defer_head, *defer_tail;
     struct starpu_gb300_runtime_stats stats;
 };
 
@@ -144,6 +149,10 @@ unsigned rt_ctx_resolve(struct starpu_task *t);
 int rt_ctx_has_worker(unsigned ctx, int worker);
 void rt_ctx_count(unsigned ctx, int delta);
 void rt_ctx_reset(void);
+
+/* rt_task.c: runs the deferred prologues and NOWHERE terminations; call it
+ * without the lock after any section that may have pushed jobs */
+void rt_drain(void);
 
 /* rt_sched.c */
 void rt_sched_push(struct rt_job *j);

@@ -79,6 +79,17 @@ static double transfer_time(struct starpu_task *t, struct rt_worker *w)
 void rt_sched_push(struct rt_job *j)
 {
     struct starpu_task *t = j->task;
+    /* a prologue callback runs as the task becomes ready, before it is
+     * scheduled (sched_policy.c:583-588); a STARPU_NOWHERE task needs no
+     * worker.  Both may call back into the runtime: rt_drain takes them
+     * outside the lock. */
+    if ((t->prologue_callback_func && !j->prologue_done) || t->where == STARPU_NOWHERE) {
+        j->defer_next = NULL;
+        if (rt.defer_tail) rt.defer_tail->defer_next = j;
+        else rt.defer_head = j;
+        rt.defer_tail = j;
+        return;
+    }
     double now = starpu_timing_now();
     int best = -1;
     double best_fit = INFINITY, best_len = 0;

@@ -34,8 +34,10 @@ void starpu_task_clean(struct starpu_task *t)
 {
     if (t->cl_arg_free && t->cl_arg) free(t->cl_arg);
     if (t->callback_arg_free && t->callback_arg) free(t->callback_arg);
+    if (t->prologue_callback_arg_free && t->prologue_callback_arg) free(t->prologue_callback_arg);
     t->cl_arg = NULL;
     t->callback_arg = NULL;
+    t->prologue_callback_arg = NULL;
 }
 
 void starpu_task_destroy(struct starpu_task *t)
@@ -167,6 +169,7 @@ void starpu_tag_notify_from_apps(starpu_tag_t id)
     tag_release_waiters(e);
     pthread_cond_broadcast(&tag_cond);
     rt_unlock();
+    rt_drain();
 }
 
 /* ---------------------------------------------------------- dependencies */
@@ -214,7 +217,7 @@ int rt_can_execute(struct rt_worker *w, struct starpu_task *t)
     return 1;
 }
 
-int starpu_task_submit(struct starpu_task *t)
+static int rt_submit(struct starpu_task *t, int nodeps)
 {
     STARPU_ASSERT(rt.initialized);
     if (t->cl) {
@@ -225,7 +228,10 @@ int starpu_task_submit(struct starpu_task *t)
             if (!t->modes[i]) t->modes[i] = t->cl->modes[i];
     }
     t->sched_ctx = rt_ctx_resolve(t);
-    if (t->cl) {
+    STARPU_ASSERT_MSG(!rt.graph_mode || (!t->prologue_callback_func && t->where != STARPU_NOWHERE),
+                      "prologue callbacks and STARPU_NOWHERE tasks need task-by-task execution "
+                      "(STARPU_GB300_GRAPH=0, or a CPU worker beside the CUDA worker)");
+    if (t->cl && t->where != STARPU_NOWHERE) {
         /* a worker of the task's context must be able to run it
          * (workers.c _starpu_worker_exists) */
         int ok = 0;
@@ -248,7 +254,7 @@ int starpu_task_submit(struct starpu_task *t)
     rt.nsubmitted++;
     rt_ctx_count(t->sched_ctx, +1);
     j->ndeps = 1; /* held until submission completes */
-    if (t->sequential_consistency) {
+    if (t->sequential_consistency && !nodeps) {
         for (int i = 0; i < t->nbuffers; ++i) {
             starpu_data_handle_t h = t->handles[i];
             enum starpu_data_access_mode m = t->modes[i];
@@ -264,7 +270,7 @@ int starpu_task_submit(struct starpu_task *t)
             }
         }
     }
-    if (t->use_tag) {
+    if (t->use_tag && !nodeps) {
         struct tag_entry *e = tag_get(t->tag_id, 1);
         for (int d = 0; d < e->ndeps; ++d) {
             struct tag_entry *p = tag_get(e->deps[d], 1);
@@ -301,8 +307,58 @@ int starpu_task_submit(struct starpu_task *t)
         rt_sched_push(j);
     }
     rt_unlock();
+    rt_drain();
     if (sync) starpu_task_wait(t);
     return 0;
+}
+
+int starpu_task_submit(struct starpu_task *t) { return rt_submit(t, 0); }
+
+/* task.c:1577: no data or tag dependencies -- the caller holds the data */
+int starpu_task_submit_nodeps(struct starpu_task *t) { return rt_submit(t, 1); }
+
+void rt_drain(void)
+{
+    for (;;) {
+        rt_lock();
+        struct rt_job *j = rt.defer_head;
+        if (j) {
+            rt.defer_head = j->defer_next;
+            if (!rt.defer_head) rt.defer_tail = NULL;
+        }
+        rt_unlock();
+        if (!j) return;
+        struct starpu_task *t = j->task;
+        if (t->prologue_callback_func && !j->prologue_done) {
+            j->prologue_done = 1;
+            struct starpu_task *prev = rt_current_task_get();
+            rt_current_task_set(t);
+            t->prologue_callback_func(t->prologue_callback_arg);
+            rt_current_task_set(prev);
+        }
+        if (t->where == STARPU_NOWHERE) {
+            rt_job_terminate(j, 0.0); /* nothing to run (sched_policy.c:676) */
+        } else {
+            rt_lock();
+            rt_sched_push(j);
+            rt_unlock();
+        }
+    }
+}
+
+/* before or after the task's submission (jobs.c:355-361) */
+void starpu_task_end_dep_add(struct starpu_task *t, int nb_deps)
+{
+    rt_lock();
+    t->nb_termination_call_required += nb_deps;
+    rt_unlock();
+}
+
+void starpu_task_end_dep_release(struct starpu_task *t)
+{
+    struct rt_job *j = t->starpu_private;
+    STARPU_ASSERT_MSG(j, "starpu_task_end_dep_release on a task that is not submitted");
+    rt_job_terminate(j, 0.0);
 }
 
 /* Called with the runtime lock NOT held, after the job's work completed. */
@@ -313,7 +369,21 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
         int w = j->worker;
         rt_perfmodel_feedback(t, &rt.workers[w >= 0 ? w : 0].arch, measured_us);
     }
-    if (t->callback_func) t->callback_func(t->callback_arg);
+    /* a termination held by starpu_task_end_dep_add needs one more call per
+     * added dependency (jobs.c:363-373) */
+    rt_lock();
+    if (t->nb_termination_call_required > 0) {
+        t->nb_termination_call_required--;
+        rt_unlock();
+        return;
+    }
+    rt_unlock();
+    if (t->callback_func) {
+        struct starpu_task *prev = rt_current_task_get();
+        rt_current_task_set(t);
+        t->callback_func(t->callback_arg);
+        rt_current_task_set(prev);
+    }
     rt_lock();
     j->terminated = 1;
     t->status = STARPU_TASK_FINISHED;
@@ -350,6 +420,7 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
     pthread_cond_broadcast(&rt.all_done);
     rt_unlock();
     if (destroy) starpu_task_destroy(t);
+    rt_drain();
 }
 
 /* Graph mode: hand the pending jobs to the CUDA driver as one graph, in a
@@ -508,6 +579,11 @@ static int build_task(struct starpu_task *t, struct starpu_codelet *cl, va_list 
             t->callback_arg = va_arg(ap, void *);
         } else if (type == STARPU_CALLBACK_ARG) {
             t->callback_arg = va_arg(ap, void *);
+        } else if (type == STARPU_PROLOGUE_CALLBACK) {
+            t->prologue_callback_func = va_arg(ap, void (*)(void *));
+        } else if (type == STARPU_PROLOGUE_CALLBACK_ARG || type == STARPU_PROLOGUE_CALLBACK_ARG_NFREE) {
+            t->prologue_callback_arg = va_arg(ap, void *);
+            t->prologue_callback_arg_free = type == STARPU_PROLOGUE_CALLBACK_ARG;
         } else if (type == STARPU_PRIORITY) {
             t->priority = va_arg(ap, int);
         } else if (type == STARPU_FLOPS) {
@@ -612,3 +688,79 @@ void starpu_codelet_unpack_args(void *cl_arg, ...)
     }
     va_end(ap);
 }
+
+/* ------------------------------------------------------- fault tolerance
+ *
+ * src/core/task.c:2474-2575.  starpu_task_ft_prologue, given as a task's
+ * prologue callback, turns that task into a meta task: it keeps its data
+ * dependencies and runs nothing (STARPU_NOWHERE); a copy submitted without
+ * dependencies does the work, and the copy's callback (check_ft) either
+ * releases the meta task's termination or submits another copy when the work
+ * called starpu_task_ft_failed. */
+
+static void ft_check_support(const struct starpu_task *t)
+{
+    for (int i = 0; i < t->nbuffers; ++i)
+        STARPU_ASSERT_MSG(t->modes[i] == STARPU_R || t->modes[i] == STARPU_W,
+                          "starpu_task_failed is only supported for tasks with access modes STARPU_R and STARPU_W");
+}
+
+struct starpu_task *starpu_task_ft_create_retry(const struct starpu_task *meta_task,
+                                                const struct starpu_task *template_task, void (*check_ft)(void *))
+{
+    STARPU_ASSERT_MSG(!meta_task->cl_arg_free || !meta_task->cl_arg, "not supported yet");
+    STARPU_ASSERT_MSG(!meta_task->callback_func, "not supported");
+    struct starpu_task *n = starpu_task_create();
+    *n = *template_task;
+    n->prologue_callback_func = NULL;
+    n->prologue_callback_arg = NULL;
+    n->prologue_callback_arg_free = 0;
+    n->cl_arg_free = 0; /* the meta task keeps its argument */
+    n->callback_func = check_ft;
+    n->callback_arg = (void *)meta_task;
+    n->callback_arg_free = 0;
+    n->use_tag = 0;
+    n->synchronous = 0;
+    n->destroy = 1;
+    n->regenerate = 0;
+    n->no_submitorder = 1;
+    n->failed = 0;
+    n->nb_termination_call_required = 0;
+    n->status = STARPU_TASK_INIT;
+    n->starpu_private = NULL;
+    return n;
+}
+
+static void default_check_ft(void *arg)
+{
+    struct starpu_task *meta_task = arg;
+    struct starpu_task *current = starpu_task_get_current();
+    if (!current->failed) {
+        starpu_task_ft_success(meta_task);
+        return;
+    }
+    struct starpu_task *n = starpu_task_ft_create_retry(meta_task, current, default_check_ft);
+    const int rc = starpu_task_submit_nodeps(n);
+    STARPU_ASSERT(!rc);
+}
+
+void starpu_task_ft_prologue(void *arg)
+{
+    struct starpu_task *meta_task = starpu_task_get_current();
+    void (*check_ft)(void *) = arg ? (void (*)(void *))arg : default_check_ft;
+    struct starpu_task *n = starpu_task_ft_create_retry(meta_task, meta_task, check_ft);
+    /* the meta task's termination waits for the work's success; held before
+     * the work is submitted, so that a fast success cannot come first */
+    starpu_task_end_dep_add(meta_task, 1);
+    meta_task->where = STARPU_NOWHERE;
+    const int rc = starpu_task_submit_nodeps(n);
+    STARPU_ASSERT(!rc);
+}
+
+void starpu_task_ft_failed(struct starpu_task *t)
+{
+    ft_check_support(t);
+    t->failed = 1;
+}
+
+void starpu_task_ft_success(struct starpu_task *meta_task) { starpu_task_end_dep_release(meta_task); }

@@ -70,6 +70,22 @@ static void where_k(void *descr[], void *arg)
 }
 static struct starpu_codelet cl_where = {.cpu_funcs = {where_k}, .nbuffers = 0};
 
+/* b = a + 1, reported as failed on its first three runs */
+static int ft_attempts = 0;
+static void flaky_inc(void *descr[], void *arg)
+{
+    (void)arg;
+    *(long *)STARPU_VARIABLE_GET_PTR(descr[1]) = *(long *)STARPU_VARIABLE_GET_PTR(descr[0]) + 1;
+    if (++ft_attempts < 4) starpu_task_ft_failed(starpu_task_get_current());
+}
+static struct starpu_codelet cl_flaky = {.cpu_funcs = {flaky_inc}, .nbuffers = 2, .modes = {STARPU_R, STARPU_W}};
+
+static void release_later(void *arg)
+{
+    usleep(20000);
+    starpu_task_end_dep_release((struct starpu_task *)arg);
+}
+
 static int cb_count = 0;
 static void cb(void *arg) { __sync_fetch_and_add(&cb_count, *(int *)arg); }
 
@@ -201,6 +217,52 @@ int main(void)
         struct starpu_perfmodel loaded;
         CHECK(starpu_perfmodel_load_symbol("gb300_test_tile_inc", &loaded) == 0, "perfmodel_reload");
         starpu_perfmodel_unload_model(&loaded);
+    }
+    /* fault tolerance with the default retry policy (task.c:2522-2541): the
+     * work runs until it stops failing; a task reading its output waits for
+     * the meta task, which holds the data until then */
+    {
+        long a = 5, b = 0, c = 0;
+        starpu_data_handle_t ha, hb, hc;
+        starpu_variable_data_register(&ha, STARPU_MAIN_RAM, (uintptr_t)&a, sizeof a);
+        starpu_variable_data_register(&hb, STARPU_MAIN_RAM, (uintptr_t)&b, sizeof b);
+        starpu_variable_data_register(&hc, STARPU_MAIN_RAM, (uintptr_t)&c, sizeof c);
+        int rc = starpu_task_insert(&cl_flaky, STARPU_PROLOGUE_CALLBACK, starpu_task_ft_prologue,
+                                    STARPU_PROLOGUE_CALLBACK_ARG_NFREE, NULL, STARPU_R, ha, STARPU_W, hb, 0);
+        rc |= starpu_task_insert(&cl_copy, STARPU_R, hb, STARPU_W, hc, 0);
+        starpu_task_wait_for_all();
+        starpu_data_unregister(ha);
+        starpu_data_unregister(hb);
+        starpu_data_unregister(hc);
+        CHECK(rc == 0 && ft_attempts == 4 && b == 6 && c == 6 && a == 5, "ft_default_retry");
+    }
+    /* end dependencies (jobs.c:339-373): a STARPU_NOWHERE task holding its
+     * data terminates only on the release, and its reader waits for that */
+    {
+        long v = 0, w = -1;
+        starpu_data_handle_t hv, hw;
+        starpu_variable_data_register(&hv, STARPU_MAIN_RAM, (uintptr_t)&v, sizeof v);
+        starpu_variable_data_register(&hw, STARPU_MAIN_RAM, (uintptr_t)&w, sizeof w);
+        struct starpu_task *hold = starpu_task_create();
+        hold->cl = &cl_flaky;
+        hold->handles[0] = hv;
+        hold->handles[1] = hv;
+        hold->modes[0] = STARPU_R;
+        hold->modes[1] = STARPU_W;
+        hold->where = STARPU_NOWHERE;
+        starpu_task_end_dep_add(hold, 1); /* before submission */
+        int rc = starpu_task_submit(hold);
+        rc |= starpu_task_insert(&cl_copy, STARPU_R, hv, STARPU_W, hw, 0);
+        usleep(5000);
+        const long before = w; /* the copy cannot have run yet */
+        v = 42;                /* the held data, written while the meta task owns it */
+        pthread_t th;
+        pthread_create(&th, NULL, (void *(*)(void *))release_later, hold);
+        starpu_task_wait_for_all();
+        pthread_join(th, NULL);
+        starpu_data_unregister(hv);
+        starpu_data_unregister(hw);
+        CHECK(rc == 0 && before == -1 && w == 42, "end_dep_holds_termination");
     }
     /* scheduling contexts (src/core/sched_ctx.c): a context's tasks run on
      * its workers only; a context without a capable worker refuses tasks;

@@ -195,6 +195,24 @@ def test_unchanged_driver_empty_contexts_submit_nothing():
     assert nums[:2] == [0.0, 0.0], r.stdout
 
 
+@pytest.mark.parametrize("ncpu", [1, 4])
+def test_unchanged_fault_tolerance_retry_test(ncpu):
+    """StarPU's own tests/fault-tolerance/retry.c, compiled unchanged (oracle
+    recipe `ref-ft`): its task reports a failure ten times through
+    starpu_task_ft_failed; starpu_task_ft_prologue and the test's check_ft
+    callback resubmit it without dependencies until it succeeds, while the
+    meta task holds the data.  x must stay 12 and y become 13."""
+    if not os.path.isfile(os.path.join(REF, "tests", "fault-tolerance", "retry.c")):
+        pytest.skip("reference tree not available on this machine")
+    _lib()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={REF}", "_ref/ft_retry_ref"], check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", "ft_retry_ref")
+    r = subprocess.run([exe], env=_env(STARPU_NCUDA=0, STARPU_NCPU=ncpu), capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stderr.count("failing\n") == 10 and r.stderr.count("succeed\n") == 1, r.stderr
+    assert "Value x = 12 (expected 12)" in r.stderr and "Value y = 13 (expected 13)" in r.stderr, r.stderr
+
+
 def test_unchanged_reference_driver_links_gb300_codelets():
     exe = _ref_driver("_ref/cholesky_implicit_gb300")
     r = subprocess.run([exe, "-size", "256", "-nblocks", "2"], env=_env(STARPU_NCUDA=0, STARPU_NCPU=2),
