@@ -91,6 +91,8 @@ typedef pthread_barrier_t starpu_pthread_barrier_t;
 #define STARPU_PTHREAD_CREATE(thread, attr, routine, arg) \
     _STARPU_PTHREAD_CHECK(pthread_create(thread, attr, routine, arg), "pthread_create")
 #define STARPU_PTHREAD_JOIN(thread, retval) _STARPU_PTHREAD_CHECK(pthread_join(thread, retval), "pthread_join")
+#define STARPU_PTHREAD_MUTEX_INITIALIZER PTHREAD_MUTEX_INITIALIZER
+#define STARPU_PTHREAD_COND_INITIALIZER PTHREAD_COND_INITIALIZER
 #define STARPU_PTHREAD_MUTEX_INIT(mutex, attr) _STARPU_PTHREAD_CHECK(pthread_mutex_init(mutex, attr), "pthread_mutex_init")
 #define STARPU_PTHREAD_MUTEX_DESTROY(mutex) _STARPU_PTHREAD_CHECK(pthread_mutex_destroy(mutex), "pthread_mutex_destroy")
 #define STARPU_PTHREAD_MUTEX_LOCK(mutex) _STARPU_PTHREAD_CHECK(pthread_mutex_lock(mutex), "pthread_mutex_lock")
@@ -366,10 +368,17 @@ struct starpu_task {
     unsigned color;        /* display colour of the task in traces */
     unsigned failed;       /* set by starpu_task_ft_failed */
     int nb_termination_call_required; /* starpu_task_end_dep_add calls not yet released */
+    struct starpu_task **declared_deps; /* runtime-private: starpu_task_declare_deps_array */
+    unsigned ndeclared_deps;
     void *starpu_private;  /* runtime job */
 };
 
 #define STARPU_TASK_INVALID 0
+#define STARPU_VARIABLE_NBUFFERS (-1) /* the task's own nbuffers */
+
+/* a codelet that does nothing, on every kind of worker */
+extern struct starpu_codelet starpu_codelet_nop;
+void starpu_codelet_nop_func(void *descr[], void *arg);
 #define STARPU_DEFAULT_PRIO 0
 
 void starpu_task_init(struct starpu_task *task);
@@ -378,11 +387,19 @@ void starpu_task_clean(struct starpu_task *task);
 void starpu_task_destroy(struct starpu_task *task);
 int starpu_task_submit(struct starpu_task *task);
 int starpu_task_wait(struct starpu_task *task);
+int starpu_task_wait_array(struct starpu_task **tasks, unsigned nb_tasks);
+#define STARPU_TASK_GET_NBUFFERS(task) ((unsigned)((task)->cl->nbuffers == STARPU_VARIABLE_NBUFFERS ? (task)->nbuffers : (task)->cl->nbuffers))
+#define STARPU_TASK_GET_HANDLE(task, i) ((task)->handles[i])
+#define STARPU_TASK_GET_MODE(task, i) ((task)->cl->nbuffers == STARPU_VARIABLE_NBUFFERS || !(task)->cl->modes[i] ? (task)->modes[i] : (task)->cl->modes[i])
 int starpu_task_wait_for_all(void);
 int starpu_task_wait_for_n_submitted(unsigned n);
 int starpu_task_nsubmitted(void);
 int starpu_task_nready(void);
 struct starpu_task *starpu_task_get_current(void);
+/* explicit task dependencies (starpu_task_dep.h): before `task` is submitted;
+ * the tasks it waits for may be submitted before or after it, or be done */
+void starpu_task_declare_deps_array(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[]);
+void starpu_task_declare_deps(struct starpu_task *task, unsigned ndeps, ...);
 /* submission without data or tag dependencies (the caller already holds the data) */
 int starpu_task_submit_nodeps(struct starpu_task *task);
 /* termination of `task` waits for nb_deps more starpu_task_end_dep_release calls */
@@ -609,6 +626,12 @@ int starpu_conf_noworker(struct starpu_conf *conf);
 /* integer environment variables (starpu_helper.h): -1 when unset; a value
  * that is not a non-negative integer aborts */
 int starpu_get_env_number(const char *str);
+void starpu_usleep(float nb_micro_sec);
+int starpu_worker_get_count_by_type(enum starpu_worker_archtype type);
+/* a handle without data, for dependencies only */
+void starpu_void_data_register(starpu_data_handle_t *handle);
+#define STARPU_ATOMIC_ADD(ptr, value) (__sync_fetch_and_add((ptr), (value)) + (value))
+#define STARPU_ATTRIBUTE_ALIGNED(size) __attribute__((aligned(size)))
 static inline int starpu_get_env_number_default(const char *str, int defval)
 {
     const int n = starpu_get_env_number(str);

@@ -10,6 +10,7 @@
  * CUDA worker; default 1).
  */
 #define _GNU_SOURCE
+#include <errno.h>
 #include <stdarg.h>
 #include <string.h>
 #include <sched.h>
@@ -78,6 +79,24 @@ int starpu_get_env_number(const char *str)
     if (*end || n < 0) starpu_gb300_abort_msg(__FILE__, __LINE__, __func__,
                                               "The %s environment variable must contain a non-negative integer", str);
     return (int)n;
+}
+
+void starpu_usleep(float nb_micro_sec)
+{
+    if (nb_micro_sec <= 0) return;
+    struct timespec ts;
+    ts.tv_sec = (time_t)(nb_micro_sec / 1e6f);
+    ts.tv_nsec = (long)((nb_micro_sec - (float)ts.tv_sec * 1e6f) * 1e3f);
+    if (ts.tv_nsec >= 1000000000L) ts.tv_nsec = 999999999L;
+    while (nanosleep(&ts, &ts) != 0 && errno == EINTR) {
+    }
+}
+
+int starpu_worker_get_count_by_type(enum starpu_worker_archtype type)
+{
+    int n = 0;
+    for (int i = 0; i < rt.nworkers; ++i) n += rt.workers[i].type == type;
+    return n;
 }
 
 int starpu_conf_noworker(struct starpu_conf *conf)

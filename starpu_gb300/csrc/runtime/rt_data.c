@@ -90,6 +90,15 @@ void starpu_variable_data_register(starpu_data_handle_t *handle, int home_node, 
     *handle = h;
 }
 
+/* a handle that carries no data (void_interface.c): a zero-byte variable at
+ * a static host address, valid in RAM from the start, so tasks order on it
+ * and no copy ever moves a byte */
+void starpu_void_data_register(starpu_data_handle_t *handle)
+{
+    static char nothing;
+    starpu_variable_data_register(handle, STARPU_MAIN_RAM, (uintptr_t)&nothing, 0);
+}
+
 void starpu_data_set_name(starpu_data_handle_t handle, const char *name)
 {
     if (handle && name) snprintf(handle->name, sizeof handle->name, "%s", name);

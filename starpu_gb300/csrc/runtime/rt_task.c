@@ -35,9 +35,12 @@ void starpu_task_clean(struct starpu_task *t)
     if (t->cl_arg_free && t->cl_arg) free(t->cl_arg);
     if (t->callback_arg_free && t->callback_arg) free(t->callback_arg);
     if (t->prologue_callback_arg_free && t->prologue_callback_arg) free(t->prologue_callback_arg);
+    free(t->declared_deps);
     t->cl_arg = NULL;
     t->callback_arg = NULL;
     t->prologue_callback_arg = NULL;
+    t->declared_deps = NULL;
+    t->ndeclared_deps = 0;
 }
 
 void starpu_task_destroy(struct starpu_task *t)
@@ -172,6 +175,11 @@ void starpu_tag_notify_from_apps(starpu_tag_t id)
     rt_drain();
 }
 
+/* rt_submit flags: no data or tag dependencies; already counted as submitted
+ * (a regenerated task) */
+enum { SUBMIT_NODEPS = 1, SUBMIT_COUNTED = 2 };
+static int rt_submit(struct starpu_task *t, int flags);
+
 /* ---------------------------------------------------------- dependencies */
 
 static void add_edge(struct rt_job *from, struct rt_job *to)
@@ -189,6 +197,77 @@ static void add_edge(struct rt_job *from, struct rt_job *to)
         to->prev = realloc(to->prev, sizeof *to->prev * to->capprev);
     }
     to->prev[to->nprev++] = from;
+}
+
+/* Explicit task dependencies (src/core/dependencies/task_deps.c semantics):
+ * a declared predecessor that is done adds nothing, a submitted one an edge;
+ * one not submitted yet holds the dependent (counted with its tag waits, so
+ * that graph mode keeps it pending) until the predecessor is submitted. */
+struct task_waiter {
+    struct starpu_task *pred;
+    struct rt_job *job;
+    struct task_waiter *next;
+};
+static struct task_waiter *task_waiters; /* guarded by the runtime lock */
+
+void starpu_task_declare_deps_array(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[])
+{
+    if (!ndeps) return;
+    STARPU_ASSERT_MSG(!task->starpu_private, "dependencies must be declared before the task is submitted");
+    task->declared_deps = realloc(task->declared_deps, sizeof *task->declared_deps * (task->ndeclared_deps + ndeps));
+    memcpy(task->declared_deps + task->ndeclared_deps, task_array, sizeof *task_array * ndeps);
+    task->ndeclared_deps += ndeps;
+}
+
+void starpu_task_declare_deps(struct starpu_task *task, unsigned ndeps, ...)
+{
+    if (!ndeps) return;
+    struct starpu_task **deps = malloc(sizeof *deps * ndeps);
+    va_list ap;
+    va_start(ap, ndeps);
+    for (unsigned i = 0; i < ndeps; ++i) deps[i] = va_arg(ap, struct starpu_task *);
+    va_end(ap);
+    starpu_task_declare_deps_array(task, ndeps, deps);
+    free(deps);
+}
+
+/* called with the runtime lock held, as job j of its task is submitted */
+static void link_declared_deps(struct rt_job *j)
+{
+    struct starpu_task *t = j->task;
+    for (unsigned i = 0; i < t->ndeclared_deps; ++i) {
+        struct starpu_task *p = t->declared_deps[i];
+        if (!p || p == t || p->status == STARPU_TASK_FINISHED) continue;
+        if (p->starpu_private) {
+            add_edge(p->starpu_private, j);
+        } else {
+            struct task_waiter *w = malloc(sizeof *w);
+            w->pred = p;
+            w->job = j;
+            w->next = task_waiters;
+            task_waiters = w;
+            j->ndeps++;
+            j->tag_waits++;
+        }
+    }
+}
+
+/* called with the runtime lock held, as job j of its task is submitted:
+ * tasks that declared a dependency on it before now wait for it */
+static void link_waiting_successors(struct rt_job *j)
+{
+    for (struct task_waiter **pw = &task_waiters; *pw;) {
+        struct task_waiter *w = *pw;
+        if (w->pred != j->task) {
+            pw = &w->next;
+            continue;
+        }
+        add_edge(j, w->job);
+        w->job->ndeps--;
+        w->job->tag_waits--;
+        *pw = w->next;
+        free(w);
+    }
 }
 
 static void add_reader(starpu_data_handle_t h, struct rt_job *j)
@@ -217,8 +296,9 @@ int rt_can_execute(struct rt_worker *w, struct starpu_task *t)
     return 1;
 }
 
-static int rt_submit(struct starpu_task *t, int nodeps)
+static int rt_submit(struct starpu_task *t, int flags)
 {
+    const int nodeps = flags & SUBMIT_NODEPS;
     STARPU_ASSERT(rt.initialized);
     if (t->cl) {
         int nb = t->cl->nbuffers >= 0 ? t->cl->nbuffers : t->nbuffers;
@@ -251,8 +331,10 @@ static int rt_submit(struct starpu_task *t, int nodeps)
 
     rt_lock();
     j->seq = rt.seq++;
-    rt.nsubmitted++;
-    rt_ctx_count(t->sched_ctx, +1);
+    if (!(flags & SUBMIT_COUNTED)) {
+        rt.nsubmitted++;
+        rt_ctx_count(t->sched_ctx, +1);
+    }
     j->ndeps = 1; /* held until submission completes */
     if (t->sequential_consistency && !nodeps) {
         for (int i = 0; i < t->nbuffers; ++i) {
@@ -294,6 +376,8 @@ static int rt_submit(struct starpu_task *t, int nodeps)
         j->tag = t->tag_id;
         j->has_tag = 1;
     }
+    if (!nodeps && t->ndeclared_deps) link_declared_deps(j);
+    if (task_waiters) link_waiting_successors(j);
     if (rt.graph_mode) {
         if (rt.npending == rt.cappending) {
             rt.cappending = rt.cappending ? 2 * rt.cappending : 1024;
@@ -315,7 +399,7 @@ static int rt_submit(struct starpu_task *t, int nodeps)
 int starpu_task_submit(struct starpu_task *t) { return rt_submit(t, 0); }
 
 /* task.c:1577: no data or tag dependencies -- the caller holds the data */
-int starpu_task_submit_nodeps(struct starpu_task *t) { return rt_submit(t, 1); }
+int starpu_task_submit_nodeps(struct starpu_task *t) { return rt_submit(t, SUBMIT_NODEPS); }
 
 void rt_drain(void)
 {
@@ -384,9 +468,15 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
         t->callback_func(t->callback_arg);
         rt_current_task_set(prev);
     }
+    /* a task still marked regenerate after its callback runs again
+     * (jobs.c): this run's job is released first, the task stays counted as
+     * submitted (so waits for all tasks do not end in between), then it is
+     * submitted anew */
+    const int regen = t->regenerate;
+    if (regen) STARPU_ASSERT_MSG(t->detach && !t->synchronous, "a regenerated task must be detached and asynchronous");
     rt_lock();
     j->terminated = 1;
-    t->status = STARPU_TASK_FINISHED;
+    if (!regen) t->status = STARPU_TASK_FINISHED;
     for (int i = 0; i < t->nbuffers; ++i)
         if (t->handles[i]) rt_data_forget_job(t->handles[i], j);
     for (int s = 0; s < j->nsucc; ++s) {
@@ -410,15 +500,22 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
         }
         pthread_cond_broadcast(&tag_cond);
     }
-    int destroy = t->destroy && t->detach;
+    int destroy = !regen && t->destroy && t->detach;
     t->starpu_private = NULL;
     free(j->succ);
     free(j->prev);
     free(j);
-    rt.nsubmitted--;
-    rt_ctx_count(t->sched_ctx, -1);
+    if (!regen) {
+        rt.nsubmitted--;
+        rt_ctx_count(t->sched_ctx, -1);
+    }
     pthread_cond_broadcast(&rt.all_done);
     rt_unlock();
+    if (regen) {
+        t->starpu_private = NULL;
+        const int rc = rt_submit(t, SUBMIT_COUNTED);
+        STARPU_ASSERT_MSG(rc == 0, "regenerating task %s failed (%d)", t->name ? t->name : "?", rc);
+    }
     if (destroy) starpu_task_destroy(t);
     rt_drain();
 }
@@ -526,6 +623,15 @@ int starpu_task_wait(struct starpu_task *t)
     rt_lock();
     while (t->status != STARPU_TASK_FINISHED) pthread_cond_wait(&rt.all_done, &rt.lock);
     rt_unlock();
+    return 0;
+}
+
+int starpu_task_wait_array(struct starpu_task **tasks, unsigned nb_tasks)
+{
+    for (unsigned i = 0; i < nb_tasks; ++i) {
+        const int rc = starpu_task_wait(tasks[i]);
+        if (rc) return rc;
+    }
     return 0;
 }
 
@@ -726,6 +832,8 @@ struct starpu_task *starpu_task_ft_create_retry(const struct starpu_task *meta_t
     n->no_submitorder = 1;
     n->failed = 0;
     n->nb_termination_call_required = 0;
+    n->declared_deps = NULL;
+    n->ndeclared_deps = 0;
     n->status = STARPU_TASK_INIT;
     n->starpu_private = NULL;
     return n;
@@ -764,3 +872,15 @@ void starpu_task_ft_failed(struct starpu_task *t)
 }
 
 void starpu_task_ft_success(struct starpu_task *meta_task) { starpu_task_end_dep_release(meta_task); }
+
+void starpu_codelet_nop_func(void *descr[], void *arg)
+{
+    (void)descr;
+    (void)arg;
+}
+
+struct starpu_codelet starpu_codelet_nop = {
+    .cpu_funcs = {starpu_codelet_nop_func},
+    .cuda_funcs = {starpu_codelet_nop_func},
+    .nbuffers = 0,
+};
