@@ -678,6 +678,8 @@ int starpu_profiling_status_set(int status);
 int starpu_profiling_status_get(void);
 /* prints the runtime's host<->device transfer totals (starpu_profiling.h) */
 void starpu_profiling_bus_helper_display_summary(void);
+/* with STARPU_WORKER_STATS=1: tasks run per worker (also printed at shutdown) */
+void starpu_profiling_worker_helper_display_summary(void);
 void starpu_bound_print_dot(FILE *output);
 
 /* ================================================= random numbers (starpu_rand.h) */

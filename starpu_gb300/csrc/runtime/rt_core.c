@@ -198,6 +198,7 @@ void starpu_shutdown(void)
     if (!rt.initialized) return;
     if (--rt.initialized > 0) return;
     starpu_task_wait_for_all();
+    starpu_profiling_worker_helper_display_summary();
     rt_lock();
     rt.shutting_down = 1;
     for (int i = 0; i < rt.nworkers; ++i) pthread_cond_broadcast(&rt.workers[i].cond);
@@ -527,6 +528,27 @@ void starpu_profiling_bus_helper_display_summary(void)
     fprintf(stderr, "\tNUMA 0 -> CUDA 0\t%.4f MB\n", h2d / 1048576.0);
     fprintf(stderr, "\tCUDA 0 -> NUMA 0\t%.4f MB\n", d2h / 1048576.0);
     fprintf(stderr, "Total transfers: %.4f MB\n#---------------------\n", (h2d + d2h) / 1048576.0);
+}
+
+/* STARPU_WORKER_STATS=1: tasks run per worker, printed at shutdown to
+ * stderr or STARPU_WORKER_STATS_FILE, in the layout of
+ * profiling_helpers.c:88-181 without per-task profiling (time splits need
+ * STARPU_PROFILING, which this runtime does not record) */
+void starpu_profiling_worker_helper_display_summary(void)
+{
+    const char *on = getenv("STARPU_WORKER_STATS");
+    if (!on || !atoi(on)) return;
+    const char *path = getenv("STARPU_WORKER_STATS_FILE");
+    FILE *f = path && *path ? fopen(path, "w") : stderr;
+    if (!f) starpu_gb300_abort_msg(__FILE__, __LINE__, __func__, "cannot open %s for the worker stats", path);
+    fprintf(f, "\n#---------------------\nWorker stats:\n");
+    for (int w = 0; w < rt.nworkers; ++w) {
+        char name[64];
+        starpu_worker_get_name(w, name, sizeof name);
+        fprintf(f, "%-32s\n\t%d task(s)\n", name, (int)rt.workers[w].ntasks);
+    }
+    fprintf(f, "#---------------------\n");
+    if (f != stderr) fclose(f);
 }
 
 static int profiling_status = 0;

@@ -55,6 +55,22 @@ def test_runtime_c_suite(runtime_test_binary, tmp_path, ncpu):
     assert (tmp_path / "codelets" / "45" / "gb300_test_tile_inc.testhost").exists()
 
 
+def test_worker_stats_at_shutdown(runtime_test_binary, tmp_path):
+    """STARPU_WORKER_STATS=1 prints, at shutdown, the tasks each worker ran
+    (profiling_helpers.c:88-181 without per-task profiling)."""
+    out = tmp_path / "stats.txt"
+    r = subprocess.run([runtime_test_binary], env=_env(STARPU_NCUDA=0, STARPU_NCPU=2, STARPU_PERF_MODEL_DIR=tmp_path,
+                                                         STARPU_HISTORY_MAX_ERROR=100000, STARPU_WORKER_STATS=1,
+                                                         STARPU_WORKER_STATS_FILE=out),
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    text = out.read_text()
+    assert text.startswith("\n#---------------------\nWorker stats:\n") and text.endswith("#---------------------\n")
+    counts = [int(c) for c in re.findall(r"^\t(\d+) task\(s\)$", text, re.M)]
+    names = re.findall(r"^(CPU \d+) *$", text, re.M)
+    assert names == ["CPU 0", "CPU 1"] and len(counts) == 2 and sum(counts) > 100, text
+
+
 def _ref_driver(target):
     if not os.path.isdir(os.path.join(REF, "examples", "cholesky")):
         pytest.skip("reference tree not available on this machine")
