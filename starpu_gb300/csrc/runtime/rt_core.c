@@ -168,6 +168,12 @@ int starpu_initialize(struct starpu_conf *user_conf, int *argc, char ***argv)
     rt.ncuda = ndev;
     rt.ncpu = ncpu;
     rt.graph_mode = (ndev > 0 && ncpu == 0) ? env_int("STARPU_GB300_GRAPH", 1) : 0;
+    /* STARPU_COMMUTE writers of one handle run in any order, one at a time,
+     * where every worker is a CPU worker (they run their tasks synchronously);
+     * with a CUDA worker they keep their submission order (a valid order of
+     * commuting tasks).  STARPU_GB300_COMMUTE=0 keeps that order everywhere. */
+    rt.relaxed_commute = ndev == 0 && env_int("STARPU_GB300_COMMUTE", 1) != 0;
+    pthread_cond_init(&rt.commute_cond, NULL);
     for (int i = 0; i < rt.nworkers; ++i) {
         struct rt_worker *w = &rt.workers[i];
         w->dev.type = w->type;

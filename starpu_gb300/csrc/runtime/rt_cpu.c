@@ -11,6 +11,7 @@ static void run_cpu(struct rt_worker *w, struct rt_job *j)
 {
     struct starpu_task *t = j->task;
     rt_lock();
+    if (rt.relaxed_commute) rt_commute_acquire(t);
     for (int i = 0; i < t->nbuffers; ++i) {
         starpu_data_handle_t h = t->handles[i];
         if (!h) continue;
@@ -27,6 +28,7 @@ static void run_cpu(struct rt_worker *w, struct rt_job *j)
     rt_lock();
     for (int i = 0; i < t->nbuffers; ++i)
         if (t->handles[i] && (t->modes[i] & STARPU_W)) rt_data_after_write(t->handles[i], RT_NODE_RAM);
+    if (rt.relaxed_commute) rt_commute_release(t);
     rt.stats.tasks_cpu++;
     w->ntasks++;
     rt_unlock();

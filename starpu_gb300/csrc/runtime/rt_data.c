@@ -409,6 +409,11 @@ void rt_data_forget_job(starpu_data_handle_t h, struct rt_job *j)
             h->readers[i] = h->readers[--h->nreaders];
             --i;
         }
+    for (int i = 0; i < h->ncommuters; ++i)
+        if (h->commuters[i] == j) {
+            h->commuters[i] = h->commuters[--h->ncommuters];
+            --i;
+        }
 }
 
 /* Bring every child's data to `node`; returns whether all children are valid on the other node. */
@@ -435,6 +440,7 @@ static void free_children(starpu_data_handle_t h)
         struct _starpu_data_state *c = h->children[i];
         if (c->partitioned) free_children(c);
         free(c->readers);
+        free(c->commuters);
         free(c);
     }
     free(h->children);
@@ -485,6 +491,7 @@ static void unregister(starpu_data_handle_t h, int coherent)
     if (h->owned[RT_NODE_GPU]) rt_cuda_free(h->owned[RT_NODE_GPU]);
     if (h->owned[RT_NODE_RAM]) free(h->owned[RT_NODE_RAM]);
     free(h->readers);
+    free(h->commuters);
     free(h);
 }
 

@@ -55,6 +55,11 @@ struct _starpu_data_state {
     struct rt_job *last_writer;
     struct rt_job **readers;
     int nreaders, capreaders;
+    /* STARPU_COMMUTE writers since the last plain writer (rt.relaxed_commute):
+     * unordered among themselves, run one at a time (commute_busy) */
+    struct rt_job **commuters;
+    int ncommuters, capcommuters;
+    int commute_busy;
     char name[48];
 };
 
@@ -104,6 +109,8 @@ struct rt_state {
     int nworkers, ncpu, ncuda;
     int graph_mode;             /* CUDA-only runs: whole-DAG CUDA graphs */
     int default_seq_consistency;
+    int relaxed_commute;        /* STARPU_COMMUTE writers unordered (runs without a CUDA worker) */
+    pthread_cond_t commute_cond;
     int paused;
     uint64_t seq;
     long nsubmitted;            /* submitted and not terminated */
@@ -149,6 +156,10 @@ unsigned rt_ctx_resolve(struct starpu_task *t);
 int rt_ctx_has_worker(unsigned ctx, int worker);
 void rt_ctx_count(unsigned ctx, int delta);
 void rt_ctx_reset(void);
+
+/* rt_task.c: the busy flags of a task's STARPU_COMMUTE handles (runtime lock held) */
+void rt_commute_acquire(struct starpu_task *t);
+void rt_commute_release(struct starpu_task *t);
 
 /* rt_task.c: runs the deferred prologues and NOWHERE terminations; call it
  * without the lock after any section that may have pushed jobs */

@@ -270,6 +270,58 @@ static void link_waiting_successors(struct rt_job *j)
     }
 }
 
+static void add_commuter(starpu_data_handle_t h, struct rt_job *j)
+{
+    if (h->ncommuters == h->capcommuters) {
+        h->capcommuters = h->capcommuters ? 2 * h->capcommuters : 8;
+        h->commuters = realloc(h->commuters, sizeof *h->commuters * h->capcommuters);
+    }
+    h->commuters[h->ncommuters++] = j;
+}
+
+/* Commuting writers of one handle run one at a time: a task takes the busy
+ * flag of each handle it writes with STARPU_COMMUTE before it runs (in
+ * handle-address order, so two tasks never wait for each other) and gives
+ * them back when it is done.  Called with the runtime lock held. */
+static int commute_handles(struct starpu_task *t, starpu_data_handle_t *hs)
+{
+    int n = 0;
+    for (int i = 0; i < t->nbuffers; ++i) {
+        starpu_data_handle_t h = t->handles[i];
+        if (!h || !(t->modes[i] & STARPU_COMMUTE) || !(t->modes[i] & STARPU_W)) continue;
+        int k = n;
+        while (k > 0 && (uintptr_t)hs[k - 1] > (uintptr_t)h) {
+            hs[k] = hs[k - 1];
+            --k;
+        }
+        if (k > 0 && hs[k - 1] == h) { /* the same handle twice */
+            for (int q = k; q < n; ++q) hs[q] = hs[q + 1];
+            continue;
+        }
+        hs[k] = h;
+        ++n;
+    }
+    return n;
+}
+
+void rt_commute_acquire(struct starpu_task *t)
+{
+    starpu_data_handle_t hs[STARPU_NMAXBUFS];
+    const int n = commute_handles(t, hs);
+    for (int k = 0; k < n; ++k) {
+        while (hs[k]->commute_busy) pthread_cond_wait(&rt.commute_cond, &rt.lock);
+        hs[k]->commute_busy = 1;
+    }
+}
+
+void rt_commute_release(struct starpu_task *t)
+{
+    starpu_data_handle_t hs[STARPU_NMAXBUFS];
+    const int n = commute_handles(t, hs);
+    for (int k = 0; k < n; ++k) hs[k]->commute_busy = 0;
+    if (n) pthread_cond_broadcast(&rt.commute_cond);
+}
+
 static void add_reader(starpu_data_handle_t h, struct rt_job *j)
 {
     if (h->nreaders == h->capreaders) {
@@ -341,13 +393,23 @@ static int rt_submit(struct starpu_task *t, int flags)
             starpu_data_handle_t h = t->handles[i];
             enum starpu_data_access_mode m = t->modes[i];
             if (!h || !h->seq_consistency || (m & STARPU_SCRATCH) || (m & STARPU_REDUX)) continue;
-            if (m & STARPU_W) {
+            if ((m & STARPU_W) && (m & STARPU_COMMUTE) && rt.relaxed_commute) {
+                /* after the last plain writer and the readers since, in any
+                 * order with the other commuting writers
+                 * (implicit_data_deps.c) */
                 add_edge(h->last_writer, j);
                 for (int r = 0; r < h->nreaders; ++r) add_edge(h->readers[r], j);
+                add_commuter(h, j);
+            } else if (m & STARPU_W) {
+                add_edge(h->last_writer, j);
+                for (int r = 0; r < h->nreaders; ++r) add_edge(h->readers[r], j);
+                for (int c = 0; c < h->ncommuters; ++c) add_edge(h->commuters[c], j);
                 h->nreaders = 0;
+                h->ncommuters = 0;
                 h->last_writer = j;
             } else if (m & STARPU_R) {
                 add_edge(h->last_writer, j);
+                for (int c = 0; c < h->ncommuters; ++c) add_edge(h->commuters[c], j);
                 add_reader(h, j);
             }
         }

@@ -86,6 +86,19 @@ static void release_later(void *arg)
     starpu_task_end_dep_release((struct starpu_task *)arg);
 }
 
+/* v += k, flagging any overlap with another commuting writer of v */
+static int commute_active = 0, commute_overlap = 0;
+static void commute_add(void *descr[], void *arg)
+{
+    int k;
+    starpu_codelet_unpack_args(arg, &k, NULL);
+    if (__sync_add_and_fetch(&commute_active, 1) != 1) __sync_fetch_and_add(&commute_overlap, 1);
+    usleep(1000);
+    *(long *)STARPU_VARIABLE_GET_PTR(descr[0]) += k;
+    __sync_sub_and_fetch(&commute_active, 1);
+}
+static struct starpu_codelet cl_commute = {.cpu_funcs = {commute_add}, .nbuffers = 1, .modes = {STARPU_RW | STARPU_COMMUTE}};
+
 static int cb_count = 0;
 static void cb(void *arg) { __sync_fetch_and_add(&cb_count, *(int *)arg); }
 
@@ -263,6 +276,21 @@ int main(void)
         starpu_data_unregister(hv);
         starpu_data_unregister(hw);
         CHECK(rc == 0 && before == -1 && w == 42, "end_dep_holds_termination");
+    }
+    /* commuting writers (STARPU_RW | STARPU_COMMUTE): any order, never two at
+     * once on one handle; a plain reader after them sees all of them */
+    {
+        long v = 0, w = -1;
+        starpu_data_handle_t hv, hw;
+        starpu_variable_data_register(&hv, STARPU_MAIN_RAM, (uintptr_t)&v, sizeof v);
+        starpu_variable_data_register(&hw, STARPU_MAIN_RAM, (uintptr_t)&w, sizeof w);
+        int rc = 0;
+        for (int k = 1; k <= 16; ++k) rc |= starpu_task_insert(&cl_commute, STARPU_VALUE, &k, sizeof k, STARPU_RW | STARPU_COMMUTE, hv, 0);
+        rc |= starpu_task_insert(&cl_copy, STARPU_R, hv, STARPU_W, hw, 0);
+        starpu_task_wait_for_all();
+        starpu_data_unregister(hv);
+        starpu_data_unregister(hw);
+        CHECK(rc == 0 && commute_overlap == 0 && v == 136 && w == 136, "commute_exclusive_then_reader");
     }
     /* scheduling contexts (src/core/sched_ctx.c): a context's tasks run on
      * its workers only; a context without a capable worker refuses tasks;
