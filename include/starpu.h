@@ -242,6 +242,9 @@ void starpu_matrix_filter_block(void *father_interface, void *child_interface, s
                                 unsigned id, unsigned nparts);
 void starpu_matrix_filter_vertical_block(void *father_interface, void *child_interface, struct starpu_data_filter *f,
                                          unsigned id, unsigned nparts);
+/* vectors: nx split into nparts blocks, the remainder to the first ones */
+void starpu_vector_filter_block(void *father_interface, void *child_interface, struct starpu_data_filter *f,
+                                unsigned id, unsigned nparts);
 void starpu_filter_nparts_compute_chunk_size_and_offset(unsigned n, unsigned nparts, size_t elemsize, unsigned id,
                                                         size_t blocksize, size_t *chunk_size, size_t *offset);
 void starpu_data_partition(starpu_data_handle_t initial_handle, struct starpu_data_filter *f);

@@ -198,9 +198,18 @@ void starpu_matrix_filter_vertical_block(void *father, void *child, struct starp
     matrix_block(1, father, child, id, nparts);
 }
 
+/* nx split into nparts blocks, the remainder going to the first ones
+ * (vector_filters.c); the runtime hands its filters the nx x 1 matrix view */
+void starpu_vector_filter_block(void *father, void *child, struct starpu_data_filter *f, unsigned id, unsigned nparts)
+{
+    (void)f;
+    matrix_block(0, father, child, id, nparts);
+}
+
 void starpu_data_partition(starpu_data_handle_t h, struct starpu_data_filter *f)
 {
-    STARPU_ASSERT_MSG(h->id == STARPU_MATRIX_INTERFACE_ID, "only matrix handles can be partitioned");
+    STARPU_ASSERT_MSG(h->id == STARPU_MATRIX_INTERFACE_ID || h->id == STARPU_VECTOR_INTERFACE_ID,
+                      "only matrix and vector handles can be partitioned");
     STARPU_ASSERT_MSG(!h->partitioned, "handle already partitioned");
     unsigned n = f->get_nchildren ? f->get_nchildren(f, h) : f->nchildren;
     STARPU_ASSERT(n > 0);
@@ -398,6 +407,21 @@ void rt_data_after_write(starpu_data_handle_t h, int node)
 void *rt_data_interface(starpu_data_handle_t h, int node)
 {
     if (h->id == STARPU_VARIABLE_INTERFACE_ID) return &h->var[node];
+    if (h->id == STARPU_VECTOR_INTERFACE_ID) {
+        /* a vector is kept as an nx x 1 matrix; its codelets read the vector
+         * interface's layout (elemsize where a matrix has ny) */
+        const struct starpu_matrix_interface *m = &h->mat[node];
+        struct starpu_vector_interface *v = &h->vec[node];
+        v->id = STARPU_VECTOR_INTERFACE_ID;
+        v->ptr = m->ptr;
+        v->dev_handle = m->dev_handle;
+        v->offset = m->offset;
+        v->nx = m->nx;
+        v->elemsize = m->elemsize;
+        v->allocsize = m->nx * m->elemsize;
+        v->slice_base = 0;
+        return v;
+    }
     return &h->mat[node];
 }
 

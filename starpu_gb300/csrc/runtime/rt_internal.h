@@ -41,6 +41,7 @@ struct _starpu_data_state {
     size_t elemsize;
     struct starpu_matrix_interface mat[RT_NODES];    /* matrix / vector views per node */
     struct starpu_variable_interface var[RT_NODES];  /* variable per node */
+    struct starpu_vector_interface vec[RT_NODES];    /* a vector's codelet view of mat[] */
     int valid[RT_NODES];
     int allocated[RT_NODES];
     void *owned[RT_NODES];      /* buffers this handle allocated (roots only) */

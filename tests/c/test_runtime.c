@@ -99,6 +99,17 @@ static void commute_add(void *descr[], void *arg)
 }
 static struct starpu_codelet cl_commute = {.cpu_funcs = {commute_add}, .nbuffers = 1, .modes = {STARPU_RW | STARPU_COMMUTE}};
 
+/* every element of the vector block += its element size, read through the
+ * vector interface */
+static void vec_add_elemsize(void *descr[], void *arg)
+{
+    (void)arg;
+    int *p = (int *)STARPU_VECTOR_GET_PTR(descr[0]);
+    const size_t nx = STARPU_VECTOR_GET_NX(descr[0]), es = STARPU_VECTOR_GET_ELEMSIZE(descr[0]);
+    for (size_t i = 0; i < nx; ++i) p[i] += (int)es;
+}
+static struct starpu_codelet cl_vec = {.cpu_funcs = {vec_add_elemsize}, .nbuffers = 1, .modes = {STARPU_RW}};
+
 static int cb_count = 0;
 static void cb(void *arg) { __sync_fetch_and_add(&cb_count, *(int *)arg); }
 
@@ -276,6 +287,23 @@ int main(void)
         starpu_data_unregister(hv);
         starpu_data_unregister(hw);
         CHECK(rc == 0 && before == -1 && w == 42, "end_dep_holds_termination");
+    }
+    /* vectors: the codelet's view has the vector layout, and 3 blocks of 10
+     * elements (4, 3, 3: vector_filters.c) cover every element once */
+    {
+        int vv[10] = {0};
+        starpu_data_handle_t hv;
+        starpu_vector_data_register(&hv, STARPU_MAIN_RAM, (uintptr_t)vv, 10, sizeof(int));
+        struct starpu_data_filter f = {.filter_func = starpu_vector_filter_block, .nchildren = 3};
+        starpu_data_partition(hv, &f);
+        int rc = 0;
+        for (unsigned c = 0; c < 3; ++c) rc |= starpu_task_insert(&cl_vec, STARPU_RW, starpu_data_get_sub_data(hv, 1, c), 0);
+        starpu_task_wait_for_all();
+        starpu_data_unpartition(hv, STARPU_MAIN_RAM);
+        starpu_data_unregister(hv);
+        int ok = rc == 0;
+        for (int i = 0; i < 10; ++i) ok &= vv[i] == (int)sizeof(int);
+        CHECK(ok, "vector_blocks_and_elemsize");
     }
     /* commuting writers (STARPU_RW | STARPU_COMMUTE): any order, never two at
      * once on one handle; a plain reader after them sees all of them */

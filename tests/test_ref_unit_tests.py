@@ -2,14 +2,15 @@
 runtime's CPU workers (tests/main and tests/datawizard of the reference:
 insert_task, explicit task dependencies declared before or after the
 predecessors' submission and from callbacks, tags, regenerated, restarted
-and synchronous tasks, empty tasks as sync points, readers/writers,
+and synchronous tasks, empty tasks as sync points, vector partitions,
+readers/writers,
 commuting writers (unordered among themselves, also against explicit
 dependencies), void handles, pause/resume, tasks pinned to a worker, task
 fault tolerance).  oracle/Makefile `ref-unit-tests` compiles each one
 against include/ and links it with libstarpu_gb300.so; each must exit 0.
 
 Not in the list: tests of what this runtime does not have (OpenCL/HIP
-workers, NUMA nodes, memory reclaiming, hwloc, the vector interface,
+workers, NUMA nodes, memory reclaiming, hwloc, asynchronous partitioning,
 reductions, more than STARPU_NMAXBUFS buffers per task), main/deadlock (a dependency cycle
 that hangs by design), and main/tag_task_data_deps (passes, in about a
 minute)."""
