@@ -461,6 +461,8 @@ int starpu_task_insert(struct starpu_codelet *cl, ...);
 int starpu_insert_task(struct starpu_codelet *cl, ...);
 struct starpu_task *starpu_task_build(struct starpu_codelet *cl, ...);
 void starpu_codelet_unpack_args(void *cl_arg, ...);
+void starpu_codelet_pack_args(void **arg_buffer, size_t *arg_buffer_size, ...);
+void starpu_codelet_unpack_args_and_copyleft(void *cl_arg, void *buffer, size_t buffer_size, ...);
 
 /* ====================================================================== tags */
 void starpu_tag_declare_deps(starpu_tag_t id, unsigned ndeps, ...);

@@ -179,6 +179,7 @@ void starpu_tag_notify_from_apps(starpu_tag_t id)
  * (a regenerated task) */
 enum { SUBMIT_NODEPS = 1, SUBMIT_COUNTED = 2 };
 static int rt_submit(struct starpu_task *t, int flags);
+static void pack_value(void **buf, size_t *size, const void *p, size_t sz);
 
 /* ---------------------------------------------------------- dependencies */
 
@@ -704,6 +705,7 @@ static int build_task(struct starpu_task *t, struct starpu_codelet *cl, va_list 
     t->cl = cl;
     int nb = 0;
     int type;
+    int got_value = 0, got_cl_args = 0, bad_mix = 0; /* STARPU_VALUE and STARPU_CL_ARGS exclude each other */
     while ((type = va_arg(ap, int)) != 0) {
         if ((type & ~((1 << STARPU_MODE_SHIFT) - 1)) == 0) {
             /* an access mode (possibly with flags) followed by a handle */
@@ -729,17 +731,24 @@ static int build_task(struct starpu_task *t, struct starpu_codelet *cl, va_list 
         } else if (type == STARPU_VALUE) {
             void *p = va_arg(ap, void *);
             size_t sz = va_arg(ap, size_t);
-            /* packed as in starpu_codelet_pack_args: [size][bytes]... appended */
-            size_t old = t->cl_arg_size;
-            t->cl_arg = realloc(t->cl_arg, old + sizeof(size_t) + sz);
-            memcpy((char *)t->cl_arg + old, &sz, sizeof(size_t));
-            memcpy((char *)t->cl_arg + old + sizeof(size_t), p, sz);
-            t->cl_arg_size = old + sizeof(size_t) + sz;
+            if (got_cl_args) {
+                bad_mix = 1;
+                continue;
+            }
+            pack_value(&t->cl_arg, &t->cl_arg_size, p, sz); /* as starpu_codelet_pack_args packs */
             t->cl_arg_free = 1;
+            got_value = 1;
         } else if (type == STARPU_CL_ARGS || type == STARPU_CL_ARGS_NFREE) {
-            t->cl_arg = va_arg(ap, void *);
-            t->cl_arg_size = va_arg(ap, size_t);
+            void *arg = va_arg(ap, void *);
+            const size_t size = va_arg(ap, size_t);
+            if (got_value) {
+                bad_mix = 1;
+                continue;
+            }
+            t->cl_arg = arg;
+            t->cl_arg_size = size;
             t->cl_arg_free = type == STARPU_CL_ARGS;
+            got_cl_args = 1;
         } else if (type == STARPU_CALLBACK) {
             t->callback_func = va_arg(ap, void (*)(void *));
         } else if (type == STARPU_CALLBACK_WITH_ARG) {
@@ -787,6 +796,10 @@ static int build_task(struct starpu_task *t, struct starpu_codelet *cl, va_list 
             fprintf(stderr, "[starpu_gb300] unsupported task_insert argument %d\n", type);
             return -EINVAL;
         }
+    }
+    if (bad_mix) {
+        fprintf(stderr, "[starpu_gb300] STARPU_CL_ARGS and STARPU_VALUE cannot be used in the same call\n");
+        return -EINVAL;
     }
     t->nbuffers = nb;
     if (cl && cl->nbuffers >= 0)
@@ -842,19 +855,100 @@ int starpu_insert_task(struct starpu_codelet *cl, ...)
 
 /* Unpack STARPU_VALUE arguments in order: each destination pointer receives
  * the bytes of the corresponding packed value. */
+/* Packed STARPU_VALUE arguments (task_insert_utils.c, task_insert.c:54-104):
+ * an int count, then per value its size_t length and its bytes.  Unpacking
+ * fills at most `count` destinations and stops early at a 0 / NULL one, so
+ * callers may or may not end their list with 0. */
+static void pack_value(void **buf, size_t *size, const void *p, size_t sz)
+{
+    char *b = *buf;
+    size_t n = *size;
+    if (n == 0) {
+        b = malloc(sizeof(int));
+        const int zero = 0;
+        memcpy(b, &zero, sizeof zero);
+        n = sizeof(int);
+    }
+    b = realloc(b, n + sizeof sz + sz);
+    memcpy(b + n, &sz, sizeof sz);
+    memcpy(b + n + sizeof sz, p, sz);
+    int count;
+    memcpy(&count, b, sizeof count);
+    ++count;
+    memcpy(b, &count, sizeof count);
+    *buf = b;
+    *size = n + sizeof sz + sz;
+}
+
+/* returns the number of values consumed; *pos is left after them */
+static int unpack_values(const char *arg, size_t *pos, int count, va_list ap)
+{
+    int k = 0;
+    for (; k < count; ++k) {
+        void *dst = va_arg(ap, void *);
+        if (!dst) break;
+        size_t sz;
+        memcpy(&sz, arg + *pos, sizeof sz);
+        memcpy(dst, arg + *pos + sizeof sz, sz);
+        *pos += sizeof sz + sz;
+    }
+    return k;
+}
+
 void starpu_codelet_unpack_args(void *cl_arg, ...)
 {
+    int count;
+    memcpy(&count, cl_arg, sizeof count);
+    size_t pos = sizeof count;
     va_list ap;
     va_start(ap, cl_arg);
-    char *p = (char *)cl_arg;
-    void *dst;
-    while ((dst = va_arg(ap, void *)) != NULL) {
-        size_t sz;
-        memcpy(&sz, p, sizeof sz);
-        memcpy(dst, p + sizeof sz, sz);
-        p += sizeof sz + sz;
+    unpack_values((const char *)cl_arg, &pos, count, ap);
+    va_end(ap);
+}
+
+void starpu_codelet_pack_args(void **arg_buffer, size_t *arg_buffer_size, ...)
+{
+    va_list ap;
+    va_start(ap, arg_buffer_size);
+    void *buf = NULL;
+    size_t n = 0;
+    int type;
+    while ((type = va_arg(ap, int)) != 0) {
+        STARPU_ASSERT_MSG(type == STARPU_VALUE, "starpu_codelet_pack_args takes STARPU_VALUE arguments");
+        const void *p = va_arg(ap, const void *);
+        const size_t sz = va_arg(ap, size_t);
+        pack_value(&buf, &n, p, sz);
     }
     va_end(ap);
+    *arg_buffer = buf;
+    *arg_buffer_size = n;
+}
+
+/* Unpacks the first values and writes the others, packed again (count
+ * first), into `buffer` for a later starpu_codelet_unpack_args. */
+void starpu_codelet_unpack_args_and_copyleft(void *cl_arg, void *buffer, size_t buffer_size, ...)
+{
+    const char *arg = cl_arg;
+    int count;
+    memcpy(&count, arg, sizeof count);
+    size_t pos = sizeof count;
+    va_list ap;
+    va_start(ap, buffer_size);
+    const int used = unpack_values(arg, &pos, count, ap);
+    va_end(ap);
+    if (!buffer_size) return;
+    const int left = count - used;
+    size_t rest = 0;
+    for (int k = 0, q = (int)pos; k < left; ++k) {
+        size_t sz;
+        memcpy(&sz, arg + q, sizeof sz);
+        rest += sizeof sz + sz;
+        q += (int)(sizeof sz + sz);
+    }
+    STARPU_ASSERT_MSG(sizeof left + rest <= buffer_size, "%zu bytes of arguments left, the buffer holds %zu",
+                      sizeof left + rest, buffer_size);
+    memcpy(buffer, &left, sizeof left);
+    memcpy((char *)buffer + sizeof left, arg + pos, rest);
 }
 
 /* ------------------------------------------------------- fault tolerance
