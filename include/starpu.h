@@ -217,6 +217,10 @@ void starpu_data_wont_use(starpu_data_handle_t handle);
 void starpu_data_invalidate(starpu_data_handle_t handle);
 int starpu_data_acquire(starpu_data_handle_t handle, enum starpu_data_access_mode mode);
 void starpu_data_release(starpu_data_handle_t handle);
+/* asynchronous acquisition: `callback` runs once the data is available in
+ * RAM; the access lasts until starpu_data_release */
+int starpu_data_acquire_cb(starpu_data_handle_t handle, enum starpu_data_access_mode mode, void (*callback)(void *),
+                           void *arg);
 size_t starpu_data_get_size(starpu_data_handle_t handle);
 uint32_t starpu_data_get_footprint(starpu_data_handle_t handle);
 void *starpu_data_get_local_ptr(starpu_data_handle_t handle);
@@ -632,6 +636,7 @@ int starpu_conf_noworker(struct starpu_conf *conf);
  * that is not a non-negative integer aborts */
 int starpu_get_env_number(const char *str);
 void starpu_usleep(float nb_micro_sec);
+void starpu_do_schedule(void);
 int starpu_worker_get_count_by_type(enum starpu_worker_archtype type);
 /* a handle without data, for dependencies only */
 void starpu_void_data_register(starpu_data_handle_t *handle);

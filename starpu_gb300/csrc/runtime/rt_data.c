@@ -500,7 +500,75 @@ int starpu_data_acquire(starpu_data_handle_t h, enum starpu_data_access_mode mod
     return 0;
 }
 
-void starpu_data_release(starpu_data_handle_t h) { (void)h; }
+/* Asynchronous acquisition (datawizard/user_interactions.c): an internal
+ * STARPU_NOWHERE task takes the access with the usual dependencies; its
+ * prologue brings the data to RAM and calls `callback`, and an end
+ * dependency keeps the access until starpu_data_release, so later tasks on
+ * the handle wait for the release.  A graph-mode runtime (which records the
+ * DAG before anything runs) acquires synchronously, then calls back. */
+struct acquire_cb {
+    starpu_data_handle_t h;
+    enum starpu_data_access_mode mode;
+    void (*callback)(void *);
+    void *arg;
+};
+
+static void acquire_prologue(void *p)
+{
+    struct acquire_cb *a = p;
+    rt_lock();
+    if (a->mode & STARPU_R) gather(a->h, RT_NODE_RAM);
+    if (a->mode & STARPU_W) rt_data_after_write(a->h, RT_NODE_RAM);
+    rt_unlock();
+    if (a->callback) a->callback(a->arg);
+}
+
+int starpu_data_acquire_cb(starpu_data_handle_t h, enum starpu_data_access_mode mode, void (*callback)(void *),
+                           void *arg)
+{
+    if (rt.graph_mode) {
+        starpu_data_acquire(h, mode);
+        if (callback) callback(arg);
+        return 0;
+    }
+    struct acquire_cb *a = malloc(sizeof *a);
+    a->h = h;
+    a->mode = mode;
+    a->callback = callback;
+    a->arg = arg;
+    struct starpu_task *t = starpu_task_create();
+    t->name = "acquire_cb";
+    t->nbuffers = 1;
+    t->handles[0] = h;
+    t->modes[0] = mode;
+    t->where = STARPU_NOWHERE;
+    t->prologue_callback_func = acquire_prologue;
+    t->prologue_callback_arg = a;
+    t->prologue_callback_arg_free = 1;
+    starpu_task_end_dep_add(t, 1);
+    rt_lock();
+    if (h->nacquired == h->capacquired) {
+        h->capacquired = h->capacquired ? 2 * h->capacquired : 4;
+        h->acquired = realloc(h->acquired, sizeof *h->acquired * h->capacquired);
+    }
+    h->acquired[h->nacquired++] = t;
+    rt_unlock();
+    return starpu_task_submit(t);
+}
+
+/* ends the oldest pending asynchronous acquisition of h; a synchronous one
+ * holds nothing */
+void starpu_data_release(starpu_data_handle_t h)
+{
+    struct starpu_task *t = NULL;
+    rt_lock();
+    if (h->nacquired) {
+        t = h->acquired[0];
+        memmove(h->acquired, h->acquired + 1, sizeof *h->acquired * --h->nacquired);
+    }
+    rt_unlock();
+    if (t) starpu_task_end_dep_release(t);
+}
 
 static void unregister(starpu_data_handle_t h, int coherent)
 {
@@ -516,6 +584,7 @@ static void unregister(starpu_data_handle_t h, int coherent)
     if (h->owned[RT_NODE_RAM]) free(h->owned[RT_NODE_RAM]);
     free(h->readers);
     free(h->commuters);
+    free(h->acquired);
     free(h);
 }
 

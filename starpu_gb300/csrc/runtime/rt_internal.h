@@ -61,6 +61,8 @@ struct _starpu_data_state {
     struct rt_job **commuters;
     int ncommuters, capcommuters;
     int commute_busy;
+    struct starpu_task **acquired;  /* pending starpu_data_acquire_cb accesses, released in order */
+    int nacquired, capacquired;
     char name[48];
 };
 
