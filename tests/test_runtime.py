@@ -1,7 +1,9 @@
 """The StarPU-API runtime of libstarpu_gb300.so on CPU workers.
 
 * tests/c/test_runtime.c: implicit dependencies, filters, tags, values,
-  callbacks, -ENODEV and history perfmodels (no GPU needed).
+  callbacks, -ENODEV, history perfmodels, scheduling contexts, task fault
+  tolerance (default retry policy), end dependencies, commuting writers and
+  vector partitions (no GPU needed).
 * The reference's own, unchanged examples/cholesky/cholesky_implicit.c
   compiled against include/ and linked with this runtime (oracle/Makefile
   `ref-driver`): with the reference's CPU codelets it must pass the
