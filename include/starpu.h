@@ -407,6 +407,9 @@ struct starpu_task *starpu_task_get_current(void);
  * the tasks it waits for may be submitted before or after it, or be done */
 void starpu_task_declare_deps_array(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[]);
 void starpu_task_declare_deps(struct starpu_task *task, unsigned ndeps, ...);
+/* `task` terminates only once these tasks have too (done, submitted or not yet) */
+void starpu_task_declare_end_deps_array(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[]);
+void starpu_task_declare_end_deps(struct starpu_task *task, unsigned ndeps, ...);
 /* submission without data or tag dependencies (the caller already holds the data) */
 int starpu_task_submit_nodeps(struct starpu_task *task);
 /* termination of `task` waits for nb_deps more starpu_task_end_dep_release calls */
@@ -637,6 +640,7 @@ int starpu_conf_noworker(struct starpu_conf *conf);
 int starpu_get_env_number(const char *str);
 void starpu_usleep(float nb_micro_sec);
 void starpu_do_schedule(void);
+void starpu_sleep(float nb_sec);
 int starpu_worker_get_count_by_type(enum starpu_worker_archtype type);
 /* a handle without data, for dependencies only */
 void starpu_void_data_register(starpu_data_handle_t *handle);

@@ -92,6 +92,8 @@ void starpu_usleep(float nb_micro_sec)
     }
 }
 
+void starpu_sleep(float nb_sec) { starpu_usleep(nb_sec * 1e6f); }
+
 /* every ready task is pushed as it becomes ready: nothing waits for this */
 void starpu_do_schedule(void) {}
 

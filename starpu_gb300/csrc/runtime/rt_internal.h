@@ -87,6 +87,8 @@ struct rt_job {
     int tag_waits;              /* tags awaited whose task is not submitted yet */
     int prologue_done;
     struct rt_job *defer_next;  /* queue of ready jobs whose prologue / NOWHERE step runs unlocked */
+    struct starpu_task **end_release; /* tasks whose termination also waits for this one */
+    int nend_release, capend_release;
 };
 
 struct rt_worker {

@@ -323,6 +323,72 @@ void rt_commute_release(struct starpu_task *t)
     if (n) pthread_cond_broadcast(&rt.commute_cond);
 }
 
+/* End dependencies on other tasks (starpu_task_dep.h): `task` terminates
+ * only once each of them has.  A task done already adds nothing; one
+ * submitted releases `task` when it terminates; one not submitted yet is
+ * recorded until it is. */
+struct end_waiter {
+    struct starpu_task *pred, *task;
+    struct end_waiter *next;
+};
+static struct end_waiter *end_waiters; /* guarded by the runtime lock */
+
+static void add_end_release(struct rt_job *j, struct starpu_task *task)
+{
+    if (j->nend_release == j->capend_release) {
+        j->capend_release = j->capend_release ? 2 * j->capend_release : 4;
+        j->end_release = realloc(j->end_release, sizeof *j->end_release * j->capend_release);
+    }
+    j->end_release[j->nend_release++] = task;
+}
+
+void starpu_task_declare_end_deps_array(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[])
+{
+    rt_lock();
+    for (unsigned i = 0; i < ndeps; ++i) {
+        struct starpu_task *p = task_array[i];
+        if (!p || p == task || p->status == STARPU_TASK_FINISHED) continue;
+        task->nb_termination_call_required++;
+        if (p->starpu_private) {
+            add_end_release(p->starpu_private, task);
+        } else {
+            struct end_waiter *w = malloc(sizeof *w);
+            w->pred = p;
+            w->task = task;
+            w->next = end_waiters;
+            end_waiters = w;
+        }
+    }
+    rt_unlock();
+}
+
+void starpu_task_declare_end_deps(struct starpu_task *task, unsigned ndeps, ...)
+{
+    if (!ndeps) return;
+    struct starpu_task **deps = malloc(sizeof *deps * ndeps);
+    va_list ap;
+    va_start(ap, ndeps);
+    for (unsigned i = 0; i < ndeps; ++i) deps[i] = va_arg(ap, struct starpu_task *);
+    va_end(ap);
+    starpu_task_declare_end_deps_array(task, ndeps, deps);
+    free(deps);
+}
+
+/* runtime lock held, as job j of its task is submitted */
+static void link_end_waiters(struct rt_job *j)
+{
+    for (struct end_waiter **pw = &end_waiters; *pw;) {
+        struct end_waiter *w = *pw;
+        if (w->pred != j->task) {
+            pw = &w->next;
+            continue;
+        }
+        add_end_release(j, w->task);
+        *pw = w->next;
+        free(w);
+    }
+}
+
 static void add_reader(starpu_data_handle_t h, struct rt_job *j)
 {
     if (h->nreaders == h->capreaders) {
@@ -441,6 +507,7 @@ static int rt_submit(struct starpu_task *t, int flags)
     }
     if (!nodeps && t->ndeclared_deps) link_declared_deps(j);
     if (task_waiters) link_waiting_successors(j);
+    if (end_waiters) link_end_waiters(j);
     if (rt.graph_mode) {
         if (rt.npending == rt.cappending) {
             rt.cappending = rt.cappending ? 2 * rt.cappending : 1024;
@@ -564,6 +631,8 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
         pthread_cond_broadcast(&tag_cond);
     }
     int destroy = !regen && t->destroy && t->detach;
+    struct starpu_task **release = j->end_release;
+    const int nrelease = j->nend_release;
     t->starpu_private = NULL;
     free(j->succ);
     free(j->prev);
@@ -574,6 +643,8 @@ void rt_job_terminate(struct rt_job *j, double measured_us)
     }
     pthread_cond_broadcast(&rt.all_done);
     rt_unlock();
+    for (int k = 0; k < nrelease; ++k) starpu_task_end_dep_release(release[k]);
+    free(release);
     if (regen) {
         t->starpu_private = NULL;
         const int rc = rt_submit(t, SUBMIT_COUNTED);

@@ -110,6 +110,16 @@ static void vec_add_elemsize(void *descr[], void *arg)
 }
 static struct starpu_codelet cl_vec = {.cpu_funcs = {vec_add_elemsize}, .nbuffers = 1, .modes = {STARPU_RW}};
 
+static int slow_done = 0;
+static void slow_fn(void *descr[], void *arg)
+{
+    (void)descr;
+    (void)arg;
+    usleep(20000);
+    __sync_fetch_and_add(&slow_done, 1);
+}
+static struct starpu_codelet cl_slow = {.cpu_funcs = {slow_fn}, .nbuffers = 0};
+
 static int cb_count = 0;
 static void cb(void *arg) { __sync_fetch_and_add(&cb_count, *(int *)arg); }
 
@@ -287,6 +297,26 @@ int main(void)
         starpu_data_unregister(hv);
         starpu_data_unregister(hw);
         CHECK(rc == 0 && before == -1 && w == 42, "end_dep_holds_termination");
+    }
+    /* end dependencies on tasks (starpu_task_dep.h): m is reported done only
+     * once s1 (submitted) and s2 (submitted after the declaration) are */
+    {
+        struct starpu_task *m = starpu_task_create(), *s1 = starpu_task_create(), *s2 = starpu_task_create();
+        m->cl = &cl_noop;
+        m->detach = 0;
+        m->destroy = 0;
+        s1->cl = &cl_slow;
+        s2->cl = &cl_slow;
+        int rc = starpu_task_submit(s1);
+        starpu_task_declare_end_deps(m, 2, s1, s2);
+        rc |= starpu_task_submit(m);
+        usleep(2000);
+        rc |= starpu_task_submit(s2);
+        rc |= starpu_task_wait(m);
+        const int done_at_wait = slow_done;
+        starpu_task_destroy(m);
+        starpu_task_wait_for_all();
+        CHECK(rc == 0 && done_at_wait == 2, "end_deps_on_tasks");
     }
     /* vectors: the codelet's view has the vector layout, and 3 blocks of 10
      * elements (4, 3, 3: vector_filters.c) cover every element once */
