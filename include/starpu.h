@@ -410,6 +410,8 @@ void starpu_task_declare_deps(struct starpu_task *task, unsigned ndeps, ...);
 /* `task` terminates only once these tasks have too (done, submitted or not yet) */
 void starpu_task_declare_end_deps_array(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[]);
 void starpu_task_declare_end_deps(struct starpu_task *task, unsigned ndeps, ...);
+int starpu_task_get_task_succs(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[]);
+struct starpu_task *starpu_tag_get_task(starpu_tag_t id);
 /* submission without data or tag dependencies (the caller already holds the data) */
 int starpu_task_submit_nodeps(struct starpu_task *task);
 /* termination of `task` waits for nb_deps more starpu_task_end_dep_release calls */

@@ -68,6 +68,7 @@ int starpu_task_nready(void)
 struct tag_entry {
     starpu_tag_t id;
     struct rt_job *job;     /* last submitted task with this tag (NULL once done) */
+    struct starpu_task *task; /* that task, kept after it is done (starpu_tag_get_task) */
     int done;               /* completed (or notified from the application) */
     starpu_tag_t *deps;
     int ndeps;
@@ -493,6 +494,7 @@ static int rt_submit(struct starpu_task *t, int flags)
             }
         }
         e->job = j;
+        e->task = t;
         e->done = 0;
         /* tasks that waited for this tag before it had a task now depend on it */
         for (int w = 0; w < e->nwaiters; ++w) {
@@ -1111,3 +1113,33 @@ struct starpu_codelet starpu_codelet_nop = {
     .cuda_funcs = {starpu_codelet_nop_func},
     .nbuffers = 0,
 };
+
+/* the last task submitted with tag `id`, also once it is done; NULL when
+ * none was (tags.c) */
+struct starpu_task *starpu_tag_get_task(starpu_tag_t id)
+{
+    rt_lock();
+    struct tag_entry *e = tag_get(id, 0);
+    struct starpu_task *t = e ? e->task : NULL;
+    rt_unlock();
+    return t;
+}
+
+/* the distinct tasks that wait for `task` (submitted, not terminated):
+ * their count, of which the first `ndeps` go to task_array (task.c) */
+int starpu_task_get_task_succs(struct starpu_task *task, unsigned ndeps, struct starpu_task *task_array[])
+{
+    rt_lock();
+    struct rt_job *j = task->starpu_private;
+    int n = 0;
+    for (int k = 0; j && k < j->nsucc; ++k) {
+        struct starpu_task *u = j->succ[k]->task;
+        int seen = 0;
+        for (int q = 0; q < k && !seen; ++q) seen = j->succ[q]->task == u;
+        if (seen) continue;
+        if ((unsigned)n < ndeps) task_array[n] = u;
+        ++n;
+    }
+    rt_unlock();
+    return n;
+}
